@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark: minidisk Godunov update, cell-updates/s on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload minidisk-4096|minidisk-256] [--precision mixed|fp64]
+
+Default workload (the large-minidisk configuration): [-8,8]^2 on 4096^2 cells
+(64x64 blocks of 64^2), mass ratio 0.5, eccentricity 0.1, Mach 20, viscosity
+5e-4, softening/sink radius 0.05, sink rate 10, buffer rate 100 / scale 0.2,
+PLM theta 1.5, RK2, CFL 0.3 with the fastest-wavespeed reduction, seeded +-1%
+density perturbation; FP32 fluxes/sources with FP64 state accumulation. A step
+is one RK2 step of the whole mesh; inputs are synthetic (seeded), resident in
+HBM; the 403 MB FP64 state exceeds the 129 MB L2, so no flush is needed.
+
+One JSON line on rank 0. `value` is device-timed cell-updates/s over all ranks;
+`e2e` is the same metric through the reference-facing host-buffer call
+(mara_minidisk_advance_host: H2D state, step, D2H state, every step); the
+roofline line is for the dominant stage kernel, timed with CUDA events on the
+stream it runs on. With --gpus N under torchrun each rank advances its own
+independent replica (replicas only; no data-path collective).
+
+--impl reference times the reference's CPU scheme (the oracle restatement of
+problems/minidisk_scheme.cpp, run per block on all host threads as the
+reference's thread-pool executor does) on a bounded window of the same mesh.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # BASELINE configuration 2 (large minidisk)
+    "minidisk-4096": dict(block_size=64, depth=6, omega_frame=1.0, mach_number=20.0, nu=5e-4, domain_radius=8.0,
+                          softening_length=0.05, eccentricity=0.1, mass_ratio=0.5, sink_radius=0.05, sink_rate=10.0,
+                          buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=1.5),
+    # BASELINE configuration 1 (256^2, 4x4 blocks of 64^2)
+    "minidisk-256": dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3, domain_radius=4.0,
+                         softening_length=0.05, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.05, sink_rate=10.0,
+                         buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=1.5),
+}
+# Algorithmic HBM bytes per cell for each stage kernel (FP64 state = 24 B/cell,
+# FP32 increment = 12 B/cell):
+#   mixed stage 1: read u0 (24) + write d1 (12)                  = 36
+#   mixed stage 2: read u0 (24) + read d1 (12) + write u (24)    = 60
+#   fp64 stage 1 : read u0 (24) + write u1 (24)                  = 48
+#   fp64 stage 2 : read u1 (24) + read u0 (24) + write u (24)    = 72
+STAGE_BYTES = {("mixed", 1): 36, ("mixed", 2): 60, ("fp64", 1): 48, ("fp64", 2): 72}
+L2_BYTES = 129 * 2**20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="minidisk-4096")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.device)], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for name, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class CpuBaseline:
+    """Oracle restatement of the reference scheme on all host threads, on a
+    bounded window of blocks of the same mesh: one RK2 step = two substeps,
+    one task per block per substep (the reference's compute_threaded shape)."""
+
+    def __init__(self, sd_kw: dict, seconds: float):
+        from oracle.oracle import MinidiskParams, dptr, load_oracle
+        self.o, self.dptr = load_oracle(), dptr
+        self.p = MinidiskParams(**sd_kw)
+        p = self.p
+        self.N = p.block_size << p.depth
+        self.nb = 1 << p.depth
+        self.threads = os.cpu_count() or 1
+        self.u = np.zeros(3 * self.N * self.N)
+        self.o.oracle_minidisk_initial_conserved(ctypes.byref(p), ctypes.c_uint64(1), ctypes.c_double(0.01),
+                                                 dptr(self.u))
+        self.out = np.zeros_like(self.u)
+        self.t = 1.0
+        self.dt = self.o.oracle_minidisk_dt_formula(ctypes.byref(p), ctypes.c_double(1.0))
+        probe = min(max(self.threads, 16), self.nb * self.nb)
+        per_block = self.step(probe) / probe
+        self.count = int(min(self.nb * self.nb, max(self.threads, seconds / max(per_block, 1e-9))))
+
+    def step(self, count=None) -> float:
+        count = self.count if count is None else count
+        o, p, d = self.o, self.p, self.dptr
+        t0 = time.perf_counter()
+        o.oracle_minidisk_substep_blocks(ctypes.byref(p), d(self.u), d(self.out), ctypes.c_double(self.t),
+                                         ctypes.c_double(self.dt), self.threads, 0, count)
+        o.oracle_minidisk_substep_blocks(ctypes.byref(p), d(self.out), d(self.u), ctypes.c_double(self.t + self.dt),
+                                         ctypes.c_double(self.dt), self.threads, 0, count)
+        return time.perf_counter() - t0
+
+    def measure(self) -> dict:
+        elapsed = self.step()
+        cells = self.count * self.p.block_size ** 2
+        return {"value": cells / elapsed, "unit": "cell-updates/s", "cores": self.threads, "kind": "port",
+                "sample": f"one RK2 step on {self.count} of {self.nb * self.nb} blocks ({cells} cells) of the "
+                          f"{self.N}^2 mesh, {elapsed:.1f} s, {self.threads} threads, one task per block per substep"}
+
+
+def cpu_baseline(sd_kw: dict, seconds: float) -> dict:
+    return CpuBaseline(sd_kw, seconds).measure()
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    sd_kw = WORKLOADS[args.workload]
+    cb = CpuBaseline(sd_kw, seconds=min(args.cpu_sample_seconds, 3.0))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cb.measure()
+        if i >= args.warmup:
+            vals.append(r["value"])
+    value = float(np.mean(vals))
+    N = sd_kw["block_size"] << sd_kw["depth"]
+    line = {
+        "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N * N / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "cells": N * N, "scheme": "PLM+HLLE+viscosity+sources, RK2",
+                   "precision": "fp64 (reference CPU scheme)"},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": r["cores"], "kind": r["kind"],
+                         "sample": r["sample"]},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import mara3p_gb300.minidisk as md
+    from mara3p_gb300._capi import check, lib
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    sd = md.SolverData(**WORKLOADS[args.workload])
+    N = sd.cells_per_side
+    cells = N * N
+    prec = md.MIXED if args.precision == "mixed" else md.FP64
+    u0 = md.initial_conserved(sd, seed=1 + rank, amplitude=0.01)
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=prec, dt_mode=md.DT_CFL)
+    stream = torch.cuda.current_stream()
+
+    run.advance(args.warmup)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as sampler:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run.advance(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * args.steps * world / (ms * 1e-3)
+    gpu_launches = 1 + 3 * args.steps     # clock begin + per step (stage 1, stage 2, clock)
+
+    # Per-stage kernel durations (dominant kernel for the roofline): the same
+    # stage kernels, launched one by one through mara_minidisk_stage on the
+    # same stream with CUDA events around each launch.
+    c = sd.to_c()
+    ws = run.workspace
+    clock = run.clock.data_ptr()
+    d1 = ws.data_ptr() + 3 * cells * 8
+    alt = ws.data_ptr()
+    kind1, kind2 = (1, 2) if prec == md.MIXED else (0, 0)
+    reps = max(3, min(args.steps, 10))
+    t1, t2 = [], []
+    for _ in range(reps):
+        a, b, d = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        a.record(stream)
+        if prec == md.MIXED:
+            check(lib.mara_minidisk_stage(ctypes.byref(c), kind1, run.u.data_ptr(), None, None, None, d1, clock, 0, 0,
+                                          stream.cuda_stream))
+            b.record(stream)
+            check(lib.mara_minidisk_stage(ctypes.byref(c), kind2, run.u.data_ptr(), d1, None, alt, None, clock, 1, 1,
+                                          stream.cuda_stream))
+        else:
+            check(lib.mara_minidisk_stage(ctypes.byref(c), 0, run.u.data_ptr(), None, None, alt, None, clock, 0, 0,
+                                          stream.cuda_stream))
+            b.record(stream)
+            check(lib.mara_minidisk_stage(ctypes.byref(c), 0, alt, None, run.u.data_ptr(), run.u.data_ptr(), None,
+                                          clock, 1, 1, stream.cuda_stream))
+        d.record(stream)
+        torch.cuda.synchronize()
+        t1.append(a.elapsed_time(b))
+        t2.append(b.elapsed_time(d))
+    pname = args.precision
+    s1, s2 = float(np.median(t1)), float(np.median(t2))
+    dominant = 2 if s2 >= s1 else 1
+    dom_ms = s2 if dominant == 2 else s1
+    dom_bytes = STAGE_BYTES[(pname, dominant)] * cells
+    peak, peak_kind = measured_peaks()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        tk = json.loads(tfile.read_text()).get(f"{args.workload}/{pname}/stage{dominant}")
+        if tk is not None:
+            traffic = float(tk["bytes_per_cell"]) * cells
+    step_bytes = (STAGE_BYTES[(pname, 1)] + STAGE_BYTES[(pname, 2)]) * cells
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": f"stage_kernel<{'float' if prec == md.MIXED else 'double'}, "
+                                             f"stage {dominant}>",
+                "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "peak_source": f"{peak_kind} hbm_gbs",
+                "stage_ms": [s1, s2],
+                "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
+
+    # e2e: the reference-facing host-buffer call, H2D + step + D2H every step.
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty((3, N, N), dtype=torch.float64, pin_memory=True)
+        host_out = torch.empty_like(host_in)
+        host_in.copy_(run.u.cpu())
+        hws = torch.empty(lib.mara_minidisk_host_workspace_bytes(ctypes.byref(c), 2, prec), dtype=torch.uint8,
+                          device="cuda")
+        tout = ctypes.c_double()
+        e2e_steps = max(2, min(args.steps, 10))
+
+        def host_step():
+            check(lib.mara_minidisk_advance_host(ctypes.byref(c), host_in.data_ptr(), host_out.data_ptr(), 1.0, 1, 2,
+                                                 prec, md.DT_CFL, ctypes.byref(tout), hws.data_ptr(),
+                                                 stream.cuda_stream))
+        host_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            host_step()
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": cells * e2e_steps * world / el, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": 3 * cells * 8, "d2h_bytes_per_step": 3 * cells * 8,
+               "call": "mara_minidisk_advance_host (pinned host state in/out, 1 RK2 step per call)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(WORKLOADS[args.workload], args.cpu_sample_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 compute, f64 state" if prec == md.MIXED else "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": cells, "mesh": f"{N}^2 ({1 << sd.depth}x{1 << sd.depth} "
+                       f"blocks of {sd.block_size}^2)", "scheme": "PLM(theta=1.5)+HLLE+viscosity+gravity/sink/buffer "
+                       "sources, RK2, CFL 0.3 wavespeed reduction", "precision": args.precision,
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"no flush: FP64 state {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+            "clocks": sampler.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/*
+ * mara_gb300 — C ABI of the GB300-native Godunov finite-volume update.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (MARA_OK = 0, else a mara_status code; the message of
+ * the last failure on the calling host thread is mara_last_error()).
+ * Buffers marked "device" are caller-owned device memory; calls are
+ * stream-ordered on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * and return before the GPU work finishes. The library allocates no device
+ * memory on its own except where a function says so.
+ *
+ * Mesh layout (minidisk): structure-of-arrays, component-major [3][N][N]
+ * (Σ, Σvx, Σvy); axis 0 = x is the slow index, axis 1 = y is contiguous,
+ * N = block_size << depth; the reference's block (level=depth, bi, bj) owns
+ * rows [bi*n, bi*n+n) and columns [bj*n, bj*n+n) of that mesh (the same
+ * row-major cell order as the reference's nd::shared_array, src/core_ndarray.hpp:188).
+ */
+#ifndef MARA_GB300_H
+#define MARA_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum mara_status {
+    MARA_OK = 0,
+    MARA_ERR_ARGUMENT = 1,   /* invalid argument (message says which) */
+    MARA_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    MARA_ERR_NUMERIC = 3,    /* a zone failed (negative pressure, no convergence) */
+};
+
+enum mara_precision {
+    MARA_FP64 = 0,           /* plain FP64 path: the drop-in for the reference scheme */
+    MARA_MIXED = 1,          /* FP32 reconstruction/fluxes/sources, FP64 state accumulation */
+};
+
+enum mara_dt_mode {
+    MARA_DT_FORMULA = 0,     /* problems/minidisk.cpp:204-206 fixed formula with start-up ramp */
+    MARA_DT_CFL = 1,         /* cfl * dl / max fastest wavespeed (reduction over the mesh) */
+};
+
+/* Field-for-field minidisk::solver_data_t (problems/minidisk.hpp:77-93), plus
+ * the PLM theta that the reference hard-codes to 2.0
+ * (problems/minidisk_scheme.cpp:313-314). */
+typedef struct mara_minidisk_params {
+    int32_t block_size;        /* zones per block side */
+    int32_t depth;             /* mesh levels: 2^depth blocks per side */
+    double omega_frame;        /* frame rotation rate */
+    double mach_number;
+    double nu;                 /* kinematic viscosity */
+    double domain_radius;      /* half-size of the domain */
+    double softening_length;
+    double eccentricity;
+    double mass_ratio;
+    double sink_radius;
+    double sink_rate;
+    double buffer_rate;
+    double buffer_scale;
+    double cfl;
+    double plm_theta;
+} mara_minidisk_params;
+
+/* Device-resident simulation clock of one minidisk run. The step functions
+ * read and advance it on the device, so a sequence of steps needs no host
+ * round trip (and can be captured in a CUDA graph). */
+typedef struct mara_minidisk_clock {
+    double time;               /* simulation time at the start of the next step */
+    double dt;                 /* time step of the last / current step */
+    double max_wavespeed;      /* fastest wavespeed of the current state (CFL mode) */
+    int64_t iteration;         /* completed steps */
+    double binary[2][6];       /* per RK stage: m1, x1, y1, m2, x2, y2 in the rotating frame */
+} mara_minidisk_clock;
+
+/* ---------------------------------------------------------------- library */
+const char* mara_last_error(void);
+const char* mara_version(void);
+
+/* ---------------------------------------------------------------- minidisk */
+
+/* Binary state at time t in the rotating frame, computed on the host in FP64:
+ * out = {m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2}. Replaces
+ * two_body::orbital_state + two_body::rotate as used at
+ * problems/minidisk_scheme.cpp:329-335 (src/physics_two_body.hpp:109-157, 395-444). */
+int mara_minidisk_binary(const mara_minidisk_params* sd, double time, double* out);
+
+/* Fixed-formula time step (problems/minidisk.cpp:204-206). Host. */
+int mara_minidisk_dt_formula(const mara_minidisk_params* sd, double time, double* dt);
+
+/* Drop-in for minidisk::updated_conserved (problems/minidisk.hpp:164-170,
+ * problems/minidisk_scheme.cpp:294-355): one forward-Euler update of one mesh
+ * block, plain FP64. Device buffers in the reference's AoS tuple layout:
+ * uc = n*n*3 conserved, pe = (n+4)*(n+4)*3 primitives with a 2-zone halo,
+ * u1 = n*n*3 out; n = sd->block_size. (level, bi, bj) is the block index. */
+int mara_minidisk_updated_conserved(const mara_minidisk_params* sd, const double* uc, const double* pe,
+                                    double time, double dt, uint32_t level, uint64_t bi, uint64_t bj,
+                                    double* u1, void* stream);
+
+/* Drop-in for minidisk::recover_primitive_array (problems/minidisk_scheme.cpp:208-211):
+ * count AoS cells (3 doubles each), device buffers. */
+int mara_minidisk_recover_primitive(const double* u, int64_t count, double* p, void* stream);
+
+/* Drop-in for minidisk::estimate_gradient (problems/minidisk_scheme.cpp:213-216):
+ * AoS primitives of shape (n0, n1) -> (n0-2, n1) for axis 0, (n0, n1-2) for axis 1. */
+int mara_minidisk_estimate_gradient(const double* pc, int64_t n0, int64_t n1, int32_t axis, double theta,
+                                    double* out, void* stream);
+
+/* Whole-mesh forward-Euler substep, plain FP64, SoA device buffers (the
+ * reference's per-block encode_substep over every block, problems/minidisk.cpp:172-189,
+ * with the periodic halo of extend, :87-120):
+ *   u_out = L(u_in) at (time, dt);
+ *   if u_avg != NULL: u_out = u_avg*0.5 + L(u_in)*0.5, the RK2 second stage
+ *   (src/app_control.hpp:178-183, src/mesh_amr.hpp:456-467).
+ * u_out may alias u_avg but not u_in. */
+int mara_minidisk_substep(const mara_minidisk_params* sd, const double* u_in, const double* u_avg, double* u_out,
+                          double time, double dt, void* stream);
+
+/* Initial conserved state (problems/minidisk_scheme.cpp:87-99, 182-191) with a
+ * seeded density perturbation Σ(1 + amplitude*(2U-1)), U from a counter-based
+ * hash of (seed, cell index); amplitude 0 reproduces the reference exactly. */
+int mara_minidisk_initial_conserved(const mara_minidisk_params* sd, uint64_t seed, double amplitude,
+                                    double* u, void* stream);
+
+/* Bytes of device workspace that mara_minidisk_advance needs for this mesh. */
+int64_t mara_minidisk_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision);
+
+/* Set clock->time, reset the iteration count, and (CFL mode) reduce the
+ * fastest wavespeed of u into clock->max_wavespeed. clock is device memory. */
+int mara_minidisk_clock_init(const mara_minidisk_params* sd, const double* u, double time,
+                             mara_minidisk_clock* clock, void* stream);
+
+/* Advance the SoA state u (device) by `steps` steps of order rk_order (1 or 2)
+ * with the time step of dt_mode, in the given precision. Time, dt and the
+ * binary position live in *clock (device); the CFL reduction of the next step
+ * is fused into the last stage of each step. workspace: device buffer of
+ * mara_minidisk_workspace_bytes. The result is always left in u. */
+int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                          int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                          void* workspace, void* stream);
+
+/* Host-buffer form of mara_minidisk_advance: copies u_in
+ * (host, 3*N*N doubles, SoA; pinned memory gives full bandwidth) to the
+ * device, advances `steps` steps from `time`, copies the state back to u_out
+ * (host) and writes the final time to *time_out. Device buffers come from
+ * the caller's `workspace` of mara_minidisk_host_workspace_bytes. Synchronous
+ * on `stream`. This is the reference-facing call: state in host memory, as
+ * the reference's nd::shared_array holds it. */
+int64_t mara_minidisk_host_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision);
+int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_in, double* u_out, double time,
+                               int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                               double* time_out, void* workspace, void* stream);
+
+/* One stage kernel of mara_minidisk_advance, for callers that drive the RK
+ * loop themselves (the role of control::advance_runge_kutta,
+ * src/app_control.hpp:169-195). dt and the binary come from clock->dt and
+ * clock->binary[stage]. kind:
+ *   0  FP64:    u_out = L(u_in); with u_avg: u_out = u_avg*0.5 + L(u_in)*0.5
+ *   1  mixed 1: d_out = dt*L(u_in) (FP32); with d_out NULL: u_out = u_in + dt*L(u_in)
+ *   2  mixed 2: u_out = u_in + (d1 + dt*L(f32(u_in) + d1))/2
+ * reduce_wavespeed != 0 also folds the fastest wavespeed of u_out into
+ * clock->max_wavespeed. u_out must not alias u_in (kind 0 may alias u_avg). */
+int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const double* u_in, const float* d1,
+                        const double* u_avg, double* u_out, float* d_out, mara_minidisk_clock* clock,
+                        int32_t stage, int32_t reduce_wavespeed, void* stream);
+
+/* Device clock bookkeeping between stages: end_step advances time and the
+ * iteration count of the step that ran (RK2: t = t*0.5 + (t+2dt)*0.5);
+ * begin_step picks the next dt (dt_mode) and the binary of both stages. */
+int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int32_t dt_mode,
+                               int32_t rk_order, int32_t end_step, int32_t begin_step, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARA_GB300_H */

@@ -1,0 +1,105 @@
+"""ctypes binding of include/mara_gb300.h.
+
+The library is loaded from this package directory. There is no fallback: if
+libmara_gb300.so is missing or fails to load, importing raises, so nothing can
+silently run on the CPU instead.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libmara_gb300.so"
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+
+
+class MinidiskParams(ctypes.Structure):
+    """mara_minidisk_params: field-for-field minidisk::solver_data_t
+    (problems/minidisk.hpp:77-93) plus plm_theta."""
+
+    _fields_ = [
+        ("block_size", ctypes.c_int32),
+        ("depth", ctypes.c_int32),
+        ("omega_frame", ctypes.c_double),
+        ("mach_number", ctypes.c_double),
+        ("nu", ctypes.c_double),
+        ("domain_radius", ctypes.c_double),
+        ("softening_length", ctypes.c_double),
+        ("eccentricity", ctypes.c_double),
+        ("mass_ratio", ctypes.c_double),
+        ("sink_radius", ctypes.c_double),
+        ("sink_rate", ctypes.c_double),
+        ("buffer_rate", ctypes.c_double),
+        ("buffer_scale", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("plm_theta", ctypes.c_double),
+    ]
+
+
+class MinidiskClock(ctypes.Structure):
+    _fields_ = [
+        ("time", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("max_wavespeed", ctypes.c_double),
+        ("iteration", ctypes.c_int64),
+        ("binary", ctypes.c_double * 12),
+    ]
+
+
+# (name, restype, argtypes) for every exported entry point of include/mara_gb300.h.
+_vp = ctypes.c_void_p
+_MP = ctypes.POINTER(MinidiskParams)
+SIGNATURES = {
+    "mara_last_error": (ctypes.c_char_p, []),
+    "mara_version": (ctypes.c_char_p, []),
+    "mara_minidisk_binary": (ctypes.c_int, [_MP, ctypes.c_double, c_double_p]),
+    "mara_minidisk_dt_formula": (ctypes.c_int, [_MP, ctypes.c_double, c_double_p]),
+    "mara_minidisk_updated_conserved": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_double, ctypes.c_double,
+                                                       ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp]),
+    "mara_minidisk_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp]),
+    "mara_minidisk_estimate_gradient": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                                                       ctypes.c_double, _vp, _vp]),
+    "mara_minidisk_substep": (ctypes.c_int, [_MP, _vp, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]),
+    "mara_minidisk_initial_conserved": (ctypes.c_int, [_MP, ctypes.c_uint64, ctypes.c_double, _vp, _vp]),
+    "mara_minidisk_workspace_bytes": (ctypes.c_int64, [_MP, ctypes.c_int32, ctypes.c_int32]),
+    "mara_minidisk_clock_init": (ctypes.c_int, [_MP, _vp, ctypes.c_double, _vp, _vp]),
+    "mara_minidisk_advance": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_int32, _vp, _vp]),
+    "mara_minidisk_host_workspace_bytes": (ctypes.c_int64, [_MP, ctypes.c_int32, ctypes.c_int32]),
+    "mara_minidisk_advance_host": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.c_int32, ctypes.c_int32, c_double_p, _vp, _vp]),
+    "mara_minidisk_stage": (ctypes.c_int, [_MP, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32,
+                                           ctypes.c_int32, _vp]),
+    "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.c_int32, _vp]),
+}
+
+
+class MaraError(RuntimeError):
+    pass
+
+
+def load(path: Path = LIB_PATH) -> ctypes.CDLL:
+    if not path.exists():
+        raise ImportError(
+            f"{path.name} is not built: run `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA extension is required; there is no CPU fallback)")
+    lib = ctypes.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = load()
+
+
+def check(status: int, what: str = "") -> None:
+    """Raise MaraError with the library's message on a non-zero status."""
+    if status != 0:
+        msg = lib.mara_last_error().decode(errors="replace")
+        raise MaraError(f"{what or 'mara call'} failed (status {status}): {msg}")

@@ -1,0 +1,1013 @@
+// Locally-isothermal binary-minidisk Godunov update on the GPU.
+//
+// One CTA updates a TX x TY tile of the mesh (x rows slow, y contiguous):
+//   phase 1  load the (TX+4) x (TY+4) halo tile of the stage state (periodic
+//            wrap), recover primitives into shared memory
+//   phase 2  PLM limited slopes along x and y (scheme_plm_gradient.hpp:44-70)
+//   phase 3  HLLE + viscous fluxes on the TX+1 x-face rows and TY+1 y-face
+//            columns (problems/minidisk_scheme.cpp:222-288, physics_iso2d.hpp:156-173)
+//   phase 4  flux divergence + gravity, sink, rotating-frame and buffer
+//            sources, stage update (problems/minidisk_scheme.cpp:294-355),
+//            optionally fused with the RK2 average and the CFL wavespeed
+//            reduction of the new state.
+//
+// Two arithmetic paths share the template:
+//   FP64   (R = double): the drop-in path. Every expression keeps the
+//          reference's evaluation order; only FMA contraction and CUDA's libm
+//          (sqrt/exp/tanh, x^1.5 as x*sqrt(x), x^3 as x*x*x) differ.
+//   MIXED  (R = float): reconstruction, fluxes and sources in FP32; the state
+//          stays FP64 in HBM and is accumulated in FP64. RK2 keeps only the
+//          FP32 stage-1 increment d1 = dt*L(u0) between stages; stage 2 uses
+//          u1 = f32(u0) + d1 for its fluxes and writes u0 + (d1 + d2)/2 in FP64.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include "common.cuh"
+
+namespace mara {
+namespace md {
+
+constexpr int TX = 16, TY = 32, NT = 256;
+constexpr int EX = TX + 4, EY = TY + 4;     // halo tile
+constexpr int GX = TX + 2, GY = TY + 2;     // slope region
+constexpr int NFX = (TX + 1) * TY;          // x faces
+constexpr int NFY = TX * (TY + 1);          // y faces
+
+enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3 };
+
+struct Args
+{
+    int N;                 // cells per side of the mesh (K_BLOCK: block size)
+    int n;                 // block size (zones per block side)
+    int level;             // block level (2^level blocks per side)
+    int tiles_y;
+    uint64_t bi, bj;       // K_BLOCK: block coordinates
+    double R, dl;
+    double rs2;            // softening_length^2 (std::pow(rs, 2.0) on the host)
+    double mach, nu, omega, sink_rate, s6, buffer_rate, buffer_scale, theta;
+    double dt;             // used when clock == nullptr
+    double bin[6];         // m1, x1, y1, m2, x2, y2; used when clock == nullptr
+    const mara_minidisk_clock* clock;
+    int stage;             // which clock->binary row this stage uses
+    const double* u_in;    // FP64/MIX: stage state (FP64) or u0; K_BLOCK: uc AoS
+    const double* u_avg;   // K_FP64: optional RK2 average partner
+    const float* d1;       // K_MIX2: FP32 stage-1 increment
+    double* u_out;         // FP64 result
+    float* d_out;          // K_MIX1 + RK2: increment out
+    const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
+    unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
+};
+
+// ------------------------------------------------------------- geometry
+// vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
+__host__ __device__ inline double vertex(double R, int n, int level, uint64_t b, int k)
+{
+    double dlv = double(1 << level);
+    double x0 = R * (-1 + double(2 * b) / dlv);
+    double x1 = R * (-1 + double(2 * (b + 1)) / dlv);
+    return x0 + (x1 - x0) * double(k) / double(n);
+}
+
+__device__ inline int wrap(int g, int N)
+{
+    g %= N;
+    return g < 0 ? g + N : g;
+}
+
+// ------------------------------------------------------------- PLM
+// Generalised minmod on unit spacing (scheme_plm_gradient.hpp:56-63). The
+// reference's 0.25*|sa+sb|*(sa+sc)*min(|a|,|b|,|c|) equals copysign(min, a)
+// when a, b, c share a sign and zero otherwise; that is what is computed here.
+__device__ inline double plm(double yl, double y0, double yr, double theta)
+{
+    double a = (y0 - yl) * theta;
+    double b = (yr - yl) * 0.5;
+    double c = (yr - y0) * theta;
+    double m = fmin(fmin(fabs(a), fabs(b)), fabs(c));
+    long long sa = __double_as_longlong(a), sb = __double_as_longlong(b), sc = __double_as_longlong(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0 : copysign(m, a);
+}
+
+__device__ inline float plm(float yl, float y0, float yr, float theta)
+{
+    float a = (y0 - yl) * theta;
+    float b = (yr - yl) * 0.5f;
+    float c = (yr - y0) * theta;
+    float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
+    int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
+}
+
+// ------------------------------------------------------------- face flux
+// HLLE flux (physics_iso2d.hpp:156-173) plus viscous stress
+// (problems/minidisk_scheme.cpp:242-281) at one face. pa/pb: left/right cell
+// primitives; ga/gb: their slopes along the face normal; ta/tb: transverse.
+template<int AXIS>
+__device__ inline void face_flux(const double pa[3], const double pb[3], const double ga[3], const double gb[3],
+                                 const double ta[3], const double tb[3], double x, double y,
+                                 const Args& A, double F[3])
+{
+    double L[3], Rr[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        L[k] = pa[k] + 0.5 * ga[k];     // (pc + g/2) of the left cell
+        Rr[k] = pb[k] - 0.5 * gb[k];    // (pc - g/2) of the right cell
+    }
+    // sound_speed_squared at the face (problems/minidisk_scheme.cpp:127-132)
+    double ph = -1.0 / sqrt((x * x + y * y) + A.rs2);
+    double cs2 = -ph / A.mach / A.mach;
+    double cs = sqrt(cs2);
+    double vl = AXIS == 0 ? L[1] : L[2];
+    double vr = AXIS == 0 ? Rr[1] : Rr[2];
+    double ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
+    double ur[3] = {Rr[0], Rr[0] * Rr[1], Rr[0] * Rr[2]};
+    double pgl = L[0] * cs2, pgr = Rr[0] * cs2;
+    double fl[3] = {vl * ul[0], vl * ul[1] + (AXIS == 0 ? pgl : 0.0), vl * ul[2] + (AXIS == 0 ? 0.0 : pgl)};
+    double fr[3] = {vr * ur[0], vr * ur[1] + (AXIS == 0 ? pgr : 0.0), vr * ur[2] + (AXIS == 0 ? 0.0 : pgr)};
+    double ap = fmax(0.0, fmax(vl + cs, vr + cs));
+    double am = fmin(0.0, fmin(vl - cs, vr - cs));
+    for (int k = 0; k < 3; ++k)
+        F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am) / (ap - am);
+
+    if (A.nu != 0.0)
+    {
+        double mu = A.nu * 0.5 * (Rr[0] + L[0]);
+        double vx_long = 0.5 * (ga[1] + gb[1]) / A.dl;
+        double vy_long = 0.5 * (ga[2] + gb[2]) / A.dl;
+        double vx_tran = 0.5 * (ta[1] + tb[1]) / A.dl;
+        double vy_tran = 0.5 * (ta[2] + tb[2]) / A.dl;
+        if (AXIS == 0)
+        {
+            double tauxx = mu * (vx_long - vy_tran);
+            double tauxy = mu * (vy_long + vx_tran);
+            F[1] = F[1] + -tauxx;
+            F[2] = F[2] + -tauxy;
+        }
+        else
+        {
+            double tauyx = mu * (vy_tran + vx_long);
+            double tauyy = -mu * (vx_tran - vy_long);
+            F[1] = F[1] + -tauyx;
+            F[2] = F[2] + -tauyy;
+        }
+    }
+}
+
+template<int AXIS>
+__device__ inline void face_flux(const float pa[3], const float pb[3], const float ga[3], const float gb[3],
+                                 const float ta[3], const float tb[3], float x, float y,
+                                 const Args& A, float F[3])
+{
+    float L[3], Rr[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        L[k] = fmaf(0.5f, ga[k], pa[k]);
+        Rr[k] = fmaf(-0.5f, gb[k], pb[k]);
+    }
+    const float inv_mach2 = float(1.0 / (A.mach * A.mach));
+    float rinv = rsqrtf(fmaf(x, x, fmaf(y, y, float(A.rs2))));
+    float cs2 = rinv * inv_mach2;
+    float cs = sqrtf(cs2);
+    float vl = AXIS == 0 ? L[1] : L[2];
+    float vr = AXIS == 0 ? Rr[1] : Rr[2];
+    float ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
+    float ur[3] = {Rr[0], Rr[0] * Rr[1], Rr[0] * Rr[2]};
+    float pgl = L[0] * cs2, pgr = Rr[0] * cs2;
+    float fl[3] = {vl * ul[0], fmaf(vl, ul[1], AXIS == 0 ? pgl : 0.0f), fmaf(vl, ul[2], AXIS == 0 ? 0.0f : pgl)};
+    float fr[3] = {vr * ur[0], fmaf(vr, ur[1], AXIS == 0 ? pgr : 0.0f), fmaf(vr, ur[2], AXIS == 0 ? 0.0f : pgr)};
+    float ap = fmaxf(0.0f, fmaxf(vl, vr) + cs);
+    float am = fminf(0.0f, fminf(vl, vr) - cs);
+    float inv = __frcp_rn(ap - am);
+    float apam = ap * am;
+    for (int k = 0; k < 3; ++k)
+        F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * apam) * inv;
+
+    if (A.nu != 0.0)
+    {
+        const float half_inv_dl = float(0.5 / A.dl);
+        float mu = float(A.nu * 0.5) * (Rr[0] + L[0]);
+        float vx_long = (ga[1] + gb[1]) * half_inv_dl;
+        float vy_long = (ga[2] + gb[2]) * half_inv_dl;
+        float vx_tran = (ta[1] + tb[1]) * half_inv_dl;
+        float vy_tran = (ta[2] + tb[2]) * half_inv_dl;
+        if (AXIS == 0)
+        {
+            F[1] -= mu * (vx_long - vy_tran);
+            F[2] -= mu * (vy_long + vx_tran);
+        }
+        else
+        {
+            F[1] -= mu * (vy_tran + vx_long);
+            F[2] += mu * (vx_tran - vy_long);
+        }
+    }
+}
+
+// ------------------------------------------------------------- shared layout
+template<typename R>
+struct Smem
+{
+    R p[3][EX][EY];        // primitives of the halo tile
+    R gx[3][GX][GY];       // x slopes of halo-tile cells [1, TX+3) x [1, TY+3)
+    R gy[3][GX][GY];       // y slopes, same cells
+    R fx[3][TX + 1][TY];   // x-face fluxes
+    R fy[3][TX][TY + 1];   // y-face fluxes
+    R xv[TX + 1], xc[TX], yv[TY + 1], yc[TY];
+    double wmax[NT / 32];
+};
+
+template<typename R>
+__device__ inline R to_r(double v) { return R(v); }
+
+// ------------------------------------------------------------- stage kernel
+template<typename R, int KIND>
+__global__ void __launch_bounds__(NT) stage_kernel(const Args A)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<R>& S = *reinterpret_cast<Smem<R>*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int tx = blockIdx.x / A.tiles_y, ty = blockIdx.x % A.tiles_y;
+    const int gx0 = tx * TX, gy0 = ty * TY;
+    const int N = A.N;
+    const size_t NN = size_t(N) * N;
+
+    // coordinates of this tile's vertices and centres, reference formulae in FP64
+    for (int e = tid; e < (TX + 1) + TX + (TY + 1) + TY; e += NT)
+    {
+        int q = e;
+        if (q < TX + 1 + TX)
+        {
+            bool is_center = q > TX;
+            int k = is_center ? q - (TX + 1) : q;
+            int I = gx0 + k;
+            uint64_t b; int kk;
+            if (KIND == K_BLOCK) { b = A.bi; kk = I; }
+            else { b = uint64_t(min(I / A.n, (1 << A.level) - 1)); kk = I - int(b) * A.n; }
+            double v = is_center ? 0.5 * (vertex(A.R, A.n, A.level, b, kk) + vertex(A.R, A.n, A.level, b, kk + 1))
+                                 : vertex(A.R, A.n, A.level, b, kk);
+            if (is_center) S.xc[k] = to_r<R>(v); else S.xv[k] = to_r<R>(v);
+        }
+        else
+        {
+            q -= TX + 1 + TX;
+            bool is_center = q > TY;
+            int k = is_center ? q - (TY + 1) : q;
+            int J = gy0 + k;
+            uint64_t b; int kk;
+            if (KIND == K_BLOCK) { b = A.bj; kk = J; }
+            else { b = uint64_t(min(J / A.n, (1 << A.level) - 1)); kk = J - int(b) * A.n; }
+            double v = is_center ? 0.5 * (vertex(A.R, A.n, A.level, b, kk) + vertex(A.R, A.n, A.level, b, kk + 1))
+                                 : vertex(A.R, A.n, A.level, b, kk);
+            if (is_center) S.yc[k] = to_r<R>(v); else S.yv[k] = to_r<R>(v);
+        }
+    }
+
+    // phase 1: halo tile -> primitives
+    for (int e = tid; e < EX * EY; e += NT)
+    {
+        int ei = e / EY, ej = e - (e / EY) * EY;
+        R p0, p1, p2;
+        if (KIND == K_BLOCK)
+        {
+            int i = min(gx0 + ei, A.n + 3), j = min(gy0 + ej, A.n + 3);
+            const double* q = A.pe + (size_t(i) * (A.n + 4) + j) * 3;
+            p0 = R(q[0]); p1 = R(q[1]); p2 = R(q[2]);
+        }
+        else
+        {
+            size_t idx = size_t(wrap(gx0 + ei - 2, N)) * N + wrap(gy0 + ej - 2, N);
+            double s = __ldg(A.u_in + idx), m1 = __ldg(A.u_in + NN + idx), m2 = __ldg(A.u_in + 2 * NN + idx);
+            if (KIND == K_FP64)
+            {
+                p0 = R(s); p1 = R(m1 / s); p2 = R(m2 / s);
+            }
+            else
+            {
+                float fs = float(s), f1 = float(m1), f2 = float(m2);
+                if (KIND == K_MIX2)
+                {
+                    fs += __ldg(A.d1 + idx); f1 += __ldg(A.d1 + NN + idx); f2 += __ldg(A.d1 + 2 * NN + idx);
+                }
+                float inv = __frcp_rn(fs);
+                p0 = R(fs); p1 = R(f1 * inv); p2 = R(f2 * inv);
+            }
+        }
+        S.p[0][ei][ej] = p0; S.p[1][ei][ej] = p1; S.p[2][ei][ej] = p2;
+    }
+    __syncthreads();
+
+    // phase 2: slopes
+    const R theta = R(A.theta);
+    for (int e = tid; e < GX * GY; e += NT)
+    {
+        int gi = e / GY, gj = e - (e / GY) * GY;
+        for (int k = 0; k < 3; ++k)
+        {
+            S.gx[k][gi][gj] = plm(S.p[k][gi][gj + 1], S.p[k][gi + 1][gj + 1], S.p[k][gi + 2][gj + 1], theta);
+            S.gy[k][gi][gj] = plm(S.p[k][gi + 1][gj], S.p[k][gi + 1][gj + 1], S.p[k][gi + 1][gj + 2], theta);
+        }
+    }
+    __syncthreads();
+
+    // phase 3: face fluxes
+    for (int e = tid; e < NFX + NFY; e += NT)
+    {
+        R pa[3], pb[3], ga[3], gb[3], ta[3], tb[3], F[3];
+        if (e < NFX)
+        {
+            int fi = e / TY, j = e - (e / TY) * TY;
+            // left cell ext (fi+1, j+2) = slope (fi, j+1); right ext (fi+2, j+2) = slope (fi+1, j+1)
+            for (int k = 0; k < 3; ++k)
+            {
+                pa[k] = S.p[k][fi + 1][j + 2]; pb[k] = S.p[k][fi + 2][j + 2];
+                ga[k] = S.gx[k][fi][j + 1];    gb[k] = S.gx[k][fi + 1][j + 1];
+                ta[k] = S.gy[k][fi][j + 1];    tb[k] = S.gy[k][fi + 1][j + 1];
+            }
+            face_flux<0>(pa, pb, ga, gb, ta, tb, S.xv[fi], S.yc[j], A, F);
+            for (int k = 0; k < 3; ++k) S.fx[k][fi][j] = F[k];
+        }
+        else
+        {
+            int q = e - NFX;
+            int i = q / (TY + 1), fj = q - (q / (TY + 1)) * (TY + 1);
+            // left cell ext (i+2, fj+1) = slope (i+1, fj); right ext (i+2, fj+2) = slope (i+1, fj+1)
+            for (int k = 0; k < 3; ++k)
+            {
+                pa[k] = S.p[k][i + 2][fj + 1]; pb[k] = S.p[k][i + 2][fj + 2];
+                ga[k] = S.gy[k][i + 1][fj];    gb[k] = S.gy[k][i + 1][fj + 1];
+                ta[k] = S.gx[k][i + 1][fj];    tb[k] = S.gx[k][i + 1][fj + 1];
+            }
+            face_flux<1>(pa, pb, ga, gb, ta, tb, S.xc[i], S.yv[fj], A, F);
+            for (int k = 0; k < 3; ++k) S.fy[k][i][fj] = F[k];
+        }
+    }
+    __syncthreads();
+
+    // phase 4: divergence, sources, update
+    double dt;
+    double b6[6];
+    if (A.clock)
+    {
+        dt = A.clock->dt;
+        for (int k = 0; k < 6; ++k) b6[k] = A.clock->binary[A.stage][k];
+    }
+    else
+    {
+        dt = A.dt;
+        for (int k = 0; k < 6; ++k) b6[k] = A.bin[k];
+    }
+    double local_max = 0.0;
+    const int cells_x = KIND == K_BLOCK ? A.n : N;
+
+    for (int e = tid; e < TX * TY; e += NT)
+    {
+        int i = e / TY, j = e - (e / TY) * TY;
+        int gi = gx0 + i, gj = gy0 + j;
+        if (gi >= cells_x || gj >= cells_x) continue;
+        R pc[3] = {S.p[0][i + 2][j + 2], S.p[1][i + 2][j + 2], S.p[2][i + 2][j + 2]};
+        R dfx[3], dfy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            dfx[k] = S.fx[k][i + 1][j] - S.fx[k][i][j];
+            dfy[k] = S.fy[k][i][j + 1] - S.fy[k][i][j];
+        }
+
+        if (KIND == K_FP64 || KIND == K_BLOCK)
+        {
+            const double x = S.xc[i], y = S.yc[j];
+            double uc[3];
+            size_t idx = size_t(gi) * N + gj;
+            if (KIND == K_BLOCK)
+                for (int k = 0; k < 3; ++k) uc[k] = A.u_in[(size_t(gi) * A.n + gj) * 3 + k];
+            else
+                for (int k = 0; k < 3; ++k) uc[k] = A.u_in[k * NN + idx];
+
+            // two_body::gravitational_acceleration (physics_two_body.hpp:209-218)
+            double dx1 = x - b6[1], dy1 = y - b6[2];
+            double t1 = (dx1 * dx1 + dy1 * dy1) + A.rs2;
+            double g1 = -1.0 * b6[0] / (t1 * sqrt(t1));
+            double dx2 = x - b6[4], dy2 = y - b6[5];
+            double t2 = (dx2 * dx2 + dy2 * dy2) + A.rs2;
+            double g2 = -1.0 * b6[3] / (t2 * sqrt(t2));
+            double ag1x = g1 * dx1, ag1y = g1 * dy1, ag2x = g2 * dx2, ag2y = g2 * dy2;
+            // sink_rate_field (problems/minidisk_scheme.cpp:57-65)
+            double d1 = 0.0 + dx1 * dx1 + dy1 * dy1;
+            double d2 = 0.0 + dx2 * dx2 + dy2 * dy2;
+            double sr1 = A.sink_rate * exp(-(d1 * d1 * d1) / A.s6);
+            double sr2 = A.sink_rate * exp(-(d2 * d2 * d2) / A.s6);
+            // buffer_rate_field (problems/minidisk_scheme.cpp:47-55)
+            double rr = sqrt(0.0 + x * x + y * y);
+            double br = 0.5 * A.buffer_rate * (1.0 + tanh((rr - A.R) / A.buffer_scale));
+            // initial_primitive -> conserved (problems/minidisk_scheme.cpp:87-99)
+            double ph = -1.0 / sqrt((x * x + y * y) + A.rs2);
+            double r0 = sqrt(x * x + y * y);
+            double vp = sqrt(-ph) - A.omega * r0;
+            double ui[3] = {1.0, 1.0 * (vp * (-y / r0)), 1.0 * (vp * (x / r0))};
+            // coriolis_term / centrifugal_term (problems/minidisk_scheme.cpp:67-76)
+            double sig = pc[0];
+            double corx = 2.0 * A.omega * double(pc[2]);
+            double cory = 2.0 * A.omega * -double(pc[1]);
+            double cenx = A.omega * A.omega * x;
+            double ceny = A.omega * A.omega * y;
+            double sg1[3] = {0.0, sig * ag1x, sig * ag1y};
+            double sg2[3] = {0.0, sig * ag2x, sig * ag2y};
+            double sf1[3] = {0.0, sig * cenx, sig * ceny};
+            double sf2[3] = {0.0, sig * corx, sig * cory};
+            double out[3];
+            for (int k = 0; k < 3; ++k)
+            {
+                double ss1 = -uc[k] * sr1;
+                double ss2 = -uc[k] * sr2;
+                double sb = -(uc[k] - ui[k]) * br;
+                double u1 = uc[k] - (double(dfx[k]) + double(dfy[k])) * dt / A.dl
+                          + (sg1[k] + sg2[k] + ss1 + ss2 + sf1[k] + sf2[k] + sb) * dt;
+                out[k] = u1;
+            }
+            if (KIND == K_BLOCK)
+            {
+                for (int k = 0; k < 3; ++k) A.u_out[(size_t(gi) * A.n + gj) * 3 + k] = out[k];
+            }
+            else
+            {
+                if (A.u_avg)
+                    for (int k = 0; k < 3; ++k) out[k] = A.u_avg[k * NN + idx] * 0.5 + out[k] * (1.0 - 0.5);
+                for (int k = 0; k < 3; ++k) A.u_out[k * NN + idx] = out[k];
+                if (A.amax)
+                {
+                    // iso2d::fastest_wavespeed at the cell-centre sound speed
+                    double cs = sqrt(-(-1.0 / sqrt((x * x + y * y) + A.rs2)) / A.mach / A.mach);
+                    double vx = out[1] / out[0], vy = out[2] / out[0];
+                    double a = fmax(fmax(fabs(vx - cs), fabs(vx + cs)), fmax(fabs(vy - cs), fabs(vy + cs)));
+                    local_max = fmax(local_max, a);
+                }
+            }
+        }
+        else
+        {
+            const float x = float(S.xc[i]), y = float(S.yc[j]);
+            const float rs2 = float(A.rs2);
+            const float om = float(A.omega);
+            size_t idx = size_t(gi) * N + gj;
+            float uc[3] = {float(pc[0]), float(pc[0]) * float(pc[1]), float(pc[0]) * float(pc[2])};
+            float dx1 = x - float(b6[1]), dy1 = y - float(b6[2]);
+            float dx2 = x - float(b6[4]), dy2 = y - float(b6[5]);
+            float q1 = fmaf(dx1, dx1, dy1 * dy1), q2 = fmaf(dx2, dx2, dy2 * dy2);
+            float i1 = rsqrtf(q1 + rs2), i2 = rsqrtf(q2 + rs2);
+            float g1 = -float(b6[0]) * i1 * i1 * i1;
+            float g2 = -float(b6[3]) * i2 * i2 * i2;
+            const float inv_s6 = float(1.0 / A.s6);
+            float sr1 = float(A.sink_rate) * __expf(-(q1 * q1 * q1) * inv_s6);
+            float sr2 = float(A.sink_rate) * __expf(-(q2 * q2 * q2) * inv_s6);
+            float r2 = fmaf(x, x, y * y);
+            float rinv = rsqrtf(r2);
+            float rr = r2 * rinv;
+            // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
+            float br = float(A.buffer_rate) * __frcp_rn(1.0f + __expf(-2.0f * (rr - float(A.R)) * float(1.0 / A.buffer_scale)));
+            float vp = sqrtf(rsqrtf(r2 + rs2)) - om * rr;
+            float ui[3] = {1.0f, -vp * y * rinv, vp * x * rinv};
+            float sig = pc[0];
+            float ax = g1 * dx1 + g2 * dx2 + om * om * x + 2.0f * om * float(pc[2]);
+            float ay = g1 * dy1 + g2 * dy2 + om * om * y - 2.0f * om * float(pc[1]);
+            float src[3];
+            for (int k = 0; k < 3; ++k) src[k] = -(uc[k] * (sr1 + sr2)) - (uc[k] - ui[k]) * br;
+            src[1] = fmaf(sig, ax, src[1]);
+            src[2] = fmaf(sig, ay, src[2]);
+            const float dtf = float(dt);
+            const float inv_dl = float(1.0 / A.dl);
+            float du[3];
+            for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (float(dfx[k]) + float(dfy[k])) * inv_dl);
+
+            double out[3];
+            if (KIND == K_MIX1 && A.d_out)
+            {
+                for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
+            }
+            else
+            {
+                for (int k = 0; k < 3; ++k)
+                {
+                    float inc = KIND == K_MIX2 ? 0.5f * (__ldg(A.d1 + k * NN + idx) + du[k]) : du[k];
+                    out[k] = __ldg(A.u_in + k * NN + idx) + double(inc);
+                    A.u_out[k * NN + idx] = out[k];
+                }
+                if (A.amax)
+                {
+                    float fs = float(out[0]);
+                    float inv = __frcp_rn(fs);
+                    float vx = float(out[1]) * inv, vy = float(out[2]) * inv;
+                    float cs = sqrtf(rsqrtf(r2 + rs2) * float(1.0 / (A.mach * A.mach)));
+                    float a = fmaxf(fabsf(vx) + cs, fabsf(vy) + cs);
+                    local_max = fmax(local_max, double(a));
+                }
+            }
+        }
+    }
+
+    if (A.amax)
+    {
+        for (int o = 16; o > 0; o >>= 1) local_max = fmax(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+        if ((tid & 31) == 0) S.wmax[tid >> 5] = local_max;
+        __syncthreads();
+        if (tid == 0)
+        {
+            double m = 0.0;
+            for (int w = 0; w < NT / 32; ++w) m = fmax(m, S.wmax[w]);
+            atomicMax(A.amax, (unsigned long long)__double_as_longlong(m));
+        }
+    }
+}
+
+// ------------------------------------------------------------- clock kernel
+struct ClockArgs
+{
+    double R, dl, cfl, softening_length, mass_ratio, eccentricity, omega;
+    int dt_mode, rk_order;
+    int end_step;     // 1: finish the step that just ran (advance time, iteration)
+    int begin_step;   // 1: choose dt and stage binaries of the next step
+};
+
+__device__ inline void store_binary(double* dst, const Binary& b)
+{
+    dst[0] = b.m1; dst[1] = b.x1; dst[2] = b.y1; dst[3] = b.m2; dst[4] = b.x2; dst[5] = b.y2;
+}
+
+__global__ void clock_kernel(mara_minidisk_clock* c, const ClockArgs a)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (a.end_step)
+    {
+        double t = c->time, dt = c->dt;
+        if (a.rk_order == 2)
+        {
+            double t2 = (t + dt) + dt;
+            c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
+        }
+        else
+        {
+            c->time = t + dt;
+        }
+        c->iteration += 1;
+    }
+    if (a.begin_step)
+    {
+        double t = c->time, dt;
+        if (a.dt_mode == MARA_DT_FORMULA)
+        {
+            // problems/minidisk.cpp:204-206
+            double vmax = sqrt(1.0 * 0.5 / a.softening_length);
+            double cfl = a.cfl * fmin(1.0, 0.01 + t / 0.05);
+            dt = a.dl / vmax * cfl;
+        }
+        else
+        {
+            dt = a.cfl * a.dl / c->max_wavespeed;   // scheme_mhd_v1.cpp:287 form
+        }
+        c->dt = dt;
+        store_binary(c->binary[0], binary_state(a.mass_ratio, a.eccentricity, a.omega, t));
+        store_binary(c->binary[1], binary_state(a.mass_ratio, a.eccentricity, a.omega, t + dt));
+        c->max_wavespeed = 0.0;
+    }
+}
+
+// ------------------------------------------------------------- small kernels
+__global__ void initial_kernel(int N, int n, int level, double R, double rs2, double omega,
+                               uint64_t seed, double amplitude, double* u)
+{
+    size_t NN = size_t(N) * N;
+    for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
+    {
+        int i = int(c / N), j = int(c % N);
+        uint64_t bi = uint64_t(i / n), bj = uint64_t(j / n);
+        int ki = i - int(bi) * n, kj = j - int(bj) * n;
+        double x = 0.5 * (vertex(R, n, level, bi, ki) + vertex(R, n, level, bi, ki + 1));
+        double y = 0.5 * (vertex(R, n, level, bj, kj) + vertex(R, n, level, bj, kj + 1));
+        double ph = -1.0 / sqrt((x * x + y * y) + rs2);
+        double r0 = sqrt(x * x + y * y);
+        double vp = sqrt(-ph) - omega * r0;
+        double vx = vp * (-y / r0);
+        double vy = vp * (x / r0);
+        double sig = 1.0;
+        if (amplitude != 0.0)
+        {
+            uint64_t z = seed + (uint64_t(c) + 1) * 0x9E3779B97F4A7C15ull;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            double r = 2.0 * (double(z >> 11) * 0x1.0p-53) - 1.0;
+            sig = sig * (1.0 + amplitude * r);
+        }
+        u[c] = sig;
+        u[NN + c] = sig * vx;
+        u[2 * NN + c] = sig * vy;
+    }
+}
+
+// Fastest wavespeed of a state (for the first CFL step).
+__global__ void wavespeed_kernel(int N, int n, int level, double R, double rs2, double mach,
+                                 const double* u, unsigned long long* amax)
+{
+    __shared__ double wm[NT / 32];
+    size_t NN = size_t(N) * N;
+    double m = 0.0;
+    for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
+    {
+        int i = int(c / N), j = int(c % N);
+        uint64_t bi = uint64_t(i / n), bj = uint64_t(j / n);
+        int ki = i - int(bi) * n, kj = j - int(bj) * n;
+        double x = 0.5 * (vertex(R, n, level, bi, ki) + vertex(R, n, level, bi, ki + 1));
+        double y = 0.5 * (vertex(R, n, level, bj, kj) + vertex(R, n, level, bj, kj + 1));
+        double cs = sqrt(-(-1.0 / sqrt((x * x + y * y) + rs2)) / mach / mach);
+        double vx = u[NN + c] / u[c], vy = u[2 * NN + c] / u[c];
+        m = fmax(m, fmax(fmax(fabs(vx - cs), fabs(vx + cs)), fmax(fabs(vy - cs), fabs(vy + cs))));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double r = 0.0;
+        for (int w = 0; w < int(blockDim.x / 32); ++w) r = fmax(r, wm[w]);
+        atomicMax(amax, (unsigned long long)__double_as_longlong(r));
+    }
+}
+
+__global__ void recover_primitive_kernel(const double* u, int64_t count, double* p)
+{
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < count; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        double s = u[3 * c], m1 = u[3 * c + 1], m2 = u[3 * c + 2];
+        p[3 * c] = s; p[3 * c + 1] = m1 / s; p[3 * c + 2] = m2 / s;
+    }
+}
+
+__global__ void gradient_kernel(const double* pc, int64_t n0, int64_t n1, int axis, double theta, double* out)
+{
+    const int64_t m0 = axis == 0 ? n0 - 2 : n0, m1 = axis == 0 ? n1 : n1 - 2;
+    const int64_t di = axis == 0 ? 1 : 0, dj = axis == 0 ? 0 : 1;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < m0 * m1 * 3; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        int64_t k = c % 3, cell = c / 3, i = cell / m1, j = cell % m1;
+        double yl = pc[(i * n1 + j) * 3 + k];
+        double y0 = pc[((i + di) * n1 + j + dj) * 3 + k];
+        double yr = pc[((i + 2 * di) * n1 + j + 2 * dj) * 3 + k];
+        out[c] = plm(yl, y0, yr, theta);
+    }
+}
+
+// ------------------------------------------------------------- host helpers
+int check_params(const mara_minidisk_params* sd)
+{
+    MARA_REQUIRE(sd != nullptr, "minidisk: params is null");
+    MARA_REQUIRE(sd->block_size >= 1 && sd->block_size <= (1 << 16), "minidisk: block_size out of range");
+    MARA_REQUIRE(sd->depth >= 0 && sd->depth <= 12, "minidisk: depth out of range");
+    MARA_REQUIRE(int64_t(sd->block_size) << sd->depth <= 65536, "minidisk: mesh wider than 65536 cells");
+    MARA_REQUIRE(sd->mach_number > 0.0, "minidisk: mach_number must be positive");
+    MARA_REQUIRE(sd->buffer_scale > 0.0, "minidisk: buffer_scale must be positive");
+    MARA_REQUIRE(sd->mass_ratio > 0.0, "minidisk: mass_ratio must be positive");
+    MARA_REQUIRE(sd->eccentricity >= 0.0 && sd->eccentricity < 1.0, "minidisk: eccentricity must be in [0, 1)");
+    return MARA_OK;
+}
+
+inline double cell_size(const mara_minidisk_params* sd, int level)
+{
+    return 2.0 * sd->domain_radius / double(sd->block_size) / double(1 << level);
+}
+
+Args base_args(const mara_minidisk_params* sd)
+{
+    Args A;
+    std::memset(&A, 0, sizeof A);
+    A.n = sd->block_size;
+    A.level = sd->depth;
+    A.N = sd->block_size << sd->depth;
+    A.R = sd->domain_radius;
+    A.dl = cell_size(sd, sd->depth);
+    A.rs2 = std::pow(sd->softening_length, 2.0);
+    A.mach = sd->mach_number;
+    A.nu = sd->nu;
+    A.omega = sd->omega_frame;
+    A.sink_rate = sd->sink_rate;
+    A.s6 = std::pow(sd->sink_radius, 6.0);
+    A.buffer_rate = sd->buffer_rate;
+    A.buffer_scale = sd->buffer_scale;
+    A.theta = sd->plm_theta;
+    return A;
+}
+
+void set_binary(Args& A, const mara_minidisk_params* sd, double t)
+{
+    Binary b = binary_state(sd->mass_ratio, sd->eccentricity, sd->omega_frame, t);
+    double v[6] = {b.m1, b.x1, b.y1, b.m2, b.x2, b.y2};
+    std::memcpy(A.bin, v, sizeof v);
+}
+
+template<typename R, int KIND>
+int launch_stage(const Args& A, int tiles, cudaStream_t s)
+{
+    static std::once_flag flags[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::call_once(flags[dev & 63], [] {
+        cudaFuncSetAttribute(stage_kernel<R, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(Smem<R>)));
+    });
+    stage_kernel<R, KIND><<<tiles, NT, sizeof(Smem<R>), s>>>(A);
+    return launch_status("minidisk stage kernel");
+}
+
+int grid_stage(Args A, int kind, cudaStream_t s)
+{
+    int tiles_x = (A.N + TX - 1) / TX;
+    A.tiles_y = (A.N + TY - 1) / TY;
+    int tiles = tiles_x * A.tiles_y;
+    switch (kind)
+    {
+        case K_FP64: return launch_stage<double, K_FP64>(A, tiles, s);
+        case K_MIX1: return launch_stage<float, K_MIX1>(A, tiles, s);
+        case K_MIX2: return launch_stage<float, K_MIX2>(A, tiles, s);
+    }
+    return fail(MARA_ERR_ARGUMENT, "minidisk: bad stage kind");
+}
+
+int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
+               int end_step, int begin_step, cudaStream_t s)
+{
+    ClockArgs a;
+    a.R = sd->domain_radius;
+    a.dl = cell_size(sd, sd->depth);
+    a.cfl = sd->cfl;
+    a.softening_length = sd->softening_length;
+    a.mass_ratio = sd->mass_ratio;
+    a.eccentricity = sd->eccentricity;
+    a.omega = sd->omega_frame;
+    a.dt_mode = dt_mode;
+    a.rk_order = rk_order;
+    a.end_step = end_step;
+    a.begin_step = begin_step;
+    clock_kernel<<<1, 32, 0, s>>>(clock, a);
+    return launch_status("minidisk clock kernel");
+}
+
+} // namespace md
+} // namespace mara
+
+using namespace mara;
+using namespace mara::md;
+
+extern "C" {
+
+int mara_minidisk_binary(const mara_minidisk_params* sd, double time, double* out)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(out != nullptr, "mara_minidisk_binary: out is null");
+    Binary b = binary_state(sd->mass_ratio, sd->eccentricity, sd->omega_frame, time);
+    double v[10] = {b.m1, b.x1, b.y1, b.vx1, b.vy1, b.m2, b.x2, b.y2, b.vx2, b.vy2};
+    std::memcpy(out, v, sizeof v);
+    return MARA_OK;
+}
+
+int mara_minidisk_dt_formula(const mara_minidisk_params* sd, double time, double* dt)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(dt != nullptr, "mara_minidisk_dt_formula: dt is null");
+    double dx = 2.0 * sd->domain_radius / double(sd->block_size) / double(1 << sd->depth);
+    double vmax = std::sqrt(1.0 * 0.5 / sd->softening_length);
+    double cfl = sd->cfl * std::min(1.0, 0.01 + time / 0.05);
+    *dt = dx / vmax * cfl;
+    return MARA_OK;
+}
+
+int mara_minidisk_updated_conserved(const mara_minidisk_params* sd, const double* uc, const double* pe,
+                                    double time, double dt, uint32_t level, uint64_t bi, uint64_t bj,
+                                    double* u1, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(uc && pe && u1, "mara_minidisk_updated_conserved: null buffer");
+    MARA_REQUIRE(level <= 30 && bi < (uint64_t(1) << level) && bj < (uint64_t(1) << level),
+                 "mara_minidisk_updated_conserved: block index outside its level");
+    Args A = base_args(sd);
+    A.level = int(level);
+    A.N = sd->block_size;
+    A.dl = cell_size(sd, int(level));
+    A.bi = bi;
+    A.bj = bj;
+    A.dt = dt;
+    set_binary(A, sd, time);
+    A.u_in = uc;
+    A.pe = pe;
+    A.u_out = u1;
+    int tiles_x = (A.n + TX - 1) / TX;
+    A.tiles_y = (A.n + TY - 1) / TY;
+    return launch_stage<double, K_BLOCK>(A, tiles_x * A.tiles_y, as_stream(stream));
+}
+
+int mara_minidisk_recover_primitive(const double* u, int64_t count, double* p, void* stream)
+{
+    MARA_REQUIRE(count >= 0, "mara_minidisk_recover_primitive: negative count");
+    if (count == 0) return MARA_OK;
+    MARA_REQUIRE(u && p, "mara_minidisk_recover_primitive: null buffer");
+    int blocks = int(std::min<int64_t>((count + 255) / 256, 152 * 16));
+    recover_primitive_kernel<<<blocks, 256, 0, as_stream(stream)>>>(u, count, p);
+    return launch_status("recover_primitive_kernel");
+}
+
+int mara_minidisk_estimate_gradient(const double* pc, int64_t n0, int64_t n1, int32_t axis, double theta,
+                                    double* out, void* stream)
+{
+    MARA_REQUIRE(axis == 0 || axis == 1, "mara_minidisk_estimate_gradient: axis must be 0 or 1");
+    MARA_REQUIRE((axis == 0 ? n0 : n1) >= 2 && n0 >= 0 && n1 >= 0, "mara_minidisk_estimate_gradient: array too small");
+    int64_t total = (axis == 0 ? (n0 - 2) * n1 : n0 * (n1 - 2)) * 3;
+    if (total == 0) return MARA_OK;
+    MARA_REQUIRE(pc && out, "mara_minidisk_estimate_gradient: null buffer");
+    int blocks = int(std::min<int64_t>((total + 255) / 256, 152 * 16));
+    gradient_kernel<<<blocks, 256, 0, as_stream(stream)>>>(pc, n0, n1, axis, theta, out);
+    return launch_status("gradient_kernel");
+}
+
+int mara_minidisk_substep(const mara_minidisk_params* sd, const double* u_in, const double* u_avg, double* u_out,
+                          double time, double dt, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u_in && u_out, "mara_minidisk_substep: null buffer");
+    MARA_REQUIRE(u_in != u_out, "mara_minidisk_substep: u_out must not alias u_in");
+    Args A = base_args(sd);
+    A.dt = dt;
+    set_binary(A, sd, time);
+    A.u_in = u_in;
+    A.u_avg = u_avg;
+    A.u_out = u_out;
+    return grid_stage(A, K_FP64, as_stream(stream));
+}
+
+int mara_minidisk_initial_conserved(const mara_minidisk_params* sd, uint64_t seed, double amplitude,
+                                    double* u, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u != nullptr, "mara_minidisk_initial_conserved: u is null");
+    int N = sd->block_size << sd->depth;
+    int64_t NN = int64_t(N) * N;
+    int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 32));
+    initial_kernel<<<blocks, 256, 0, as_stream(stream)>>>(N, sd->block_size, sd->depth, sd->domain_radius,
+        std::pow(sd->softening_length, 2.0), sd->omega_frame, seed, amplitude, u);
+    return launch_status("initial_kernel");
+}
+
+int64_t mara_minidisk_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision)
+{
+    if (check_params(sd)) return -1;
+    int64_t NN = int64_t(sd->block_size << sd->depth) * (sd->block_size << sd->depth);
+    int64_t state = 3 * NN * int64_t(sizeof(double));
+    if (precision == MARA_MIXED && rk_order == 2) return state + 3 * NN * int64_t(sizeof(float));
+    return state;
+}
+
+int mara_minidisk_clock_init(const mara_minidisk_params* sd, const double* u, double time,
+                             mara_minidisk_clock* clock, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u && clock, "mara_minidisk_clock_init: null buffer");
+    cudaStream_t s = as_stream(stream);
+    mara_minidisk_clock c;
+    std::memset(&c, 0, sizeof c);
+    c.time = time;
+    // The host value lives on this stack frame: copy synchronously w.r.t. the host.
+    MARA_CUDA(cudaMemcpyAsync(clock, &c, sizeof c, cudaMemcpyHostToDevice, s));
+    MARA_CUDA(cudaStreamSynchronize(s));
+    int N = sd->block_size << sd->depth;
+    int64_t NN = int64_t(N) * N;
+    int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
+    wavespeed_kernel<<<blocks, NT, 0, s>>>(N, sd->block_size, sd->depth, sd->domain_radius,
+        std::pow(sd->softening_length, 2.0), sd->mach_number, u,
+        reinterpret_cast<unsigned long long*>(&clock->max_wavespeed));
+    return launch_status("wavespeed_kernel");
+}
+
+int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                          int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                          void* workspace, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u && clock && workspace, "mara_minidisk_advance: null buffer");
+    MARA_REQUIRE(steps >= 0, "mara_minidisk_advance: negative step count");
+    MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_minidisk_advance: rk_order must be 1 or 2");
+    MARA_REQUIRE(precision == MARA_FP64 || precision == MARA_MIXED, "mara_minidisk_advance: bad precision");
+    MARA_REQUIRE(dt_mode == MARA_DT_FORMULA || dt_mode == MARA_DT_CFL, "mara_minidisk_advance: bad dt_mode");
+    if (steps == 0) return MARA_OK;
+    cudaStream_t s = as_stream(stream);
+    const int N = sd->block_size << sd->depth;
+    const size_t NN = size_t(N) * N;
+    double* ws_state = static_cast<double*>(workspace);
+    float* ws_d1 = reinterpret_cast<float*>(ws_state + 3 * NN);
+    unsigned long long* amax = dt_mode == MARA_DT_CFL ? reinterpret_cast<unsigned long long*>(&clock->max_wavespeed) : nullptr;
+
+    Args A = base_args(sd);
+    A.clock = clock;
+    double* cur = u;
+    double* alt = ws_state;
+
+    if (int r = clock_step(sd, clock, dt_mode, rk_order, 0, 1, s)) return r;
+    for (int step = 0; step < steps; ++step)
+    {
+        if (precision == MARA_FP64 && rk_order == 2)
+        {
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = ws_state;
+            if (int r = grid_stage(a1, K_FP64, s)) return r;
+            Args a2 = A; a2.stage = 1; a2.u_in = ws_state; a2.u_avg = cur; a2.u_out = cur; a2.amax = amax;
+            if (int r = grid_stage(a2, K_FP64, s)) return r;
+        }
+        else if (precision == MARA_FP64)
+        {
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax;
+            if (int r = grid_stage(a1, K_FP64, s)) return r;
+            std::swap(cur, alt);
+        }
+        else if (rk_order == 2)
+        {
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1;
+            if (int r = grid_stage(a1, K_MIX1, s)) return r;
+            Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = alt; a2.amax = amax;
+            if (int r = grid_stage(a2, K_MIX2, s)) return r;
+            std::swap(cur, alt);
+        }
+        else
+        {
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax;
+            if (int r = grid_stage(a1, K_MIX1, s)) return r;
+            std::swap(cur, alt);
+        }
+        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s)) return r;
+    }
+    if (cur != u)
+        MARA_CUDA(cudaMemcpyAsync(u, cur, 3 * NN * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return MARA_OK;
+}
+
+int64_t mara_minidisk_host_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision)
+{
+    int64_t ws = mara_minidisk_workspace_bytes(sd, rk_order, precision);
+    if (ws < 0) return ws;
+    int64_t NN = int64_t(sd->block_size << sd->depth) * (sd->block_size << sd->depth);
+    return ws + 3 * NN * int64_t(sizeof(double)) + 256;
+}
+
+int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_in, double* u_out, double time,
+                               int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                               double* time_out, void* workspace, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u_in && u_out && workspace, "mara_minidisk_advance_host: null buffer");
+    cudaStream_t s = as_stream(stream);
+    const int N = sd->block_size << sd->depth;
+    const size_t bytes = 3 * size_t(N) * N * sizeof(double);
+    char* base = static_cast<char*>(workspace);
+    double* u = reinterpret_cast<double*>(base);
+    auto* clock = reinterpret_cast<mara_minidisk_clock*>(base + bytes);
+    void* ws = base + bytes + 256;
+    MARA_CUDA(cudaMemcpyAsync(u, u_in, bytes, cudaMemcpyHostToDevice, s));
+    if (int r = mara_minidisk_clock_init(sd, u, time, clock, stream)) return r;
+    if (int r = mara_minidisk_advance(sd, u, clock, steps, rk_order, precision, dt_mode, ws, stream)) return r;
+    MARA_CUDA(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToHost, s));
+    mara_minidisk_clock c;
+    MARA_CUDA(cudaMemcpyAsync(&c, clock, sizeof c, cudaMemcpyDeviceToHost, s));
+    MARA_CUDA(cudaStreamSynchronize(s));
+    if (time_out) *time_out = c.time;
+    return MARA_OK;
+}
+
+int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const double* u_in, const float* d1,
+                        const double* u_avg, double* u_out, float* d_out, mara_minidisk_clock* clock,
+                        int32_t stage, int32_t reduce_wavespeed, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(kind >= 0 && kind <= 2, "mara_minidisk_stage: kind must be 0, 1 or 2");
+    MARA_REQUIRE(stage == 0 || stage == 1, "mara_minidisk_stage: stage must be 0 or 1");
+    MARA_REQUIRE(u_in && clock, "mara_minidisk_stage: null buffer");
+    MARA_REQUIRE(kind != 2 || (d1 && u_out), "mara_minidisk_stage: kind 2 needs d1 and u_out");
+    MARA_REQUIRE(kind != 1 || d_out || u_out, "mara_minidisk_stage: kind 1 needs d_out or u_out");
+    MARA_REQUIRE(kind != 0 || u_out, "mara_minidisk_stage: kind 0 needs u_out");
+    MARA_REQUIRE(u_out != u_in, "mara_minidisk_stage: u_out must not alias u_in");
+    Args A = base_args(sd);
+    A.clock = clock;
+    A.stage = stage;
+    A.u_in = u_in;
+    A.d1 = d1;
+    A.u_avg = kind == 0 ? u_avg : nullptr;
+    A.u_out = u_out;
+    A.d_out = kind == 1 ? d_out : nullptr;
+    bool writes_state = !(kind == 1 && d_out);
+    A.amax = reduce_wavespeed && writes_state ? reinterpret_cast<unsigned long long*>(&clock->max_wavespeed) : nullptr;
+    return grid_stage(A, kind == 0 ? K_FP64 : (kind == 1 ? K_MIX1 : K_MIX2), as_stream(stream));
+}
+
+int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int32_t dt_mode,
+                               int32_t rk_order, int32_t end_step, int32_t begin_step, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(clock != nullptr, "mara_minidisk_clock_update: clock is null");
+    MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_minidisk_clock_update: rk_order must be 1 or 2");
+    MARA_REQUIRE(dt_mode == MARA_DT_FORMULA || dt_mode == MARA_DT_CFL, "mara_minidisk_clock_update: bad dt_mode");
+    return clock_step(sd, clock, dt_mode, rk_order, end_step != 0, begin_step != 0, as_stream(stream));
+}
+
+} // extern "C"

@@ -1,0 +1,248 @@
+// ORACLE — test infrastructure only (see oracle_common.hpp).
+//
+// C entry points around the reference's OWN compiled scheme and physics code.
+// This file is compiled together with the reference's sources (read in place
+// from the reference checkout by oracle/Makefile) into oracle/_ref/libref.so.
+// It exists to pin the oracle restatement and to produce golden fixtures; it
+// contains only marshalling between flat double buffers and the reference's
+// nd::shared_array / numeric::tuple_t types, plus the reference's driver loop
+// restated where the original translation unit cannot be built here
+// (problems/minidisk.cpp needs HDF5 and MPI).
+#include <cstdint>
+#include <cstring>
+#include <utility>
+#include <vector>
+#include "minidisk.hpp"
+#include "parallel_thread_pool.hpp"
+#include "physics_srhd.hpp"
+#include "physics_two_body.hpp"
+#include "scheme_plm_gradient.hpp"
+
+namespace {
+
+template<typename Tuple, std::size_t... I>
+void load_tuple(Tuple& t, const double* src, std::index_sequence<I...>)
+{
+    ((std::get<I>(t.impl).value = src[I]), ...);
+}
+
+template<typename Tuple, std::size_t... I>
+void store_tuple(const Tuple& t, double* dst, std::index_sequence<I...>)
+{
+    ((dst[I] = std::get<I>(t.impl).value), ...);
+}
+
+template<typename Tuple>
+constexpr std::size_t tuple_size_v = std::tuple_size_v<decltype(Tuple().impl)>;
+
+template<typename Tuple>
+Tuple to_tuple(const double* src)
+{
+    Tuple t;
+    load_tuple(t, src, std::make_index_sequence<tuple_size_v<Tuple>>());
+    return t;
+}
+
+template<typename Tuple>
+void from_tuple(const Tuple& t, double* dst)
+{
+    store_tuple(t, dst, std::make_index_sequence<tuple_size_v<Tuple>>());
+}
+
+template<typename Tuple>
+nd::shared_array<Tuple, 2> make_array2(const double* data, std::size_t n0, std::size_t n1)
+{
+    constexpr auto K = tuple_size_v<Tuple>;
+    auto a = nd::make_unique_array<Tuple, 2>(nd::uivec(n0, n1));
+    for (std::size_t i = 0; i < n0; ++i)
+        for (std::size_t j = 0; j < n1; ++j)
+            a(i, j) = to_tuple<Tuple>(data + (i * n1 + j) * K);
+    return nd::make_shared_array(std::move(a));
+}
+
+template<typename Tuple>
+void read_array2(const nd::shared_array<Tuple, 2>& a, double* out)
+{
+    constexpr auto K = tuple_size_v<Tuple>;
+    auto n0 = shape(a, 0), n1 = shape(a, 1);
+    for (std::size_t i = 0; i < n0; ++i)
+        for (std::size_t j = 0; j < n1; ++j)
+            from_tuple(a(i, j), out + (i * n1 + j) * K);
+}
+
+minidisk::solver_data_t solver_data(const double* v)
+{
+    // v = {block_size, depth, omega_frame, mach_number, nu, domain_radius,
+    //      softening_length, eccentricity, mass_ratio, sink_radius, sink_rate,
+    //      buffer_rate, buffer_scale, cfl}
+    return minidisk::solver_data_t{
+        int(v[0]), int(v[1]), v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12], v[13]};
+}
+
+mesh::block_index_t<2> block_index(unsigned long level, unsigned long bi, unsigned long bj)
+{
+    return mesh::block_index_t<2>{level, numeric::array(bi, bj)};
+}
+
+} // namespace
+
+extern "C" {
+
+// minidisk::updated_conserved on one block (problems/minidisk_scheme.cpp:294).
+int ref_minidisk_updated_conserved(const double* sdv, const double* uc, const double* pe,
+                                   double time, double dt, uint32_t level, uint64_t bi, uint64_t bj, double* u1)
+{
+    try {
+        auto sd = solver_data(sdv);
+        auto n = std::size_t(sd.block_size);
+        auto ua = make_array2<iso2d::conserved_density_t>(uc, n, n);
+        auto pa = make_array2<iso2d::primitive_t>(pe, n + 4, n + 4);
+        auto r = minidisk::updated_conserved(ua, pa, time, dt, block_index(level, bi, bj), sd);
+        read_array2(r, u1);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// minidisk::estimate_gradient (problems/minidisk_scheme.cpp:213) on an AoS
+// primitive array of shape (n0, n1).
+int ref_minidisk_estimate_gradient(const double* pc, uint64_t n0, uint64_t n1, uint32_t axis, double theta, double* out)
+{
+    auto pa = make_array2<iso2d::primitive_t>(pc, n0, n1);
+    read_array2(minidisk::estimate_gradient(pa, axis, theta), out);
+    return 0;
+}
+
+// One forward-Euler substep over a periodic uniform mesh of depth `depth`,
+// SoA [3][N][N] in and out, one mara::ThreadPool task per block per phase,
+// in the shape of problems/minidisk.cpp:172-189 (recover_primitive_array per
+// block, extend from the 3x3 neighbours, updated_conserved per block).
+int ref_minidisk_substep(const double* sdv, const double* u, double* out, double t, double dt, int32_t threads)
+{
+    auto sd = solver_data(sdv);
+    const std::size_t n = sd.block_size, nb = std::size_t(1) << sd.depth, N = n * nb;
+    auto pool = mara::ThreadPool(threads < 1 ? 1 : threads);
+
+    std::vector<minidisk::primitive_array_t> pc(nb * nb);
+    std::vector<minidisk::conserved_array_t> uc(nb * nb);
+    {
+        std::vector<std::future<int>> fut;
+        for (std::size_t b = 0; b < nb * nb; ++b)
+        {
+            fut.push_back(pool.enqueue(0, [&, b] {
+                std::size_t bi = b / nb, bj = b % nb;
+                std::vector<double> buf(n * n * 3);
+                for (std::size_t i = 0; i < n; ++i)
+                    for (std::size_t j = 0; j < n; ++j)
+                        for (int k = 0; k < 3; ++k)
+                            buf[(i * n + j) * 3 + k] = u[(k * N + bi * n + i) * N + bj * n + j];
+                uc[b] = make_array2<iso2d::conserved_density_t>(buf.data(), n, n);
+                pc[b] = minidisk::recover_primitive_array(uc[b]);
+                return 0;
+            }));
+        }
+        for (auto& f : fut) f.get();
+    }
+    std::vector<std::future<int>> fut;
+    for (std::size_t b = 0; b < nb * nb; ++b)
+    {
+        fut.push_back(pool.enqueue(0, [&, b] {
+            std::size_t bi = b / nb, bj = b % nb;
+            // extend (problems/minidisk.cpp:87-120): halo 2 from the 3x3 neighbours, periodic
+            auto pe = nd::make_unique_array<iso2d::primitive_t, 2>(nd::uivec(n + 4, n + 4));
+            for (std::size_t i = 0; i < n + 4; ++i)
+            {
+                for (std::size_t j = 0; j < n + 4; ++j)
+                {
+                    std::size_t ci = i < 2 ? (bi + nb - 1) % nb : (i >= n + 2 ? (bi + 1) % nb : bi);
+                    std::size_t cj = j < 2 ? (bj + nb - 1) % nb : (j >= n + 2 ? (bj + 1) % nb : bj);
+                    std::size_t ii = i < 2 ? i - 2 + n : (i >= n + 2 ? i - 2 - n : i - 2);
+                    std::size_t jj = j < 2 ? j - 2 + n : (j >= n + 2 ? j - 2 - n : j - 2);
+                    pe(i, j) = pc[ci * nb + cj](ii, jj);
+                }
+            }
+            auto r = minidisk::updated_conserved(uc[b], nd::make_shared_array(std::move(pe)), t, dt,
+                                                 block_index(sd.depth, bi, bj), sd);
+            for (std::size_t i = 0; i < n; ++i)
+                for (std::size_t j = 0; j < n; ++j)
+                {
+                    double v[3];
+                    from_tuple(r(i, j), v);
+                    for (int k = 0; k < 3; ++k) out[(k * N + bi * n + i) * N + bj * n + j] = v[k];
+                }
+            return 0;
+        }));
+    }
+    for (auto& f : fut) f.get();
+    return 0;
+}
+
+// Binary state in the rotating frame, as updated_conserved computes it
+// (problems/minidisk_scheme.cpp:329-335): out = {m1,x1,y1,vx1,vy1,m2,x2,y2,vx2,vy2}.
+void ref_minidisk_binary(double mass_ratio, double eccentricity, double omega_frame, double t, double* out)
+{
+    auto el = two_body::orbital_elements(1.0, 1.0, mass_ratio, eccentricity);
+    auto s = two_body::rotate(two_body::orbital_state(el, t), -dimensional::unit_rate(omega_frame) * dimensional::unit_time(t));
+    double v[10] = {s.first.mass.value, s.first.position_x.value, s.first.position_y.value,
+                    s.first.velocity_x.value, s.first.velocity_y.value,
+                    s.second.mass.value, s.second.position_x.value, s.second.position_y.value,
+                    s.second.velocity_x.value, s.second.velocity_y.value};
+    std::memcpy(out, v, sizeof v);
+}
+
+// srhd::recover_primitive (src/physics_srhd.hpp:231-285) over n AoS zones of 5;
+// status[i] = 0 ok, 1 the reference threw.
+void ref_srhd_recover_primitive(const double* u, int64_t n, double gamma_law_index, double temperature_floor,
+                                double* p, int32_t* status)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        try {
+            auto r = srhd::recover_primitive(to_tuple<srhd::conserved_density_t>(u + 5 * i), gamma_law_index, temperature_floor);
+            from_tuple(r, p + 5 * i);
+            status[i] = 0;
+        } catch (...) {
+            for (int k = 0; k < 5; ++k) p[5 * i + k] = 0.0;
+            status[i] = 1;
+        }
+    }
+}
+
+// srhd::conserved_density (src/physics_srhd.hpp:291-304) over n zones.
+void ref_srhd_conserved_density(const double* p, int64_t n, double gamma_law_index, double* u)
+{
+    for (int64_t i = 0; i < n; ++i)
+        from_tuple(srhd::conserved_density(to_tuple<srhd::primitive_t>(p + 5 * i), gamma_law_index), u + 5 * i);
+}
+
+// srhd::riemann_hlle / riemann_hllc (src/physics_srhd.hpp:489-507) over n
+// face pairs; axis in {1,2,3}; hllc != 0 selects HLLC.
+int ref_srhd_riemann(const double* pl, const double* pr, int64_t n, uint32_t axis, double gamma_law_index,
+                     int32_t hllc, double* f)
+{
+    try {
+        auto nhat = geometric::unit_vector_on(axis);
+        for (int64_t i = 0; i < n; ++i)
+        {
+            auto a = to_tuple<srhd::primitive_t>(pl + 5 * i);
+            auto b = to_tuple<srhd::primitive_t>(pr + 5 * i);
+            auto r = hllc ? srhd::riemann_hllc(a, b, nhat, gamma_law_index) : srhd::riemann_hlle(a, b, nhat, gamma_law_index);
+            from_tuple(r, f + 5 * i);
+        }
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// mara::plm_gradient on unit coordinates (src/scheme_plm_gradient.hpp:44-70),
+// on dimensional quantities as every scheme calls it (with raw doubles the
+// reference's unqualified abs() would bind to the int overload).
+double ref_plm_gradient(double theta, double yl, double y0, double yr)
+{
+    using q = dimensional::unit_scalar;
+    return mara::plm_gradient_scalar_t<double>{0.0, 1.0, 2.0, theta}(numeric::tuple(q(yl), q(y0), q(yr))).value;
+}
+
+} // extern "C"

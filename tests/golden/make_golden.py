@@ -1,0 +1,178 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Run where the reference checkout is present (it is not on the GPU hosts):
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+oracle/_ref/libref.so is the reference's own scheme and physics code
+(problems/minidisk_scheme.cpp, src/physics_*.hpp, src/scheme_*) compiled in
+place with oracle/ref_harness.cpp. Every output below is produced by that
+library; inputs are seeded. The fixtures pin the oracle restatement
+(tests/test_oracle_golden.py) and, through it, the GPU kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+from oracle.oracle import MinidiskParams, dptr, iptr, load_oracle, load_reference, solver_vector  # noqa: E402
+
+MINIDISK_CASES = {
+    # name: solver_data (block_size 16, depth 2 -> 64^2 mesh), seed, perturbation, time, dt scale
+    "config1_like": dict(block_size=16, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3, domain_radius=1.0,
+                         softening_length=0.05, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.05, sink_rate=10.0,
+                         buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=2.0),
+    "eccentric_unequal": dict(block_size=16, depth=2, omega_frame=1.0, mach_number=20.0, nu=5e-4, domain_radius=1.0,
+                              softening_length=0.05, eccentricity=0.1, mass_ratio=0.5, sink_radius=0.05,
+                              sink_rate=10.0, buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=2.0),
+    "inviscid_defaults": dict(block_size=8, depth=3, omega_frame=1.0, mach_number=10.0, nu=0.0, domain_radius=1.5,
+                              softening_length=0.01, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.01,
+                              sink_rate=1e3, buffer_rate=1e2, buffer_scale=0.2, cfl=0.3, plm_theta=2.0),
+}
+
+
+def minidisk_fixtures(o, r) -> dict[str, np.ndarray]:
+    out = {}
+    for name, kw in MINIDISK_CASES.items():
+        p = MinidiskParams(**kw)
+        N = p.block_size << p.depth
+        u0 = np.zeros(3 * N * N)
+        o.oracle_minidisk_initial_conserved(ctypes.byref(p), ctypes.c_uint64(1234), ctypes.c_double(0.01), dptr(u0))
+        sdv = solver_vector(p)
+        # one forward-Euler substep at t = 0.37 with the reference dt formula
+        t = 0.37
+        dt = o.oracle_minidisk_dt_formula(ctypes.byref(p), ctypes.c_double(t))
+        u1 = np.zeros_like(u0)
+        assert r.ref_minidisk_substep(dptr(sdv), dptr(u0), dptr(u1), ctypes.c_double(t), ctypes.c_double(dt), 4) == 0
+        # 5 RK2 steps from t = 0, control::advance_runge_kutta semantics
+        u = u0.copy()
+        tt = 0.0
+        a = np.zeros_like(u0)
+        b = np.zeros_like(u0)
+        for _ in range(5):
+            dts = o.oracle_minidisk_dt_formula(ctypes.byref(p), ctypes.c_double(tt))
+            r.ref_minidisk_substep(dptr(sdv), dptr(u), dptr(a), ctypes.c_double(tt), ctypes.c_double(dts), 4)
+            r.ref_minidisk_substep(dptr(sdv), dptr(a), dptr(b), ctypes.c_double(tt + dts), ctypes.c_double(dts), 4)
+            u = u * 0.5 + b * (1.0 - 0.5)
+            tt = tt * 0.5 + ((tt + dts) + dts) * (1.0 - 0.5)
+        out[f"{name}/u0"] = u0
+        out[f"{name}/t"] = np.array([t, dt])
+        out[f"{name}/substep"] = u1
+        out[f"{name}/rk2_5"] = u
+        out[f"{name}/rk2_5_time"] = np.array([tt])
+        out[f"{name}/params"] = sdv
+        out[f"{name}/theta"] = np.array([p.plm_theta])
+    return out
+
+
+def block_fixture(r) -> dict[str, np.ndarray]:
+    """updated_conserved on one block (level 2, block (1, 3)) with seeded pe/uc."""
+    kw = MINIDISK_CASES["config1_like"]
+    p = MinidiskParams(**kw)
+    n = p.block_size
+    rng = np.random.default_rng(99)
+    x = np.linspace(-1, 1, n + 4)
+    base = np.stack(np.meshgrid(x, x, indexing="ij"), -1)
+    pe = np.empty((n + 4, n + 4, 3))
+    pe[..., 0] = 1.0 + 0.2 * np.sin(3 * base[..., 0]) * np.cos(2 * base[..., 1]) + 0.01 * rng.standard_normal((n + 4, n + 4))
+    pe[..., 1] = 0.3 * np.cos(base[..., 1] * 4) + 0.02 * rng.standard_normal((n + 4, n + 4))
+    pe[..., 2] = -0.2 * np.sin(base[..., 0] * 5) + 0.02 * rng.standard_normal((n + 4, n + 4))
+    pc = pe[2:-2, 2:-2]
+    uc = np.stack([pc[..., 0], pc[..., 0] * pc[..., 1], pc[..., 0] * pc[..., 2]], -1).copy()
+    pe = np.ascontiguousarray(pe)
+    out_u = np.zeros_like(uc)
+    assert r.ref_minidisk_updated_conserved(dptr(solver_vector(p)), dptr(uc), dptr(pe), ctypes.c_double(0.81),
+                                            ctypes.c_double(2e-3), 2, 1, 3, dptr(out_u)) == 0
+    res = {"block/pe": pe, "block/uc": uc, "block/u1": out_u, "block/params": solver_vector(p),
+           "block/index": np.array([2, 1, 3]), "block/time_dt": np.array([0.81, 2e-3])}
+    for theta in (1.5, 2.0):
+        for axis in (0, 1):
+            g = np.zeros((n + 2, n + 4, 3) if axis == 0 else (n + 4, n + 2, 3))
+            r.ref_minidisk_estimate_gradient(dptr(pe), n + 4, n + 4, axis, ctypes.c_double(theta), dptr(g))
+            res[f"gradient/theta{theta}/axis{axis}"] = g
+    return res
+
+
+def plm_fixture(r) -> dict[str, np.ndarray]:
+    rng = np.random.default_rng(5)
+    y = rng.standard_normal((512, 3))
+    y[::7, 1] = y[::7, 0]            # flat left
+    y[::11, 2] = y[::11, 1]          # flat right
+    y[::13] = 0.0                     # all zero
+    thetas = np.array([1.0, 1.5, 2.0])
+    g = np.array([[r.ref_plm_gradient(th, *row) for row in y] for th in thetas])
+    return {"plm/y": y, "plm/theta": thetas, "plm/g": g}
+
+
+def binary_fixture(r) -> dict[str, np.ndarray]:
+    cases = np.array([[1.0, 0.0, 1.0], [0.5, 0.1, 1.0], [0.3, 0.5, 0.0], [1.0, 0.4, 0.7]])
+    times = np.array([0.0, 0.37, 2.3, 31.4159, 100.0])
+    res = np.zeros((len(cases), len(times), 10))
+    for i, (q, e, om) in enumerate(cases):
+        for j, t in enumerate(times):
+            buf = np.zeros(10)
+            r.ref_minidisk_binary(ctypes.c_double(q), ctypes.c_double(e), ctypes.c_double(om), ctypes.c_double(t), dptr(buf))
+            res[i, j] = buf
+    return {"binary/cases": cases, "binary/times": times, "binary/state": res}
+
+
+def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
+    g = 4.0 / 3.0
+    n = 4096
+    prim = np.zeros(5 * n)
+    cons = np.zeros(5 * n)
+    # the BASELINE config-4(a) distribution: rho 1e-4..1, p 1e-6..10, W 1..50
+    o.oracle_srhd_seeded_zones(ctypes.c_uint64(4242), ctypes.c_int64(n), ctypes.c_double(1e-4), ctypes.c_double(1.0),
+                               ctypes.c_double(1e-6), ctypes.c_double(10.0), ctypes.c_double(50.0), ctypes.c_double(g),
+                               dptr(prim), dptr(cons))
+    cref = np.zeros(5 * n)
+    r.ref_srhd_conserved_density(dptr(prim), ctypes.c_int64(n), ctypes.c_double(g), dptr(cref))
+    rec = np.zeros(5 * n)
+    st = np.zeros(n, np.int32)
+    r.ref_srhd_recover_primitive(dptr(cref), ctypes.c_int64(n), ctypes.c_double(g), ctypes.c_double(0.0), dptr(rec), iptr(st))
+    out = {"srhd/prim": prim, "srhd/cons": cref, "srhd/recovered": rec, "srhd/status": st}
+    # the reference's own known-answer states (src/physics_srhd.hpp:534-537)
+    kat = np.array([[1.0, 0, 0, 0, 1.0], [1.5, 0, 0, 0, 1e3], [1.0, 0, 0, 0, 1.0], [5.7, 1.0, 2.0, 3.0, 5.0]]).ravel()
+    kc = np.zeros_like(kat)
+    r.ref_srhd_conserved_density(dptr(kat), ctypes.c_int64(4), ctypes.c_double(g), dptr(kc))
+    kr = np.zeros_like(kat)
+    ks = np.zeros(4, np.int32)
+    r.ref_srhd_recover_primitive(dptr(kc), ctypes.c_int64(4), ctypes.c_double(g), ctypes.c_double(0.0), dptr(kr), iptr(ks))
+    out.update({"srhd_kat/prim": kat, "srhd_kat/cons": kc, "srhd_kat/recovered": kr})
+    m = 1000
+    pl = prim[: 5 * m].copy()
+    pr = prim[5 * m: 10 * m].copy()
+    out["srhd_riemann/pl"] = pl
+    out["srhd_riemann/pr"] = pr
+    for hllc in (0, 1):
+        for axis in (1, 2, 3):
+            f = np.zeros(5 * m)
+            assert r.ref_srhd_riemann(dptr(pl), dptr(pr), ctypes.c_int64(m), axis, ctypes.c_double(g), hllc, dptr(f)) == 0
+            out[f"srhd_riemann/{'hllc' if hllc else 'hlle'}/axis{axis}"] = f
+    return out
+
+
+def main() -> None:
+    o = load_oracle()
+    r = load_reference()
+    if r is None:
+        raise SystemExit("oracle/_ref/libref.so is missing: run `make -C oracle ref` where the reference is present")
+    fixtures = {}
+    fixtures.update(minidisk_fixtures(o, r))
+    fixtures.update(block_fixture(r))
+    fixtures.update(plm_fixture(r))
+    fixtures.update(binary_fixture(r))
+    np.savez_compressed(HERE / "minidisk_golden.npz", **fixtures)
+    np.savez_compressed(HERE / "srhd_golden.npz", **srhd_fixtures(o, r))
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

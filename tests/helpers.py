@@ -1,0 +1,28 @@
+"""Shared test helpers (not collected as tests)."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle.oracle import MinidiskParams
+
+CONFIG1_PARAMS = dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3, domain_radius=4.0,
+                      softening_length=0.05, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.05, sink_rate=10.0,
+                      buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=2.0)
+
+SMALL_PARAMS = dict(CONFIG1_PARAMS, block_size=16, depth=2, domain_radius=1.0)
+
+
+def params_from_vector(v: np.ndarray, theta: float = 2.0) -> MinidiskParams:
+    keys = ("block_size depth omega_frame mach_number nu domain_radius softening_length eccentricity "
+            "mass_ratio sink_radius sink_rate buffer_rate buffer_scale cfl").split()
+    kw = {k: (int(x) if k in ("block_size", "depth") else float(x)) for k, x in zip(keys, v)}
+    return MinidiskParams(**kw, plm_theta=theta)
+
+
+def rel_l1_components(a: np.ndarray, b: np.ndarray, ncomp: int = 3) -> float:
+    """Largest per-component relative L1 difference, sum|a-b| / sum|b|."""
+    a = np.asarray(a, dtype=np.float64).reshape(ncomp, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(ncomp, -1)
+    num = np.abs(a - b).sum(axis=1)
+    den = np.abs(b).sum(axis=1)
+    return float(np.max(num / np.where(den > 0, den, 1.0)))

@@ -1,0 +1,191 @@
+"""GPU parity of the minidisk path, through the C ABI, against the oracle and
+the reference's golden fixtures.
+
+Tolerances (relative L1 per component, sum|gpu - ref| / sum|ref|):
+  plain FP64 path: 1e-12 after one step, 1e-9 after 1000 steps (only FMA
+  contraction and CUDA-vs-glibc libm rounding differ);
+  integer-like / order-free operations (primitive recovery, PLM slopes,
+  initial state): bit-exact.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import dptr, params
+from tests.golden.make_golden import MINIDISK_CASES
+from tests.helpers import CONFIG1_PARAMS, SMALL_PARAMS, params_from_vector, rel_l1_components
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FP64_ONE_STEP = 1e-12
+FP64_1000_STEPS = 1e-9
+
+
+@pytest.fixture(scope="module")
+def md():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import mara3p_gb300.minidisk as m
+    return m
+
+
+def sd_from(md, p):
+    return md.SolverData(**{name: getattr(p, name) for name, _ in p._fields_})
+
+
+def to_gpu(a, shape):
+    return torch.from_numpy(np.ascontiguousarray(a).reshape(shape)).cuda()
+
+
+@pytest.mark.parametrize("case", list(MINIDISK_CASES))
+def test_substep_fp64_matches_reference(md, golden, case):
+    p = params_from_vector(golden[f"{case}/params"], float(golden[f"{case}/theta"][0]))
+    sd = sd_from(md, p)
+    N = sd.cells_per_side
+    u0 = to_gpu(golden[f"{case}/u0"], (3, N, N))
+    t, dt = golden[f"{case}/t"]
+    out = md.substep(sd, u0, float(t), float(dt)).cpu().numpy()
+    assert rel_l1_components(out, golden[f"{case}/substep"]) < FP64_ONE_STEP
+
+
+@pytest.mark.parametrize("case", list(MINIDISK_CASES))
+def test_rk2_device_clock_matches_reference(md, golden, case):
+    p = params_from_vector(golden[f"{case}/params"], float(golden[f"{case}/theta"][0]))
+    sd = sd_from(md, p)
+    N = sd.cells_per_side
+    run = md.Run(sd, to_gpu(golden[f"{case}/u0"], (3, N, N)).clone(), time=0.0, rk_order=2,
+                 precision=md.FP64, dt_mode=md.DT_FORMULA)
+    run.advance(5)
+    torch.cuda.synchronize()
+    assert rel_l1_components(run.u.cpu().numpy(), golden[f"{case}/rk2_5"]) < FP64_ONE_STEP * 10
+    assert abs(run.time - golden[f"{case}/rk2_5_time"][0]) < 1e-15
+
+
+def test_block_updated_conserved_dropin(md, golden):
+    p = params_from_vector(golden["block/params"])
+    sd = sd_from(md, p)
+    n = sd.block_size
+    level, bi, bj = (int(x) for x in golden["block/index"])
+    t, dt = golden["block/time_dt"]
+    u1 = md.updated_conserved(to_gpu(golden["block/uc"], (n, n, 3)), to_gpu(golden["block/pe"], (n + 4, n + 4, 3)),
+                              float(t), float(dt), (level, bi, bj), sd)
+    got = u1.cpu().numpy().reshape(-1, 3).T
+    ref = golden["block/u1"].reshape(-1, 3).T
+    assert rel_l1_components(got, ref) < FP64_ONE_STEP
+
+
+@pytest.mark.parametrize("theta", [1.5, 2.0])
+@pytest.mark.parametrize("axis", [0, 1])
+def test_estimate_gradient_bitexact(md, golden, theta, axis):
+    pe = golden["block/pe"]
+    g = md.estimate_gradient(to_gpu(pe, pe.shape), axis, theta).cpu().numpy()
+    assert np.array_equal(g, golden[f"gradient/theta{theta}/axis{axis}"])
+
+
+def test_recover_primitive_bitexact(md, oracle, golden):
+    uc = golden["block/uc"]
+    got = md.recover_primitive_array(to_gpu(uc, uc.shape)).cpu().numpy()
+    ref = np.zeros_like(uc)
+    oracle.oracle_minidisk_recover_primitive(dptr(uc), ctypes.c_int64(uc.size // 3), dptr(ref))
+    assert np.array_equal(got, ref)
+
+
+def test_recover_primitive_empty(md):
+    out = md.recover_primitive_array(torch.empty((0, 3), dtype=torch.float64, device="cuda"))
+    assert out.shape == (0, 3)
+
+
+@pytest.mark.parametrize("amplitude", [0.0, 0.01])
+def test_initial_conserved_bitexact(md, oracle, amplitude):
+    sd = md.SolverData(**CONFIG1_PARAMS)
+    u = md.initial_conserved(sd, seed=77, amplitude=amplitude).cpu().numpy()
+    ref = np.zeros(u.size)
+    oracle.oracle_minidisk_initial_conserved(ctypes.byref(params(sd)), ctypes.c_uint64(77), ctypes.c_double(amplitude),
+                                             dptr(ref))
+    assert np.array_equal(u.ravel(), ref)
+
+
+def test_config1_one_step_and_1000_steps_fp64(md, oracle):
+    """Plain FP64 GPU vs the oracle on the same seeded input: one RK2 step at
+    1e-12 and 1000 RK2 steps at 1e-9 (64^2 mesh, config-1 physics)."""
+    sd = md.SolverData(**SMALL_PARAMS)
+    u0 = md.initial_conserved(sd, seed=5, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)
+    run.advance(1)
+    t = oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 1, 2, 0, 8)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
+    run.advance(999)
+    t = oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(t), 999, 2, 0, 8)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_1000_STEPS
+    assert abs(run.time - t) <= 1e-12 * t
+
+
+def test_config1_full_size_one_step(md, oracle):
+    """Config 1 itself (256^2, 4x4 blocks of 64^2): one RK2 step at 1e-12."""
+    sd = md.SolverData(**CONFIG1_PARAMS)
+    u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)
+    run.advance(2)
+    oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 2, 2, 0, 8)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
+
+
+def test_cfl_dt_matches_oracle(md, oracle):
+    sd = md.SolverData(**SMALL_PARAMS)
+    u0 = md.initial_conserved(sd, seed=3, amplitude=0.01)
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
+    run.advance(1)
+    dt_gpu = run.clock_state().dt
+    dt_ref = oracle.oracle_minidisk_dt_cfl(ctypes.byref(params(sd)), dptr(u0.cpu().numpy().ravel().copy()))
+    assert abs(dt_gpu - dt_ref) <= 1e-14 * dt_ref
+    # the fused reduction of the new state seeds the next step's dt
+    run.advance(1)
+    ref = run.u.cpu().numpy().ravel().copy()
+    u_prev = u0.cpu().numpy().ravel().copy()
+    oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(u_prev), ctypes.c_double(0.0), 2, 2, 1, 8)
+    assert rel_l1_components(ref, u_prev) < FP64_ONE_STEP * 10
+
+
+def test_rk1_fp64_matches_oracle(md, oracle):
+    sd = md.SolverData(**SMALL_PARAMS)
+    u0 = md.initial_conserved(sd, seed=9, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    run = md.Run(sd, u0.clone(), rk_order=1, precision=md.FP64, dt_mode=md.DT_FORMULA)
+    run.advance(3)
+    oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 3, 1, 0, 8)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
+
+
+@pytest.mark.parametrize("rk_order", [1, 2])
+def test_mixed_precision_close_to_fp64(md, rk_order):
+    """Mixed path (FP32 fluxes/sources, FP64 accumulation) vs plain FP64 GPU
+    after 200 steps: density and momentum relative L1 below 1e-6."""
+    sd = md.SolverData(**SMALL_PARAMS)
+    u0 = md.initial_conserved(sd, seed=11, amplitude=0.01)
+    a = md.Run(sd, u0.clone(), rk_order=rk_order, precision=md.FP64, dt_mode=md.DT_FORMULA)
+    b = md.Run(sd, u0.clone(), rk_order=rk_order, precision=md.MIXED, dt_mode=md.DT_FORMULA)
+    a.advance(200)
+    b.advance(200)
+    err = rel_l1_components(b.u.cpu().numpy(), a.u.cpu().numpy())
+    assert err < 1e-6, err
+    assert a.time == b.time
+
+
+def test_mass_conservation_full_size(md):
+    """Size-independent property at the config-2 size (4096^2): with sinks,
+    buffer and viscosity off, the flux divergence telescopes and total mass
+    is conserved to rounding, in both precisions."""
+    sd = md.SolverData(block_size=64, depth=6, domain_radius=8.0, softening_length=0.05, mach_number=20.0,
+                       sink_rate=0.0, buffer_rate=0.0, nu=0.0, sink_radius=0.05, eccentricity=0.1, mass_ratio=0.5)
+    u0 = md.initial_conserved(sd, seed=2, amplitude=0.01)
+    m0 = u0[0].sum().item()
+    for precision in (md.MIXED, md.FP64):
+        run = md.Run(sd, u0.clone(), rk_order=2, precision=precision, dt_mode=md.DT_CFL)
+        run.advance(2)
+        assert abs(run.u[0].sum().item() - m0) < 1e-11 * m0

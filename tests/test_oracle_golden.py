@@ -1,0 +1,125 @@
+"""The oracle restatement against golden fixtures produced by the reference's
+own compiled code (tests/golden/make_golden.py). CPU only; bit-exact."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import MinidiskParams, dptr, iptr
+from tests.golden.make_golden import MINIDISK_CASES
+from tests.helpers import params_from_vector
+
+CASES = list(MINIDISK_CASES)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_minidisk_substep_bitexact(oracle, golden, case):
+    p = params_from_vector(golden[f"{case}/params"], float(golden[f"{case}/theta"][0]))
+    u0 = golden[f"{case}/u0"]
+    t, dt = golden[f"{case}/t"]
+    out = np.zeros_like(u0)
+    oracle.oracle_minidisk_substep(ctypes.byref(p), dptr(u0), dptr(out), ctypes.c_double(t), ctypes.c_double(dt), 2)
+    assert np.array_equal(out, golden[f"{case}/substep"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_minidisk_rk2_bitexact(oracle, golden, case):
+    p = params_from_vector(golden[f"{case}/params"], float(golden[f"{case}/theta"][0]))
+    u = golden[f"{case}/u0"].copy()
+    t = oracle.oracle_minidisk_advance(ctypes.byref(p), dptr(u), ctypes.c_double(0.0), 5, 2, 0, 2)
+    assert np.array_equal(u, golden[f"{case}/rk2_5"])
+    assert t == golden[f"{case}/rk2_5_time"][0]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_minidisk_initial_state_matches_reference_formula(oracle, golden, case):
+    p = params_from_vector(golden[f"{case}/params"])
+    u = np.zeros_like(golden[f"{case}/u0"])
+    oracle.oracle_minidisk_initial_conserved(ctypes.byref(p), ctypes.c_uint64(1234), ctypes.c_double(0.01), dptr(u))
+    assert np.array_equal(u, golden[f"{case}/u0"])
+
+
+def test_minidisk_block_update_bitexact(oracle, golden):
+    p = params_from_vector(golden["block/params"])
+    level, bi, bj = (int(x) for x in golden["block/index"])
+    t, dt = golden["block/time_dt"]
+    out = np.zeros_like(golden["block/uc"])
+    oracle.oracle_minidisk_updated_conserved(ctypes.byref(p), dptr(golden["block/uc"]), dptr(golden["block/pe"]),
+                                             ctypes.c_double(t), ctypes.c_double(dt), level, bi, bj, dptr(out))
+    assert np.array_equal(out, golden["block/u1"])
+
+
+@pytest.mark.parametrize("theta", [1.5, 2.0])
+@pytest.mark.parametrize("axis", [0, 1])
+def test_estimate_gradient_bitexact(oracle, golden, theta, axis):
+    pe = golden["block/pe"]
+    ref = golden[f"gradient/theta{theta}/axis{axis}"]
+    out = np.zeros_like(ref)
+    oracle.oracle_minidisk_estimate_gradient(dptr(pe), pe.shape[0], pe.shape[1], axis, ctypes.c_double(theta), dptr(out))
+    assert np.array_equal(out, ref)
+
+
+def test_plm_gradient_scalar_cases(oracle, golden):
+    """plm_gradient on crafted triples (flat sides, zeros) at theta 1, 1.5, 2."""
+    y = golden["plm/y"]
+    for k, theta in enumerate(golden["plm/theta"]):
+        pc = np.repeat(y.T[:, :, None], 3, axis=2).copy()      # (3, m, 3): the triple along axis 0
+        out = np.zeros((1, y.shape[0], 3))
+        oracle.oracle_minidisk_estimate_gradient(dptr(pc), 3, y.shape[0], 0, ctypes.c_double(theta), dptr(out))
+        assert np.array_equal(out[0, :, 0], golden["plm/g"][k])
+
+
+def test_binary_orbit_bitexact(oracle, golden):
+    for i, (q, e, om) in enumerate(golden["binary/cases"]):
+        p = MinidiskParams(block_size=8, depth=0, omega_frame=om, mach_number=10, nu=0, domain_radius=1,
+                           softening_length=0.1, eccentricity=e, mass_ratio=q, sink_radius=0.1, sink_rate=1,
+                           buffer_rate=1, buffer_scale=1, cfl=0.3, plm_theta=2.0)
+        for j, t in enumerate(golden["binary/times"]):
+            out = np.zeros(10)
+            oracle.oracle_minidisk_binary(ctypes.byref(p), ctypes.c_double(t), dptr(out))
+            assert np.array_equal(out, golden["binary/state"][i, j])
+
+
+def test_srhd_conserved_and_recovery_bitexact(oracle, srhd_golden):
+    g = 4.0 / 3.0
+    prim = srhd_golden["srhd/prim"]
+    n = prim.size // 5
+    cons = np.zeros_like(prim)
+    oracle.oracle_srhd_conserved_density(dptr(prim), ctypes.c_int64(n), ctypes.c_double(g), dptr(cons))
+    assert np.array_equal(cons, srhd_golden["srhd/cons"])
+    rec = np.zeros_like(prim)
+    it = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    oracle.oracle_srhd_recover_primitive(dptr(cons), ctypes.c_int64(n), ctypes.c_double(g), ctypes.c_double(0.0),
+                                         None, dptr(rec), iptr(it), iptr(st))
+    assert np.array_equal(st, srhd_golden["srhd/status"])
+    assert np.array_equal(rec, srhd_golden["srhd/recovered"])
+    assert 4.0 < it.mean() < 6.0 and it.max() <= 51
+
+
+def test_srhd_reference_known_answers(oracle, srhd_golden):
+    """test_srhd's cons->prim round trips (src/physics_srhd.hpp:528-537): |p1 - p0| < 1e-10."""
+    g = 4.0 / 3.0
+    kat = srhd_golden["srhd_kat/prim"]
+    cons = np.zeros_like(kat)
+    oracle.oracle_srhd_conserved_density(dptr(kat), ctypes.c_int64(4), ctypes.c_double(g), dptr(cons))
+    assert np.array_equal(cons, srhd_golden["srhd_kat/cons"])
+    rec = np.zeros_like(kat)
+    oracle.oracle_srhd_recover_primitive(dptr(cons), ctypes.c_int64(4), ctypes.c_double(g), ctypes.c_double(0.0),
+                                         None, dptr(rec), None, None)
+    assert np.array_equal(rec, srhd_golden["srhd_kat/recovered"])
+    assert np.all(np.abs(rec - kat) < 1e-10)
+
+
+@pytest.mark.parametrize("solver", ["hlle", "hllc"])
+@pytest.mark.parametrize("axis", [1, 2, 3])
+def test_srhd_riemann_bitexact(oracle, srhd_golden, solver, axis):
+    pl, pr = srhd_golden["srhd_riemann/pl"], srhd_golden["srhd_riemann/pr"]
+    n = pl.size // 5
+    f = np.zeros_like(pl)
+    bad = oracle.oracle_srhd_riemann(dptr(pl), dptr(pr), ctypes.c_int64(n), axis, ctypes.c_double(4.0 / 3.0),
+                                     int(solver == "hllc"), dptr(f))
+    assert bad == 0
+    assert np.array_equal(f, srhd_golden[f"srhd_riemann/{solver}/axis{axis}"])
