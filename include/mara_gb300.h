@@ -169,6 +169,50 @@ int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const doub
 int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int32_t dt_mode,
                                int32_t rk_order, int32_t end_step, int32_t begin_step, void* stream);
 
+/* ---------------------------------------------------------------- srhd */
+
+/* Conserved -> primitive recovery of n zones, replacing srhd::recover_primitive
+ * (src/physics_srhd.hpp:231-285). Zone i, component k (D, S1, S2, S3, tau in;
+ * rho, u1, u2, u3, p out) lives at [k*component_stride + i*zone_stride]: SoA is
+ * (n, 1), the reference's AoS tuple layout is (1, 5). All buffers device.
+ *   mlp_weights == NULL and refine32 == 0: the reference's method, Newton from
+ *     p = 0, 50+1 iterations, |f| < 1e-12 (1e-8 on the last); bit-identical to it.
+ *   mlp_weights != NULL: Newton starts from the learned guess
+ *     (mara_srhd_mlp_*), optionally sharpened by refine32 FP32 Newton steps;
+ *     FP64 Newton then polishes with the same stopping rule within
+ *     seeded_budget iterations, else restarts from p = 0 with the full budget.
+ *   mlp_weights == NULL and refine32 > 0: the same, from p = 0.
+ * iterations[i] (nullable) = FP64 Newton iterations run; status[i] (nullable)
+ * = 0 ok, 1 not converged, 2 non-positive pressure (the reference throws);
+ * failed zones get zero primitives; *failures (nullable, device) counts them. */
+int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component_stride, int64_t zone_stride,
+                                double gamma_law_index, double temperature_floor, const void* mlp_weights,
+                                int32_t refine32, int32_t seeded_budget, double* prim, int32_t* iterations,
+                                int32_t* status, unsigned long long* failures, void* stream);
+
+/* Learned pressure guess (4-64-64-1 MLP, BF16 tensor-core inference). No
+ * counterpart in the reference. The weights are one device buffer of
+ * mara_srhd_mlp_weights_bytes() bytes. Training data are n zones in SoA
+ * [5][n] (cons, and prim from mara_srhd_recover_primitive); workspace is
+ * mara_srhd_mlp_workspace_bytes(n) bytes of device memory. */
+int64_t mara_srhd_mlp_weights_bytes(void);
+int32_t mara_srhd_mlp_param_count(void);
+int64_t mara_srhd_mlp_workspace_bytes(int64_t n);
+/* Features, targets, normalisation and Glorot initialisation of the weights. */
+int mara_srhd_mlp_prepare(const double* cons, const double* prim, int64_t n, void* weights, uint64_t seed,
+                          void* workspace, void* stream);
+/* Mean-squared-error loss and its gradient (FP32) over all n prepared zones;
+ * grad holds mara_srhd_mlp_param_count() floats, loss one float (device). */
+int mara_srhd_mlp_gradient(const void* weights, const void* workspace, int64_t n, float* grad, float* loss,
+                           void* stream);
+/* `steps` Adam steps on mini-batches of `batch` zones taken in the order of
+ * `order` (device int64[n]); loss_history (nullable, device) gets one float
+ * per step. Ends by refreshing the BF16 copy used for inference. */
+int mara_srhd_mlp_train(void* weights, void* workspace, int64_t n, const int64_t* order, int32_t steps,
+                        int32_t batch, float lr, float* loss_history, void* stream);
+/* Inference on n rows of raw features (float[n][4]): y[i] = network output. */
+int mara_srhd_mlp_infer(const void* weights, const float* features, int64_t n, float* y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

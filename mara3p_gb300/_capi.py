@@ -75,6 +75,17 @@ SIGNATURES = {
                                            ctypes.c_int32, _vp]),
     "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp]),
+    "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                                   ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int32,
+                                                   ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    "mara_srhd_mlp_weights_bytes": (ctypes.c_int64, []),
+    "mara_srhd_mlp_param_count": (ctypes.c_int32, []),
+    "mara_srhd_mlp_workspace_bytes": (ctypes.c_int64, [ctypes.c_int64]),
+    "mara_srhd_mlp_prepare": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint64, _vp, _vp]),
+    "mara_srhd_mlp_gradient": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp]),
+    "mara_srhd_mlp_train": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_float, _vp, _vp]),
+    "mara_srhd_mlp_infer": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp]),
 }
 
 

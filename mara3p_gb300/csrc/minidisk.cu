@@ -37,6 +37,15 @@ constexpr int NFY = TX * (TY + 1);          // y faces
 
 enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3 };
 
+// Single-precision constants of the mixed path, prepared on the host so that
+// no FP64 instruction (GB300 runs FP64 at 1/64 of the FP32 rate) is issued
+// for them on the device.
+struct FloatConsts
+{
+    float rs2, inv_mach2, half_nu, half_inv_dl, inv_dl, theta, R, dl;
+    float sink_rate, inv_s6, buffer_rate, neg2_inv_buffer_scale, omega, omega2, two_omega;
+};
+
 struct Args
 {
     int N;                 // cells per side of the mesh (K_BLOCK: block size)
@@ -58,7 +67,32 @@ struct Args
     float* d_out;          // K_MIX1 + RK2: increment out
     const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
     unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
+    FloatConsts f;
 };
+
+// double -> float (round to nearest even) and float -> double (exact) with
+// integer instructions; values outside the normal float range take the
+// hardware conversion.
+__device__ inline float d2f(double x)
+{
+    const unsigned long long b = __double_as_longlong(x);
+    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    if (e < 897u || e > 1150u) return __double2float_rn(x);
+    unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1FFFFFFFu;
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f);
+}
+
+__device__ inline double f2d(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xFFu;
+    if (e == 0u || e == 255u) return double(x);
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+    return __hiloint2double(int(hi), int(b << 29));
+}
 
 // ------------------------------------------------------------- geometry
 // vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
@@ -166,9 +200,8 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
         L[k] = fmaf(0.5f, ga[k], pa[k]);
         Rr[k] = fmaf(-0.5f, gb[k], pb[k]);
     }
-    const float inv_mach2 = float(1.0 / (A.mach * A.mach));
-    float rinv = rsqrtf(fmaf(x, x, fmaf(y, y, float(A.rs2))));
-    float cs2 = rinv * inv_mach2;
+    float rinv = rsqrtf(fmaf(x, x, fmaf(y, y, A.f.rs2)));
+    float cs2 = rinv * A.f.inv_mach2;
     float cs = sqrtf(cs2);
     float vl = AXIS == 0 ? L[1] : L[2];
     float vr = AXIS == 0 ? Rr[1] : Rr[2];
@@ -184,10 +217,10 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
     for (int k = 0; k < 3; ++k)
         F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * apam) * inv;
 
-    if (A.nu != 0.0)
+    if (A.f.half_nu != 0.0f)
     {
-        const float half_inv_dl = float(0.5 / A.dl);
-        float mu = float(A.nu * 0.5) * (Rr[0] + L[0]);
+        const float half_inv_dl = A.f.half_inv_dl;
+        float mu = A.f.half_nu * (Rr[0] + L[0]);
         float vx_long = (ga[1] + gb[1]) * half_inv_dl;
         float vy_long = (ga[2] + gb[2]) * half_inv_dl;
         float vx_tran = (ta[1] + tb[1]) * half_inv_dl;
@@ -233,7 +266,20 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
     const int N = A.N;
     const size_t NN = size_t(N) * N;
 
-    // coordinates of this tile's vertices and centres, reference formulae in FP64
+    // coordinates of this tile's vertices and centres: the reference's
+    // per-block linspace in FP64 for the FP64 path, x = -R + i*dl in FP32 for
+    // the mixed path
+    if (sizeof(R) == sizeof(float))
+    {
+        for (int e = tid; e < (TX + 1) + TX + (TY + 1) + TY; e += NT)
+        {
+            if (e < TX + 1) S.xv[e] = R(fmaf(float(gx0 + e), A.f.dl, -A.f.R));
+            else if (e < 2 * TX + 1) S.xc[e - (TX + 1)] = R(fmaf(float(gx0 + e - (TX + 1)) + 0.5f, A.f.dl, -A.f.R));
+            else if (e < 2 * TX + TY + 2) S.yv[e - (2 * TX + 1)] = R(fmaf(float(gy0 + e - (2 * TX + 1)), A.f.dl, -A.f.R));
+            else S.yc[e - (2 * TX + TY + 2)] = R(fmaf(float(gy0 + e - (2 * TX + TY + 2)) + 0.5f, A.f.dl, -A.f.R));
+        }
+    }
+    else
     for (int e = tid; e < (TX + 1) + TX + (TY + 1) + TY; e += NT)
     {
         int q = e;
@@ -285,7 +331,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
             }
             else
             {
-                float fs = float(s), f1 = float(m1), f2 = float(m2);
+                float fs = d2f(s), f1 = d2f(m1), f2 = d2f(m2);
                 if (KIND == K_MIX2)
                 {
                     fs += __ldg(A.d1 + idx); f1 += __ldg(A.d1 + NN + idx); f2 += __ldg(A.d1 + 2 * NN + idx);
@@ -299,7 +345,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
     __syncthreads();
 
     // phase 2: slopes
-    const R theta = R(A.theta);
+    const R theta = sizeof(R) == sizeof(float) ? R(A.f.theta) : R(A.theta);
     for (int e = tid; e < GX * GY; e += NT)
     {
         int gi = e / GY, gj = e - (e / GY) * GY;
@@ -359,6 +405,10 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
         for (int k = 0; k < 6; ++k) b6[k] = A.bin[k];
     }
     double local_max = 0.0;
+    float local_max_f = 0.0f;
+    float bf[6];
+    for (int k = 0; k < 6; ++k) bf[k] = d2f(b6[k]);
+    const float dtf = d2f(dt);
     const int cells_x = KIND == K_BLOCK ? A.n : N;
 
     for (int e = tid; e < TX * TY; e += NT)
@@ -446,60 +496,55 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
         }
         else
         {
+            const FloatConsts& F = A.f;
             const float x = float(S.xc[i]), y = float(S.yc[j]);
-            const float rs2 = float(A.rs2);
-            const float om = float(A.omega);
             size_t idx = size_t(gi) * N + gj;
             float uc[3] = {float(pc[0]), float(pc[0]) * float(pc[1]), float(pc[0]) * float(pc[2])};
-            float dx1 = x - float(b6[1]), dy1 = y - float(b6[2]);
-            float dx2 = x - float(b6[4]), dy2 = y - float(b6[5]);
+            float dx1 = x - bf[1], dy1 = y - bf[2];
+            float dx2 = x - bf[4], dy2 = y - bf[5];
             float q1 = fmaf(dx1, dx1, dy1 * dy1), q2 = fmaf(dx2, dx2, dy2 * dy2);
-            float i1 = rsqrtf(q1 + rs2), i2 = rsqrtf(q2 + rs2);
-            float g1 = -float(b6[0]) * i1 * i1 * i1;
-            float g2 = -float(b6[3]) * i2 * i2 * i2;
-            const float inv_s6 = float(1.0 / A.s6);
-            float sr1 = float(A.sink_rate) * __expf(-(q1 * q1 * q1) * inv_s6);
-            float sr2 = float(A.sink_rate) * __expf(-(q2 * q2 * q2) * inv_s6);
+            float i1 = rsqrtf(q1 + F.rs2), i2 = rsqrtf(q2 + F.rs2);
+            float g1 = -bf[0] * i1 * i1 * i1;
+            float g2 = -bf[3] * i2 * i2 * i2;
+            float sr1 = F.sink_rate * __expf(-(q1 * q1 * q1) * F.inv_s6);
+            float sr2 = F.sink_rate * __expf(-(q2 * q2 * q2) * F.inv_s6);
             float r2 = fmaf(x, x, y * y);
             float rinv = rsqrtf(r2);
             float rr = r2 * rinv;
             // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
-            float br = float(A.buffer_rate) * __frcp_rn(1.0f + __expf(-2.0f * (rr - float(A.R)) * float(1.0 / A.buffer_scale)));
-            float vp = sqrtf(rsqrtf(r2 + rs2)) - om * rr;
+            float br = F.buffer_rate * __frcp_rn(1.0f + __expf((rr - F.R) * F.neg2_inv_buffer_scale));
+            float vp = sqrtf(rsqrtf(r2 + F.rs2)) - F.omega * rr;
             float ui[3] = {1.0f, -vp * y * rinv, vp * x * rinv};
             float sig = pc[0];
-            float ax = g1 * dx1 + g2 * dx2 + om * om * x + 2.0f * om * float(pc[2]);
-            float ay = g1 * dy1 + g2 * dy2 + om * om * y - 2.0f * om * float(pc[1]);
+            float ax = g1 * dx1 + g2 * dx2 + F.omega2 * x + F.two_omega * float(pc[2]);
+            float ay = g1 * dy1 + g2 * dy2 + F.omega2 * y - F.two_omega * float(pc[1]);
             float src[3];
             for (int k = 0; k < 3; ++k) src[k] = -(uc[k] * (sr1 + sr2)) - (uc[k] - ui[k]) * br;
             src[1] = fmaf(sig, ax, src[1]);
             src[2] = fmaf(sig, ay, src[2]);
-            const float dtf = float(dt);
-            const float inv_dl = float(1.0 / A.dl);
             float du[3];
-            for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (float(dfx[k]) + float(dfy[k])) * inv_dl);
+            for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (float(dfx[k]) + float(dfy[k])) * F.inv_dl);
 
-            double out[3];
             if (KIND == K_MIX1 && A.d_out)
             {
                 for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
             }
             else
             {
+                double out[3];
                 for (int k = 0; k < 3; ++k)
                 {
                     float inc = KIND == K_MIX2 ? 0.5f * (__ldg(A.d1 + k * NN + idx) + du[k]) : du[k];
-                    out[k] = __ldg(A.u_in + k * NN + idx) + double(inc);
+                    out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
                     A.u_out[k * NN + idx] = out[k];
                 }
                 if (A.amax)
                 {
-                    float fs = float(out[0]);
+                    float fs = d2f(out[0]);
                     float inv = __frcp_rn(fs);
-                    float vx = float(out[1]) * inv, vy = float(out[2]) * inv;
-                    float cs = sqrtf(rsqrtf(r2 + rs2) * float(1.0 / (A.mach * A.mach)));
-                    float a = fmaxf(fabsf(vx) + cs, fabsf(vy) + cs);
-                    local_max = fmax(local_max, double(a));
+                    float vx = d2f(out[1]) * inv, vy = d2f(out[2]) * inv;
+                    float cs = sqrtf(rsqrtf(r2 + F.rs2) * F.inv_mach2);
+                    local_max_f = fmaxf(local_max_f, fmaxf(fabsf(vx), fabsf(vy)) + cs);
                 }
             }
         }
@@ -507,6 +552,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
 
     if (A.amax)
     {
+        if (sizeof(R) == sizeof(float)) local_max = double(local_max_f);
         for (int o = 16; o > 0; o >>= 1) local_max = fmax(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
         if ((tid & 31) == 0) S.wmax[tid >> 5] = local_max;
         __syncthreads();
@@ -583,11 +629,13 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
         int ki = i - int(bi) * n, kj = j - int(bj) * n;
         double x = 0.5 * (vertex(R, n, level, bi, ki) + vertex(R, n, level, bi, ki + 1));
         double y = 0.5 * (vertex(R, n, level, bj, kj) + vertex(R, n, level, bj, kj + 1));
-        double ph = -1.0 / sqrt((x * x + y * y) + rs2);
-        double r0 = sqrt(x * x + y * y);
-        double vp = sqrt(-ph) - omega * r0;
-        double vx = vp * (-y / r0);
-        double vy = vp * (x / r0);
+        // explicit round-to-nearest operations: bit-identical to the host formulae
+        double r2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+        double ph = __ddiv_rn(-1.0, __dsqrt_rn(__dadd_rn(r2, rs2)));
+        double r0 = __dsqrt_rn(r2);
+        double vp = __dadd_rn(__dsqrt_rn(-ph), -__dmul_rn(omega, r0));
+        double vx = __dmul_rn(vp, __ddiv_rn(-y, r0));
+        double vy = __dmul_rn(vp, __ddiv_rn(x, r0));
         double sig = 1.0;
         if (amplitude != 0.0)
         {
@@ -595,12 +643,14 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
             z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
             z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
             z ^= z >> 31;
-            double r = 2.0 * (double(z >> 11) * 0x1.0p-53) - 1.0;
-            sig = sig * (1.0 + amplitude * r);
+            double r = __dadd_rn(__dmul_rn(2.0, double(z >> 11) * 0x1.0p-53), -1.0);
+            sig = __dmul_rn(sig, __dadd_rn(1.0, __dmul_rn(amplitude, r)));
         }
+        vx = __dmul_rn(sig, vx);
+        vy = __dmul_rn(sig, vy);
         u[c] = sig;
-        u[NN + c] = sig * vx;
-        u[2 * NN + c] = sig * vy;
+        u[NN + c] = vx;
+        u[2 * NN + c] = vy;
     }
 }
 
@@ -693,6 +743,22 @@ Args base_args(const mara_minidisk_params* sd)
     A.buffer_rate = sd->buffer_rate;
     A.buffer_scale = sd->buffer_scale;
     A.theta = sd->plm_theta;
+    FloatConsts& f = A.f;
+    f.rs2 = float(A.rs2);
+    f.inv_mach2 = float(1.0 / (A.mach * A.mach));
+    f.half_nu = float(A.nu * 0.5);
+    f.half_inv_dl = float(0.5 / A.dl);
+    f.inv_dl = float(1.0 / A.dl);
+    f.theta = float(A.theta);
+    f.R = float(A.R);
+    f.dl = float(A.dl);
+    f.sink_rate = float(A.sink_rate);
+    f.inv_s6 = float(1.0 / A.s6);
+    f.buffer_rate = float(A.buffer_rate);
+    f.neg2_inv_buffer_scale = float(-2.0 / A.buffer_scale);
+    f.omega = float(A.omega);
+    f.omega2 = float(A.omega * A.omega);
+    f.two_omega = float(2.0 * A.omega);
     return A;
 }
 

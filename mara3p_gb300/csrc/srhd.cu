@@ -1,0 +1,259 @@
+// Special-relativistic hydrodynamics: conserved -> primitive recovery.
+//
+// srhd::recover_primitive (src/physics_srhd.hpp:231-285): Newton iteration on
+// the pressure, at most 50+1 iterations, converged when |f| < 1e-12 (or
+// < 1e-8 on the last iteration), starting from p = 0. One thread per zone;
+// zones are read with a (component stride, zone stride) pair so that both the
+// GPU's SoA layout and the reference's AoS tuples are accepted.
+//
+// The default-guess path is written with explicit round-to-nearest
+// intrinsics (__dadd_rn, __dmul_rn, __ddiv_rn, __dsqrt_rn) in the reference's
+// evaluation order, so no multiply-add is fused and every zone reproduces the
+// reference's FP64 result bit for bit.
+//
+// The learned path (mlp != nullptr) seeds Newton with the pressure predicted
+// by a 4-64-64-1 MLP evaluated in BF16 on the tensor cores (see srhd_mlp.cu);
+// the same Newton loop and stopping rule then polish in FP64. A zone that
+// does not converge within the seeded budget restarts from p = 0 with the
+// reference's full budget, so the guess changes the iteration count only.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include "common.cuh"
+#include "srhd_mlp.cuh"
+
+namespace mara {
+namespace srhd {
+
+struct Zone { double D, S1, S2, S3, tau; };
+
+// Newton on p from p_start (physics_srhd.hpp:231-285). Returns status
+// 0 ok / 1 not converged / 2 non-positive pressure; writes the primitive
+// (rho, u1, u2, u3, p) and the number of iterations run.
+__device__ inline int newton(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
+                             double prim[5], int& iterations)
+{
+    const double c2 = 1.0;
+    const double tol = 1e-12;
+    const double D = z.D, tau = z.tau;
+    const double SS = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(z.S1, z.S1)), __dmul_rn(z.S2, z.S2)),
+                                __dmul_rn(z.S3, z.S3));
+    const double Dc2 = __dmul_rn(D, c2);
+    const double gm1 = __dadd_rn(gm, -1.0);
+    const double b2max = 1.0 - 1e-10;
+    bool found = false;
+    int iteration = 0;
+    double W0 = 1.0;
+    double p = p_start;
+
+    while (iteration <= iter_max)
+    {
+        double Et = __dadd_rn(__dadd_rn(tau, p), Dc2);
+        double b2 = fmin(__ddiv_rn(__ddiv_rn(__dmul_rn(SS, c2), Et), Et), b2max);
+        double W2 = __ddiv_rn(1.0, __dadd_rn(1.0, -b2));
+        double W = __dsqrt_rn(W2);
+        double e = __ddiv_rn(__dadd_rn(__dadd_rn(tau, __dmul_rn(Dc2, __dadd_rn(1.0, -W))), __dmul_rn(p, __dadd_rn(1.0, -W2))),
+                             __dmul_rn(D, W));
+        double d = __ddiv_rn(D, W);
+        double h = __dadd_rn(__dadd_rn(c2, e), __ddiv_rn(p, d));
+        double a2 = __ddiv_rn(__dmul_rn(gm, p), __dmul_rn(d, h));
+        double f = __dadd_rn(__dmul_rn(__dmul_rn(d, e), gm1), -p);
+        double g = __dadd_rn(__dmul_rn(b2, a2), -1.0);
+
+        p = __dadd_rn(p, -__ddiv_rn(f, g));
+
+        if (fabs(f) < tol || (fabs(f) < tol * 1e4 && iteration == iter_max))
+        {
+            W0 = W;
+            found = true;
+            break;
+        }
+        ++iteration;
+    }
+    iterations = found ? iteration + 1 : iteration;
+    if (temperature_floor > 0.0)
+        p = fmax(p, __dmul_rn(__dmul_rn(temperature_floor, D), c2));
+    if (!found) return 1;
+    if (temperature_floor <= 0.0 && p <= 0.0) return 2;
+    double Et = __dadd_rn(__dadd_rn(tau, Dc2), p);
+    prim[0] = __ddiv_rn(D, W0);
+    prim[1] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S1), Et), 1.0);
+    prim[2] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S2), Et), 1.0);
+    prim[3] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S3), Et), 1.0);
+    prim[4] = p;
+    return 0;
+}
+
+struct C2PArgs
+{
+    const double* cons;
+    double* prim;
+    int64_t n, cs, zs;           // zone count, component stride, zone stride
+    double gamma, floor;
+    int32_t* iterations;
+    int32_t* status;
+    unsigned long long* failures;   // nullable: count of failed zones
+    const mlp::Weights* mlp;        // nullable
+    int refine32;                   // FP32 Newton iterations applied to the guess
+    int seeded_budget;              // FP64 Newton iterations allowed from the guess
+};
+
+__device__ inline void store(const C2PArgs& a, int64_t i, const double prim[5], int it, int st)
+{
+    double* o = a.prim + i * a.zs;
+    for (int k = 0; k < 5; ++k) o[k * a.cs] = st == 0 ? prim[k] : 0.0;
+    if (a.iterations) a.iterations[i] = it;
+    if (a.status) a.status[i] = st;
+    if (st != 0 && a.failures) atomicAdd(a.failures, 1ull);
+}
+
+__global__ void c2p_default_kernel(const C2PArgs a)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < a.n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        const double* c = a.cons + i * a.zs;
+        Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
+        double prim[5] = {0, 0, 0, 0, 0};
+        int it = 0;
+        int st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it);
+        store(a, i, prim, it, st);
+    }
+}
+
+// The same Newton update in FP32, used to sharpen a pressure guess cheaply
+// before the FP64 polish. Returns the guess unchanged if it goes bad.
+__device__ inline double refine_fp32(const Zone& z, double gm, double p0, int iters)
+{
+    const float D = float(z.D), tau = float(z.tau), g = float(gm);
+    const float SS = float(z.S1) * float(z.S1) + float(z.S2) * float(z.S2) + float(z.S3) * float(z.S3);
+    float p = float(p0);
+    for (int k = 0; k < iters; ++k)
+    {
+        float Et = tau + p + D;
+        float b2 = fminf(SS / (Et * Et), 1.0f - 1e-7f);
+        float W2 = 1.0f / (1.0f - b2);
+        float W = sqrtf(W2);
+        float e = (tau + D * (1.0f - W) + p * (1.0f - W2)) / (D * W);
+        float d = D / W;
+        float h = 1.0f + e + p / d;
+        float a2 = g * p / (d * h);
+        float f = d * e * (g - 1.0f) - p;
+        float gg = b2 * a2 - 1.0f;
+        float pn = p - f / gg;
+        if (!(pn > 0.0f) || !isfinite(pn)) break;
+        p = pn;
+    }
+    return double(p);
+}
+
+__device__ inline void polish(const C2PArgs& a, int64_t i, const Zone& z, double guess)
+{
+    if (a.refine32 > 0) guess = refine_fp32(z, a.gamma, guess, a.refine32);
+    double prim[5] = {0, 0, 0, 0, 0};
+    int it = 0, it2 = 0;
+    int st = newton(z, a.gamma, a.floor, guess, a.seeded_budget, prim, it);
+    if (st != 0)
+    {
+        // fall back to the reference's start and budget
+        st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it2);
+        it += it2;
+    }
+    store(a, i, prim, it, st);
+}
+
+// No network: start from p = 0, sharpen in FP32, polish in FP64.
+__global__ void c2p_refined_kernel(const C2PArgs a)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < a.n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        const double* c = a.cons + i * a.zs;
+        Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
+        polish(a, i, z, 0.0);
+    }
+}
+
+// Learned guess: the MLP predicts p for kZones zones per CTA (srhd_mlp.cuh),
+// then each thread polishes its zone.
+__global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
+{
+    __shared__ mlp::Shared sm;
+    mlp::load_weights(*a.mlp, sm);
+    for (int64_t base = int64_t(blockIdx.x) * mlp::kZones; base < a.n; base += int64_t(gridDim.x) * mlp::kZones)
+    {
+        __syncthreads();
+        for (int t = threadIdx.x; t < mlp::kZones; t += blockDim.x)
+        {
+            int64_t i = base + t;
+            float feat[4] = {0.f, 0.f, 0.f, 0.f};
+            if (i < a.n)
+            {
+                const double* c = a.cons + i * a.zs;
+                mlp::features(c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs], feat);
+            }
+            mlp::stage_features(sm, t, feat);
+        }
+        __syncthreads();
+        mlp::forward(sm);
+        __syncthreads();
+        for (int t = threadIdx.x; t < mlp::kZones; t += blockDim.x)
+        {
+            int64_t i = base + t;
+            if (i >= a.n) continue;
+            const double* c = a.cons + i * a.zs;
+            Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
+            polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.tau));
+        }
+    }
+}
+
+} // namespace srhd
+} // namespace mara
+
+using namespace mara;
+
+extern "C" {
+
+int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component_stride, int64_t zone_stride,
+                                double gamma_law_index, double temperature_floor, const void* mlp_weights,
+                                int32_t refine32, int32_t seeded_budget, double* prim, int32_t* iterations,
+                                int32_t* status, unsigned long long* failures, void* stream)
+{
+    MARA_REQUIRE(n >= 0, "mara_srhd_recover_primitive: negative zone count");
+    if (n == 0) return MARA_OK;
+    MARA_REQUIRE(cons && prim, "mara_srhd_recover_primitive: null buffer");
+    MARA_REQUIRE(component_stride > 0 && zone_stride > 0, "mara_srhd_recover_primitive: strides must be positive");
+    MARA_REQUIRE(gamma_law_index > 1.0, "mara_srhd_recover_primitive: gamma_law_index must exceed 1");
+    MARA_REQUIRE(refine32 >= 0 && refine32 <= 16, "mara_srhd_recover_primitive: refine32 must be in [0, 16]");
+    const bool seeded = mlp_weights != nullptr || refine32 > 0;
+    MARA_REQUIRE(!seeded || (seeded_budget >= 1 && seeded_budget <= 50),
+                 "mara_srhd_recover_primitive: seeded_budget must be in [1, 50]");
+    srhd::C2PArgs a;
+    a.cons = cons;
+    a.prim = prim;
+    a.n = n;
+    a.cs = component_stride;
+    a.zs = zone_stride;
+    a.gamma = gamma_law_index;
+    a.floor = temperature_floor;
+    a.iterations = iterations;
+    a.status = status;
+    a.failures = failures;
+    a.mlp = static_cast<const mlp::Weights*>(mlp_weights);
+    a.refine32 = refine32;
+    a.seeded_budget = seeded_budget;
+    cudaStream_t s = as_stream(stream);
+    if (mlp_weights == nullptr)
+    {
+        int blocks = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
+        if (refine32 == 0)
+            srhd::c2p_default_kernel<<<blocks, 256, 0, s>>>(a);
+        else
+            srhd::c2p_refined_kernel<<<blocks, 256, 0, s>>>(a);
+        return launch_status("c2p kernel");
+    }
+    int blocks = int(std::min<int64_t>((n + mlp::kZones - 1) / mlp::kZones, 152 * 8));
+    srhd::c2p_mlp_kernel<<<blocks, mlp::kThreads, 0, s>>>(a);
+    return launch_status("c2p_mlp_kernel");
+}
+
+} // extern "C"

@@ -1,0 +1,102 @@
+"""Host-side mirror of the reference's SRHD primitive recovery
+(src/physics_srhd.hpp:231-285, srhd::recover_primitive) plus the learned
+pressure guess. Arrays are torch CUDA tensors; zones are SoA (5, n) unless a
+stride pair says otherwise."""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import torch
+
+from ._capi import check, lib
+
+STATUS_OK, STATUS_NOT_CONVERGED, STATUS_NEGATIVE_PRESSURE = 0, 1, 2
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _f64(t: torch.Tensor) -> int:
+    if not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError("expected a contiguous CUDA float64 tensor")
+    return t.data_ptr()
+
+
+@dataclass
+class Recovery:
+    prim: torch.Tensor          # (5, n): rho, u1, u2, u3, p
+    iterations: torch.Tensor    # (n,) int32, FP64 Newton iterations
+    status: torch.Tensor        # (n,) int32
+
+
+def recover_primitive(cons: torch.Tensor, gamma_law_index: float = 4.0 / 3.0, temperature_floor: float = 0.0,
+                      mlp: "PressureGuess | None" = None, refine32: int = 0, seeded_budget: int = 12,
+                      layout: str = "soa") -> Recovery:
+    """srhd::recover_primitive over many zones. cons is (5, n) for layout 'soa'
+    or (n, 5) for 'aos' (the reference's tuple layout)."""
+    if layout == "soa":
+        n = cons.shape[1]
+        cs, zs = n, 1
+    elif layout == "aos":
+        n = cons.shape[0]
+        cs, zs = 1, 5
+    else:
+        raise ValueError("layout must be 'soa' or 'aos'")
+    prim = torch.empty_like(cons)
+    it = torch.empty(n, dtype=torch.int32, device=cons.device)
+    st = torch.empty(n, dtype=torch.int32, device=cons.device)
+    check(lib.mara_srhd_recover_primitive(_f64(cons), n, cs, zs, gamma_law_index, temperature_floor,
+                                          mlp.weights.data_ptr() if mlp else None, refine32, seeded_budget,
+                                          prim.data_ptr(), it.data_ptr(), st.data_ptr(), None, _stream()),
+          "srhd recover_primitive")
+    return Recovery(prim, it, st)
+
+
+class PressureGuess:
+    """The 4-64-64-1 MLP that seeds the recovery, trained on the GPU by the
+    library's own kernels on (conserved, primitive) pairs."""
+
+    def __init__(self, device="cuda"):
+        self.weights = torch.zeros(lib.mara_srhd_mlp_weights_bytes(), dtype=torch.uint8, device=device)
+        self.workspace = None
+        self.n = 0
+
+    def prepare(self, cons: torch.Tensor, prim: torch.Tensor, seed: int = 0) -> None:
+        n = cons.shape[1]
+        self.n = n
+        self.workspace = torch.empty(lib.mara_srhd_mlp_workspace_bytes(n), dtype=torch.uint8, device=cons.device)
+        check(lib.mara_srhd_mlp_prepare(_f64(cons), _f64(prim), n, self.weights.data_ptr(), seed,
+                                        self.workspace.data_ptr(), _stream()), "mlp prepare")
+
+    def gradient(self) -> tuple[torch.Tensor, float]:
+        grad = torch.empty(lib.mara_srhd_mlp_param_count(), dtype=torch.float32, device=self.weights.device)
+        loss = torch.empty(1, dtype=torch.float32, device=self.weights.device)
+        check(lib.mara_srhd_mlp_gradient(self.weights.data_ptr(), self.workspace.data_ptr(), self.n,
+                                         grad.data_ptr(), loss.data_ptr(), _stream()), "mlp gradient")
+        return grad, float(loss.item())
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 2e-3, seed: int = 0) -> torch.Tensor:
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        order = torch.randperm(self.n, generator=g).to(self.weights.device, torch.int64)
+        hist = torch.empty(max(steps, 1), dtype=torch.float32, device=self.weights.device)
+        check(lib.mara_srhd_mlp_train(self.weights.data_ptr(), self.workspace.data_ptr(), self.n,
+                                      order.data_ptr(), steps, batch, lr, hist.data_ptr(), _stream()),
+              "mlp train")
+        return hist[:steps]
+
+    def infer(self, features: torch.Tensor) -> torch.Tensor:
+        y = torch.empty(features.shape[0], dtype=torch.float32, device=features.device)
+        check(lib.mara_srhd_mlp_infer(self.weights.data_ptr(), features.data_ptr(), features.shape[0],
+                                      y.data_ptr(), _stream()), "mlp infer")
+        return y
+
+    def parameters_f32(self) -> dict:
+        """Host copy of the FP32 parameters (for checks against the CPU oracle)."""
+        raw = self.weights.cpu().numpy()
+        f = raw[: (len(raw) // 4) * 4].view("float32")
+        o = {"norm_shift": f[0:4], "norm_scale": f[4:8], "w1": f[8:264].reshape(64, 4), "b1": f[264:328],
+             "w2": f[328:4424].reshape(64, 64), "b2": f[4424:4488], "w3": f[4488:4552], "b3": f[4552],
+             "out_shift": f[4553], "out_scale": f[4554]}
+        return o

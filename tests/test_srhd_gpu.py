@@ -1,0 +1,175 @@
+"""GPU parity of SRHD primitive recovery (through the C ABI) against the
+reference's golden fixtures and the oracle; the learned pressure guess:
+gradients against the CPU oracle, training, BF16 inference, and what the
+trained network gains over recovery without it."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import dptr, iptr
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+GAMMA = 4.0 / 3.0
+
+
+@pytest.fixture(scope="module")
+def sr():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import mara3p_gb300.srhd as s
+    return s
+
+
+def seeded_zones(oracle, n, seed=4242):
+    prim = np.zeros(5 * n)
+    cons = np.zeros(5 * n)
+    oracle.oracle_srhd_seeded_zones(ctypes.c_uint64(seed), ctypes.c_int64(n), ctypes.c_double(1e-4),
+                                    ctypes.c_double(1.0), ctypes.c_double(1e-6), ctypes.c_double(10.0),
+                                    ctypes.c_double(50.0), ctypes.c_double(GAMMA), dptr(prim), dptr(cons))
+    return prim, cons
+
+
+def oracle_recover(oracle, cons_aos, p_start=None):
+    n = cons_aos.size // 5
+    prim = np.zeros_like(cons_aos)
+    it = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    oracle.oracle_srhd_recover_primitive(dptr(cons_aos), ctypes.c_int64(n), ctypes.c_double(GAMMA), ctypes.c_double(0.0),
+                                         None if p_start is None else dptr(p_start), dptr(prim), iptr(it), iptr(st))
+    return prim, it, st
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_default_recovery_bitexact_with_reference(sr, srhd_golden, layout):
+    cons = srhd_golden["srhd/cons"].reshape(-1, 5)
+    t = torch.from_numpy(cons.T.copy() if layout == "soa" else cons.copy()).cuda()
+    r = sr.recover_primitive(t, GAMMA, layout=layout)
+    prim = r.prim.cpu().numpy()
+    prim = prim.T if layout == "soa" else prim
+    assert np.array_equal(prim.ravel(), srhd_golden["srhd/recovered"])
+    assert np.array_equal(r.status.cpu().numpy(), srhd_golden["srhd/status"])
+
+
+def test_default_recovery_iterations_match_oracle(sr, oracle):
+    _, cons = seeded_zones(oracle, 1 << 16, seed=9)
+    _, it, st = oracle_recover(oracle, cons)
+    r = sr.recover_primitive(torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda(), GAMMA)
+    assert np.array_equal(r.iterations.cpu().numpy(), it)
+    assert np.array_equal(r.status.cpu().numpy(), st)
+    assert 4.0 < it.mean() < 6.0
+
+
+def test_reference_known_answers(sr, srhd_golden):
+    """test_srhd round trips (src/physics_srhd.hpp:528-537) on the GPU."""
+    kat = srhd_golden["srhd_kat/prim"].reshape(-1, 5)
+    cons = torch.from_numpy(srhd_golden["srhd_kat/cons"].reshape(-1, 5).copy()).cuda()
+    r = sr.recover_primitive(cons, GAMMA, layout="aos")
+    assert np.all(np.abs(r.prim.cpu().numpy() - kat) < 1e-10)
+
+
+def test_failure_statuses_match_reference_semantics(sr, oracle):
+    """Zones the reference rejects: negative pressure -> status 2 with zero
+    primitives; the status agrees with the oracle zone by zone."""
+    cons = np.array([[1.0, 0.0, 0.0, 0.0, -0.5],       # tau < 0: negative pressure
+                     [1.0, 0.3, 0.0, 0.0, 2.0],        # regular
+                     [1e-3, 5.0, 0.0, 0.0, 1e-9]]).ravel()  # |S| >> tau + D
+    prim_o, it_o, st_o = oracle_recover(oracle, cons)
+    r = sr.recover_primitive(torch.from_numpy(cons.reshape(-1, 5).copy()).cuda(), GAMMA, layout="aos")
+    assert np.array_equal(r.status.cpu().numpy(), st_o)
+    assert st_o[0] == 2 and st_o[1] == 0
+    assert np.array_equal(r.prim.cpu().numpy().ravel(), prim_o)
+
+
+def test_empty_batch(sr):
+    r = sr.recover_primitive(torch.empty((5, 0), dtype=torch.float64, device="cuda"), GAMMA)
+    assert r.prim.shape == (5, 0)
+
+
+@pytest.fixture(scope="module")
+def trained(sr, oracle):
+    """Train the pressure guess on pairs from the library's own FP64 recovery."""
+    _, cons = seeded_zones(oracle, 1 << 18, seed=77)
+    c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
+    rec = sr.recover_primitive(c, GAMMA)
+    assert int((rec.status != 0).sum()) == 0
+    net = sr.PressureGuess()
+    net.prepare(c, rec.prim, seed=1)
+    hist = net.train(steps=3000, batch=8192, lr=2e-3, seed=1)
+    torch.cuda.synchronize()
+    return net, c, rec, hist.cpu().numpy()
+
+
+def test_mlp_gradient_matches_cpu_oracle(sr, oracle):
+    from oracle.mlp_oracle import loss_and_gradient, raw_features
+    _, cons = seeded_zones(oracle, 4096, seed=123)
+    c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
+    rec = sr.recover_primitive(c, GAMMA)
+    net = sr.PressureGuess()
+    net.prepare(c, rec.prim, seed=3)
+    grad, loss = net.gradient()
+    p = net.parameters_f32()
+    cons_soa = cons.reshape(-1, 5).T
+    feat = raw_features(cons_soa)
+    target = np.log(rec.prim[4].cpu().numpy() / (cons_soa[4] + cons_soa[0])).astype(np.float32)
+    ref_loss, ref_grad = loss_and_gradient(p, feat, target)
+    g = grad.cpu().numpy().astype(np.float64)
+    assert abs(loss - ref_loss) <= 1e-4 * abs(ref_loss)
+    assert np.linalg.norm(g - ref_grad) <= 1e-3 * np.linalg.norm(ref_grad)
+
+
+def test_mlp_training_reduces_loss(trained):
+    _, _, _, hist = trained
+    assert np.all(np.isfinite(hist))
+    assert hist[-200:].mean() < 0.05 * hist[:20].mean()
+
+
+def test_mlp_bf16_inference_matches_fp32_oracle(sr, trained):
+    from oracle.mlp_oracle import forward, raw_features
+    net, c, rec, _ = trained
+    sub = c[:, :8192].contiguous()
+    feat = raw_features(sub.cpu().numpy())
+    y = net.infer(torch.from_numpy(feat).cuda()).cpu().numpy()
+    *_, ref = forward(net.parameters_f32(), feat)
+    # BF16 operands in layer 2 and tanh.approx: |dy| well under the target spread
+    assert np.abs(y - ref).max() < 0.05
+    assert np.abs(y - ref).mean() < 0.01
+
+
+def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
+    """The learned guess changes the FP64 Newton iteration count, never the
+    answer: primitives agree with the default recovery to 1e-10 relative."""
+    net, _, _, _ = trained
+    _, cons = seeded_zones(oracle, 1 << 18, seed=2024)
+    c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
+    base = sr.recover_primitive(c, GAMMA)
+    seeded = sr.recover_primitive(c, GAMMA, mlp=net, refine32=2)
+    assert int((seeded.status != 0).sum()) == 0
+    a, b = base.prim.cpu().numpy(), seeded.prim.cpu().numpy()
+    rel = np.abs(a - b) / np.maximum(np.abs(a), 1e-300)
+    assert np.max(rel[[0, 4]]) < 1e-10
+    big = np.abs(a[1:4]) > 1e-8
+    assert np.max(rel[1:4][big]) < 1e-9
+    mean_base = base.iterations.float().mean().item()
+    mean_seeded = seeded.iterations.float().mean().item()
+    assert mean_seeded * 2.0 <= mean_base, (mean_base, mean_seeded)
+
+
+def test_mlp_gain_over_no_network(sr, oracle, trained):
+    """What the trained network adds: at the same FP32 refinement budget,
+    starting from its guess needs fewer FP64 Newton iterations than starting
+    from p = 0, and so does the guess alone vs the reference's start."""
+    net, _, _, _ = trained
+    _, cons = seeded_zones(oracle, 1 << 18, seed=31337)
+    c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
+    means = {}
+    for name, kw in {"default": {}, "refine_only": dict(refine32=2), "mlp_only": dict(mlp=net),
+                     "mlp_refine": dict(mlp=net, refine32=2)}.items():
+        r = sr.recover_primitive(c, GAMMA, **kw)
+        assert int((r.status != 0).sum()) == 0
+        means[name] = r.iterations.float().mean().item()
+    assert means["mlp_only"] < means["default"]
+    assert means["mlp_refine"] < means["refine_only"]
