@@ -169,6 +169,31 @@ int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const doub
 int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int32_t dt_mode,
                                int32_t rk_order, int32_t end_step, int32_t begin_step, void* stream);
 
+/* Allocation-free form of mara_minidisk_advance (no counterpart in the
+ * reference). For callers that cannot allocate device memory — a host that
+ * has given all of the GPU's memory to its own pool allocator, or a plugin
+ * that only receives the caller's state and clock buffers through this ABI —
+ * the workspace comes from a static device array inside the library instead
+ * of a caller-owned buffer. Limits and rules:
+ *   - the mesh may hold at most MARA_MINIDISK_NOALLOC_MAX_CELLS cells
+ *     ((block_size << depth)^2); larger meshes are rejected with
+ *     MARA_ERR_ARGUMENT and a message naming the limit;
+ *   - the array (36 bytes per cell of that limit, 9 MiB) is held by every GPU
+ *     that loads the library until the process exits;
+ *   - the first call on a device looks up the array's device address with
+ *     that device current (cudaGetSymbolAddress); make that first call before
+ *     any stream capture;
+ *   - all calls share the one array: calls whose GPU work overlaps (other
+ *     streams, other threads) race and corrupt each other's results.
+ *     Nothing in it needs to start at zero: every step writes its scratch
+ *     before reading it.
+ * No cudaMalloc/cudaFree or allocating library routine is called. u and
+ * clock are caller-owned device buffers as for mara_minidisk_advance. */
+#define MARA_MINIDISK_NOALLOC_MAX_CELLS (512 * 512)
+int mara_minidisk_advance_noalloc(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                                  int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                                  void* stream);
+
 /* ---------------------------------------------------------------- srhd */
 
 /* Conserved -> primitive recovery of n zones, replacing srhd::recover_primitive

@@ -75,6 +75,8 @@ SIGNATURES = {
                                            ctypes.c_int32, _vp]),
     "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp]),
+    "mara_minidisk_advance_noalloc": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                     ctypes.c_int32, _vp]),
     "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                                    ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int32,
                                                    ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include "common.cuh"
 
 namespace mara {
@@ -1077,3 +1078,59 @@ int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clo
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------- allocation-free advance
+// Some callers cannot allocate device memory for a workspace: a host program
+// that has handed all of the GPU's memory to its own pool allocator, or a
+// plugin that only ever receives the caller's state and clock buffers through
+// the C ABI and has no allocator of its own to call. For them the scratch of
+// mara_minidisk_advance lives in this file-scope device array instead. It is
+// sized for meshes of at most MARA_MINIDISK_NOALLOC_MAX_CELLS cells (36 bytes
+// per cell: one FP64 state buffer plus the FP32 RK2 increment), and every GPU
+// that loads the library holds it until the process exits.
+namespace {
+
+constexpr int64_t kNoAllocBytesPerCell = 3 * (sizeof(double) + sizeof(float));
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MARA_MINIDISK_NOALLOC_MAX_CELLS * kNoAllocBytesPerCell];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[64] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (with that device current). In host code the symbol itself is
+// only a host-side stand-in and must never be passed to a kernel.
+int noalloc_scratch(void** out)
+{
+    int dev = 0;
+    MARA_CUDA(cudaGetDevice(&dev));
+    MARA_REQUIRE(dev >= 0 && dev < 64, "mara_minidisk_advance_noalloc: device index above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_address[dev] == nullptr)
+    {
+        void* p = nullptr;
+        MARA_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_address[dev] = p;
+    }
+    *out = g_noalloc_address[dev];
+    return MARA_OK;
+}
+
+} // namespace
+
+extern "C" int mara_minidisk_advance_noalloc(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                                             int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                                             void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    const int64_t cells = int64_t(sd->block_size << sd->depth) * int64_t(sd->block_size << sd->depth);
+    if (cells > MARA_MINIDISK_NOALLOC_MAX_CELLS)
+        return fail(MARA_ERR_ARGUMENT, "mara_minidisk_advance_noalloc: mesh of " + std::to_string(cells) +
+                    " cells exceeds the static scratch limit of " + std::to_string(MARA_MINIDISK_NOALLOC_MAX_CELLS) +
+                    " cells (use mara_minidisk_advance with a caller-owned workspace)");
+    const int64_t need = mara_minidisk_workspace_bytes(sd, rk_order, precision);
+    MARA_REQUIRE(need >= 0 && need <= int64_t(sizeof(g_noalloc_scratch)),
+                 "mara_minidisk_advance_noalloc: workspace larger than the static scratch");
+    void* scratch = nullptr;
+    if (int r = noalloc_scratch(&scratch)) return r;
+    return mara_minidisk_advance(sd, u, clock, steps, rk_order, precision, dt_mode, scratch, stream);
+}
