@@ -295,8 +295,8 @@ def run_ours(args):
             traffic = float(tk["bytes_per_cell"]) * cells
     step_bytes = (STAGE_BYTES[(pname, 1)] + STAGE_BYTES[(pname, 2)]) * cells
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": f"stage_kernel<{'float' if prec == md.MIXED else 'double'}, "
-                                             f"stage {dominant}>",
+                "traffic": traffic,
+                "kernel": f"sweep_kernel<{dominant}>" if prec == md.MIXED else f"stage_kernel<double, 0> (stage {dominant})",
                 "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "peak_source": f"{peak_kind} hbm_gbs",
                 "stage_ms": [s1, s2],
                 "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}

@@ -53,6 +53,7 @@ struct Args
     int n;                 // block size (zones per block side)
     int level;             // block level (2^level blocks per side)
     int tiles_y;
+    int sweep_rows;        // mixed sweep: rows per warp
     uint64_t bi, bj;       // K_BLOCK: block coordinates
     double R, dl;
     double rs2;            // softening_length^2 (std::pow(rs, 2.0) on the host)
@@ -72,17 +73,21 @@ struct Args
 };
 
 // double -> float (round to nearest even) and float -> double (exact) with
-// integer instructions; values outside the normal float range take the
-// hardware conversion.
+// integer instructions only, so that the mixed path issues no FP64-pipe work
+// for them. Magnitudes below the smallest normal float (1.2e-38) become signed
+// zero; overflow gives infinity; NaN stays NaN.
 __device__ inline float d2f(double x)
 {
     const unsigned long long b = __double_as_longlong(x);
     const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
+    const unsigned sign = hi & 0x80000000u;
     const unsigned e = (hi >> 20) & 0x7FFu;
-    if (e < 897u || e > 1150u) return __double2float_rn(x);
-    unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    unsigned f = sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
     const unsigned rest = lo & 0x1FFFFFFFu;
     f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    const bool nan = e == 0x7FFu && ((hi & 0xFFFFFu) | lo) != 0u;
+    f = e < 897u ? sign : f;
+    f = e > 1150u ? (sign | (nan ? 0x7FC00000u : 0x7F800000u)) : f;
     return __uint_as_float(f);
 }
 
@@ -90,9 +95,43 @@ __device__ inline double f2d(float x)
 {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xFFu;
-    if (e == 0u || e == 255u) return double(x);
-    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
-    return __hiloint2double(int(hi), int(b << 29));
+    const unsigned m = b & 0x7FFFFFu;
+    const unsigned ee = e == 255u ? 2047u : e + 896u;
+    unsigned hi = (b & 0x80000000u) | (ee << 20) | (m >> 3);
+    unsigned lo = m << 29;
+    hi = e == 0u ? (b & 0x80000000u) : hi;
+    lo = e == 0u ? 0u : lo;
+    return __hiloint2double(int(hi), int(lo));
+}
+
+// Single-MUFU approximations for the mixed path (relative error ~1e-7,
+// well inside the FP32 budget of the fluxes; denormals flush to zero).
+__device__ inline float rcp_fast(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float sqrt_fast(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float rsqrt_fast(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float exp_fast(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+    return y;
 }
 
 // ------------------------------------------------------------- geometry
@@ -201,9 +240,9 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
         L[k] = fmaf(0.5f, ga[k], pa[k]);
         Rr[k] = fmaf(-0.5f, gb[k], pb[k]);
     }
-    float rinv = rsqrtf(fmaf(x, x, fmaf(y, y, A.f.rs2)));
+    float rinv = rsqrt_fast(fmaf(x, x, fmaf(y, y, A.f.rs2)));
     float cs2 = rinv * A.f.inv_mach2;
-    float cs = sqrtf(cs2);
+    float cs = sqrt_fast(cs2);
     float vl = AXIS == 0 ? L[1] : L[2];
     float vr = AXIS == 0 ? Rr[1] : Rr[2];
     float ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
@@ -213,7 +252,7 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
     float fr[3] = {vr * ur[0], fmaf(vr, ur[1], AXIS == 0 ? pgr : 0.0f), fmaf(vr, ur[2], AXIS == 0 ? 0.0f : pgr)};
     float ap = fmaxf(0.0f, fmaxf(vl, vr) + cs);
     float am = fminf(0.0f, fminf(vl, vr) - cs);
-    float inv = __frcp_rn(ap - am);
+    float inv = rcp_fast(ap - am);
     float apam = ap * am;
     for (int k = 0; k < 3; ++k)
         F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * apam) * inv;
@@ -236,6 +275,63 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
             F[1] -= mu * (vy_tran + vx_long);
             F[2] += mu * (vx_tran - vy_long);
         }
+    }
+}
+
+// ------------------------------------------------------------- mixed cell update
+// Flux divergence, sources and stage update of one cell in the mixed path
+// (FP32 arithmetic, FP64 state): gravity of both point masses, sinks,
+// rotating-frame terms and the outer buffer (problems/minidisk_scheme.cpp:337-352).
+template<int KIND>
+__device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
+                                  const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
+                                  float& local_max)
+{
+    const FloatConsts& F = A.f;
+    float uc[3] = {pc[0], pc[0] * pc[1], pc[0] * pc[2]};
+    float dx1 = x - bf[1], dy1 = y - bf[2];
+    float dx2 = x - bf[4], dy2 = y - bf[5];
+    float q1 = fmaf(dx1, dx1, dy1 * dy1), q2 = fmaf(dx2, dx2, dy2 * dy2);
+    float i1 = rsqrt_fast(q1 + F.rs2), i2 = rsqrt_fast(q2 + F.rs2);
+    float g1 = -bf[0] * i1 * i1 * i1;
+    float g2 = -bf[3] * i2 * i2 * i2;
+    float sr1 = F.sink_rate * exp_fast(-(q1 * q1 * q1) * F.inv_s6);
+    float sr2 = F.sink_rate * exp_fast(-(q2 * q2 * q2) * F.inv_s6);
+    float r2 = fmaf(x, x, y * y);
+    float rinv = rsqrt_fast(r2);
+    float rr = r2 * rinv;
+    // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
+    float br = F.buffer_rate * rcp_fast(1.0f + exp_fast((rr - F.R) * F.neg2_inv_buffer_scale));
+    float vp = sqrt_fast(rsqrt_fast(r2 + F.rs2)) - F.omega * rr;
+    float ui[3] = {1.0f, -vp * y * rinv, vp * x * rinv};
+    float sig = pc[0];
+    float ax = g1 * dx1 + g2 * dx2 + F.omega2 * x + F.two_omega * pc[2];
+    float ay = g1 * dy1 + g2 * dy2 + F.omega2 * y - F.two_omega * pc[1];
+    float src[3];
+    for (int k = 0; k < 3; ++k) src[k] = -(uc[k] * (sr1 + sr2)) - (uc[k] - ui[k]) * br;
+    src[1] = fmaf(sig, ax, src[1]);
+    src[2] = fmaf(sig, ay, src[2]);
+    float du[3];
+    for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (dfx[k] + dfy[k]) * F.inv_dl);
+
+    if (KIND == K_MIX1 && A.d_out)
+    {
+        for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
+        return;
+    }
+    double out[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        float inc = KIND == K_MIX2 ? 0.5f * (__ldg(A.d1 + k * NN + idx) + du[k]) : du[k];
+        out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
+        A.u_out[k * NN + idx] = out[k];
+    }
+    if (A.amax)
+    {
+        float inv = rcp_fast(d2f(out[0]));
+        float vx = d2f(out[1]) * inv, vy = d2f(out[2]) * inv;
+        float cs = sqrt_fast(rsqrt_fast(r2 + F.rs2) * F.inv_mach2);
+        local_max = fmaxf(local_max, fmaxf(fabsf(vx), fabsf(vy)) + cs);
     }
 }
 
@@ -337,7 +433,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
                 {
                     fs += __ldg(A.d1 + idx); f1 += __ldg(A.d1 + NN + idx); f2 += __ldg(A.d1 + 2 * NN + idx);
                 }
-                float inv = __frcp_rn(fs);
+                float inv = rcp_fast(fs);
                 p0 = R(fs); p1 = R(f1 * inv); p2 = R(f2 * inv);
             }
         }
@@ -497,57 +593,11 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
         }
         else
         {
-            const FloatConsts& F = A.f;
-            const float x = float(S.xc[i]), y = float(S.yc[j]);
             size_t idx = size_t(gi) * N + gj;
-            float uc[3] = {float(pc[0]), float(pc[0]) * float(pc[1]), float(pc[0]) * float(pc[2])};
-            float dx1 = x - bf[1], dy1 = y - bf[2];
-            float dx2 = x - bf[4], dy2 = y - bf[5];
-            float q1 = fmaf(dx1, dx1, dy1 * dy1), q2 = fmaf(dx2, dx2, dy2 * dy2);
-            float i1 = rsqrtf(q1 + F.rs2), i2 = rsqrtf(q2 + F.rs2);
-            float g1 = -bf[0] * i1 * i1 * i1;
-            float g2 = -bf[3] * i2 * i2 * i2;
-            float sr1 = F.sink_rate * __expf(-(q1 * q1 * q1) * F.inv_s6);
-            float sr2 = F.sink_rate * __expf(-(q2 * q2 * q2) * F.inv_s6);
-            float r2 = fmaf(x, x, y * y);
-            float rinv = rsqrtf(r2);
-            float rr = r2 * rinv;
-            // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
-            float br = F.buffer_rate * __frcp_rn(1.0f + __expf((rr - F.R) * F.neg2_inv_buffer_scale));
-            float vp = sqrtf(rsqrtf(r2 + F.rs2)) - F.omega * rr;
-            float ui[3] = {1.0f, -vp * y * rinv, vp * x * rinv};
-            float sig = pc[0];
-            float ax = g1 * dx1 + g2 * dx2 + F.omega2 * x + F.two_omega * float(pc[2]);
-            float ay = g1 * dy1 + g2 * dy2 + F.omega2 * y - F.two_omega * float(pc[1]);
-            float src[3];
-            for (int k = 0; k < 3; ++k) src[k] = -(uc[k] * (sr1 + sr2)) - (uc[k] - ui[k]) * br;
-            src[1] = fmaf(sig, ax, src[1]);
-            src[2] = fmaf(sig, ay, src[2]);
-            float du[3];
-            for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (float(dfx[k]) + float(dfy[k])) * F.inv_dl);
-
-            if (KIND == K_MIX1 && A.d_out)
-            {
-                for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
-            }
-            else
-            {
-                double out[3];
-                for (int k = 0; k < 3; ++k)
-                {
-                    float inc = KIND == K_MIX2 ? 0.5f * (__ldg(A.d1 + k * NN + idx) + du[k]) : du[k];
-                    out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
-                    A.u_out[k * NN + idx] = out[k];
-                }
-                if (A.amax)
-                {
-                    float fs = d2f(out[0]);
-                    float inv = __frcp_rn(fs);
-                    float vx = d2f(out[1]) * inv, vy = d2f(out[2]) * inv;
-                    float cs = sqrtf(rsqrtf(r2 + F.rs2) * F.inv_mach2);
-                    local_max_f = fmaxf(local_max_f, fmaxf(fabsf(vx), fabsf(vy)) + cs);
-                }
-            }
+            const float p3[3] = {float(pc[0]), float(pc[1]), float(pc[2])};
+            const float fx3[3] = {float(dfx[0]), float(dfx[1]), float(dfx[2])};
+            const float fy3[3] = {float(dfy[0]), float(dfy[1]), float(dfy[2])};
+            mixed_cell<KIND>(A, float(S.xc[i]), float(S.yc[j]), p3, fx3, fy3, bf, dtf, idx, NN, local_max_f);
         }
     }
 
@@ -564,6 +614,187 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
             atomicMax(A.amax, (unsigned long long)__double_as_longlong(m));
         }
     }
+}
+
+// ------------------------------------------------------------- warp-strip sweep (mixed path)
+// One warp updates a strip of SW_COLS columns (its 32 lanes hold columns
+// j0-2 .. j0+29: two halo columns each side) over A.sweep_rows rows, marching
+// along x. A three-row window of primitives, the x and y slopes of two rows
+// and the previous x-face flux stay in registers; y neighbours come from warp
+// shuffles. Every x face and y face of the strip is computed once, with no
+// shared memory and no barrier. Requires N >= 64 (halo wrap by one period).
+constexpr int SW_COLS = 28, SW_WARPS = 4;
+
+__device__ inline int wrap1(int g, int N) { return g < 0 ? g + N : (g >= N ? g - N : g); }
+
+// One row of this lane's column, raw: FP64 state (+ FP32 stage-1 increment).
+struct RawRow
+{
+    double u[3];
+    float d[3];
+};
+
+template<int KIND>
+__device__ inline void sweep_fetch(const Args& A, int row, int jg, size_t NN, RawRow& r)
+{
+    const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
+    for (int k = 0; k < 3; ++k) r.u[k] = __ldg(A.u_in + k * NN + idx);
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) r.d[k] = __ldg(A.d1 + k * NN + idx);
+}
+
+template<int KIND>
+__device__ inline void sweep_prim(const RawRow& r, float p[3])
+{
+    float s = d2f(r.u[0]), m1 = d2f(r.u[1]), m2 = d2f(r.u[2]);
+    if (KIND == K_MIX2)
+    {
+        s += r.d[0];
+        m1 += r.d[1];
+        m2 += r.d[2];
+    }
+    const float inv = rcp_fast(s);
+    p[0] = s;
+    p[1] = m1 * inv;
+    p[2] = m2 * inv;
+}
+
+__device__ inline void slope_y(const float p[3], float theta, float g[3])
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        float l = __shfl_up_sync(0xffffffffu, p[k], 1);
+        float r = __shfl_down_sync(0xffffffffu, p[k], 1);
+        g[k] = plm(l, p[k], r, theta);
+    }
+}
+
+template<int KIND>
+__global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * SW_WARPS + (threadIdx.x >> 5);
+    const int N = A.N;
+    const int sx = warp / A.tiles_y, sy = warp - (warp / A.tiles_y) * A.tiles_y;
+    const int i0 = sx * A.sweep_rows;
+    if (i0 >= N) return;                      // uniform per warp
+    const int i1 = min(i0 + A.sweep_rows, N);
+    const int jcol = sy * SW_COLS - 2 + lane;  // unwrapped column of this lane
+    const int jg = wrap1(jcol, N);
+    const bool interior = lane >= 2 && lane < 2 + SW_COLS && jcol < N;
+    const size_t NN = size_t(N) * N;
+    const FloatConsts& F = A.f;
+    const float theta = F.theta;
+
+    float bf[6];
+    double dt;
+    if (A.clock)
+    {
+        dt = A.clock->dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.clock->binary[A.stage][k]);
+    }
+    else
+    {
+        dt = A.dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.bin[k]);
+    }
+    const float dtf = d2f(dt);
+    const float yc = fmaf(float(jcol) + 0.5f, F.dl, -F.R);   // this lane's cell centre
+    const float yv = fmaf(float(jcol), F.dl, -F.R);          // face between lanes l-1 and l
+
+    // prologue: rows i0-2 .. i0+1, and the fetch of row i0+2
+    float pm2[3], pm1[3], p0[3], p1[3];
+    RawRow raw;
+    sweep_fetch<KIND>(A, i0 - 2, jg, NN, raw);
+    sweep_prim<KIND>(raw, pm2);
+    sweep_fetch<KIND>(A, i0 - 1, jg, NN, raw);
+    sweep_prim<KIND>(raw, pm1);
+    sweep_fetch<KIND>(A, i0, jg, NN, raw);
+    sweep_prim<KIND>(raw, p0);
+    sweep_fetch<KIND>(A, i0 + 1, jg, NN, raw);
+    sweep_prim<KIND>(raw, p1);
+    sweep_fetch<KIND>(A, i0 + 2, jg, NN, raw);
+    float gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        gxm1[k] = plm(pm2[k], pm1[k], p0[k], theta);
+        gx0[k] = plm(pm1[k], p0[k], p1[k], theta);
+    }
+    slope_y(pm1, theta, gym1);
+    slope_y(p0, theta, gy0);
+    face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
+
+    float local_max = 0.0f;
+    for (int i = i0; i < i1; ++i)
+    {
+        float p2[3], gx1[3], gy1[3], fxp[3];
+        sweep_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
+        sweep_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+        for (int k = 0; k < 3; ++k) gx1[k] = plm(p0[k], p1[k], p2[k], theta);
+        slope_y(p1, theta, gy1);
+        face_flux<0>(p0, p1, gx0, gx1, gy0, gy1, fmaf(float(i + 1), F.dl, -F.R), yc, A, fxp);
+
+        // y face on this lane's left side, from lane l-1 (row i)
+        float pl[3], gl[3], tl[3], fy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            pl[k] = __shfl_up_sync(0xffffffffu, p0[k], 1);
+            gl[k] = __shfl_up_sync(0xffffffffu, gy0[k], 1);
+            tl[k] = __shfl_up_sync(0xffffffffu, gx0[k], 1);
+        }
+        const float xc = fmaf(float(i) + 0.5f, F.dl, -F.R);
+        face_flux<1>(pl, p0, gl, gy0, tl, gx0, xc, yv, A, fy);
+        float dfx[3], dfy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            dfy[k] = __shfl_down_sync(0xffffffffu, fy[k], 1) - fy[k];
+            dfx[k] = fxp[k] - fxm[k];
+        }
+        if (interior)
+            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
+
+        for (int k = 0; k < 3; ++k)
+        {
+            p0[k] = p1[k];
+            p1[k] = p2[k];
+            gx0[k] = gx1[k];
+            gy0[k] = gy1[k];
+            fxm[k] = fxp[k];
+        }
+    }
+    if (A.amax)
+    {
+        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
+    }
+}
+
+// Rows per warp: enough segments along x that all strips run as one wave of
+// resident warps (no half-empty tail wave), but never fewer than 32 rows so
+// the two halo rows stay a small overhead.
+template<int KIND>
+int launch_sweep(Args A, cudaStream_t s)
+{
+    static int blocks_per_sm[64] = {};
+    static int sm_count[64] = {};
+    int dev = 0;
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (blocks_per_sm[dev & 63] == 0)
+    {
+        int b = 0, n = 0;
+        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND>, SW_WARPS * 32, 0));
+        MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        sm_count[dev & 63] = n;
+        blocks_per_sm[dev & 63] = b > 0 ? b : 1;
+    }
+    A.tiles_y = (A.N + SW_COLS - 1) / SW_COLS;
+    const int capacity = blocks_per_sm[dev & 63] * SW_WARPS * sm_count[dev & 63];
+    const int segments = std::max(1, capacity / A.tiles_y);
+    A.sweep_rows = std::max(32, (A.N + segments - 1) / segments);
+    const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
+    const int warps = strips_x * A.tiles_y;
+    sweep_kernel<KIND><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
+    return launch_status("minidisk sweep kernel");
 }
 
 // ------------------------------------------------------------- clock kernel
@@ -655,7 +886,34 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
     }
 }
 
-// Fastest wavespeed of a state (for the first CFL step).
+// Fastest wavespeed of a state in FP32 (mixed-precision runs): the same
+// estimate as the fused reduction of the mixed stage kernels.
+__global__ void wavespeed_f32_kernel(int N, FloatConsts F, const double* u, unsigned long long* amax)
+{
+    __shared__ float wm[NT / 32];
+    size_t NN = size_t(N) * N;
+    float m = 0.0f;
+    for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
+    {
+        int i = int(c / N), j = int(c % N);
+        float x = fmaf(float(i) + 0.5f, F.dl, -F.R), y = fmaf(float(j) + 0.5f, F.dl, -F.R);
+        float cs = sqrt_fast(rsqrt_fast(fmaf(x, x, y * y) + F.rs2) * F.inv_mach2);
+        float inv = rcp_fast(d2f(u[c]));
+        float vx = d2f(u[NN + c]) * inv, vy = d2f(u[2 * NN + c]) * inv;
+        m = fmaxf(m, fmaxf(fabsf(vx), fabsf(vy)) + cs);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        float r = 0.0f;
+        for (int w = 0; w < int(blockDim.x / 32); ++w) r = fmaxf(r, wm[w]);
+        atomicMax(amax, (unsigned long long)__double_as_longlong(double(r)));
+    }
+}
+
+// Fastest wavespeed of a state (for the first CFL step), FP64.
 __global__ void wavespeed_kernel(int N, int n, int level, double R, double rs2, double mach,
                                  const double* u, unsigned long long* amax)
 {
@@ -785,6 +1043,8 @@ int launch_stage(const Args& A, int tiles, cudaStream_t s)
 
 int grid_stage(Args A, int kind, cudaStream_t s)
 {
+    if (A.N >= 64 && kind == K_MIX1) return launch_sweep<K_MIX1>(A, s);
+    if (A.N >= 64 && kind == K_MIX2) return launch_sweep<K_MIX2>(A, s);
     int tiles_x = (A.N + TX - 1) / TX;
     A.tiles_y = (A.N + TY - 1) / TY;
     int tiles = tiles_x * A.tiles_y;
@@ -929,25 +1189,45 @@ int64_t mara_minidisk_workspace_bytes(const mara_minidisk_params* sd, int32_t rk
     return state;
 }
 
-int mara_minidisk_clock_init(const mara_minidisk_params* sd, const double* u, double time,
-                             mara_minidisk_clock* clock, void* stream)
+} // extern "C"
+
+namespace mara {
+namespace md {
+
+int clock_init(const mara_minidisk_params* sd, const double* u, double time, mara_minidisk_clock* clock,
+               int precision, cudaStream_t s)
 {
-    if (int r = check_params(sd)) return r;
-    MARA_REQUIRE(u && clock, "mara_minidisk_clock_init: null buffer");
-    cudaStream_t s = as_stream(stream);
     mara_minidisk_clock c;
     std::memset(&c, 0, sizeof c);
     c.time = time;
     // The host value lives on this stack frame: copy synchronously w.r.t. the host.
     MARA_CUDA(cudaMemcpyAsync(clock, &c, sizeof c, cudaMemcpyHostToDevice, s));
     MARA_CUDA(cudaStreamSynchronize(s));
-    int N = sd->block_size << sd->depth;
-    int64_t NN = int64_t(N) * N;
-    int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
+    const int N = sd->block_size << sd->depth;
+    const int64_t NN = int64_t(N) * N;
+    const int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
+    auto* amax = reinterpret_cast<unsigned long long*>(&clock->max_wavespeed);
+    if (precision == MARA_MIXED)
+    {
+        wavespeed_f32_kernel<<<blocks, NT, 0, s>>>(N, base_args(sd).f, u, amax);
+        return launch_status("wavespeed_f32_kernel");
+    }
     wavespeed_kernel<<<blocks, NT, 0, s>>>(N, sd->block_size, sd->depth, sd->domain_radius,
-        std::pow(sd->softening_length, 2.0), sd->mach_number, u,
-        reinterpret_cast<unsigned long long*>(&clock->max_wavespeed));
+        std::pow(sd->softening_length, 2.0), sd->mach_number, u, amax);
     return launch_status("wavespeed_kernel");
+}
+
+} // namespace md
+} // namespace mara
+
+extern "C" {
+
+int mara_minidisk_clock_init(const mara_minidisk_params* sd, const double* u, double time,
+                             mara_minidisk_clock* clock, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u && clock, "mara_minidisk_clock_init: null buffer");
+    return clock_init(sd, u, time, clock, MARA_FP64, as_stream(stream));
 }
 
 int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
@@ -1032,7 +1312,7 @@ int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_i
     auto* clock = reinterpret_cast<mara_minidisk_clock*>(base + bytes);
     void* ws = base + bytes + 256;
     MARA_CUDA(cudaMemcpyAsync(u, u_in, bytes, cudaMemcpyHostToDevice, s));
-    if (int r = mara_minidisk_clock_init(sd, u, time, clock, stream)) return r;
+    if (int r = clock_init(sd, u, time, clock, precision, s)) return r;
     if (int r = mara_minidisk_advance(sd, u, clock, steps, rk_order, precision, dt_mode, ws, stream)) return r;
     MARA_CUDA(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToHost, s));
     mara_minidisk_clock c;

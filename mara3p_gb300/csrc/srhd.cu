@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
             if (i >= a.n) continue;
             const double* c = a.cons + i * a.zs;
             Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
-            polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.tau));
+            polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau));
         }
     }
 }

@@ -3,7 +3,7 @@
 //
 // Training pairs are (conserved, primitive) zones whose primitives come from
 // the library's own FP64 recovery (mara_srhd_recover_primitive); the target
-// is y = log(p / (tau + D)). Loss: mean squared error of y.
+// is y = log(p E / q) (srhd_mlp.cuh). Loss: mean squared error of y.
 //
 // Trainable parameters are the contiguous float run w1, b1, w2, b2, w3, b3 of
 // mlp::Weights. Gradients of a batch are accumulated per CTA (128 zones) in
@@ -49,7 +49,9 @@ __global__ void prepare_kernel(const double* cons, const double* prim, int64_t n
         float f[4];
         raw_features(D, S1, S2, S3, tau, f);
         for (int k = 0; k < 4; ++k) feat[4 * i + k] = f[k];
-        target[i] = float(log(prim[4 * n + i] / (tau + D)));
+        double E, q, SS;
+        zone_invariants(D, S1, S2, S3, tau, E, q, SS);
+        target[i] = q > 0.0 ? float(log(prim[4 * n + i] * E / q)) : 0.0f;
     }
 }
 

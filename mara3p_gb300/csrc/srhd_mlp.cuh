@@ -1,10 +1,14 @@
 // Learned pressure guess for SRHD primitive recovery: a 4-64-64-1 MLP.
 //
-//   features  x = normalised (log D, log(tau/D), |S|/(tau+D), log(|S|/D + 1e-30))
+// With E = tau + D, S = |S| and q = E^2 - S^2 - D^2 (computed in FP64: it is a
+// small difference of large terms for fast, cold zones), the exact pressure
+// satisfies p*E/q in [1/6, 1/3] for gamma = 4/3 (q = 6 p rho W^2 + 8 p^2 W^2
+// + p^2), so the network learns y = log(p E / q), a smooth O(1) correction:
+//   features  x = normalised (log(q/E^2), S/E, D/E, log((E - S)/E))
 //   layer 1   h1 = tanh(W1 x + b1)        FP32 on the CUDA cores (K = 4)
 //   layer 2   h2 = tanh(W2 h1 + b2)       BF16 operands, FP32 accumulate, tensor cores
 //   layer 3   y  = w3 . h2 + b3           FP32
-//   guess     p  = (tau + D) * exp(out_shift + out_scale * y)
+//   guess     p  = exp(out_shift + out_scale * y) * q / E
 //
 // Weights live in one device struct (Weights) written by the training kernels
 // in srhd_mlp.cu. One CTA of kThreads threads evaluates kZones zones: each
@@ -71,20 +75,37 @@ __device__ inline void load_weights(const Weights& w, Shared& s)
     }
 }
 
-// Raw (un-normalised) features of one zone.
-__host__ __device__ inline void raw_features(double D, double S1, double S2, double S3, double tau, float f[4])
+// E = tau + D and q = E^2 - S^2 - D^2 of one zone, in FP64.
+__host__ __device__ inline void zone_invariants(double D, double S1, double S2, double S3, double tau,
+                                                double& E, double& q, double& SS)
 {
-    float d = float(D), t = float(tau);
-    float s = sqrtf(float(S1) * float(S1) + float(S2) * float(S2) + float(S3) * float(S3));
-    f[0] = logf(d);
-    f[1] = logf(fmaxf(t, 1e-30f) / d);
-    f[2] = s / (t + d);
-    f[3] = logf(s / d + 1e-30f);
+    E = tau + D;
+    SS = S1 * S1 + S2 * S2 + S3 * S3;
+    q = (E - D) * (E + D) - SS;
 }
 
-__device__ inline void features(double D, double S1, double S2, double S3, double tau, float f[4])
+// Raw (un-normalised) features of one zone; false if the zone has no
+// physical solution (q <= 0 or E <= 0), in which case no guess is made.
+__host__ __device__ inline bool raw_features(double D, double S1, double S2, double S3, double tau, float f[4])
 {
-    raw_features(D, S1, S2, S3, tau, f);
+    double E, q, SS;
+    zone_invariants(D, S1, S2, S3, tau, E, q, SS);
+    if (!(q > 0.0) || !(E > 0.0) || !(D > 0.0))
+    {
+        f[0] = f[1] = f[2] = f[3] = 0.0f;
+        return false;
+    }
+    float Ef = float(E), S = sqrtf(float(SS));
+    f[0] = logf(float(q / (E * E)));
+    f[1] = S / Ef;
+    f[2] = float(D) / Ef;
+    f[3] = logf(float(q + D * D) / ((Ef + S) * Ef));
+    return true;
+}
+
+__device__ inline bool features(double D, double S1, double S2, double S3, double tau, float f[4])
+{
+    return raw_features(D, S1, S2, S3, tau, f);
 }
 
 __device__ inline void stage_features(Shared& s, int zone, const float f[4])
@@ -175,9 +196,14 @@ __device__ inline void forward(Shared& s)
     }
 }
 
-__device__ inline double pressure_from_output(float y, double D, double tau)
+// Pressure guess from the network output; 0 (the reference's start) when the
+// zone has no physical solution.
+__device__ inline double pressure_from_output(float y, double D, double S1, double S2, double S3, double tau)
 {
-    return (tau + D) * double(__expf(y));
+    double E, q, SS;
+    zone_invariants(D, S1, S2, S3, tau, E, q, SS);
+    if (!(q > 0.0) || !(E > 0.0)) return 0.0;
+    return double(__expf(y)) * (q / E);
 }
 
 } // namespace mlp

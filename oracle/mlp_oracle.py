@@ -3,21 +3,37 @@
 numpy (float64) restatement of the pressure-guess MLP's forward pass, loss
 and gradient, to check the library's hand-written GPU training kernels. The
 network has no counterpart in the reference: it is defined by
-mara3p_gb300/csrc/srhd_mlp.cuh (4-64-64-1, tanh, y = log(p / (tau + D))).
+mara3p_gb300/csrc/srhd_mlp.cuh (4-64-64-1, tanh, y = log(p E / q)).
 """
 from __future__ import annotations
 
 import numpy as np
 
 
+def invariants(cons: np.ndarray):
+    """E = tau + D, q = E^2 - S^2 - D^2 and S^2 in float64, as the kernels do."""
+    D, S1, S2, S3, tau = (cons[k] for k in range(5))
+    E = tau + D
+    SS = S1 * S1 + S2 * S2 + S3 * S3
+    q = (E - D) * (E + D) - SS
+    return E, q, SS
+
+
 def raw_features(cons: np.ndarray) -> np.ndarray:
-    """cons (5, n) -> features (n, 4) in float32 arithmetic, as the kernels do."""
-    D, S1, S2, S3, tau = (cons[k].astype(np.float32) for k in range(5))
-    s = np.sqrt(S1 * S1 + S2 * S2 + S3 * S3)
-    with np.errstate(divide="ignore"):
-        f = np.stack([np.log(D), np.log(np.maximum(tau, np.float32(1e-30)) / D), s / (tau + D),
-                      np.log(s / D + np.float32(1e-30))], axis=1)
+    """cons (5, n) -> features (n, 4): log(q/E^2), S/E, D/E, log((E - S)/E)."""
+    E, q, SS = invariants(cons)
+    D = cons[0]
+    Ef = E.astype(np.float32)
+    S = np.sqrt(SS.astype(np.float32))
+    f = np.stack([np.log((q / (E * E)).astype(np.float32)), S / Ef, D.astype(np.float32) / Ef,
+                  np.log((q + D * D).astype(np.float32) / ((Ef + S) * Ef))], axis=1)
     return f.astype(np.float32)
+
+
+def target(cons: np.ndarray, p: np.ndarray) -> np.ndarray:
+    """y = log(p E / q)."""
+    E, q, _ = invariants(cons)
+    return np.log(p * E / q).astype(np.float32)
 
 
 def forward(p: dict, feat: np.ndarray):

@@ -162,12 +162,13 @@ def test_rk1_fp64_matches_oracle(md, oracle):
     assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
 
 
-@pytest.mark.parametrize("rk_order,steps", [(1, 20), (2, 200)])
-def test_mixed_precision_close_to_fp64(md, rk_order, steps):
+@pytest.mark.parametrize("rk_order,steps,block_size", [(1, 20, 16), (2, 200, 16), (2, 200, 8)])
+def test_mixed_precision_close_to_fp64(md, rk_order, steps, block_size):
     """Mixed path (FP32 fluxes/sources, FP64 accumulation) vs plain FP64 GPU:
     density and momentum relative L1 below 1e-6 (forward Euler with PLM is
-    not stable for long runs, so RK1 runs 20 steps)."""
-    sd = md.SolverData(**SMALL_PARAMS)
+    not stable for long runs, so RK1 runs 20 steps). 64^2 meshes run the
+    warp-strip sweep kernel, 32^2 meshes the tiled one."""
+    sd = md.SolverData(**dict(SMALL_PARAMS, block_size=block_size))
     u0 = md.initial_conserved(sd, seed=11, amplitude=0.01)
     a = md.Run(sd, u0.clone(), rk_order=rk_order, precision=md.FP64, dt_mode=md.DT_FORMULA)
     b = md.Run(sd, u0.clone(), rk_order=rk_order, precision=md.MIXED, dt_mode=md.DT_FORMULA)

@@ -98,13 +98,13 @@ def trained(sr, oracle):
     assert int((rec.status != 0).sum()) == 0
     net = sr.PressureGuess()
     net.prepare(c, rec.prim, seed=1)
-    hist = net.train(steps=3000, batch=8192, lr=2e-3, seed=1)
+    hist = net.train(steps=2000, batch=8192, lr=2e-3, seed=1)
     torch.cuda.synchronize()
     return net, c, rec, hist.cpu().numpy()
 
 
 def test_mlp_gradient_matches_cpu_oracle(sr, oracle):
-    from oracle.mlp_oracle import loss_and_gradient, raw_features
+    from oracle.mlp_oracle import loss_and_gradient, raw_features, target as mlp_target
     _, cons = seeded_zones(oracle, 4096, seed=123)
     c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
     rec = sr.recover_primitive(c, GAMMA)
@@ -114,7 +114,7 @@ def test_mlp_gradient_matches_cpu_oracle(sr, oracle):
     p = net.parameters_f32()
     cons_soa = cons.reshape(-1, 5).T
     feat = raw_features(cons_soa)
-    target = np.log(rec.prim[4].cpu().numpy() / (cons_soa[4] + cons_soa[0])).astype(np.float32)
+    target = mlp_target(cons_soa, rec.prim[4].cpu().numpy())
     ref_loss, ref_grad = loss_and_gradient(p, feat, target)
     g = grad.cpu().numpy().astype(np.float64)
     assert abs(loss - ref_loss) <= 1e-4 * abs(ref_loss)
@@ -134,25 +134,54 @@ def test_mlp_bf16_inference_matches_fp32_oracle(sr, trained):
     feat = raw_features(sub.cpu().numpy())
     y = net.infer(torch.from_numpy(feat).cuda()).cpu().numpy()
     *_, ref = forward(net.parameters_f32(), feat)
-    # BF16 operands in layer 2 and tanh.approx: |dy| well under the target spread
-    assert np.abs(y - ref).max() < 0.05
-    assert np.abs(y - ref).mean() < 0.01
+    # BF16 operands in layer 2 and tanh.approx; y = log(pE/q) spans about 0.7
+    assert np.abs(y - ref).max() < 0.02
+    assert np.abs(y - ref).mean() < 0.003
+
+
+def round_trip_error(oracle, cons_soa, prim_soa):
+    """max_k |cons(prim)_k - cons_k| / (tau + D) per zone, cons() from the oracle."""
+    prim_aos = np.ascontiguousarray(prim_soa.T).ravel()
+    back = np.zeros_like(prim_aos)
+    oracle.oracle_srhd_conserved_density(dptr(prim_aos), ctypes.c_int64(prim_aos.size // 5),
+                                         ctypes.c_double(GAMMA), dptr(back))
+    back = back.reshape(-1, 5).T
+    E = cons_soa[4] + cons_soa[0]
+    return np.max(np.abs(back - cons_soa), axis=0) / E
 
 
 def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
-    """The learned guess changes the FP64 Newton iteration count, never the
-    answer: primitives agree with the default recovery to 1e-10 relative."""
+    """The learned guess changes the FP64 Newton iteration count, not the
+    answer. The reference stops when |f| < 1e-12 and returns the pressure of
+    one more Newton step but the Lorentz factor W of the step before
+    (src/physics_srhd.hpp:257-265), so its own answer is defined only to:
+      p      — to rounding where well conditioned (p > 1e-3 (tau + D));
+      rho, u — to |dW/W| <~ W^2 * 1e-12 / (tau + D) (the last iterate's spread).
+    The seeded recovery must meet those bounds against the reference method,
+    and reproduce the conserved state at least as well."""
     net, _, _, _ = trained
     _, cons = seeded_zones(oracle, 1 << 18, seed=2024)
-    c = torch.from_numpy(cons.reshape(-1, 5).T.copy()).cuda()
+    cons_soa = cons.reshape(-1, 5).T.copy()
+    c = torch.from_numpy(cons_soa).cuda()
     base = sr.recover_primitive(c, GAMMA)
     seeded = sr.recover_primitive(c, GAMMA, mlp=net, refine32=2)
     assert int((seeded.status != 0).sum()) == 0
     a, b = base.prim.cpu().numpy(), seeded.prim.cpu().numpy()
+    err_a = round_trip_error(oracle, cons_soa, a)
+    err_b = round_trip_error(oracle, cons_soa, b)
+    assert err_b.max() <= max(10.0 * err_a.max(), 1e-13), (err_a.max(), err_b.max())
+    assert err_b.mean() <= 2.0 * err_a.mean() + 1e-16
+    E = cons_soa[4] + cons_soa[0]
+    # zones where the reference's Newton met only its relaxed last-iteration
+    # tolerance (|f| < 1e-8 at iteration 51) are excluded
+    strict = base.iterations.cpu().numpy() <= 50
     rel = np.abs(a - b) / np.maximum(np.abs(a), 1e-300)
-    assert np.max(rel[[0, 4]]) < 1e-10
-    big = np.abs(a[1:4]) > 1e-8
-    assert np.max(rel[1:4][big]) < 1e-9
+    well = strict & (a[4] > 1e-3 * E)
+    assert np.max(rel[4][well]) < 1e-10
+    W = np.sqrt(1.0 + (a[1:4] ** 2).sum(axis=0))
+    bound = 10.0 * W ** 2 * 1e-12 / E + 1e-13
+    assert np.all(rel[0][strict] <= bound[strict])
+    assert np.all(rel[1:4][:, strict].max(axis=0) <= bound[strict] + 1e-12)
     mean_base = base.iterations.float().mean().item()
     mean_seeded = seeded.iterations.float().mean().item()
     assert mean_seeded * 2.0 <= mean_base, (mean_base, mean_seeded)
