@@ -194,6 +194,60 @@ int mara_minidisk_advance_noalloc(const mara_minidisk_params* sd, double* u, mar
                                   int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
                                   void* stream);
 
+/* ---------------------------------------------------------------- mhd */
+
+/* One periodic cube of ideal MHD with constrained transport, the scheme of
+ * mara::advance_mhd_ct (src/scheme_mhd_v1.hpp:102-117, src/scheme_mhd_v1.cpp:265-299)
+ * with local_periodic_boundary_extension. dl = 1/N. */
+typedef struct mara_mhd_params {
+    int32_t N;                  /* cells per side */
+    double gamma_law_index;     /* the reference's scheme uses 5/3 */
+    double cfl;
+    double plm_theta;           /* 0 is not supported (PLM only) */
+} mara_mhd_params;
+
+/* Device clock of an MHD run (opaque, mara_mhd_clock_bytes() bytes): time,
+ * the CFL dt of each RK stage, iteration, count of zones whose primitive
+ * recovery failed (negative density or pressure; the reference throws). */
+int64_t mara_mhd_clock_bytes(void);
+int mara_mhd_clock_init(void* clock, double time, void* stream);
+/* The clock's time is its first double; failures its last 8 bytes. */
+
+/* Workspace (device) for mara_mhd_advance_ct (rk_order 1) / mara_mhd_advance (2). */
+int64_t mara_mhd_workspace_bytes(const mara_mhd_params* mp, int32_t rk_order, int32_t precision);
+
+/* Drop-in for mara::advance_mhd_ct: one CFL-limited step of the cube, time in
+ * the clock advanced by dt. uc element (component q, cell c) at
+ * uc[q*component_stride + c*cell_stride] (the reference's AoS tuples: 1, 5;
+ * SoA: N^3, 1); uc_out is SoA [5][N^3]. bf1 [N+1][N][N], bf2 [N][N+1][N],
+ * bf3 [N][N][N+1] hold B.dA/dA on the faces as the reference does. */
+int mara_mhd_advance_ct(const mara_mhd_params* mp, const double* uc, int64_t component_stride, int64_t cell_stride,
+                        const double* bf1, const double* bf2, const double* bf3, double* uc_out, double* bf1_out,
+                        double* bf2_out, double* bf3_out, void* clock, int32_t precision, void* workspace,
+                        void* stream);
+
+/* `steps` RK2 steps of examples/mhd3d.cpp:186-215 (advance_runge_kutta over
+ * advance_mhd_ct: each stage takes its own CFL dt; states and times averaged
+ * with weight 1/2) in place on SoA uc [5][N^3] and the face arrays. */
+int mara_mhd_advance(const mara_mhd_params* mp, double* uc, double* bf1, double* bf2, double* bf3, void* clock,
+                     int32_t steps, int32_t rk_order, int32_t precision, void* workspace, void* stream);
+
+/* Seeded Fourier-mode table (host, 11 doubles per mode: k[3], velocity phase,
+ * velocity direction[3], potential phase, potential polarisation[3] / |k|),
+ * integer wavevectors 0 < |k| <= 4. No counterpart in the reference. */
+int mara_mhd_mode_table(uint64_t seed, int32_t modes, double* table);
+
+/* Initial state in the discretisation of mara::construct_conserved
+ * (src/scheme_mhd_v1.cpp:311-342): rho = 1, p = 1, v = v_amp * sum of velocity
+ * modes, B = curl of A = a_amp * sum of potential modes taken on cell edges.
+ * table is host memory; workspace (device) needs 88*modes bytes. */
+int mara_mhd_initial_state(const mara_mhd_params* mp, const double* table, int32_t modes, double v_amp, double a_amp,
+                           double* uc, double* bf1, double* bf2, double* bf3, void* workspace, void* stream);
+
+/* max over cells of |div B| * dl (sum of the face differences), into *out (device double). */
+int mara_mhd_max_div_b(const mara_mhd_params* mp, const double* bf1, const double* bf2, const double* bf3,
+                       double* out, void* stream);
+
 /* ---------------------------------------------------------------- srhd */
 
 /* Conserved -> primitive recovery of n zones, replacing srhd::recover_primitive
@@ -214,6 +268,13 @@ int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component
                                 double gamma_law_index, double temperature_floor, const void* mlp_weights,
                                 int32_t refine32, int32_t seeded_budget, double* prim, int32_t* iterations,
                                 int32_t* status, unsigned long long* failures, void* stream);
+
+/* Seeded SRHD test zones (no counterpart in the reference): rho in
+ * [rho_lo, rho_hi] and p in [p_lo, p_hi] log-uniform, Lorentz factor
+ * log-uniform in [1, w_hi] along an isotropic direction; writes primitives and
+ * srhd::conserved_density (src/physics_srhd.hpp:291-304), SoA [5][n], device. */
+int mara_srhd_seeded_zones(uint64_t seed, int64_t n, double rho_lo, double rho_hi, double p_lo, double p_hi,
+                           double w_hi, double gamma_law_index, double* prim, double* cons, void* stream);
 
 /* Learned pressure guess (4-64-64-1 MLP, BF16 tensor-core inference). No
  * counterpart in the reference. The weights are one device buffer of

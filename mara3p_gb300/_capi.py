@@ -80,6 +80,9 @@ SIGNATURES = {
     "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                                    ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int32,
                                                    ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    "mara_srhd_seeded_zones": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp,
+                                              _vp, _vp]),
     "mara_srhd_mlp_weights_bytes": (ctypes.c_int64, []),
     "mara_srhd_mlp_param_count": (ctypes.c_int32, []),
     "mara_srhd_mlp_workspace_bytes": (ctypes.c_int64, [ctypes.c_int64]),
@@ -89,6 +92,29 @@ SIGNATURES = {
                                            ctypes.c_float, _vp, _vp]),
     "mara_srhd_mlp_infer": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp]),
 }
+
+
+class MhdParams(ctypes.Structure):
+    """mara_mhd_params."""
+
+    _fields_ = [("N", ctypes.c_int32), ("gamma_law_index", ctypes.c_double), ("cfl", ctypes.c_double),
+                ("plm_theta", ctypes.c_double)]
+
+
+_HP = ctypes.POINTER(MhdParams)
+SIGNATURES.update({
+    "mara_mhd_clock_bytes": (ctypes.c_int64, []),
+    "mara_mhd_clock_init": (ctypes.c_int, [_vp, ctypes.c_double, _vp]),
+    "mara_mhd_workspace_bytes": (ctypes.c_int64, [_HP, ctypes.c_int32, ctypes.c_int32]),
+    "mara_mhd_advance_ct": (ctypes.c_int, [_HP, _vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                           _vp, ctypes.c_int32, _vp, _vp]),
+    "mara_mhd_advance": (ctypes.c_int, [_HP, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                        _vp, _vp]),
+    "mara_mhd_mode_table": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int32, c_double_p]),
+    "mara_mhd_initial_state": (ctypes.c_int, [_HP, c_double_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp,
+                                              _vp, _vp, _vp, _vp, _vp]),
+    "mara_mhd_max_div_b": (ctypes.c_int, [_HP, _vp, _vp, _vp, _vp, _vp]),
+})
 
 
 class MaraError(RuntimeError):

@@ -1,0 +1,757 @@
+// Constrained-transport ideal MHD on one periodic cube: the GB300 form of
+// mara::advance_mhd_ct (src/scheme_mhd_v1.cpp:265-299, physics in
+// src/physics_mhd.hpp:216-390, staggered operators in
+// src/mesh_cartesian_3d.hpp:236-305) and the RK2 driver of
+// examples/mhd3d.cpp:78-88,186-215.
+//
+// One stage = four kernels:
+//   prim_kernel     face_to_cell + recover_primitive of every cell into P[8][N^3];
+//                   fastest wavespeed reduced into the clock (CFL dt)
+//   dt_kernel       dt = cfl * dl / max speed (scheme_mhd_v1.cpp:287)
+//   face_kernel<a>  PLM slopes along axis a, face states, HLLE flux F[5] and the
+//                   two transverse E-field components on all N+1 layers of the
+//                   face array (layer N uses its own normal field bf[N], as the
+//                   reference's flux_arrays does; cells are periodic)
+//   update_kernel   u -= div(F) dt/dl; B.dA -= curl(E_edge) dt/dl, edge EMFs by
+//                   the reference's face averaging (edge_emf_from_face);
+//                   optionally averaged with the RK partner state.
+// Layout: uc SoA [5][N][N][N] (any (component, cell) stride pair on input to
+// the drop-in call); bf1 [N+1][N][N], bf2 [N][N+1][N], bf3 [N][N][N+1] as the
+// reference holds them (the two periodic boundary layers stay identical).
+//
+// FP64: reference evaluation order. MIXED: P, F and E in FP32; u and B stay
+// FP64 and are accumulated in FP64; the curl of the FP32 edge EMFs is formed
+// exactly in FP64 (differences of floats are exact doubles), so div B is
+// preserved to FP64 rounding as in the FP64 path.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include "common.cuh"
+
+namespace mara {
+namespace mhd {
+
+struct Clock
+{
+    double time;
+    double dt[2];
+    unsigned long long amax[2];   // fastest wavespeed bits (positive doubles order as integers)
+    int64_t iteration;
+    unsigned long long failures;  // zones with negative density or pressure
+};
+
+struct Args
+{
+    int N;
+    double gamma, dl, cfl, theta;
+    const double* uc; int64_t ucs, uzs;          // input conserved, (component, cell) strides
+    const double* bf[3];
+    const double* uavg;                          // RK partner (SoA), or null
+    const double* bavg[3];
+    double* uc_out;                              // SoA
+    double* bf_out[3];
+    void* P;                                     // [8][N^3] (double or float)
+    void* F[3];                                  // [5][face count of axis a]
+    void* E[3];                                  // [2][face count]: the two transverse components
+    Clock* clock;
+    int stage;
+};
+
+__host__ __device__ inline int64_t nb(int N, int axis) { return int64_t(N + (axis == 0)) * (N + (axis == 1)) * (N + (axis == 2)); }
+
+__device__ inline int wrap(int i, int N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
+
+// element (i, j, k) of the face array of `axis`, (i, j, k) already in range
+__device__ inline int64_t fidx(int N, int axis, int i, int j, int k)
+{
+    const int n1 = N + (axis == 1), n2 = N + (axis == 2);
+    return (int64_t(i) * n1 + j) * n2 + k;
+}
+
+__device__ inline int64_t cidx(int N, int i, int j, int k) { return (int64_t(i) * N + j) * N + k; }
+
+template<typename R>
+struct Prim { R d, v[3], p, b[3]; };
+
+template<typename R>
+__device__ inline R sum3(const R a[3], const R b[3]) { return ((R(0) + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2]; }
+
+__device__ inline double plm(double yl, double y0, double yr, double theta)
+{
+    double a = (y0 - yl) * theta, b = (yr - yl) * 0.5, c = (yr - y0) * theta;
+    double m = fmin(fmin(fabs(a), fabs(b)), fabs(c));
+    long long sa = __double_as_longlong(a), sb = __double_as_longlong(b), sc = __double_as_longlong(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0 : copysign(m, a);
+}
+
+__device__ inline float plm(float yl, float y0, float yr, float theta)
+{
+    float a = (y0 - yl) * theta, b = (yr - yl) * 0.5f, c = (yr - y0) * theta;
+    float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
+    int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
+}
+
+// fast_speed_squared / outer_wavespeeds (physics_mhd.hpp:216-237)
+template<typename R>
+__device__ inline void outer_wavespeeds(const Prim<R>& p, int axis, R gm, R& am, R& ap)
+{
+    const R n[3] = {R(axis == 0), R(axis == 1), R(axis == 2)};
+    const R cs2 = gm * p.p / p.d;
+    const R va2 = sum3(p.b, p.b) / p.d;
+    const R bn = sum3(p.b, n);
+    const R van2 = (bn * bn) / p.d;
+    const R cf2 = cs2 + va2;
+    R disc = cf2 * cf2 - R(4) * cs2 * van2;
+    if (sizeof(R) == sizeof(float)) disc = fmax(disc, R(0));   // FP32 rounding can dip below zero
+    const R cg2 = sqrt(disc);
+    const R cf = sqrt(R(0.5) * (cf2 + cg2));
+    const R vn = sum3(n, p.v);
+    am = vn - cf;
+    ap = vn + cf;
+}
+
+template<typename R>
+__device__ inline R fastest_speed(const Prim<R>& p, R gm)
+{
+    R m[3], q[3];
+    for (int a = 0; a < 3; ++a) outer_wavespeeds(p, a, gm, m[a], q[a]);
+    return fmax(fmax(fmax(fabs(m[0]), fabs(q[0])), fmax(fabs(m[1]), fabs(q[1]))), fmax(fabs(m[2]), fabs(q[2])));
+}
+
+// conserved_density (physics_mhd.hpp:305-318)
+template<typename R>
+__device__ inline void conserved(const Prim<R>& p, R gm, R u[5])
+{
+    u[0] = p.d;
+    u[1] = p.d * p.v[0];
+    u[2] = p.d * p.v[1];
+    u[3] = p.d * p.v[2];
+    u[4] = R(0.5) * p.d * sum3(p.v, p.v) + p.p / (gm - R(1)) + R(0.5) * sum3(p.b, p.b);
+}
+
+// HLLE flux and E-field (physics_mhd.hpp:324-390), `axis` normal, bl the face B.
+template<typename R, int AXIS>
+__device__ inline void riemann_hlle(Prim<R> pl, Prim<R> pr, R bl, R gm, R F[5], R Et[2])
+{
+    pl.b[AXIS] = bl;   // with_longitudinal_field: (b - (b.n) n) + bl n
+    pr.b[AXIS] = bl;
+    R ul[5], ur[5], fl[5], fr[5];
+    conserved(pl, gm, ul);
+    conserved(pr, gm, ur);
+    auto flux = [gm] (const Prim<R>& p, const R u[5], R f[5]) {
+        const R bn = p.b[AXIS], vn = p.v[AXIS];
+        const R pt = p.p + R(0.5) * sum3(p.b, p.b);
+        const R bv = sum3(p.b, p.v);
+        f[0] = vn * u[0];
+        for (int k = 0; k < 3; ++k) f[1 + k] = vn * u[1 + k] + (k == AXIS ? pt : R(0)) + -bn * p.b[k];
+        f[4] = vn * u[4] + pt * vn + -bn * bv;
+    };
+    flux(pl, ul, fl);
+    flux(pr, ur, fr);
+    R alm, alp, arm, arp;
+    outer_wavespeeds(pl, AXIS, gm, alm, alp);
+    outer_wavespeeds(pr, AXIS, gm, arm, arp);
+    const R ap = fmax(R(0), fmax(alp, arp));
+    const R am = fmin(R(0), fmin(alm, arm));
+    for (int k = 0; k < 5; ++k) F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am) / (ap - am);
+    // induction = n x E with E = -(v x B); E-field of the face = -(n x hll_induction)
+    auto induction = [] (const Prim<R>& p, R I[3]) {
+        const R e[3] = {-(p.v[1] * p.b[2] - p.v[2] * p.b[1]), -(p.v[2] * p.b[0] - p.v[0] * p.b[2]),
+                        -(p.v[0] * p.b[1] - p.v[1] * p.b[0])};
+        const R n[3] = {R(AXIS == 0), R(AXIS == 1), R(AXIS == 2)};
+        I[0] = n[1] * e[2] - n[2] * e[1];
+        I[1] = n[2] * e[0] - n[0] * e[2];
+        I[2] = n[0] * e[1] - n[1] * e[0];
+    };
+    R il[3], ir[3], hi[3];
+    induction(pl, il);
+    induction(pr, ir);
+    for (int k = 0; k < 3; ++k) hi[k] = (ap * il[k] - am * ir[k] - (pl.b[k] - pr.b[k]) * ap * am) / (ap - am);
+    const R n[3] = {R(AXIS == 0), R(AXIS == 1), R(AXIS == 2)};
+    const R c[3] = {n[1] * hi[2] - n[2] * hi[1], n[2] * hi[0] - n[0] * hi[2], n[0] * hi[1] - n[1] * hi[0]};
+    // transverse components in increasing axis order
+    Et[0] = -c[AXIS == 0 ? 1 : 0];
+    Et[1] = -c[AXIS == 2 ? 1 : 2];
+}
+
+// ---------------------------------------------------------------- kernels
+template<typename R>
+__global__ void prim_kernel(const Args A)
+{
+    __shared__ double wmax[8];
+    const int N = A.N;
+    const int64_t NN = int64_t(N) * N * N;
+    R* P = static_cast<R*>(A.P);
+    const R gm = R(A.gamma);
+    double m = 0.0;
+    unsigned long long bad = 0;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        const double b1 = 0.5 * (A.bf[0][fidx(N, 0, i, j, k)] + A.bf[0][fidx(N, 0, i + 1, j, k)]);
+        const double b2 = 0.5 * (A.bf[1][fidx(N, 1, i, j, k)] + A.bf[1][fidx(N, 1, i, j + 1, k)]);
+        const double b3 = 0.5 * (A.bf[2][fidx(N, 2, i, j, k)] + A.bf[2][fidx(N, 2, i, j, k + 1)]);
+        double u[5];
+        for (int q = 0; q < 5; ++q) u[q] = A.uc[q * A.ucs + c * A.uzs];
+        // recover_primitive (physics_mhd.hpp:290-303)
+        const double d = u[0];
+        const double S[3] = {u[1], u[2], u[3]}, b[3] = {b1, b2, b3};
+        const double kin = 0.5 * sum3(S, S) / d;
+        const double mag = 0.5 * sum3(b, b);
+        const double pg = (u[4] - kin - mag) * (A.gamma - 1);
+        Prim<R> p;
+        p.d = R(d);
+        for (int q = 0; q < 3; ++q)
+        {
+            p.v[q] = R(S[q] / d);
+            p.b[q] = R(b[q]);
+        }
+        p.p = R(pg);
+        if (d < 0.0 || pg < 0.0) ++bad;
+        P[0 * NN + c] = p.d;
+        P[1 * NN + c] = p.v[0];
+        P[2 * NN + c] = p.v[1];
+        P[3 * NN + c] = p.v[2];
+        P[4 * NN + c] = p.p;
+        P[5 * NN + c] = p.b[0];
+        P[6 * NN + c] = p.b[1];
+        P[7 * NN + c] = p.b[2];
+        m = fmax(m, double(fastest_speed(p, gm)));
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        wmax[threadIdx.x >> 5] = m;
+        if (bad) atomicAdd(&A.clock->failures, bad);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double r = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) r = fmax(r, wmax[w]);
+        atomicMax(&A.clock->amax[A.stage], (unsigned long long)__double_as_longlong(r));
+    }
+}
+
+__global__ void dt_kernel(Clock* clock, int stage, double cfl, double dl, int begin)
+{
+    if (threadIdx.x != 0) return;
+    if (begin) { clock->amax[0] = 0ull; clock->amax[1] = 0ull; }
+    else clock->dt[stage] = cfl * dl / __longlong_as_double((long long)clock->amax[stage]);
+}
+
+template<typename R, int AXIS>
+__global__ void face_kernel(const Args A)
+{
+    const int N = A.N;
+    const int64_t NN = int64_t(N) * N * N;
+    const int64_t NF = nb(N, AXIS);
+    const int n1 = N + (AXIS == 1), n2 = N + (AXIS == 2);
+    const R* P = static_cast<const R*>(A.P);
+    R* F = static_cast<R*>(A.F[AXIS]);
+    R* E = static_cast<R*>(A.E[AXIS]);
+    const R gm = R(A.gamma), theta = R(A.theta);
+    const int di = AXIS == 0, dj = AXIS == 1, dk = AXIS == 2;
+    for (int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; f < NF; f += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        const int64_t cm2 = cidx(N, wrap(i - 2 * di, N), wrap(j - 2 * dj, N), wrap(k - 2 * dk, N));
+        const int64_t cm1 = cidx(N, wrap(i - di, N), wrap(j - dj, N), wrap(k - dk, N));
+        const int64_t c0 = cidx(N, wrap(i, N), wrap(j, N), wrap(k, N));
+        const int64_t cp1 = cidx(N, wrap(i + di, N), wrap(j + dj, N), wrap(k + dk, N));
+        R L[8], Rr[8];
+        for (int q = 0; q < 8; ++q)
+        {
+            const R a = P[q * NN + cm2], b = P[q * NN + cm1], cc = P[q * NN + c0], d = P[q * NN + cp1];
+            L[q] = b + R(0.5) * plm(a, b, cc, theta);
+            Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
+        }
+        Prim<R> pl{L[0], {L[1], L[2], L[3]}, L[4], {L[5], L[6], L[7]}};
+        Prim<R> pr{Rr[0], {Rr[1], Rr[2], Rr[3]}, Rr[4], {Rr[5], Rr[6], Rr[7]}};
+        const R bl = R(A.bf[AXIS][f]);
+        R fl[5], e[2];
+        riemann_hlle<R, AXIS>(pl, pr, bl, gm, fl, e);
+        for (int q = 0; q < 5; ++q) F[q * NF + f] = fl[q];
+        E[0 * NF + f] = e[0];
+        E[1 * NF + f] = e[1];
+    }
+}
+
+// E component `comp` on the faces of `axis`: layer index along `axis` taken
+// as is (0..N), transverse cell indices periodic; as a double. Face E arrays
+// hold the two transverse components in increasing axis order.
+template<typename R>
+__device__ inline double ef(const Args& A, int axis, int comp, int i, int j, int k)
+{
+    const int N = A.N;
+    if (axis != 0) i = wrap(i, N);
+    if (axis != 1) j = wrap(j, N);
+    if (axis != 2) k = wrap(k, N);
+    const int slot = comp < axis ? comp : comp - 1;
+    return double(static_cast<const R*>(A.E[axis])[slot * nb(N, axis) + fidx(N, axis, i, j, k)]);
+}
+
+// edge_emf_from_face (scheme_mhd_v1.cpp:76-98); edge of axis a at (i, j, k)
+// starts at corner (i, j, k). Averages in the reference's order.
+template<typename R>
+__device__ inline double ee(const Args& A, int axis, int i, int j, int k)
+{
+    double a, b;
+    if (axis == 0)
+    {
+        a = 0.5 * (ef<R>(A, 1, 0, i, j, k - 1) + ef<R>(A, 1, 0, i, j, k));
+        b = 0.5 * (ef<R>(A, 2, 0, i, j - 1, k) + ef<R>(A, 2, 0, i, j, k));
+    }
+    else if (axis == 1)
+    {
+        a = 0.5 * (ef<R>(A, 2, 1, i - 1, j, k) + ef<R>(A, 2, 1, i, j, k));
+        b = 0.5 * (ef<R>(A, 0, 1, i, j, k - 1) + ef<R>(A, 0, 1, i, j, k));
+    }
+    else
+    {
+        a = 0.5 * (ef<R>(A, 0, 2, i, j - 1, k) + ef<R>(A, 0, 2, i, j, k));
+        b = 0.5 * (ef<R>(A, 1, 2, i - 1, j, k) + ef<R>(A, 1, 2, i, j, k));
+    }
+    return 0.5 * (a + b);
+}
+
+template<typename R>
+__global__ void update_kernel(const Args A)
+{
+    const int N = A.N;
+    const int64_t NN = int64_t(N) * N * N;
+    const double dt = A.clock->dt[A.stage];
+    const double dl = A.dl;
+    const float dt_over_dl = float(dt / dl);
+    const int64_t nf0 = nb(N, 0), nf1 = nb(N, 1), nf2 = nb(N, 2);
+    const int64_t total = NN + nf0 + nf1 + nf2;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x)
+    {
+        if (t < NN)
+        {
+            const int64_t c = t;
+            const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+            const R* F0 = static_cast<const R*>(A.F[0]);
+            const R* F1 = static_cast<const R*>(A.F[1]);
+            const R* F2 = static_cast<const R*>(A.F[2]);
+            const int64_t x0 = fidx(N, 0, i, j, k), x1 = fidx(N, 0, i + 1, j, k);
+            const int64_t y0 = fidx(N, 1, i, j, k), y1 = fidx(N, 1, i, j + 1, k);
+            const int64_t z0 = fidx(N, 2, i, j, k), z1 = fidx(N, 2, i, j, k + 1);
+            for (int q = 0; q < 5; ++q)
+            {
+                double u = A.uc[q * A.ucs + c * A.uzs];
+                double out;
+                if (sizeof(R) == sizeof(double))
+                {
+                    const double dc = (double(F0[q * nf0 + x1]) - double(F0[q * nf0 + x0]))
+                                    + (double(F1[q * nf1 + y1]) - double(F1[q * nf1 + y0]))
+                                    + (double(F2[q * nf2 + z1]) - double(F2[q * nf2 + z0]));
+                    out = u - dc * dt / dl;
+                }
+                else
+                {
+                    const float dc = (float(F0[q * nf0 + x1]) - float(F0[q * nf0 + x0]))
+                                   + (float(F1[q * nf1 + y1]) - float(F1[q * nf1 + y0]))
+                                   + (float(F2[q * nf2 + z1]) - float(F2[q * nf2 + z0]));
+                    out = u - double(dc * dt_over_dl);
+                }
+                if (A.uavg) out = A.uavg[q * NN + c] * 0.5 + out * (1 - 0.5);
+                A.uc_out[q * NN + c] = out;
+            }
+            continue;
+        }
+        int64_t f = t - NN;
+        int axis = 0;
+        if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
+        const int n1 = N + (axis == 1), n2 = N + (axis == 2);
+        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        // solenoidal_difference (mesh_cartesian_3d.hpp:265-274)
+        double cf;
+        if (axis == 0)
+            cf = (ee<R>(A, 2, i, j + 1, k) - ee<R>(A, 2, i, j, k)) - (ee<R>(A, 1, i, j, k + 1) - ee<R>(A, 1, i, j, k));
+        else if (axis == 1)
+            cf = (ee<R>(A, 0, i, j, k + 1) - ee<R>(A, 0, i, j, k)) - (ee<R>(A, 2, i + 1, j, k) - ee<R>(A, 2, i, j, k));
+        else
+            cf = (ee<R>(A, 1, i + 1, j, k) - ee<R>(A, 1, i, j, k)) - (ee<R>(A, 0, i, j + 1, k) - ee<R>(A, 0, i, j, k));
+        double out = A.bf[axis][f] - cf * dt / dl;
+        if (A.bavg[axis]) out = A.bavg[axis][f] * 0.5 + out * (1 - 0.5);
+        A.bf_out[axis][f] = out;
+    }
+}
+
+__global__ void clock_end_kernel(Clock* clock, int rk_order)
+{
+    if (threadIdx.x != 0) return;
+    const double t = clock->time;
+    if (rk_order == 2)
+    {
+        const double t1 = t + clock->dt[0];
+        const double t2 = t1 + clock->dt[1];
+        clock->time = t * 0.5 + t2 * (1 - 0.5);
+    }
+    else
+    {
+        clock->time = t + clock->dt[0];
+    }
+    clock->iteration += 1;
+}
+
+__global__ void div_b_kernel(int N, const double* b1, const double* b2, const double* b3, unsigned long long* out)
+{
+    const int64_t NN = int64_t(N) * N * N;
+    double m = 0.0;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        const double d = (b1[fidx(N, 0, i + 1, j, k)] - b1[fidx(N, 0, i, j, k)])
+                       + (b2[fidx(N, 1, i, j + 1, k)] - b2[fidx(N, 1, i, j, k)])
+                       + (b3[fidx(N, 2, i, j, k + 1)] - b3[fidx(N, 2, i, j, k)]);
+        m = fmax(m, fabs(d));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// Initial state (construct_conserved discretisation, src/scheme_mhd_v1.cpp:311-342)
+struct Mode { double k[3], phase_v, v[3], phase_a, a[3]; };
+
+__device__ inline void mode_field(const Mode* modes, int count, const double x[3], int which, double amp, double out[3])
+{
+    out[0] = out[1] = out[2] = 0.0;
+    for (int m = 0; m < count; ++m)
+    {
+        const Mode& t = modes[m];
+        const double arg = 2.0 * M_PI * (t.k[0] * x[0] + t.k[1] * x[1] + t.k[2] * x[2]) + (which == 0 ? t.phase_v : t.phase_a);
+        const double s = sin(arg);
+        for (int c = 0; c < 3; ++c) out[c] += (which == 0 ? t.v[c] : t.a[c]) * s;
+    }
+    for (int c = 0; c < 3; ++c) out[c] *= amp;
+}
+
+__device__ inline double lin(int i, int N) { return 0.0 + (1.0 - 0.0) * double(i) / double(N + 1 - 1); }
+
+__device__ inline double edge_a(const Mode* modes, int count, double a_amp, int N, int axis, int i, int j, int k)
+{
+    double x[3] = {lin(i, N), lin(j, N), lin(k, N)};
+    if (axis == 0) x[0] = 0.5 * (lin(i, N) + lin(i + 1, N));
+    if (axis == 1) x[1] = 0.5 * (lin(j, N) + lin(j + 1, N));
+    if (axis == 2) x[2] = 0.5 * (lin(k, N) + lin(k + 1, N));
+    double A[3];
+    mode_field(modes, count, x, 1, a_amp, A);
+    return A[axis] * (1.0 / double(N));
+}
+
+__global__ void init_faces_kernel(int N, const Mode* modes, int count, double a_amp, double* b1, double* b2, double* b3)
+{
+    const double dl = 1.0 / double(N);
+    const double da = dl * dl;
+    const int64_t nf0 = nb(N, 0), nf1 = nb(N, 1), nf2 = nb(N, 2);
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nf0 + nf1 + nf2; t += int64_t(gridDim.x) * blockDim.x)
+    {
+        int64_t f = t;
+        int axis = 0;
+        if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
+        const int n1 = N + (axis == 1), n2 = N + (axis == 2);
+        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        auto ae = [&] (int ax, int a, int b, int c) { return edge_a(modes, count, a_amp, N, ax, a, b, c); };
+        if (axis == 0)
+            b1[f] = ((ae(2, i, j + 1, k) - ae(2, i, j, k)) - (ae(1, i, j, k + 1) - ae(1, i, j, k))) / da;
+        else if (axis == 1)
+            b2[f] = ((ae(0, i, j, k + 1) - ae(0, i, j, k)) - (ae(2, i + 1, j, k) - ae(2, i, j, k))) / da;
+        else
+            b3[f] = ((ae(1, i + 1, j, k) - ae(1, i, j, k)) - (ae(0, i, j + 1, k) - ae(0, i, j, k))) / da;
+    }
+}
+
+__global__ void init_cells_kernel(int N, const Mode* modes, int count, double v_amp, double gm, const double* b1,
+                                  const double* b2, const double* b3, double* uc)
+{
+    const int64_t NN = int64_t(N) * N * N;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        const double x[3] = {0.5 * (lin(i, N) + lin(i + 1, N)), 0.5 * (lin(j, N) + lin(j + 1, N)), 0.5 * (lin(k, N) + lin(k + 1, N))};
+        Prim<double> p;
+        p.d = 1.0;
+        mode_field(modes, count, x, 0, v_amp, p.v);
+        p.p = 1.0;
+        p.b[0] = 0.5 * (b1[fidx(N, 0, i, j, k)] + b1[fidx(N, 0, i + 1, j, k)]);
+        p.b[1] = 0.5 * (b2[fidx(N, 1, i, j, k)] + b2[fidx(N, 1, i, j + 1, k)]);
+        p.b[2] = 0.5 * (b3[fidx(N, 2, i, j, k)] + b3[fidx(N, 2, i, j, k + 1)]);
+        double u[5];
+        conserved(p, gm, u);
+        for (int q = 0; q < 5; ++q) uc[q * NN + c] = u[q];
+    }
+}
+
+// ---------------------------------------------------------------- host side
+struct Workspace
+{
+    void* P;
+    void* F[3];
+    void* E[3];
+    double* u1;
+    double* b1[3];
+};
+
+int64_t workspace_bytes(int N, int precision, bool rk2)
+{
+    const int64_t NN = int64_t(N) * N * N;
+    const int64_t NF = nb(N, 0);
+    const int64_t r = precision == MARA_MIXED ? 4 : 8;
+    // seven 256-byte aligned regions (P, F[3], E[3]) plus alignment slack
+    int64_t bytes = NN * r * 8 + NF * r * 3 * (5 + 2) + 8 * 256;
+    if (rk2) bytes += 8 * (5 * NN + nb(N, 0) + nb(N, 1) + nb(N, 2));
+    return bytes + 256;
+}
+
+Workspace carve(void* base, int N, int precision, bool rk2)
+{
+    const int64_t NN = int64_t(N) * N * N;
+    const int64_t r = precision == MARA_MIXED ? 4 : 8;
+    char* p = static_cast<char*>(base);
+    const int64_t NF = nb(N, 0);   // every face array has (N+1) N^2 entries
+    auto up = [] (char* q) { return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255)); };
+    Workspace w{};
+    w.P = p; p = up(p + 8 * NN * r);
+    for (int a = 0; a < 3; ++a) { w.F[a] = p; p = up(p + 5 * NF * r); }
+    for (int a = 0; a < 3; ++a) { w.E[a] = p; p = up(p + 2 * NF * r); }
+    if (rk2)
+    {
+        w.u1 = reinterpret_cast<double*>(p); p += 5 * NN * 8;
+        for (int a = 0; a < 3; ++a) { w.b1[a] = reinterpret_cast<double*>(p); p += nb(N, a) * 8; }
+    }
+    return w;
+}
+
+int check(const mara_mhd_params* mp)
+{
+    MARA_REQUIRE(mp != nullptr, "mhd: params is null");
+    MARA_REQUIRE(mp->N >= 4 && mp->N <= 1024, "mhd: N must be in [4, 1024]");
+    MARA_REQUIRE(mp->gamma_law_index > 1.0, "mhd: gamma_law_index must exceed 1");
+    MARA_REQUIRE(mp->cfl > 0.0, "mhd: cfl must be positive");
+    return MARA_OK;
+}
+
+inline int blocks_for(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+// One stage: u_out/b_out = advance_mhd_ct(u_in/b_in) [averaged with avg].
+template<typename R>
+int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
+          const double* u_in, int64_t ucs, int64_t uzs, const double* const b_in[3],
+          const double* uavg, const double* const bavg[3], double* u_out, double* const b_out[3], cudaStream_t s)
+{
+    const int N = mp->N;
+    const int64_t NN = int64_t(N) * N * N;
+    Args A;
+    std::memset(&A, 0, sizeof A);
+    A.N = N;
+    A.gamma = mp->gamma_law_index;
+    A.dl = 1.0 / double(N);
+    A.cfl = mp->cfl;
+    A.theta = mp->plm_theta;
+    A.uc = u_in;
+    A.ucs = ucs;
+    A.uzs = uzs;
+    A.uavg = uavg;
+    A.uc_out = u_out;
+    for (int a = 0; a < 3; ++a)
+    {
+        A.bf[a] = b_in[a];
+        A.bavg[a] = bavg ? bavg[a] : nullptr;
+        A.bf_out[a] = b_out[a];
+        A.F[a] = w.F[a];
+        A.E[a] = w.E[a];
+    }
+    A.P = w.P;
+    A.clock = clock;
+    A.stage = st;
+    prim_kernel<R><<<blocks_for(NN), 256, 0, s>>>(A);
+    if (int r = launch_status("mhd prim_kernel")) return r;
+    dt_kernel<<<1, 32, 0, s>>>(clock, st, mp->cfl, A.dl, 0);
+    if (int r = launch_status("mhd dt_kernel")) return r;
+    face_kernel<R, 0><<<blocks_for(nb(N, 0)), 256, 0, s>>>(A);
+    face_kernel<R, 1><<<blocks_for(nb(N, 1)), 256, 0, s>>>(A);
+    face_kernel<R, 2><<<blocks_for(nb(N, 2)), 256, 0, s>>>(A);
+    if (int r = launch_status("mhd face_kernel")) return r;
+    update_kernel<R><<<blocks_for(NN + nb(N, 0) + nb(N, 1) + nb(N, 2)), 256, 0, s>>>(A);
+    return launch_status("mhd update_kernel");
+}
+
+int run_stage(int precision, const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
+              const double* u_in, int64_t ucs, int64_t uzs, const double* const b_in[3], const double* uavg,
+              const double* const bavg[3], double* u_out, double* const b_out[3], cudaStream_t s)
+{
+    if (precision == MARA_MIXED)
+        return stage<float>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, s);
+    return stage<double>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, s);
+}
+
+} // namespace mhd
+} // namespace mara
+
+using namespace mara;
+using namespace mara::mhd;
+
+extern "C" {
+
+int64_t mara_mhd_clock_bytes(void) { return int64_t(sizeof(Clock)); }
+
+int64_t mara_mhd_workspace_bytes(const mara_mhd_params* mp, int32_t rk_order, int32_t precision)
+{
+    if (check(mp)) return -1;
+    return workspace_bytes(mp->N, precision, rk_order == 2);
+}
+
+int mara_mhd_clock_init(void* clock, double time, void* stream)
+{
+    MARA_REQUIRE(clock != nullptr, "mara_mhd_clock_init: clock is null");
+    Clock c;
+    std::memset(&c, 0, sizeof c);
+    c.time = time;
+    cudaStream_t s = as_stream(stream);
+    MARA_CUDA(cudaMemcpyAsync(clock, &c, sizeof c, cudaMemcpyHostToDevice, s));
+    MARA_CUDA(cudaStreamSynchronize(s));
+    return MARA_OK;
+}
+
+int mara_mhd_advance_ct(const mara_mhd_params* mp, const double* uc, int64_t component_stride, int64_t cell_stride,
+                        const double* bf1, const double* bf2, const double* bf3, double* uc_out, double* bf1_out,
+                        double* bf2_out, double* bf3_out, void* clock, int32_t precision, void* workspace,
+                        void* stream)
+{
+    if (int r = check(mp)) return r;
+    MARA_REQUIRE(uc && bf1 && bf2 && bf3 && uc_out && bf1_out && bf2_out && bf3_out && clock && workspace,
+                 "mara_mhd_advance_ct: null buffer");
+    MARA_REQUIRE(precision == MARA_FP64 || precision == MARA_MIXED, "mara_mhd_advance_ct: bad precision");
+    MARA_REQUIRE(uc_out != uc && bf1_out != bf1 && bf2_out != bf2 && bf3_out != bf3,
+                 "mara_mhd_advance_ct: outputs must not alias inputs");
+    cudaStream_t s = as_stream(stream);
+    Clock* c = static_cast<Clock*>(clock);
+    Workspace w = carve(workspace, mp->N, precision, false);
+    const double* b_in[3] = {bf1, bf2, bf3};
+    double* b_out[3] = {bf1_out, bf2_out, bf3_out};
+    dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);
+    if (int r = launch_status("mhd dt_kernel")) return r;
+    if (int r = run_stage(precision, mp, w, c, 0, uc, component_stride, cell_stride, b_in, nullptr, nullptr, uc_out,
+                          b_out, s)) return r;
+    clock_end_kernel<<<1, 32, 0, s>>>(c, 1);
+    return launch_status("mhd clock_end_kernel");
+}
+
+int mara_mhd_advance(const mara_mhd_params* mp, double* uc, double* bf1, double* bf2, double* bf3, void* clock,
+                     int32_t steps, int32_t rk_order, int32_t precision, void* workspace, void* stream)
+{
+    if (int r = check(mp)) return r;
+    MARA_REQUIRE(uc && bf1 && bf2 && bf3 && clock && workspace, "mara_mhd_advance: null buffer");
+    MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_mhd_advance: rk_order must be 1 or 2");
+    MARA_REQUIRE(precision == MARA_FP64 || precision == MARA_MIXED, "mara_mhd_advance: bad precision");
+    MARA_REQUIRE(steps >= 0, "mara_mhd_advance: negative step count");
+    MARA_REQUIRE(rk_order == 2, "mara_mhd_advance: in-place forward Euler is not supported; use mara_mhd_advance_ct");
+    cudaStream_t s = as_stream(stream);
+    Clock* c = static_cast<Clock*>(clock);
+    Workspace w = carve(workspace, mp->N, precision, true);
+    const int64_t NN = int64_t(mp->N) * mp->N * mp->N;
+    double* b0[3] = {bf1, bf2, bf3};
+    const double* b0c[3] = {bf1, bf2, bf3};
+    const double* b1c[3] = {w.b1[0], w.b1[1], w.b1[2]};
+    for (int step = 0; step < steps; ++step)
+    {
+        dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);
+        if (int r = launch_status("mhd dt_kernel")) return r;
+        // stage 1: (u1, b1) = advance_mhd_ct(u0, b0) with its own dt
+        if (int r = run_stage(precision, mp, w, c, 0, uc, NN, 1, b0c, nullptr, nullptr, w.u1, w.b1, s)) return r;
+        // stage 2: u0 <- u0/2 + advance_mhd_ct(u1, b1)/2, in place (each element reads its own u0)
+        if (int r = run_stage(precision, mp, w, c, 1, w.u1, NN, 1, b1c, uc, b0c, uc, b0, s)) return r;
+        clock_end_kernel<<<1, 32, 0, s>>>(c, 2);
+        if (int r = launch_status("mhd clock_end_kernel")) return r;
+    }
+    return MARA_OK;
+}
+
+int mara_mhd_mode_table(uint64_t seed, int32_t modes, double* table)
+{
+    MARA_REQUIRE(modes > 0 && modes <= 4096 && table, "mara_mhd_mode_table: bad argument");
+    auto hash = [seed] (uint64_t i) {
+        uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return z;
+    };
+    auto uni = [&] (uint64_t i) { return double(hash(i) >> 11) * 0x1.0p-53; };
+    uint64_t counter = 0;
+    for (int m = 0; m < modes; ++m)
+    {
+        double k[3];
+        for (int attempt = 0;; ++attempt)
+        {
+            for (int c = 0; c < 3; ++c) k[c] = double(int(hash(counter++) % 9) - 4);
+            const double kk = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+            if (kk > 0.0 && kk <= 16.0) break;
+            if (attempt > 10000) return fail(MARA_ERR_NUMERIC, "mara_mhd_mode_table: no admissible wavevector");
+        }
+        const double kn = std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+        auto unit = [&] (double out[3]) {
+            const double mu = 2.0 * uni(counter++) - 1.0, ph = 2.0 * M_PI * uni(counter++);
+            const double st = std::sqrt(1.0 - mu * mu);
+            out[0] = st * std::cos(ph); out[1] = st * std::sin(ph); out[2] = mu;
+        };
+        double* t = table + 11 * m;
+        t[0] = k[0]; t[1] = k[1]; t[2] = k[2];
+        t[3] = 2.0 * M_PI * uni(counter++);
+        unit(t + 4);
+        t[7] = 2.0 * M_PI * uni(counter++);
+        // polarisation of A transverse to k, scaled by 1/|k| so every mode of B = curl A has unit amplitude / 2pi
+        double r[3];
+        double a[3], norm2 = 0.0;
+        do {
+            unit(r);
+            const double rk = (r[0] * k[0] + r[1] * k[1] + r[2] * k[2]) / (kn * kn);
+            norm2 = 0.0;
+            for (int c = 0; c < 3; ++c) { a[c] = r[c] - rk * k[c]; norm2 += a[c] * a[c]; }
+        } while (norm2 < 1e-6);
+        for (int c = 0; c < 3; ++c) t[8 + c] = a[c] / (std::sqrt(norm2) * kn);
+    }
+    return MARA_OK;
+}
+
+int mara_mhd_initial_state(const mara_mhd_params* mp, const double* table, int32_t modes, double v_amp, double a_amp,
+                           double* uc, double* bf1, double* bf2, double* bf3, void* workspace, void* stream)
+{
+    if (int r = check(mp)) return r;
+    MARA_REQUIRE(table && modes > 0 && uc && bf1 && bf2 && bf3 && workspace, "mara_mhd_initial_state: bad argument");
+    cudaStream_t s = as_stream(stream);
+    // the mode table goes through the caller's workspace (no allocation)
+    MARA_CUDA(cudaMemcpyAsync(workspace, table, sizeof(double) * 11 * modes, cudaMemcpyHostToDevice, s));
+    MARA_CUDA(cudaStreamSynchronize(s));
+    const Mode* m = static_cast<const Mode*>(workspace);
+    const int N = mp->N;
+    init_faces_kernel<<<blocks_for(nb(N, 0) * 3), 256, 0, s>>>(N, m, modes, a_amp, bf1, bf2, bf3);
+    if (int r = launch_status("mhd init_faces_kernel")) return r;
+    init_cells_kernel<<<blocks_for(int64_t(N) * N * N), 256, 0, s>>>(N, m, modes, v_amp, mp->gamma_law_index, bf1, bf2,
+                                                                     bf3, uc);
+    return launch_status("mhd init_cells_kernel");
+}
+
+int mara_mhd_max_div_b(const mara_mhd_params* mp, const double* bf1, const double* bf2, const double* bf3,
+                       double* out, void* stream)
+{
+    if (int r = check(mp)) return r;
+    MARA_REQUIRE(bf1 && bf2 && bf3 && out, "mara_mhd_max_div_b: null buffer");
+    cudaStream_t s = as_stream(stream);
+    MARA_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+    div_b_kernel<<<blocks_for(int64_t(mp->N) * mp->N * mp->N), 256, 0, s>>>(
+        mp->N, bf1, bf2, bf3, reinterpret_cast<unsigned long long*>(out));
+    return launch_status("mhd div_b_kernel");
+}
+
+} // extern "C"

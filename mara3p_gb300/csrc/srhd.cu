@@ -206,6 +206,56 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
     }
 }
 
+// srhd::conserved_density (src/physics_srhd.hpp:291-304), c = 1
+__device__ inline void conserved_density(const double p[5], double gm, double u[5])
+{
+    const double W = sqrt(1.0 + (p[1] * p[1] + p[2] * p[2] + p[3] * p[3]));
+    const double D = p[0] * W;
+    const double h = (p[0] * 1.0 + p[4] * (1.0 + 1.0 / (gm - 1.0))) / p[0];
+    u[0] = D;
+    u[1] = D * h * p[1] / 1.0;
+    u[2] = D * h * p[2] / 1.0;
+    u[3] = D * h * p[3] / 1.0;
+    u[4] = D * (h * W - 1.0 * 1.0) - p[4];
+}
+
+__device__ inline double uniform01(uint64_t seed, uint64_t i)
+{
+    uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return double(z >> 11) * 0x1.0p-53;
+}
+
+// Seeded zones: rho, p log-uniform, Lorentz factor log-uniform in [1, w_hi]
+// in an isotropic direction; primitives and conserved, SoA [5][n].
+__global__ void seeded_zones_kernel(uint64_t seed, int64_t n, double rho_lo, double rho_hi, double p_lo, double p_hi,
+                                    double w_hi, double gm, double* prim, double* cons)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        const uint64_t k = uint64_t(i) * 5;
+        const double r0 = uniform01(seed, k), r1 = uniform01(seed, k + 1), r2 = uniform01(seed, k + 2);
+        const double r3 = uniform01(seed, k + 3), r4 = uniform01(seed, k + 4);
+        const double rho = rho_lo * exp(r0 * log(rho_hi / rho_lo));
+        const double pg = p_lo * exp(r1 * log(p_hi / p_lo));
+        const double W = exp(r2 * log(w_hi));
+        const double ub = sqrt(W * W - 1.0);
+        const double mu = 2.0 * r3 - 1.0;
+        const double ph = 2.0 * M_PI * r4;
+        const double st = sqrt(1.0 - mu * mu);
+        const double q[5] = {rho, ub * st * cos(ph), ub * st * sin(ph), ub * mu, pg};
+        double u[5];
+        conserved_density(q, gm, u);
+        for (int c = 0; c < 5; ++c)
+        {
+            prim[c * n + i] = q[c];
+            cons[c * n + i] = u[c];
+        }
+    }
+}
+
 } // namespace srhd
 } // namespace mara
 
@@ -254,6 +304,20 @@ int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component
     int blocks = int(std::min<int64_t>((n + mlp::kZones - 1) / mlp::kZones, 152 * 8));
     srhd::c2p_mlp_kernel<<<blocks, mlp::kThreads, 0, s>>>(a);
     return launch_status("c2p_mlp_kernel");
+}
+
+int mara_srhd_seeded_zones(uint64_t seed, int64_t n, double rho_lo, double rho_hi, double p_lo, double p_hi,
+                           double w_hi, double gamma_law_index, double* prim, double* cons, void* stream)
+{
+    MARA_REQUIRE(n >= 0, "mara_srhd_seeded_zones: negative count");
+    if (n == 0) return MARA_OK;
+    MARA_REQUIRE(prim && cons, "mara_srhd_seeded_zones: null buffer");
+    MARA_REQUIRE(rho_lo > 0 && rho_hi >= rho_lo && p_lo > 0 && p_hi >= p_lo && w_hi >= 1.0,
+                 "mara_srhd_seeded_zones: bad ranges");
+    int blocks = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
+    srhd::seeded_zones_kernel<<<blocks, 256, 0, as_stream(stream)>>>(seed, n, rho_lo, rho_hi, p_lo, p_hi, w_hi,
+                                                                     gamma_law_index, prim, cons);
+    return launch_status("seeded_zones_kernel");
 }
 
 } // extern "C"

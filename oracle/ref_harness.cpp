@@ -16,6 +16,7 @@
 #include "parallel_thread_pool.hpp"
 #include "physics_srhd.hpp"
 #include "physics_two_body.hpp"
+#include "scheme_mhd_v1.hpp"
 #include "scheme_plm_gradient.hpp"
 
 namespace {
@@ -243,6 +244,89 @@ double ref_plm_gradient(double theta, double yl, double y0, double yr)
 {
     using q = dimensional::unit_scalar;
     return mara::plm_gradient_scalar_t<double>{0.0, 1.0, 2.0, theta}(numeric::tuple(q(yl), q(y0), q(yr))).value;
+}
+
+// mhd::riemann_hlle (src/physics_mhd.hpp:358-390) on n face pairs of 8
+// primitives; axis in {1, 2, 3}; out: flux (5) then E-field (3) per face.
+void ref_mhd_riemann_hlle(const double* pl, const double* pr, const double* bl, int64_t n, uint32_t axis,
+                          double gamma_law_index, double* out)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        auto a = to_tuple<mhd::primitive_t>(pl + 8 * i);
+        auto b = to_tuple<mhd::primitive_t>(pr + 8 * i);
+        auto [f, e] = mhd::riemann_hlle(a, b, mhd::unit_magnetic_field(bl[i]), geometric::unit_vector_on(axis),
+                                        gamma_law_index);
+        from_tuple(f, out + 8 * i);
+        out[8 * i + 5] = e.component_1().value;
+        out[8 * i + 6] = e.component_2().value;
+        out[8 * i + 7] = e.component_3().value;
+    }
+}
+
+// mhd::conserved_density then mhd::recover_primitive (the round trip of
+// test_mhd, src/physics_mhd.hpp:405-415) on n primitive 8-tuples.
+int ref_mhd_round_trip(const double* prim, int64_t n, double gamma_law_index, double* cons, double* back)
+{
+    try {
+        for (int64_t i = 0; i < n; ++i)
+        {
+            auto p = to_tuple<mhd::primitive_t>(prim + 8 * i);
+            auto u = mhd::conserved_density(p, gamma_law_index);
+            from_tuple(u, cons + 5 * i);
+            from_tuple(mhd::recover_primitive(u, mhd::magnetic_field_vector(p), gamma_law_index), back + 8 * i);
+        }
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// mara::advance_mhd_ct (src/scheme_mhd_v1.cpp:265-299) on one periodic cube
+// with local_periodic_boundary_extension. uc [N][N][N][5]; bf1 [N+1][N][N],
+// bf2 [N][N+1][N], bf3 [N][N][N+1]. Returns t + dt, or -1 if it threw.
+double ref_mhd_advance_ct(int32_t N, double time, const double* uc, const double* bf1, const double* bf2,
+                          const double* bf3, double dl, double cfl, double plm_theta,
+                          double* uc_out, double* bf1_out, double* bf2_out, double* bf3_out)
+{
+    try {
+        using B = mhd::unit_magnetic_field;
+        const std::size_t n = N;
+        auto u = nd::make_unique_array<mhd::conserved_density_t, 3>(nd::uivec(n, n, n));
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = 0; j < n; ++j)
+                for (std::size_t k = 0; k < n; ++k)
+                    u(i, j, k) = to_tuple<mhd::conserved_density_t>(uc + ((i * n + j) * n + k) * 5);
+        auto face = [&] (const double* src, std::size_t a, std::size_t b, std::size_t c) {
+            auto f = nd::make_unique_array<B, 3>(nd::uivec(a, b, c));
+            for (std::size_t i = 0; i < a; ++i)
+                for (std::size_t j = 0; j < b; ++j)
+                    for (std::size_t k = 0; k < c; ++k)
+                        f(i, j, k) = B(src[(i * b + j) * c + k]);
+            return nd::make_shared_array(std::move(f));
+        };
+        auto bc = mara::local_periodic_boundary_extension();
+        auto [t1, u1, b1, b2, b3] = mara::advance_mhd_ct(time, nd::make_shared_array(std::move(u)),
+                                                         face(bf1, n + 1, n, n), face(bf2, n, n + 1, n),
+                                                         face(bf3, n, n, n + 1), dl, cfl, plm_theta, *bc);
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = 0; j < n; ++j)
+                for (std::size_t k = 0; k < n; ++k)
+                    from_tuple(u1(i, j, k), uc_out + ((i * n + j) * n + k) * 5);
+        auto read = [] (const auto& f, double* dst) {
+            std::size_t a = shape(f, 0), b = shape(f, 1), c = shape(f, 2);
+            for (std::size_t i = 0; i < a; ++i)
+                for (std::size_t j = 0; j < b; ++j)
+                    for (std::size_t k = 0; k < c; ++k)
+                        dst[(i * b + j) * c + k] = f(i, j, k).value;
+        };
+        read(b1, bf1_out);
+        read(b2, bf2_out);
+        read(b3, bf3_out);
+        return t1.value;
+    } catch (...) {
+        return -1.0;
+    }
 }
 
 } // extern "C"

@@ -158,6 +158,64 @@ def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
     return out
 
 
+MHD_CASE = dict(N=8, modes=12, seed=3, gamma=5.0 / 3.0, cfl=0.3, theta=1.5)
+
+
+def mhd_fixtures(o, r) -> dict[str, np.ndarray]:
+    """advance_mhd_ct and two mhd3d RK2 steps on a seeded 8^3 cube, from the reference."""
+    c = MHD_CASE
+    N, modes, g = c["N"], c["modes"], c["gamma"]
+    o.oracle_mhd_round_trip.restype = ctypes.c_int64
+    r.ref_mhd_advance_ct.restype = ctypes.c_double
+    table = np.zeros(11 * modes)
+    assert o.oracle_mhd_mode_table(ctypes.c_uint64(c["seed"]), modes, dptr(table)) == 0
+    half = np.sqrt(modes / 2.0)
+    v_amp, a_amp = 0.5 / half, np.sqrt(2.0 / 10.0) / (2.0 * np.pi * half)
+    uc = np.zeros(N ** 3 * 5)
+    bf = [np.zeros((N + 1) * N * N) for _ in range(3)]
+    o.oracle_mhd_initial(N, dptr(table), modes, ctypes.c_double(v_amp), ctypes.c_double(a_amp), ctypes.c_double(g),
+                         dptr(uc), *[dptr(b) for b in bf])
+    dl = 1.0 / N
+    out = {"mhd/table": table, "mhd/amp": np.array([v_amp, a_amp]), "mhd/uc": uc.copy(),
+           "mhd/params": np.array([N, g, c["cfl"], c["theta"]])}
+    for k in range(3):
+        out[f"mhd/bf{k + 1}"] = bf[k].copy()
+
+    def step(u, b, t):
+        u1 = np.zeros_like(u)
+        b1 = [np.zeros_like(x) for x in b]
+        t1 = r.ref_mhd_advance_ct(N, ctypes.c_double(t), dptr(u), *[dptr(x) for x in b], ctypes.c_double(dl),
+                                  ctypes.c_double(c["cfl"]), ctypes.c_double(c["theta"]), dptr(u1), *[dptr(x) for x in b1])
+        assert t1 > t
+        return u1, b1, t1
+
+    u1, b1, t1 = step(uc, bf, 0.0)
+    out["mhd/step_uc"] = u1
+    for k in range(3):
+        out[f"mhd/step_bf{k + 1}"] = b1[k]
+    out["mhd/step_time"] = np.array([t1])
+    # examples/mhd3d.cpp RK2: each stage its own dt, states and times averaged
+    u, b, t = uc.copy(), [x.copy() for x in bf], 0.0
+    for _ in range(2):
+        ua, ba, ta = step(u, b, t)
+        ub, bb, tb = step(ua, ba, ta)
+        u = u * 0.5 + ub * (1 - 0.5)
+        b = [x * 0.5 + y * (1 - 0.5) for x, y in zip(b, bb)]
+        t = t * 0.5 + tb * (1 - 0.5)
+    out["mhd/rk2_uc"] = u
+    for k in range(3):
+        out[f"mhd/rk2_bf{k + 1}"] = b[k]
+    out["mhd/rk2_time"] = np.array([t])
+    # the reference's test_mhd states (src/physics_mhd.hpp:409-413)
+    kat = np.array([[1.0, 0, 0, 0, 1.0, 0, 0, 0], [1.5, 0, 0, 0, 1e3, 0, 0, 0], [1.0, 0, 0, 0, 1.0, 0, 0, 0],
+                    [5.7, 1.0, 2.0, 3.0, 5.0, 0, 0, 0], [5.7, 1.0, 2.0, 3.0, 5.0, 3.0, 2.0, 1.0]]).ravel()
+    cons = np.zeros(5 * 5)
+    back = np.zeros_like(kat)
+    assert r.ref_mhd_round_trip(dptr(kat), ctypes.c_int64(5), ctypes.c_double(g), dptr(cons), dptr(back)) == 0
+    out.update({"mhd_kat/prim": kat, "mhd_kat/cons": cons, "mhd_kat/back": back})
+    return out
+
+
 def main() -> None:
     o = load_oracle()
     r = load_reference()
@@ -170,6 +228,7 @@ def main() -> None:
     fixtures.update(binary_fixture(r))
     np.savez_compressed(HERE / "minidisk_golden.npz", **fixtures)
     np.savez_compressed(HERE / "srhd_golden.npz", **srhd_fixtures(o, r))
+    np.savez_compressed(HERE / "mhd_golden.npz", **mhd_fixtures(o, r))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size, "bytes")
 

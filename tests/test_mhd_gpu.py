@@ -1,0 +1,123 @@
+"""GPU parity of the constrained-transport MHD scheme (through the C ABI)
+against the reference's golden fixtures and the oracle.
+
+Tolerances: FP64 relative L1 per component <= 1e-12 after one step and two
+RK2 steps (FMA contraction and libm only); div B at rounding; mixed path
+(FP32 fluxes/EMFs, FP64 state) relative L1 <= 1e-5 after 20 RK2 steps with
+div B still at FP64 rounding."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle.oracle import dptr
+from tests.helpers import rel_l1_components
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mh():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import mara3p_gb300.mhd as m
+    return m
+
+
+@pytest.fixture(scope="module")
+def mhd_golden():
+    from pathlib import Path
+    return dict(np.load(Path(__file__).resolve().parent / "golden" / "mhd_golden.npz"))
+
+
+def golden_state(mh, g):
+    N, gamma, cfl, theta = g["mhd/params"]
+    N = int(N)
+    cfg = mh.MhdConfig(N=N, gamma_law_index=gamma, cfl=cfl, plm_theta=theta)
+    s = mh.empty_state(cfg)
+    s.uc.copy_(torch.from_numpy(g["mhd/uc"].reshape(N, N, N, 5).transpose(3, 0, 1, 2).copy()))
+    shapes = [(N + 1, N, N), (N, N + 1, N), (N, N, N + 1)]
+    for k in range(3):
+        s.bf[k].copy_(torch.from_numpy(g[f"mhd/bf{k + 1}"].reshape(shapes[k])))
+    return s
+
+
+def soa(uc_aos, N):
+    return uc_aos.reshape(N, N, N, 5).transpose(3, 0, 1, 2).reshape(5, -1)
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_advance_ct_fp64_matches_reference(mh, mhd_golden, layout):
+    g = mhd_golden
+    s = golden_state(mh, g)
+    N = s.cfg.N
+    uc_in = None
+    if layout == "aos":
+        uc_in = torch.from_numpy(g["mhd/uc"].copy()).cuda()
+    out, clock = mh.advance_ct(s, uc_in=uc_in, layout=layout)
+    assert abs(clock.read()["time"] - g["mhd/step_time"][0]) <= 1e-15
+    assert rel_l1_components(out.uc.cpu().numpy().reshape(5, -1), soa(g["mhd/step_uc"], N), 5) < 1e-12
+    for k in range(3):
+        ref = g[f"mhd/step_bf{k + 1}"]
+        assert np.abs(out.bf[k].cpu().numpy().ravel() - ref).sum() / np.abs(ref).sum() < 1e-12
+
+
+def test_rk2_fp64_matches_reference(mh, mhd_golden):
+    g = mhd_golden
+    s = golden_state(mh, g)
+    N = s.cfg.N
+    run = mh.Run(s)
+    run.advance(2)
+    c = run.clock.read()
+    assert abs(c["time"] - g["mhd/rk2_time"][0]) <= 1e-15
+    assert c["failures"] == 0
+    assert rel_l1_components(s.uc.cpu().numpy().reshape(5, -1), soa(g["mhd/rk2_uc"], N), 5) < 1e-12
+    for k in range(3):
+        ref = g[f"mhd/rk2_bf{k + 1}"]
+        assert np.abs(s.bf[k].cpu().numpy().ravel() - ref).sum() / np.abs(ref).sum() < 1e-12
+
+
+def test_initial_state_matches_oracle(mh, oracle, mhd_golden):
+    g = mhd_golden
+    N = int(g["mhd/params"][0])
+    cfg = mh.MhdConfig(N=N)
+    s = mh.initial_state(cfg, seed=3, modes=12)
+    assert np.allclose(s.uc.cpu().numpy().reshape(5, -1), soa(g["mhd/uc"], N), rtol=1e-12, atol=1e-13)
+    for k in range(3):
+        assert np.allclose(s.bf[k].cpu().numpy().ravel(), g[f"mhd/bf{k + 1}"], rtol=1e-12, atol=1e-13)
+
+
+def test_rk2_fp64_matches_oracle_longer(mh, oracle):
+    """32^3, 10 RK2 steps: FP64 GPU vs the oracle, and div B at rounding."""
+    oracle.oracle_mhd_rk2.restype = ctypes.c_double
+    cfg = mh.MhdConfig(N=32)
+    s = mh.initial_state(cfg, seed=11, modes=24)
+    N = cfg.N
+    uc = np.ascontiguousarray(s.uc.cpu().numpy().reshape(5, -1).T).ravel()
+    bf = [b.cpu().numpy().ravel().copy() for b in s.bf]
+    run = mh.Run(s)
+    run.advance(10)
+    t = oracle.oracle_mhd_rk2(N, dptr(uc), *[dptr(b) for b in bf], ctypes.c_double(0.0), 10, ctypes.c_double(1.0 / N),
+                              ctypes.c_double(cfg.cfl), ctypes.c_double(cfg.plm_theta), ctypes.c_double(cfg.gamma_law_index))
+    assert abs(run.clock.read()["time"] - t) <= 1e-13 * t
+    assert rel_l1_components(s.uc.cpu().numpy().reshape(5, -1), soa(uc, N), 5) < 1e-11
+    for k in range(3):
+        assert np.abs(s.bf[k].cpu().numpy().ravel() - bf[k]).sum() / np.abs(bf[k]).sum() < 1e-11
+    b_scale = max(float(b.abs().max()) for b in s.bf)
+    assert run.max_div_b() < 1e-13 * b_scale
+
+
+def test_mixed_close_to_fp64_and_divergence_free(mh):
+    cfg = mh.MhdConfig(N=32)
+    a = mh.initial_state(cfg, seed=5, modes=24)
+    b = mh.initial_state(cfg, seed=5, modes=24)
+    ra, rb = mh.Run(a), mh.Run(b, precision=mh.MIXED)
+    ra.advance(20)
+    rb.advance(20)
+    assert rel_l1_components(b.uc.cpu().numpy().reshape(5, -1), a.uc.cpu().numpy().reshape(5, -1), 5) < 1e-5
+    b_scale = max(float(x.abs().max()) for x in b.bf)
+    assert rb.max_div_b() < 1e-13 * b_scale
+    assert rb.clock.read()["failures"] == 0

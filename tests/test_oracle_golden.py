@@ -123,3 +123,80 @@ def test_srhd_riemann_bitexact(oracle, srhd_golden, solver, axis):
                                      int(solver == "hllc"), dptr(f))
     assert bad == 0
     assert np.array_equal(f, srhd_golden[f"srhd_riemann/{solver}/axis{axis}"])
+
+
+@pytest.fixture(scope="module")
+def mhd_golden():
+    from pathlib import Path
+    return dict(np.load(Path(__file__).resolve().parent / "golden" / "mhd_golden.npz"))
+
+
+def _mhd_oracle(oracle):
+    for f in (oracle.oracle_mhd_advance_ct, oracle.oracle_mhd_rk2, oracle.oracle_mhd_max_div_b):
+        f.restype = ctypes.c_double
+    oracle.oracle_mhd_round_trip.restype = ctypes.c_int64
+    return oracle
+
+
+def test_mhd_initial_state_and_table(oracle, mhd_golden):
+    """The oracle's mode table and construct_conserved discretisation
+    reproduce the fixture's inputs; the library's host table agrees."""
+    o = _mhd_oracle(oracle)
+    N, g = int(mhd_golden["mhd/params"][0]), mhd_golden["mhd/params"][1]
+    table = mhd_golden["mhd/table"]
+    modes = table.size // 11
+    t2 = np.zeros_like(table)
+    assert o.oracle_mhd_mode_table(ctypes.c_uint64(3), modes, dptr(t2)) == 0
+    assert np.array_equal(t2, table)
+    from mara3p_gb300 import mhd
+    assert np.array_equal(mhd.mode_table(3, modes), table)
+    v_amp, a_amp = mhd_golden["mhd/amp"]
+    assert np.allclose(mhd.amplitudes(modes), (v_amp, a_amp), rtol=1e-15)
+    uc = np.zeros(N ** 3 * 5)
+    bf = [np.zeros((N + 1) * N * N) for _ in range(3)]
+    o.oracle_mhd_initial(N, dptr(table), modes, ctypes.c_double(v_amp), ctypes.c_double(a_amp), ctypes.c_double(g),
+                         dptr(uc), *[dptr(b) for b in bf])
+    assert np.array_equal(uc, mhd_golden["mhd/uc"])
+    for k in range(3):
+        assert np.array_equal(bf[k], mhd_golden[f"mhd/bf{k + 1}"])
+    assert o.oracle_mhd_max_div_b(N, *[dptr(b) for b in bf]) < 1e-14
+
+
+def test_mhd_advance_ct_bitexact(oracle, mhd_golden):
+    o = _mhd_oracle(oracle)
+    N, g, cfl, theta = mhd_golden["mhd/params"]
+    N = int(N)
+    outs = [np.zeros(N ** 3 * 5)] + [np.zeros((N + 1) * N * N) for _ in range(3)]
+    dt = o.oracle_mhd_advance_ct(N, dptr(mhd_golden["mhd/uc"]), *[dptr(mhd_golden[f"mhd/bf{k}"]) for k in (1, 2, 3)],
+                                 ctypes.c_double(1.0 / N), ctypes.c_double(cfl), ctypes.c_double(theta),
+                                 ctypes.c_double(g), *[dptr(a) for a in outs])
+    assert dt == mhd_golden["mhd/step_time"][0]
+    assert np.array_equal(outs[0], mhd_golden["mhd/step_uc"])
+    for k in range(3):
+        assert np.array_equal(outs[k + 1], mhd_golden[f"mhd/step_bf{k + 1}"])
+
+
+def test_mhd_rk2_bitexact(oracle, mhd_golden):
+    o = _mhd_oracle(oracle)
+    N, g, cfl, theta = mhd_golden["mhd/params"]
+    N = int(N)
+    uc = mhd_golden["mhd/uc"].copy()
+    bf = [mhd_golden[f"mhd/bf{k}"].copy() for k in (1, 2, 3)]
+    t = o.oracle_mhd_rk2(N, dptr(uc), *[dptr(b) for b in bf], ctypes.c_double(0.0), 2, ctypes.c_double(1.0 / N),
+                         ctypes.c_double(cfl), ctypes.c_double(theta), ctypes.c_double(g))
+    assert t == mhd_golden["mhd/rk2_time"][0]
+    assert np.array_equal(uc, mhd_golden["mhd/rk2_uc"])
+    for k in range(3):
+        assert np.array_equal(bf[k], mhd_golden[f"mhd/rk2_bf{k + 1}"])
+
+
+def test_mhd_reference_known_answers(oracle, mhd_golden):
+    """test_mhd's round trips (src/physics_mhd.hpp:405-415): within 1e-10."""
+    o = _mhd_oracle(oracle)
+    kat = mhd_golden["mhd_kat/prim"]
+    cons = np.zeros(25)
+    back = np.zeros_like(kat)
+    assert o.oracle_mhd_round_trip(dptr(kat), ctypes.c_int64(5), ctypes.c_double(5.0 / 3.0), dptr(cons), dptr(back)) == 0
+    assert np.array_equal(cons, mhd_golden["mhd_kat/cons"])
+    assert np.array_equal(back, mhd_golden["mhd_kat/back"])
+    assert np.all(np.abs(back - kat) < 1e-10)

@@ -156,7 +156,9 @@ def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
     one more Newton step but the Lorentz factor W of the step before
     (src/physics_srhd.hpp:257-265), so its own answer is defined only to:
       p      — to rounding where well conditioned (p > 1e-3 (tau + D));
-      rho, u — to |dW/W| <~ W^2 * 1e-12 / (tau + D) (the last iterate's spread).
+      rho, u — to |dW/W| <~ W^2 (1e-12 / (tau + D) + 4e-16): the stopping
+               threshold plus the rounding noise of f itself, which exceeds
+               1e-12 when tau + D is large.
     The seeded recovery must meet those bounds against the reference method,
     and reproduce the conserved state at least as well."""
     net, _, _, _ = trained
@@ -179,9 +181,11 @@ def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
     well = strict & (a[4] > 1e-3 * E)
     assert np.max(rel[4][well]) < 1e-10
     W = np.sqrt(1.0 + (a[1:4] ** 2).sum(axis=0))
-    bound = 10.0 * W ** 2 * 1e-12 / E + 1e-13
-    assert np.all(rel[0][strict] <= bound[strict])
-    assert np.all(rel[1:4][:, strict].max(axis=0) <= bound[strict] + 1e-12)
+    bound = 10.0 * W ** 2 * (1e-12 / E + 4e-16) + 1e-13
+    ratio_rho = (rel[0] / bound)[strict]
+    ratio_u = (rel[1:4].max(axis=0) / (bound + 1e-12))[strict]
+    assert ratio_rho.max() <= 1.0, f"rho differs beyond the reference's own bound: worst ratio {ratio_rho.max():.3g}"
+    assert ratio_u.max() <= 1.0, f"u differs beyond the reference's own bound: worst ratio {ratio_u.max():.3g}"
     mean_base = base.iterations.float().mean().item()
     mean_seeded = seeded.iterations.float().mean().item()
     assert mean_seeded * 2.0 <= mean_base, (mean_base, mean_seeded)
@@ -202,3 +206,16 @@ def test_mlp_gain_over_no_network(sr, oracle, trained):
         means[name] = r.iterations.float().mean().item()
     assert means["mlp_only"] < means["default"]
     assert means["mlp_refine"] < means["refine_only"]
+
+
+def test_seeded_zone_generator_matches_oracle(sr, oracle):
+    """The library's seeded SRHD zones (bench input) follow the oracle's recipe."""
+    from mara3p_gb300._capi import check, lib
+    n = 4096
+    prim_o, cons_o = seeded_zones(oracle, n, seed=77)
+    prim = torch.empty((5, n), dtype=torch.float64, device="cuda")
+    cons = torch.empty_like(prim)
+    check(lib.mara_srhd_seeded_zones(77, n, 1e-4, 1.0, 1e-6, 10.0, 50.0, GAMMA, prim.data_ptr(), cons.data_ptr(),
+                                     torch.cuda.current_stream().cuda_stream), "seeded zones")
+    assert np.allclose(prim.cpu().numpy(), prim_o.reshape(-1, 5).T, rtol=1e-13, atol=0)
+    assert np.allclose(cons.cpu().numpy(), cons_o.reshape(-1, 5).T, rtol=1e-12, atol=1e-300)
