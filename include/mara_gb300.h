@@ -299,6 +299,30 @@ int mara_srhd_mlp_train(void* weights, void* workspace, int64_t n, const int64_t
 /* Inference on n rows of raw features (float[n][4]): y[i] = network output. */
 int mara_srhd_mlp_infer(const void* weights, const float* features, int64_t n, float* y, void* stream);
 
+/* ---------------------------------------------------------------- srhd 2D scheme */
+
+/* 2D Cartesian SRHD on the unit square (the relativistic shock-tube
+ * benchmark). No counterpart scheme exists in the reference; it is composed
+ * from the reference's srhd::recover_primitive, srhd::riemann_hlle and
+ * mara::plm_gradient in the minidisk face-state pattern, with RK2 by
+ * control::advance_runge_kutta and zero-gradient boundaries. State u: SoA
+ * [4][N][N] (D, S1, S2, tau), device. clock: mara_srhd_tube_clock_bytes()
+ * bytes of device memory (time, dt, fastest speed, iteration, failed
+ * recoveries, total FP64 Newton iterations). */
+int64_t mara_srhd_tube_clock_bytes(void);
+int64_t mara_srhd_tube_workspace_bytes(int32_t N);
+/* Two states split by the line (x - 1/2) cos(angle) + (y - 1/2) sin(angle) = 0,
+ * at rest; resets the clock. */
+int mara_srhd_tube_initial(int32_t N, double angle, double rho_l, double p_l, double rho_r, double p_r,
+                           double gamma_law_index, double* u, void* clock, void* stream);
+/* `steps` RK2 steps; dt = cfl / N / max outer wavespeed of each step's
+ * initial state. guess: 0 = p = 0 (the reference's recovery, bit-identical),
+ * 1 = the learned guess (mlp_weights), 2 = the previous stage's pressure;
+ * refine32 FP32 Newton steps sharpen a guess before the FP64 polish. */
+int mara_srhd_tube_advance(int32_t N, double* u, void* clock, int32_t steps, double cfl, double plm_theta,
+                           double gamma_law_index, double temperature_floor, int32_t precision, int32_t guess,
+                           const void* mlp_weights, int32_t refine32, void* workspace, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

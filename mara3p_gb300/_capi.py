@@ -116,6 +116,14 @@ SIGNATURES.update({
     "mara_mhd_max_div_b": (ctypes.c_int, [_HP, _vp, _vp, _vp, _vp, _vp]),
 })
 
+SIGNATURES.update({
+    "mara_srhd_tube_clock_bytes": (ctypes.c_int64, []),
+    "mara_srhd_tube_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32]),
+    "mara_srhd_tube_initial": (ctypes.c_int, [ctypes.c_int32] + [ctypes.c_double] * 6 + [_vp, _vp, _vp]),
+    "mara_srhd_tube_advance": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, ctypes.c_int32] + [ctypes.c_double] * 4 +
+                               [ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp]),
+})
+
 
 class MaraError(RuntimeError):
     pass

@@ -21,68 +21,10 @@
 #include <cstdint>
 #include "common.cuh"
 #include "srhd_mlp.cuh"
+#include "srhd_physics.cuh"
 
 namespace mara {
 namespace srhd {
-
-struct Zone { double D, S1, S2, S3, tau; };
-
-// Newton on p from p_start (physics_srhd.hpp:231-285). Returns status
-// 0 ok / 1 not converged / 2 non-positive pressure; writes the primitive
-// (rho, u1, u2, u3, p) and the number of iterations run.
-__device__ inline int newton(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
-                             double prim[5], int& iterations)
-{
-    const double c2 = 1.0;
-    const double tol = 1e-12;
-    const double D = z.D, tau = z.tau;
-    const double SS = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(z.S1, z.S1)), __dmul_rn(z.S2, z.S2)),
-                                __dmul_rn(z.S3, z.S3));
-    const double Dc2 = __dmul_rn(D, c2);
-    const double gm1 = __dadd_rn(gm, -1.0);
-    const double b2max = 1.0 - 1e-10;
-    bool found = false;
-    int iteration = 0;
-    double W0 = 1.0;
-    double p = p_start;
-
-    while (iteration <= iter_max)
-    {
-        double Et = __dadd_rn(__dadd_rn(tau, p), Dc2);
-        double b2 = fmin(__ddiv_rn(__ddiv_rn(__dmul_rn(SS, c2), Et), Et), b2max);
-        double W2 = __ddiv_rn(1.0, __dadd_rn(1.0, -b2));
-        double W = __dsqrt_rn(W2);
-        double e = __ddiv_rn(__dadd_rn(__dadd_rn(tau, __dmul_rn(Dc2, __dadd_rn(1.0, -W))), __dmul_rn(p, __dadd_rn(1.0, -W2))),
-                             __dmul_rn(D, W));
-        double d = __ddiv_rn(D, W);
-        double h = __dadd_rn(__dadd_rn(c2, e), __ddiv_rn(p, d));
-        double a2 = __ddiv_rn(__dmul_rn(gm, p), __dmul_rn(d, h));
-        double f = __dadd_rn(__dmul_rn(__dmul_rn(d, e), gm1), -p);
-        double g = __dadd_rn(__dmul_rn(b2, a2), -1.0);
-
-        p = __dadd_rn(p, -__ddiv_rn(f, g));
-
-        if (fabs(f) < tol || (fabs(f) < tol * 1e4 && iteration == iter_max))
-        {
-            W0 = W;
-            found = true;
-            break;
-        }
-        ++iteration;
-    }
-    iterations = found ? iteration + 1 : iteration;
-    if (temperature_floor > 0.0)
-        p = fmax(p, __dmul_rn(__dmul_rn(temperature_floor, D), c2));
-    if (!found) return 1;
-    if (temperature_floor <= 0.0 && p <= 0.0) return 2;
-    double Et = __dadd_rn(__dadd_rn(tau, Dc2), p);
-    prim[0] = __ddiv_rn(D, W0);
-    prim[1] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S1), Et), 1.0);
-    prim[2] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S2), Et), 1.0);
-    prim[3] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S3), Et), 1.0);
-    prim[4] = p;
-    return 0;
-}
 
 struct C2PArgs
 {
@@ -118,32 +60,6 @@ __global__ void c2p_default_kernel(const C2PArgs a)
         int st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it);
         store(a, i, prim, it, st);
     }
-}
-
-// The same Newton update in FP32, used to sharpen a pressure guess cheaply
-// before the FP64 polish. Returns the guess unchanged if it goes bad.
-__device__ inline double refine_fp32(const Zone& z, double gm, double p0, int iters)
-{
-    const float D = float(z.D), tau = float(z.tau), g = float(gm);
-    const float SS = float(z.S1) * float(z.S1) + float(z.S2) * float(z.S2) + float(z.S3) * float(z.S3);
-    float p = float(p0);
-    for (int k = 0; k < iters; ++k)
-    {
-        float Et = tau + p + D;
-        float b2 = fminf(SS / (Et * Et), 1.0f - 1e-7f);
-        float W2 = 1.0f / (1.0f - b2);
-        float W = sqrtf(W2);
-        float e = (tau + D * (1.0f - W) + p * (1.0f - W2)) / (D * W);
-        float d = D / W;
-        float h = 1.0f + e + p / d;
-        float a2 = g * p / (d * h);
-        float f = d * e * (g - 1.0f) - p;
-        float gg = b2 * a2 - 1.0f;
-        float pn = p - f / gg;
-        if (!(pn > 0.0f) || !isfinite(pn)) break;
-        p = pn;
-    }
-    return double(p);
 }
 
 __device__ inline void polish(const C2PArgs& a, int64_t i, const Zone& z, double guess)
@@ -204,19 +120,6 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
             polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau));
         }
     }
-}
-
-// srhd::conserved_density (src/physics_srhd.hpp:291-304), c = 1
-__device__ inline void conserved_density(const double p[5], double gm, double u[5])
-{
-    const double W = sqrt(1.0 + (p[1] * p[1] + p[2] * p[2] + p[3] * p[3]));
-    const double D = p[0] * W;
-    const double h = (p[0] * 1.0 + p[4] * (1.0 + 1.0 / (gm - 1.0))) / p[0];
-    u[0] = D;
-    u[1] = D * h * p[1] / 1.0;
-    u[2] = D * h * p[2] / 1.0;
-    u[3] = D * h * p[3] / 1.0;
-    u[4] = D * (h * W - 1.0 * 1.0) - p[4];
 }
 
 __device__ inline double uniform01(uint64_t seed, uint64_t i)

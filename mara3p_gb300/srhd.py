@@ -100,3 +100,34 @@ class PressureGuess:
              "w2": f[328:4424].reshape(64, 64), "b2": f[4424:4488], "w3": f[4488:4552], "b3": f[4552],
              "out_shift": f[4553], "out_scale": f[4554]}
         return o
+
+
+GUESS_ZERO, GUESS_MLP, GUESS_PREVIOUS = 0, 1, 2
+
+
+class ShockTube:
+    """2D SRHD on the unit square with the reference's recovery, PLM and HLLE
+    (the relativistic shock-tube benchmark): u is (4, N, N) = (D, S1, S2, tau)."""
+
+    def __init__(self, N: int = 1024, angle: float = 3.141592653589793 / 6, left=(10.0, 13.33), right=(1.0, 1e-6),
+                 gamma_law_index: float = 4.0 / 3.0, cfl: float = 0.3, plm_theta: float = 1.5,
+                 temperature_floor: float = 1e-10, device="cuda"):
+        self.N, self.gamma, self.cfl, self.theta, self.floor = N, gamma_law_index, cfl, plm_theta, temperature_floor
+        self.u = torch.empty((4, N, N), dtype=torch.float64, device=device)
+        self.clock = torch.zeros(lib.mara_srhd_tube_clock_bytes(), dtype=torch.uint8, device=device)
+        self.workspace = torch.empty(lib.mara_srhd_tube_workspace_bytes(N), dtype=torch.uint8, device=device)
+        check(lib.mara_srhd_tube_initial(N, angle, left[0], left[1], right[0], right[1], gamma_law_index,
+                                         self.u.data_ptr(), self.clock.data_ptr(), _stream()), "tube initial")
+
+    def advance(self, steps: int, precision: int = 0, guess: int = GUESS_ZERO, mlp: "PressureGuess | None" = None,
+                refine32: int = 0) -> None:
+        check(lib.mara_srhd_tube_advance(self.N, self.u.data_ptr(), self.clock.data_ptr(), steps, self.cfl, self.theta,
+                                         self.gamma, self.floor, precision, guess, mlp.weights.data_ptr() if mlp else None,
+                                         refine32, self.workspace.data_ptr(), _stream()), "tube advance")
+
+    def clock_state(self) -> dict:
+        raw = self.clock.cpu().numpy()
+        d = raw.view("float64")
+        q = raw.view("uint64")
+        return {"time": float(d[0]), "dt": float(d[1]), "iteration": int(q[3]), "failures": int(q[4]),
+                "newton": int(q[5])}

@@ -190,9 +190,144 @@ int riemann(const Prim& pl, const Prim& pr, int axis, double gm, bool hllc, Cons
     return 0;
 }
 
+inline double plm(double yl, double y0, double yr, double theta)
+{
+    double a = (y0 - yl) / (1.0 - 0.0) * theta;
+    double b = (yr - yl) / (2.0 - 0.0);
+    double c = (yr - y0) / (2.0 - 1.0) * theta;
+    double sa = std::copysign(1.0, a), sb = std::copysign(1.0, b), sc = std::copysign(1.0, c);
+    return 0.25 * std::abs(sa + sb) * (sa + sc) * std::min(std::min(std::abs(a), std::abs(b)), std::abs(c));
+}
+
+inline double get(const Prim& p, int k) { return k == 0 ? p.rho : k == 1 ? p.u1 : k == 2 ? p.u2 : k == 3 ? p.u3 : p.p; }
+inline void put(Prim& p, int k, double v)
+{
+    if (k == 0) p.rho = v; else if (k == 1) p.u1 = v; else if (k == 2) p.u2 = v; else if (k == 3) p.u3 = v; else p.p = v;
+}
+
+// One forward-Euler stage of the 2D Cartesian SRHD scheme composed from the
+// reference's physics (the reference has no such scheme): recover_primitive
+// per cell, generalised-minmod slopes of (rho, u1, u2, u3, p), face states
+// p -/+ g/2 (the minidisk pattern, minidisk_scheme.cpp:238-240), HLLE fluxes
+// (physics_srhd.hpp:489-497), u1 = u - (dFx + dFy) dt / dl. Zero-gradient
+// boundaries (ghost cells copy the edge cell). u, out: [4][N][N] (D, S1, S2, tau).
+int tube_stage(int N, const double* u, double* out, double dt, double dl, double theta, double gm, double floor_,
+               const double* avg, std::vector<Prim>& P)
+{
+    const size_t NN = size_t(N) * N;
+    int bad = 0;
+    for (size_t c = 0; c < NN; ++c)
+    {
+        double z[5] = {u[c], u[NN + c], u[2 * NN + c], 0.0, u[3 * NN + c]};
+        int it = 0;
+        bad += recover_primitive(z, gm, floor_, 0.0, P[c], it) != 0;
+    }
+    auto at = [&] (int i, int j) -> const Prim& {
+        i = std::min(std::max(i, 0), N - 1);
+        j = std::min(std::max(j, 0), N - 1);
+        return P[size_t(i) * N + j];
+    };
+    auto state = [&] (int i, int j, int axis, double sign) {
+        const Prim& l = axis == 0 ? at(i - 1, j) : at(i, j - 1);
+        const Prim& c = at(i, j);
+        const Prim& r = axis == 0 ? at(i + 1, j) : at(i, j + 1);
+        Prim s;
+        for (int k = 0; k < 5; ++k) put(s, k, get(c, k) + sign * (0.5 * plm(get(l, k), get(c, k), get(r, k), theta)));
+        return s;
+    };
+    // face fluxes: x face (f, j) between cells (f-1, j) and (f, j), f in [0, N]
+    std::vector<Cons> fx(size_t(N + 1) * N), fy(size_t(N) * (N + 1));
+    for (int f = 0; f <= N; ++f)
+        for (int j = 0; j < N; ++j)
+            riemann(state(f - 1, j, 0, +1.0), state(f, j, 0, -1.0), 1, gm, false, fx[size_t(f) * N + j]);
+    for (int i = 0; i < N; ++i)
+        for (int f = 0; f <= N; ++f)
+            riemann(state(i, f - 1, 1, +1.0), state(i, f, 1, -1.0), 2, gm, false, fy[size_t(i) * (N + 1) + f]);
+    const int comp[4] = {0, 1, 2, 4};
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+        {
+            const size_t c = size_t(i) * N + j;
+            for (int q = 0; q < 4; ++q)
+            {
+                const int k = comp[q];
+                double dfx = fx[size_t(i + 1) * N + j].c[k] - fx[size_t(i) * N + j].c[k];
+                double dfy = fy[size_t(i) * (N + 1) + j + 1].c[k] - fy[size_t(i) * (N + 1) + j].c[k];
+                double v = u[q * NN + c] - (dfx + dfy) * dt / dl;
+                if (avg) v = avg[q * NN + c] * 0.5 + v * (1 - 0.5);
+                out[q * NN + c] = v;
+            }
+        }
+    return bad;
+}
+
+// max over cells of the outer wavespeed magnitudes on both axes
+double tube_max_speed(int N, const double* u, double gm, double floor_)
+{
+    const size_t NN = size_t(N) * N;
+    double m = 0.0;
+    for (size_t c = 0; c < NN; ++c)
+    {
+        double z[5] = {u[c], u[NN + c], u[2 * NN + c], 0.0, u[3 * NN + c]};
+        Prim p;
+        int it;
+        recover_primitive(z, gm, floor_, 0.0, p, it);
+        for (int axis = 1; axis <= 2; ++axis)
+        {
+            double am, ap;
+            outer_wavespeeds(p, axis, gm, am, ap);
+            m = std::max(m, std::max(std::abs(am), std::abs(ap)));
+        }
+    }
+    return m;
+}
+
 } // namespace
 
 extern "C" {
+
+// Relativistic shock tube on the unit square: (rho, p) = (rho_l, p_l) where
+// (x - 1/2) cos(angle) + (y - 1/2) sin(angle) < 0, else (rho_r, p_r); v = 0.
+// Cell centres x_i = (i + 1/2) / N. u: [4][N][N] (D, S1, S2, tau).
+void oracle_srhd_tube_initial(int32_t N, double angle, double rho_l, double p_l, double rho_r, double p_r,
+                              double gamma_law_index, double* u)
+{
+    const size_t NN = size_t(N) * N;
+    const double c = std::cos(angle), s = std::sin(angle);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+        {
+            const double x = (i + 0.5) / N, y = (j + 0.5) / N;
+            const bool left = (x - 0.5) * c + (y - 0.5) * s < 0.0;
+            Prim p{left ? rho_l : rho_r, 0.0, 0.0, 0.0, left ? p_l : p_r};
+            Cons w = conserved_density(p, gamma_law_index);
+            const size_t k = size_t(i) * N + j;
+            u[k] = w.c[0]; u[NN + k] = w.c[1]; u[2 * NN + k] = w.c[2]; u[3 * NN + k] = w.c[4];
+        }
+}
+
+// `steps` RK2 steps (advance_runge_kutta order 2); dt = cfl * dl / max speed
+// of the step's initial state. Returns the final time; *failures counts
+// zones whose recovery failed (status != 0).
+double oracle_srhd_tube_advance(int32_t N, double* u, double time, int32_t steps, double cfl, double theta,
+                                double gamma_law_index, double temperature_floor, int64_t* failures)
+{
+    const size_t NN = size_t(N) * N;
+    const double dl = 1.0 / N;
+    std::vector<double> u1(4 * NN), u2(4 * NN);
+    std::vector<Prim> P(NN);
+    int64_t bad = 0;
+    for (int s = 0; s < steps; ++s)
+    {
+        const double dt = cfl * dl / tube_max_speed(N, u, gamma_law_index, temperature_floor);
+        bad += tube_stage(N, u, u1.data(), dt, dl, theta, gamma_law_index, temperature_floor, nullptr, P);
+        bad += tube_stage(N, u1.data(), u, dt, dl, theta, gamma_law_index, temperature_floor, u, P);
+        const double t2 = (time + dt) + dt;
+        time = time * 0.5 + t2 * (1 - 0.5);
+    }
+    if (failures) *failures = bad;
+    return time;
+}
 
 // srhd::recover_primitive over n AoS zones (5 doubles each). p_start may be
 // null (start from p = 0, as the reference does) or hold one start pressure
