@@ -50,7 +50,14 @@ WORKLOADS = {
     "minidisk-256": dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3, domain_radius=4.0,
                          softening_length=0.05, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.05, sink_rate=10.0,
                          buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=1.5),
+    # BASELINE configuration 5: 64 seeded members (mesh 128^2..1024^2, q, e, Mach, nu drawn per member) on this
+    # base physics; the entry itself (a 256^2 member) is what the CPU reference arm times
+    "minidisk-ensemble-64": dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3,
+                                 domain_radius=4.0, softening_length=0.05, eccentricity=0.0, mass_ratio=1.0,
+                                 sink_radius=0.05, sink_rate=10.0, buffer_rate=100.0, buffer_scale=0.2, cfl=0.3,
+                                 plm_theta=1.5),
 }
+ENSEMBLE_MEMBERS = 64
 # Algorithmic HBM bytes per cell for each stage kernel (FP64 state = 24 B/cell,
 # FP32 increment = 12 B/cell):
 #   mixed stage 1: read u0 (24) + write d1 (12)                  = 36
@@ -454,6 +461,123 @@ def run_srhd(args):
         print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args):
+    """Configuration 5: 64 independent minidisk members (mesh from 128^2 to
+    1024^2, mass ratio, eccentricity, Mach number and viscosity drawn per
+    member by seed), mixed precision, RK2, CFL. One step = one RK2 step of
+    every member: one persistent sweep launch per stage and one clock launch,
+    replayed from a CUDA graph, launch shape picked by the tuner. Compared with
+    looping the single-mesh advance over the members."""
+    import dataclasses
+
+    import torch
+    import torch.distributed as dist
+
+    import mara3p_gb300.ensemble as en
+    import mara3p_gb300.minidisk as md
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    members = en.seeded_members(5 + rank, ENSEMBLE_MEMBERS, md.SolverData(**WORKLOADS[args.workload]))
+    cells = sum(sd.cells_per_side ** 2 for sd in members)
+    u0 = [md.initial_conserved(sd, seed=100 + m, amplitude=0.01) for m, sd in enumerate(members)]
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    e = en.Ensemble(members, [u.clone() for u in u0], precision=md.MIXED, dt_mode=md.DT_CFL, autotune=1)
+    tune_s = time.perf_counter() - t0
+
+    def timed(fn, steps):
+        fn(args.warmup)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn(steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    with ClockSampler(local) as sampler:
+        ms = timed(e.advance, args.steps)
+    value = cells * args.steps * world / (ms * 1e-3)
+    gpu_launches = 1 + 3 * args.steps + (args.steps % 2)   # clock begin, per step 2 sweeps + clock, copy-back
+
+    # the same members advanced one at a time through the single-mesh call
+    runs = [md.Run(sd, u.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL) for sd, u in zip(members, u0)]
+
+    def looped(k):
+        for r in runs:
+            r.advance(k)
+    ms_loop = timed(looped, args.steps)
+    value_loop = cells * args.steps * world / (ms_loop * 1e-3)
+
+    s1, s2 = e.stage_times(5)
+    peak, kind = measured_peaks()
+    dom_ms = max(s1, s2)
+    dominant = 2 if s2 >= s1 else 1
+    dom_bytes = STAGE_BYTES[("mixed", dominant)] * cells
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    step_bytes = (STAGE_BYTES[("mixed", 1)] + STAGE_BYTES[("mixed", 2)]) * cells
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": f"ensemble_sweep_kernel<{dominant}>", "kernel_ms": dom_ms,
+            "algorithmic_bytes": dom_bytes, "peak_source": f"{kind} hbm_gbs", "stage_ms": [s1, s2],
+            "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
+
+    e2e = None
+    if not args.no_e2e:
+        hosts = [torch.empty_like(u, device="cpu").pin_memory() for u in e.states]
+        for h, u in zip(hosts, e.states):
+            h.copy_(u)
+        outs = [torch.empty_like(h).pin_memory() for h in hosts]
+
+        def host_step():
+            for h, u in zip(hosts, e.states):
+                u.copy_(h, non_blocking=True)
+            e.advance(1)
+            for o, u in zip(outs, e.states):
+                o.copy_(u, non_blocking=True)
+            torch.cuda.synchronize()
+        host_step()
+        k = max(2, min(args.steps, 10))
+        t1 = time.perf_counter()
+        for _ in range(k):
+            host_step()
+        el = time.perf_counter() - t1
+        nbytes = 3 * cells * 8
+        e2e = {"value": cells * k * world / el, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes,
+               "call": "Ensemble.advance(1) with every member's state copied from and to pinned host memory"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(dataclasses.asdict(members[0]) | {"depth": 2, "block_size": 64},
+                           args.cpu_sample_seconds)
+    sizes = sorted(sd.cells_per_side for sd in members)
+    line = _line(args, world, value, "cell-updates/s", ms / args.steps, "f32 compute, f64 state",
+                 {"workload": args.workload, "members": len(members), "cells": cells,
+                  "meshes": {str(n): sizes.count(n) for n in sorted(set(sizes))},
+                  "scheme": "PLM(theta=1.5)+HLLE+viscosity+gravity/sink/buffer sources, RK2, CFL 0.3 per member",
+                  "launch": e.config, "tune_seconds": tune_s, "parallelism": f"replicas x{world}",
+                  "l2": f"no flush: FP64 states {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
+                 roof, {"looped_single_mesh": {"value": value_loop, "ms_per_step": ms_loop / args.steps,
+                                               "gpu_launches": len(members) * (1 + 3 * args.steps)},
+                        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+                        "clocks": sampler.summary()})
+    e.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def run_tube(args):
     """1024^2 relativistic shock tube (rho 10 / p 13.33 left, rho 1 / p 1e-6
     right, interface at 30 degrees), PLM + HLLE, RK2, recovery seeded by the
@@ -513,6 +637,8 @@ def main():
         run_srhd(args)
     elif args.workload == "srhd-tube":
         run_tube(args)
+    elif args.workload == "minidisk-ensemble-64":
+        run_ensemble(args)
     else:
         run_ours(args)
 

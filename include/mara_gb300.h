@@ -194,6 +194,71 @@ int mara_minidisk_advance_noalloc(const mara_minidisk_params* sd, double* u, mar
                                   int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
                                   void* stream);
 
+/* Columns per thread of the mixed-precision sweep kernels, process-wide:
+ * 0 = automatic (two wherever N is even and the buffers are 16-byte aligned;
+ * else one), 1 or 2 to force a form (2 still falls back to 1 where it cannot
+ * run). Both forms give bit-identical results. Returns the previous setting, or -1 for a bad value (the message
+ * says why). */
+int mara_minidisk_sweep_columns(int32_t columns);
+
+/* ---------------------------------------------------------------- minidisk ensemble */
+
+/* Many independent minidisk meshes (members, each with its own parameters
+ * and mesh size) advanced together: the reference runs one mesh per process
+ * and folds steps on the host (problems/minidisk.cpp:202-213); here every RK
+ * stage of all members is ONE persistent launch over a device work-list of
+ * strip segments (MARA_MIXED), and each RK step (stages + clock update of all
+ * members) is replayed from a CUDA graph captured at creation. Each member's
+ * results and clock equal those of mara_minidisk_advance on that member alone
+ * with the same arguments, up to FP32 rounding of a face flux at a work-list
+ * cut (MARA_MIXED) and exactly (MARA_FP64). */
+typedef struct mara_minidisk_ensemble mara_minidisk_ensemble;
+
+typedef struct {
+    int32_t blocks_per_sm;    /* resident 128-thread CTAs per SM of the persistent grid */
+    int32_t chunks_per_warp;  /* 1: one balanced row range per warp; >1: that many per warp, claimed dynamically */
+    int32_t cols_per_lane;    /* thread coarsening of the sweep: 1 or 2 columns per lane (2: even N only) */
+    int32_t register_variant; /* register budget of the sweep: 0 unconstrained, 1/2 compiled for more CTAs per SM */
+    double stage_ms;          /* both stages of one step of all members, as timed by the tuner (0: not timed) */
+} mara_ensemble_config;
+
+/* Host-only planner of the work-list (no GPU needed): the column strips
+ * (strip_columns = 28 for the 1-column sweep, 60 for the 2-column one) of
+ * every member's N x N mesh, rows laid end to end, cut into `chunks` ranges
+ * of equal row count; items[4*k..] = (member, strip, row begin, row end),
+ * chunk c owns items [chunk_first[c], chunk_first[c+1]). Returns the item
+ * count (-1 on bad arguments); writes at most `capacity` items; either
+ * output may be NULL. */
+int64_t mara_minidisk_ensemble_plan(const int32_t* sizes, int32_t count, int64_t chunks, int32_t strip_columns,
+                                    int32_t* items, int64_t capacity, int32_t* chunk_first);
+
+/* Create an ensemble of `count` members. params[m] describes member m;
+ * states[m] is its device SoA state (3 * N_m^2 doubles, 16-byte aligned) and
+ * clocks + m its device clock; all stay caller-owned and must outlive the
+ * ensemble. The ensemble allocates its own scratch (one FP64 state and, for
+ * MARA_MIXED RK2, one FP32 increment per member) and captures its graphs on
+ * a private stream. MARA_MIXED needs N_m >= 64. autotune: 0 = default launch
+ * shape, 1 = tune on first use of this set of mesh sizes in the process (the
+ * tuner synchronises the device, then only writes scratch), 2 = always tune. */
+int mara_minidisk_ensemble_create(const mara_minidisk_params* params, int32_t count, double* const* states,
+                                  mara_minidisk_clock* clocks, int32_t rk_order, int32_t precision,
+                                  int32_t dt_mode, int32_t autotune, mara_minidisk_ensemble** out);
+/* mara_minidisk_clock_init of every member at `time`, with the wavespeed
+ * reduction of the ensemble's precision. */
+int mara_minidisk_ensemble_clock_init(mara_minidisk_ensemble* e, double time, void* stream);
+/* `steps` RK steps of every member, stream-ordered on `stream`. */
+int mara_minidisk_ensemble_advance(mara_minidisk_ensemble* e, int32_t steps, void* stream);
+int mara_minidisk_ensemble_get_config(const mara_minidisk_ensemble* e, mara_ensemble_config* out);
+/* Replace the launch shape (recaptures the graphs; synchronises the device). */
+int mara_minidisk_ensemble_set_config(mara_minidisk_ensemble* e, const mara_ensemble_config* config);
+/* Time the candidate launch shapes on the members and keep the fastest. */
+int mara_minidisk_ensemble_tune(mara_minidisk_ensemble* e);
+/* Median CUDA-event time of each stage launch (ms[0..rk_order-1]) over
+ * `reps` phase-0 launches that write only scratch (MARA_MIXED; synchronises
+ * the device). */
+int mara_minidisk_ensemble_stage_times(mara_minidisk_ensemble* e, int32_t reps, double* ms);
+int mara_minidisk_ensemble_destroy(mara_minidisk_ensemble* e);
+
 /* ---------------------------------------------------------------- mhd */
 
 /* One periodic cube of ideal MHD with constrained transport, the scheme of

@@ -75,6 +75,7 @@ SIGNATURES = {
                                            ctypes.c_int32, _vp]),
     "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp]),
+    "mara_minidisk_sweep_columns": (ctypes.c_int, [ctypes.c_int32]),
     "mara_minidisk_advance_noalloc": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                      ctypes.c_int32, _vp]),
     "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -114,6 +115,32 @@ SIGNATURES.update({
     "mara_mhd_initial_state": (ctypes.c_int, [_HP, c_double_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp,
                                               _vp, _vp, _vp, _vp, _vp]),
     "mara_mhd_max_div_b": (ctypes.c_int, [_HP, _vp, _vp, _vp, _vp, _vp]),
+})
+
+
+class EnsembleConfig(ctypes.Structure):
+    """mara_ensemble_config."""
+
+    _fields_ = [("blocks_per_sm", ctypes.c_int32), ("chunks_per_warp", ctypes.c_int32),
+                ("cols_per_lane", ctypes.c_int32), ("register_variant", ctypes.c_int32),
+                ("stage_ms", ctypes.c_double)]
+
+
+_EC = ctypes.POINTER(EnsembleConfig)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+SIGNATURES.update({
+    "mara_minidisk_ensemble_plan": (ctypes.c_int64, [_i32p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _i32p,
+                                                     ctypes.c_int64, _i32p]),
+    "mara_minidisk_ensemble_create": (ctypes.c_int, [_MP, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p), _vp,
+                                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                     ctypes.POINTER(ctypes.c_void_p)]),
+    "mara_minidisk_ensemble_clock_init": (ctypes.c_int, [_vp, ctypes.c_double, _vp]),
+    "mara_minidisk_ensemble_advance": (ctypes.c_int, [_vp, ctypes.c_int32, _vp]),
+    "mara_minidisk_ensemble_get_config": (ctypes.c_int, [_vp, _EC]),
+    "mara_minidisk_ensemble_set_config": (ctypes.c_int, [_vp, _EC]),
+    "mara_minidisk_ensemble_tune": (ctypes.c_int, [_vp]),
+    "mara_minidisk_ensemble_stage_times": (ctypes.c_int, [_vp, ctypes.c_int32, c_double_p]),
+    "mara_minidisk_ensemble_destroy": (ctypes.c_int, [_vp]),
 })
 
 SIGNATURES.update({

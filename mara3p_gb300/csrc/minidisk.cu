@@ -25,315 +25,10 @@
 #include <cstring>
 #include <mutex>
 #include <string>
-#include "common.cuh"
+#include "minidisk_device.cuh"
 
 namespace mara {
 namespace md {
-
-constexpr int TX = 16, TY = 32, NT = 256;
-constexpr int EX = TX + 4, EY = TY + 4;     // halo tile
-constexpr int GX = TX + 2, GY = TY + 2;     // slope region
-constexpr int NFX = (TX + 1) * TY;          // x faces
-constexpr int NFY = TX * (TY + 1);          // y faces
-
-enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3 };
-
-// Single-precision constants of the mixed path, prepared on the host so that
-// no FP64 instruction (GB300 runs FP64 at 1/64 of the FP32 rate) is issued
-// for them on the device.
-struct FloatConsts
-{
-    float rs2, inv_mach2, half_nu, half_inv_dl, inv_dl, theta, R, dl;
-    float sink_rate, inv_s6, buffer_rate, neg2_inv_buffer_scale, omega, omega2, two_omega;
-};
-
-struct Args
-{
-    int N;                 // cells per side of the mesh (K_BLOCK: block size)
-    int n;                 // block size (zones per block side)
-    int level;             // block level (2^level blocks per side)
-    int tiles_y;
-    int sweep_rows;        // mixed sweep: rows per warp
-    uint64_t bi, bj;       // K_BLOCK: block coordinates
-    double R, dl;
-    double rs2;            // softening_length^2 (std::pow(rs, 2.0) on the host)
-    double mach, nu, omega, sink_rate, s6, buffer_rate, buffer_scale, theta;
-    double dt;             // used when clock == nullptr
-    double bin[6];         // m1, x1, y1, m2, x2, y2; used when clock == nullptr
-    const mara_minidisk_clock* clock;
-    int stage;             // which clock->binary row this stage uses
-    const double* u_in;    // FP64/MIX: stage state (FP64) or u0; K_BLOCK: uc AoS
-    const double* u_avg;   // K_FP64: optional RK2 average partner
-    const float* d1;       // K_MIX2: FP32 stage-1 increment
-    double* u_out;         // FP64 result
-    float* d_out;          // K_MIX1 + RK2: increment out
-    const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
-    unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
-    FloatConsts f;
-};
-
-// double -> float (round to nearest even) and float -> double (exact) with
-// integer instructions only, so that the mixed path issues no FP64-pipe work
-// for them. Magnitudes below the smallest normal float (1.2e-38) become signed
-// zero; overflow gives infinity; NaN stays NaN.
-__device__ inline float d2f(double x)
-{
-    const unsigned long long b = __double_as_longlong(x);
-    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
-    const unsigned sign = hi & 0x80000000u;
-    const unsigned e = (hi >> 20) & 0x7FFu;
-    unsigned f = sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const unsigned rest = lo & 0x1FFFFFFFu;
-    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
-    const bool nan = e == 0x7FFu && ((hi & 0xFFFFFu) | lo) != 0u;
-    f = e < 897u ? sign : f;
-    f = e > 1150u ? (sign | (nan ? 0x7FC00000u : 0x7F800000u)) : f;
-    return __uint_as_float(f);
-}
-
-__device__ inline double f2d(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xFFu;
-    const unsigned m = b & 0x7FFFFFu;
-    const unsigned ee = e == 255u ? 2047u : e + 896u;
-    unsigned hi = (b & 0x80000000u) | (ee << 20) | (m >> 3);
-    unsigned lo = m << 29;
-    hi = e == 0u ? (b & 0x80000000u) : hi;
-    lo = e == 0u ? 0u : lo;
-    return __hiloint2double(int(hi), int(lo));
-}
-
-// Single-MUFU approximations for the mixed path (relative error ~1e-7,
-// well inside the FP32 budget of the fluxes; denormals flush to zero).
-__device__ inline float rcp_fast(float x)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float sqrt_fast(float x)
-{
-    float y;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float rsqrt_fast(float x)
-{
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float exp_fast(float x)
-{
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
-    return y;
-}
-
-// ------------------------------------------------------------- geometry
-// vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
-__host__ __device__ inline double vertex(double R, int n, int level, uint64_t b, int k)
-{
-    double dlv = double(1 << level);
-    double x0 = R * (-1 + double(2 * b) / dlv);
-    double x1 = R * (-1 + double(2 * (b + 1)) / dlv);
-    return x0 + (x1 - x0) * double(k) / double(n);
-}
-
-__device__ inline int wrap(int g, int N)
-{
-    g %= N;
-    return g < 0 ? g + N : g;
-}
-
-// ------------------------------------------------------------- PLM
-// Generalised minmod on unit spacing (scheme_plm_gradient.hpp:56-63). The
-// reference's 0.25*|sa+sb|*(sa+sc)*min(|a|,|b|,|c|) equals copysign(min, a)
-// when a, b, c share a sign and zero otherwise; that is what is computed here.
-__device__ inline double plm(double yl, double y0, double yr, double theta)
-{
-    double a = (y0 - yl) * theta;
-    double b = (yr - yl) * 0.5;
-    double c = (yr - y0) * theta;
-    double m = fmin(fmin(fabs(a), fabs(b)), fabs(c));
-    long long sa = __double_as_longlong(a), sb = __double_as_longlong(b), sc = __double_as_longlong(c);
-    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0 : copysign(m, a);
-}
-
-__device__ inline float plm(float yl, float y0, float yr, float theta)
-{
-    float a = (y0 - yl) * theta;
-    float b = (yr - yl) * 0.5f;
-    float c = (yr - y0) * theta;
-    float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
-    int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
-    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
-}
-
-// ------------------------------------------------------------- face flux
-// HLLE flux (physics_iso2d.hpp:156-173) plus viscous stress
-// (problems/minidisk_scheme.cpp:242-281) at one face. pa/pb: left/right cell
-// primitives; ga/gb: their slopes along the face normal; ta/tb: transverse.
-template<int AXIS>
-__device__ inline void face_flux(const double pa[3], const double pb[3], const double ga[3], const double gb[3],
-                                 const double ta[3], const double tb[3], double x, double y,
-                                 const Args& A, double F[3])
-{
-    double L[3], Rr[3];
-    for (int k = 0; k < 3; ++k)
-    {
-        L[k] = pa[k] + 0.5 * ga[k];     // (pc + g/2) of the left cell
-        Rr[k] = pb[k] - 0.5 * gb[k];    // (pc - g/2) of the right cell
-    }
-    // sound_speed_squared at the face (problems/minidisk_scheme.cpp:127-132)
-    double ph = -1.0 / sqrt((x * x + y * y) + A.rs2);
-    double cs2 = -ph / A.mach / A.mach;
-    double cs = sqrt(cs2);
-    double vl = AXIS == 0 ? L[1] : L[2];
-    double vr = AXIS == 0 ? Rr[1] : Rr[2];
-    double ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
-    double ur[3] = {Rr[0], Rr[0] * Rr[1], Rr[0] * Rr[2]};
-    double pgl = L[0] * cs2, pgr = Rr[0] * cs2;
-    double fl[3] = {vl * ul[0], vl * ul[1] + (AXIS == 0 ? pgl : 0.0), vl * ul[2] + (AXIS == 0 ? 0.0 : pgl)};
-    double fr[3] = {vr * ur[0], vr * ur[1] + (AXIS == 0 ? pgr : 0.0), vr * ur[2] + (AXIS == 0 ? 0.0 : pgr)};
-    double ap = fmax(0.0, fmax(vl + cs, vr + cs));
-    double am = fmin(0.0, fmin(vl - cs, vr - cs));
-    for (int k = 0; k < 3; ++k)
-        F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am) / (ap - am);
-
-    if (A.nu != 0.0)
-    {
-        double mu = A.nu * 0.5 * (Rr[0] + L[0]);
-        double vx_long = 0.5 * (ga[1] + gb[1]) / A.dl;
-        double vy_long = 0.5 * (ga[2] + gb[2]) / A.dl;
-        double vx_tran = 0.5 * (ta[1] + tb[1]) / A.dl;
-        double vy_tran = 0.5 * (ta[2] + tb[2]) / A.dl;
-        if (AXIS == 0)
-        {
-            double tauxx = mu * (vx_long - vy_tran);
-            double tauxy = mu * (vy_long + vx_tran);
-            F[1] = F[1] + -tauxx;
-            F[2] = F[2] + -tauxy;
-        }
-        else
-        {
-            double tauyx = mu * (vy_tran + vx_long);
-            double tauyy = -mu * (vx_tran - vy_long);
-            F[1] = F[1] + -tauyx;
-            F[2] = F[2] + -tauyy;
-        }
-    }
-}
-
-template<int AXIS>
-__device__ inline void face_flux(const float pa[3], const float pb[3], const float ga[3], const float gb[3],
-                                 const float ta[3], const float tb[3], float x, float y,
-                                 const Args& A, float F[3])
-{
-    float L[3], Rr[3];
-    for (int k = 0; k < 3; ++k)
-    {
-        L[k] = fmaf(0.5f, ga[k], pa[k]);
-        Rr[k] = fmaf(-0.5f, gb[k], pb[k]);
-    }
-    float rinv = rsqrt_fast(fmaf(x, x, fmaf(y, y, A.f.rs2)));
-    float cs2 = rinv * A.f.inv_mach2;
-    float cs = sqrt_fast(cs2);
-    float vl = AXIS == 0 ? L[1] : L[2];
-    float vr = AXIS == 0 ? Rr[1] : Rr[2];
-    float ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
-    float ur[3] = {Rr[0], Rr[0] * Rr[1], Rr[0] * Rr[2]};
-    float pgl = L[0] * cs2, pgr = Rr[0] * cs2;
-    float fl[3] = {vl * ul[0], fmaf(vl, ul[1], AXIS == 0 ? pgl : 0.0f), fmaf(vl, ul[2], AXIS == 0 ? 0.0f : pgl)};
-    float fr[3] = {vr * ur[0], fmaf(vr, ur[1], AXIS == 0 ? pgr : 0.0f), fmaf(vr, ur[2], AXIS == 0 ? 0.0f : pgr)};
-    float ap = fmaxf(0.0f, fmaxf(vl, vr) + cs);
-    float am = fminf(0.0f, fminf(vl, vr) - cs);
-    float inv = rcp_fast(ap - am);
-    float apam = ap * am;
-    for (int k = 0; k < 3; ++k)
-        F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * apam) * inv;
-
-    if (A.f.half_nu != 0.0f)
-    {
-        const float half_inv_dl = A.f.half_inv_dl;
-        float mu = A.f.half_nu * (Rr[0] + L[0]);
-        float vx_long = (ga[1] + gb[1]) * half_inv_dl;
-        float vy_long = (ga[2] + gb[2]) * half_inv_dl;
-        float vx_tran = (ta[1] + tb[1]) * half_inv_dl;
-        float vy_tran = (ta[2] + tb[2]) * half_inv_dl;
-        if (AXIS == 0)
-        {
-            F[1] -= mu * (vx_long - vy_tran);
-            F[2] -= mu * (vy_long + vx_tran);
-        }
-        else
-        {
-            F[1] -= mu * (vy_tran + vx_long);
-            F[2] += mu * (vx_tran - vy_long);
-        }
-    }
-}
-
-// ------------------------------------------------------------- mixed cell update
-// Flux divergence, sources and stage update of one cell in the mixed path
-// (FP32 arithmetic, FP64 state): gravity of both point masses, sinks,
-// rotating-frame terms and the outer buffer (problems/minidisk_scheme.cpp:337-352).
-template<int KIND>
-__device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
-                                  const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                  float& local_max)
-{
-    const FloatConsts& F = A.f;
-    float uc[3] = {pc[0], pc[0] * pc[1], pc[0] * pc[2]};
-    float dx1 = x - bf[1], dy1 = y - bf[2];
-    float dx2 = x - bf[4], dy2 = y - bf[5];
-    float q1 = fmaf(dx1, dx1, dy1 * dy1), q2 = fmaf(dx2, dx2, dy2 * dy2);
-    float i1 = rsqrt_fast(q1 + F.rs2), i2 = rsqrt_fast(q2 + F.rs2);
-    float g1 = -bf[0] * i1 * i1 * i1;
-    float g2 = -bf[3] * i2 * i2 * i2;
-    float sr1 = F.sink_rate * exp_fast(-(q1 * q1 * q1) * F.inv_s6);
-    float sr2 = F.sink_rate * exp_fast(-(q2 * q2 * q2) * F.inv_s6);
-    float r2 = fmaf(x, x, y * y);
-    float rinv = rsqrt_fast(r2);
-    float rr = r2 * rinv;
-    // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
-    float br = F.buffer_rate * rcp_fast(1.0f + exp_fast((rr - F.R) * F.neg2_inv_buffer_scale));
-    float vp = sqrt_fast(rsqrt_fast(r2 + F.rs2)) - F.omega * rr;
-    float ui[3] = {1.0f, -vp * y * rinv, vp * x * rinv};
-    float sig = pc[0];
-    float ax = g1 * dx1 + g2 * dx2 + F.omega2 * x + F.two_omega * pc[2];
-    float ay = g1 * dy1 + g2 * dy2 + F.omega2 * y - F.two_omega * pc[1];
-    float src[3];
-    for (int k = 0; k < 3; ++k) src[k] = -(uc[k] * (sr1 + sr2)) - (uc[k] - ui[k]) * br;
-    src[1] = fmaf(sig, ax, src[1]);
-    src[2] = fmaf(sig, ay, src[2]);
-    float du[3];
-    for (int k = 0; k < 3; ++k) du[k] = dtf * (src[k] - (dfx[k] + dfy[k]) * F.inv_dl);
-
-    if (KIND == K_MIX1 && A.d_out)
-    {
-        for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
-        return;
-    }
-    double out[3];
-    for (int k = 0; k < 3; ++k)
-    {
-        float inc = KIND == K_MIX2 ? 0.5f * (__ldg(A.d1 + k * NN + idx) + du[k]) : du[k];
-        out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
-        A.u_out[k * NN + idx] = out[k];
-    }
-    if (A.amax)
-    {
-        float inv = rcp_fast(d2f(out[0]));
-        float vx = d2f(out[1]) * inv, vy = d2f(out[2]) * inv;
-        float cs = sqrt_fast(rsqrt_fast(r2 + F.rs2) * F.inv_mach2);
-        local_max = fmaxf(local_max, fmaxf(fabsf(vx), fabsf(vy)) + cs);
-    }
-}
 
 // ------------------------------------------------------------- shared layout
 template<typename R>
@@ -617,162 +312,21 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
 }
 
 // ------------------------------------------------------------- warp-strip sweep (mixed path)
-// One warp updates a strip of SW_COLS columns (its 32 lanes hold columns
-// j0-2 .. j0+29: two halo columns each side) over A.sweep_rows rows, marching
-// along x. A three-row window of primitives, the x and y slopes of two rows
-// and the previous x-face flux stay in registers; y neighbours come from warp
-// shuffles. Every x face and y face of the strip is computed once, with no
-// shared memory and no barrier. Requires N >= 64 (halo wrap by one period).
-constexpr int SW_COLS = 28, SW_WARPS = 4;
-
-__device__ inline int wrap1(int g, int N) { return g < 0 ? g + N : (g >= N ? g - N : g); }
-
-// One row of this lane's column, raw: FP64 state (+ FP32 stage-1 increment).
-struct RawRow
-{
-    double u[3];
-    float d[3];
-};
-
-template<int KIND>
-__device__ inline void sweep_fetch(const Args& A, int row, int jg, size_t NN, RawRow& r)
-{
-    const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
-    for (int k = 0; k < 3; ++k) r.u[k] = __ldg(A.u_in + k * NN + idx);
-    if (KIND == K_MIX2)
-        for (int k = 0; k < 3; ++k) r.d[k] = __ldg(A.d1 + k * NN + idx);
-}
-
-template<int KIND>
-__device__ inline void sweep_prim(const RawRow& r, float p[3])
-{
-    float s = d2f(r.u[0]), m1 = d2f(r.u[1]), m2 = d2f(r.u[2]);
-    if (KIND == K_MIX2)
-    {
-        s += r.d[0];
-        m1 += r.d[1];
-        m2 += r.d[2];
-    }
-    const float inv = rcp_fast(s);
-    p[0] = s;
-    p[1] = m1 * inv;
-    p[2] = m2 * inv;
-}
-
-__device__ inline void slope_y(const float p[3], float theta, float g[3])
-{
-    for (int k = 0; k < 3; ++k)
-    {
-        float l = __shfl_up_sync(0xffffffffu, p[k], 1);
-        float r = __shfl_down_sync(0xffffffffu, p[k], 1);
-        g[k] = plm(l, p[k], r, theta);
-    }
-}
-
-template<int KIND>
+template<int KIND, int COLS>
 __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A)
 {
-    const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * SW_WARPS + (threadIdx.x >> 5);
-    const int N = A.N;
-    const int sx = warp / A.tiles_y, sy = warp - (warp / A.tiles_y) * A.tiles_y;
+    const int sx = warp / A.tiles_y, sy = warp - sx * A.tiles_y;
     const int i0 = sx * A.sweep_rows;
-    if (i0 >= N) return;                      // uniform per warp
-    const int i1 = min(i0 + A.sweep_rows, N);
-    const int jcol = sy * SW_COLS - 2 + lane;  // unwrapped column of this lane
-    const int jg = wrap1(jcol, N);
-    const bool interior = lane >= 2 && lane < 2 + SW_COLS && jcol < N;
-    const size_t NN = size_t(N) * N;
-    const FloatConsts& F = A.f;
-    const float theta = F.theta;
-
-    float bf[6];
-    double dt;
-    if (A.clock)
-    {
-        dt = A.clock->dt;
-        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.clock->binary[A.stage][k]);
-    }
-    else
-    {
-        dt = A.dt;
-        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.bin[k]);
-    }
-    const float dtf = d2f(dt);
-    const float yc = fmaf(float(jcol) + 0.5f, F.dl, -F.R);   // this lane's cell centre
-    const float yv = fmaf(float(jcol), F.dl, -F.R);          // face between lanes l-1 and l
-
-    // prologue: rows i0-2 .. i0+1, and the fetch of row i0+2
-    float pm2[3], pm1[3], p0[3], p1[3];
-    RawRow raw;
-    sweep_fetch<KIND>(A, i0 - 2, jg, NN, raw);
-    sweep_prim<KIND>(raw, pm2);
-    sweep_fetch<KIND>(A, i0 - 1, jg, NN, raw);
-    sweep_prim<KIND>(raw, pm1);
-    sweep_fetch<KIND>(A, i0, jg, NN, raw);
-    sweep_prim<KIND>(raw, p0);
-    sweep_fetch<KIND>(A, i0 + 1, jg, NN, raw);
-    sweep_prim<KIND>(raw, p1);
-    sweep_fetch<KIND>(A, i0 + 2, jg, NN, raw);
-    float gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
-    for (int k = 0; k < 3; ++k)
-    {
-        gxm1[k] = plm(pm2[k], pm1[k], p0[k], theta);
-        gx0[k] = plm(pm1[k], p0[k], p1[k], theta);
-    }
-    slope_y(pm1, theta, gym1);
-    slope_y(p0, theta, gy0);
-    face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
-
-    float local_max = 0.0f;
-    for (int i = i0; i < i1; ++i)
-    {
-        float p2[3], gx1[3], gy1[3], fxp[3];
-        sweep_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
-        sweep_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
-        for (int k = 0; k < 3; ++k) gx1[k] = plm(p0[k], p1[k], p2[k], theta);
-        slope_y(p1, theta, gy1);
-        face_flux<0>(p0, p1, gx0, gx1, gy0, gy1, fmaf(float(i + 1), F.dl, -F.R), yc, A, fxp);
-
-        // y face on this lane's left side, from lane l-1 (row i)
-        float pl[3], gl[3], tl[3], fy[3];
-        for (int k = 0; k < 3; ++k)
-        {
-            pl[k] = __shfl_up_sync(0xffffffffu, p0[k], 1);
-            gl[k] = __shfl_up_sync(0xffffffffu, gy0[k], 1);
-            tl[k] = __shfl_up_sync(0xffffffffu, gx0[k], 1);
-        }
-        const float xc = fmaf(float(i) + 0.5f, F.dl, -F.R);
-        face_flux<1>(pl, p0, gl, gy0, tl, gx0, xc, yv, A, fy);
-        float dfx[3], dfy[3];
-        for (int k = 0; k < 3; ++k)
-        {
-            dfy[k] = __shfl_down_sync(0xffffffffu, fy[k], 1) - fy[k];
-            dfx[k] = fxp[k] - fxm[k];
-        }
-        if (interior)
-            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
-
-        for (int k = 0; k < 3; ++k)
-        {
-            p0[k] = p1[k];
-            p1[k] = p2[k];
-            gx0[k] = gx1[k];
-            gy0[k] = gy1[k];
-            fxm[k] = fxp[k];
-        }
-    }
-    if (A.amax)
-    {
-        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
-        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
-    }
+    if (i0 >= A.N) return;                    // uniform per warp
+    if (COLS == 2) sweep_strip2<KIND>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
+    else sweep_strip<KIND>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
 }
 
 // Rows per warp: enough segments along x that all strips run as one wave of
 // resident warps (no half-empty tail wave), but never fewer than 32 rows so
 // the two halo rows stay a small overhead.
-template<int KIND>
+template<int KIND, int COLS>
 int launch_sweep(Args A, cudaStream_t s)
 {
     static int blocks_per_sm[64] = {};
@@ -782,71 +336,44 @@ int launch_sweep(Args A, cudaStream_t s)
     if (blocks_per_sm[dev & 63] == 0)
     {
         int b = 0, n = 0;
-        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND>, SW_WARPS * 32, 0));
+        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS>, SW_WARPS * 32, 0));
         MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
         sm_count[dev & 63] = n;
         blocks_per_sm[dev & 63] = b > 0 ? b : 1;
     }
-    A.tiles_y = (A.N + SW_COLS - 1) / SW_COLS;
+    const int cols = COLS == 2 ? SW2_COLS : SW_COLS;
+    A.tiles_y = (A.N + cols - 1) / cols;
     const int capacity = blocks_per_sm[dev & 63] * SW_WARPS * sm_count[dev & 63];
     const int segments = std::max(1, capacity / A.tiles_y);
     A.sweep_rows = std::max(32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
     const int warps = strips_x * A.tiles_y;
-    sweep_kernel<KIND><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
+    sweep_kernel<KIND, COLS><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
     return launch_status("minidisk sweep kernel");
 }
 
-// ------------------------------------------------------------- clock kernel
-struct ClockArgs
-{
-    double R, dl, cfl, softening_length, mass_ratio, eccentricity, omega;
-    int dt_mode, rk_order;
-    int end_step;     // 1: finish the step that just ran (advance time, iteration)
-    int begin_step;   // 1: choose dt and stage binaries of the next step
-};
+// Columns per lane of the mixed sweep: 0 = automatic (two wherever the mesh
+// and buffers allow), 1 or 2 to force one form.
+int g_sweep_columns = 0;
 
-__device__ inline void store_binary(double* dst, const Binary& b)
+bool two_column_ok(const Args& A)
 {
-    dst[0] = b.m1; dst[1] = b.x1; dst[2] = b.y1; dst[3] = b.m2; dst[4] = b.x2; dst[5] = b.y2;
+    auto al = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
+    return A.N % 2 == 0 && al(A.u_in, 16) && al(A.u_out, 16) && al(A.d1, 8) && al(A.d_out, 8);
 }
 
+template<int KIND>
+int launch_sweep_auto(const Args& A, cudaStream_t s)
+{
+    const bool two = g_sweep_columns != 1 && two_column_ok(A);
+    return two ? launch_sweep<KIND, 2>(A, s) : launch_sweep<KIND, 1>(A, s);
+}
+
+// ------------------------------------------------------------- clock kernel
 __global__ void clock_kernel(mara_minidisk_clock* c, const ClockArgs a)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (a.end_step)
-    {
-        double t = c->time, dt = c->dt;
-        if (a.rk_order == 2)
-        {
-            double t2 = (t + dt) + dt;
-            c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
-        }
-        else
-        {
-            c->time = t + dt;
-        }
-        c->iteration += 1;
-    }
-    if (a.begin_step)
-    {
-        double t = c->time, dt;
-        if (a.dt_mode == MARA_DT_FORMULA)
-        {
-            // problems/minidisk.cpp:204-206
-            double vmax = sqrt(1.0 * 0.5 / a.softening_length);
-            double cfl = a.cfl * fmin(1.0, 0.01 + t / 0.05);
-            dt = a.dl / vmax * cfl;
-        }
-        else
-        {
-            dt = a.cfl * a.dl / c->max_wavespeed;   // scheme_mhd_v1.cpp:287 form
-        }
-        c->dt = dt;
-        store_binary(c->binary[0], binary_state(a.mass_ratio, a.eccentricity, a.omega, t));
-        store_binary(c->binary[1], binary_state(a.mass_ratio, a.eccentricity, a.omega, t + dt));
-        c->max_wavespeed = 0.0;
-    }
+    advance_clock(c, a);
 }
 
 // ------------------------------------------------------------- small kernels
@@ -1043,8 +570,8 @@ int launch_stage(const Args& A, int tiles, cudaStream_t s)
 
 int grid_stage(Args A, int kind, cudaStream_t s)
 {
-    if (A.N >= 64 && kind == K_MIX1) return launch_sweep<K_MIX1>(A, s);
-    if (A.N >= 64 && kind == K_MIX2) return launch_sweep<K_MIX2>(A, s);
+    if (A.N >= 64 && kind == K_MIX1) return launch_sweep_auto<K_MIX1>(A, s);
+    if (A.N >= 64 && kind == K_MIX2) return launch_sweep_auto<K_MIX2>(A, s);
     int tiles_x = (A.N + TX - 1) / TX;
     A.tiles_y = (A.N + TY - 1) / TY;
     int tiles = tiles_x * A.tiles_y;
@@ -1057,8 +584,7 @@ int grid_stage(Args A, int kind, cudaStream_t s)
     return fail(MARA_ERR_ARGUMENT, "minidisk: bad stage kind");
 }
 
-int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
-               int end_step, int begin_step, cudaStream_t s)
+ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, int end_step, int begin_step)
 {
     ClockArgs a;
     a.R = sd->domain_radius;
@@ -1072,7 +598,13 @@ int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int d
     a.rk_order = rk_order;
     a.end_step = end_step;
     a.begin_step = begin_step;
-    clock_kernel<<<1, 32, 0, s>>>(clock, a);
+    return a;
+}
+
+int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
+               int end_step, int begin_step, cudaStream_t s)
+{
+    clock_kernel<<<1, 32, 0, s>>>(clock, clock_args(sd, dt_mode, rk_order, end_step, begin_step));
     return launch_status("minidisk clock kernel");
 }
 
@@ -1345,6 +877,18 @@ int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const doub
     bool writes_state = !(kind == 1 && d_out);
     A.amax = reduce_wavespeed && writes_state ? reinterpret_cast<unsigned long long*>(&clock->max_wavespeed) : nullptr;
     return grid_stage(A, kind == 0 ? K_FP64 : (kind == 1 ? K_MIX1 : K_MIX2), as_stream(stream));
+}
+
+int mara_minidisk_sweep_columns(int32_t columns)
+{
+    if (columns < 0 || columns > 2)
+    {
+        fail(MARA_ERR_ARGUMENT, "mara_minidisk_sweep_columns: columns must be 0, 1 or 2");
+        return -1;
+    }
+    const int previous = g_sweep_columns;
+    g_sweep_columns = columns;
+    return previous;
 }
 
 int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int32_t dt_mode,

@@ -1,0 +1,819 @@
+// Device-side pieces of the minidisk Godunov update shared by the
+// single-mesh kernels (minidisk.cu) and the batched ensemble (ensemble.cu):
+// the launch arguments, the mixed-precision conversions and fast math, PLM
+// slopes, the HLLE + viscous face flux, the mixed cell update and the
+// warp-strip sweep of one strip segment.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "common.cuh"
+
+namespace mara {
+namespace md {
+
+constexpr int TX = 16, TY = 32, NT = 256;
+constexpr int EX = TX + 4, EY = TY + 4;     // halo tile
+constexpr int GX = TX + 2, GY = TY + 2;     // slope region
+constexpr int NFX = (TX + 1) * TY;          // x faces
+constexpr int NFY = TX * (TY + 1);          // y faces
+
+enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3 };
+
+// Single-precision constants of the mixed path, prepared on the host so that
+// no FP64 instruction (GB300 runs FP64 at 1/64 of the FP32 rate) is issued
+// for them on the device.
+struct FloatConsts
+{
+    float rs2, inv_mach2, half_nu, half_inv_dl, inv_dl, theta, R, dl;
+    float sink_rate, inv_s6, buffer_rate, neg2_inv_buffer_scale, omega, omega2, two_omega;
+};
+
+struct Args
+{
+    int N;                 // cells per side of the mesh (K_BLOCK: block size)
+    int n;                 // block size (zones per block side)
+    int level;             // block level (2^level blocks per side)
+    int tiles_y;
+    int sweep_rows;        // mixed sweep: rows per warp
+    uint64_t bi, bj;       // K_BLOCK: block coordinates
+    double R, dl;
+    double rs2;            // softening_length^2 (std::pow(rs, 2.0) on the host)
+    double mach, nu, omega, sink_rate, s6, buffer_rate, buffer_scale, theta;
+    double dt;             // used when clock == nullptr
+    double bin[6];         // m1, x1, y1, m2, x2, y2; used when clock == nullptr
+    const mara_minidisk_clock* clock;
+    int stage;             // which clock->binary row this stage uses
+    const double* u_in;    // FP64/MIX: stage state (FP64) or u0; K_BLOCK: uc AoS
+    const double* u_avg;   // K_FP64: optional RK2 average partner
+    const float* d1;       // K_MIX2: FP32 stage-1 increment
+    double* u_out;         // FP64 result
+    float* d_out;          // K_MIX1 + RK2: increment out
+    const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
+    unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
+    FloatConsts f;
+};
+
+// double -> float (round to nearest even) and float -> double (exact) with
+// integer instructions only, so that the mixed path issues no FP64-pipe work
+// for them. Magnitudes below the smallest normal float (1.2e-38) become signed
+// zero; overflow gives infinity; NaN stays NaN.
+__device__ inline float d2f(double x)
+{
+    const unsigned long long b = __double_as_longlong(x);
+    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    unsigned f = sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1FFFFFFFu;
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    const bool nan = e == 0x7FFu && ((hi & 0xFFFFFu) | lo) != 0u;
+    f = e < 897u ? sign : f;
+    f = e > 1150u ? (sign | (nan ? 0x7FC00000u : 0x7F800000u)) : f;
+    return __uint_as_float(f);
+}
+
+__device__ inline double f2d(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xFFu;
+    const unsigned m = b & 0x7FFFFFu;
+    const unsigned ee = e == 255u ? 2047u : e + 896u;
+    unsigned hi = (b & 0x80000000u) | (ee << 20) | (m >> 3);
+    unsigned lo = m << 29;
+    hi = e == 0u ? (b & 0x80000000u) : hi;
+    lo = e == 0u ? 0u : lo;
+    return __hiloint2double(int(hi), int(lo));
+}
+
+// Single-MUFU approximations for the mixed path (relative error ~1e-7,
+// well inside the FP32 budget of the fluxes; denormals flush to zero).
+__device__ inline float rcp_fast(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float sqrt_fast(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float rsqrt_fast(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ inline float exp_fast(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+    return y;
+}
+
+// ------------------------------------------------------------- geometry
+// vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
+__host__ __device__ inline double vertex(double R, int n, int level, uint64_t b, int k)
+{
+    double dlv = double(1 << level);
+    double x0 = R * (-1 + double(2 * b) / dlv);
+    double x1 = R * (-1 + double(2 * (b + 1)) / dlv);
+    return x0 + (x1 - x0) * double(k) / double(n);
+}
+
+__device__ inline int wrap(int g, int N)
+{
+    g %= N;
+    return g < 0 ? g + N : g;
+}
+
+// ------------------------------------------------------------- PLM
+// Generalised minmod on unit spacing (scheme_plm_gradient.hpp:56-63). The
+// reference's 0.25*|sa+sb|*(sa+sc)*min(|a|,|b|,|c|) equals copysign(min, a)
+// when a, b, c share a sign and zero otherwise; that is what is computed here.
+__device__ inline double plm(double yl, double y0, double yr, double theta)
+{
+    double a = (y0 - yl) * theta;
+    double b = (yr - yl) * 0.5;
+    double c = (yr - y0) * theta;
+    double m = fmin(fmin(fabs(a), fabs(b)), fabs(c));
+    long long sa = __double_as_longlong(a), sb = __double_as_longlong(b), sc = __double_as_longlong(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0 : copysign(m, a);
+}
+
+// ------------------------------------------------------------- FP32 lanes
+// The mixed path is written once for T = float (one column per thread) and
+// T = float2 (two adjacent columns per thread). Every operation is explicit
+// and rounded to nearest, with no contraction left to the compiler, so both
+// forms (and every kernel built from them) give bit-identical results. The
+// pair form issues two scalar instructions per operation: packed FP32x2
+// instructions were measured at most 3% faster here, and did not reproduce
+// the scalar rounding inside these kernels.
+__device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float vsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float vneg(float a) { return -a; }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return make_float2(vadd(a.x, b.x), vadd(a.y, b.y)); }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) { return make_float2(vsub(a.x, b.x), vsub(a.y, b.y)); }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return make_float2(vmul(a.x, b.x), vmul(a.y, b.y)); }
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c)
+{
+    return make_float2(vfma(a.x, b.x, c.x), vfma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 vneg(float2 a) { return make_float2(-a.x, -a.y); }
+
+template<typename T> __device__ __forceinline__ T bc(float c);
+template<> __device__ __forceinline__ float bc<float>(float c) { return c; }
+template<> __device__ __forceinline__ float2 bc<float2>(float c) { return make_float2(c, c); }
+
+#define MARA_LANEWISE(name, expr)                                                                     \
+    __device__ __forceinline__ float name(float a) { return expr(a); }                               \
+    __device__ __forceinline__ float2 name(float2 a) { return make_float2(expr(a.x), expr(a.y)); }
+MARA_LANEWISE(vrcp, rcp_fast)
+MARA_LANEWISE(vsqrt, sqrt_fast)
+MARA_LANEWISE(vrsqrt, rsqrt_fast)
+#undef MARA_LANEWISE
+
+__device__ __forceinline__ float ex2_fast(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+template<typename T>
+__device__ __forceinline__ T vexp(T a)
+{
+    const T t = vmul(a, bc<T>(1.4426950408889634f));
+    if constexpr (sizeof(T) == sizeof(float)) return ex2_fast(t);
+    else return make_float2(ex2_fast(t.x), ex2_fast(t.y));
+}
+__device__ __forceinline__ float vmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float2 vmax(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
+__device__ __forceinline__ float2 vmin(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+
+__device__ __forceinline__ float minmod_select(float a, float b, float c)
+{
+    const float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
+    const int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
+}
+
+template<typename T>
+__device__ __forceinline__ T vplm(T yl, T y0, T yr, float theta)
+{
+    const T a = vmul(vsub(y0, yl), bc<T>(theta));
+    const T b = vmul(vsub(yr, yl), bc<T>(0.5f));
+    const T c = vmul(vsub(yr, y0), bc<T>(theta));
+    if constexpr (sizeof(T) == sizeof(float)) return minmod_select(a, b, c);
+    else return make_float2(minmod_select(a.x, b.x, c.x), minmod_select(a.y, b.y, c.y));
+}
+
+__device__ inline float plm(float yl, float y0, float yr, float theta) { return vplm(yl, y0, yr, theta); }
+
+// ------------------------------------------------------------- face flux
+// HLLE flux (physics_iso2d.hpp:156-173) plus viscous stress
+// (problems/minidisk_scheme.cpp:242-281) at one face. pa/pb: left/right cell
+// primitives; ga/gb: their slopes along the face normal; ta/tb: transverse.
+template<int AXIS>
+__device__ inline void face_flux(const double pa[3], const double pb[3], const double ga[3], const double gb[3],
+                                 const double ta[3], const double tb[3], double x, double y,
+                                 const Args& A, double F[3])
+{
+    double L[3], Rr[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        L[k] = pa[k] + 0.5 * ga[k];     // (pc + g/2) of the left cell
+        Rr[k] = pb[k] - 0.5 * gb[k];    // (pc - g/2) of the right cell
+    }
+    // sound_speed_squared at the face (problems/minidisk_scheme.cpp:127-132)
+    double ph = -1.0 / sqrt((x * x + y * y) + A.rs2);
+    double cs2 = -ph / A.mach / A.mach;
+    double cs = sqrt(cs2);
+    double vl = AXIS == 0 ? L[1] : L[2];
+    double vr = AXIS == 0 ? Rr[1] : Rr[2];
+    double ul[3] = {L[0], L[0] * L[1], L[0] * L[2]};
+    double ur[3] = {Rr[0], Rr[0] * Rr[1], Rr[0] * Rr[2]};
+    double pgl = L[0] * cs2, pgr = Rr[0] * cs2;
+    double fl[3] = {vl * ul[0], vl * ul[1] + (AXIS == 0 ? pgl : 0.0), vl * ul[2] + (AXIS == 0 ? 0.0 : pgl)};
+    double fr[3] = {vr * ur[0], vr * ur[1] + (AXIS == 0 ? pgr : 0.0), vr * ur[2] + (AXIS == 0 ? 0.0 : pgr)};
+    double ap = fmax(0.0, fmax(vl + cs, vr + cs));
+    double am = fmin(0.0, fmin(vl - cs, vr - cs));
+    for (int k = 0; k < 3; ++k)
+        F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am) / (ap - am);
+
+    if (A.nu != 0.0)
+    {
+        double mu = A.nu * 0.5 * (Rr[0] + L[0]);
+        double vx_long = 0.5 * (ga[1] + gb[1]) / A.dl;
+        double vy_long = 0.5 * (ga[2] + gb[2]) / A.dl;
+        double vx_tran = 0.5 * (ta[1] + tb[1]) / A.dl;
+        double vy_tran = 0.5 * (ta[2] + tb[2]) / A.dl;
+        if (AXIS == 0)
+        {
+            double tauxx = mu * (vx_long - vy_tran);
+            double tauxy = mu * (vy_long + vx_tran);
+            F[1] = F[1] + -tauxx;
+            F[2] = F[2] + -tauxy;
+        }
+        else
+        {
+            double tauyx = mu * (vy_tran + vx_long);
+            double tauyy = -mu * (vx_tran - vy_long);
+            F[1] = F[1] + -tauyx;
+            F[2] = F[2] + -tauyy;
+        }
+    }
+}
+
+template<int AXIS, typename T>
+__device__ inline void face_flux_f(const T pa[3], const T pb[3], const T ga[3], const T gb[3], const T ta[3],
+                                   const T tb[3], T x, T y, const FloatConsts& F, T out[3])
+{
+    T L[3], Rr[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        L[k] = vfma(bc<T>(0.5f), ga[k], pa[k]);
+        Rr[k] = vfma(bc<T>(-0.5f), gb[k], pb[k]);
+    }
+    // sound_speed_squared at the face: -phi/M^2 with phi = -1/sqrt(r^2 + rs^2)
+    const T rinv = vrsqrt(vfma(x, x, vfma(y, y, bc<T>(F.rs2))));
+    const T cs2 = vmul(rinv, bc<T>(F.inv_mach2));
+    const T cs = vsqrt(cs2);
+    const T vl = AXIS == 0 ? L[1] : L[2];
+    const T vr = AXIS == 0 ? Rr[1] : Rr[2];
+    const T ul[3] = {L[0], vmul(L[0], L[1]), vmul(L[0], L[2])};
+    const T ur[3] = {Rr[0], vmul(Rr[0], Rr[1]), vmul(Rr[0], Rr[2])};
+    const T pgl = vmul(L[0], cs2), pgr = vmul(Rr[0], cs2);
+    T fl[3], fr[3];
+    fl[0] = vmul(vl, ul[0]);
+    fr[0] = vmul(vr, ur[0]);
+    fl[1] = AXIS == 0 ? vfma(vl, ul[1], pgl) : vmul(vl, ul[1]);
+    fr[1] = AXIS == 0 ? vfma(vr, ur[1], pgr) : vmul(vr, ur[1]);
+    fl[2] = AXIS == 0 ? vmul(vl, ul[2]) : vfma(vl, ul[2], pgl);
+    fr[2] = AXIS == 0 ? vmul(vr, ur[2]) : vfma(vr, ur[2], pgr);
+    const T ap = vmax(bc<T>(0.0f), vadd(vmax(vl, vr), cs));
+    const T am = vmin(bc<T>(0.0f), vsub(vmin(vl, vr), cs));
+    const T inv = vrcp(vsub(ap, am));
+    const T apam = vmul(ap, am);
+    const T nam = vneg(am);
+    for (int k = 0; k < 3; ++k)
+    {
+        // (ap*fl - am*fr - (ul - ur)*ap*am) / (ap - am)
+        T t = vmul(ap, fl[k]);
+        t = vfma(nam, fr[k], t);
+        t = vfma(vsub(ur[k], ul[k]), apam, t);
+        out[k] = vmul(t, inv);
+    }
+    if (F.half_nu != 0.0f)
+    {
+        const T h = bc<T>(F.half_inv_dl);
+        const T mu = vmul(bc<T>(F.half_nu), vadd(Rr[0], L[0]));
+        const T nmu = vneg(mu);
+        const T vx_long = vmul(vadd(ga[1], gb[1]), h);
+        const T vy_long = vmul(vadd(ga[2], gb[2]), h);
+        const T vx_tran = vmul(vadd(ta[1], tb[1]), h);
+        const T vy_tran = vmul(vadd(ta[2], tb[2]), h);
+        if (AXIS == 0)
+        {
+            out[1] = vfma(nmu, vsub(vx_long, vy_tran), out[1]);
+            out[2] = vfma(nmu, vadd(vy_long, vx_tran), out[2]);
+        }
+        else
+        {
+            out[1] = vfma(nmu, vadd(vy_tran, vx_long), out[1]);
+            out[2] = vfma(mu, vsub(vx_tran, vy_long), out[2]);
+        }
+    }
+}
+
+template<int AXIS>
+__device__ inline void face_flux(const float pa[3], const float pb[3], const float ga[3], const float gb[3],
+                                 const float ta[3], const float tb[3], float x, float y,
+                                 const Args& A, float F[3])
+{
+    face_flux_f<AXIS, float>(pa, pb, ga, gb, ta, tb, x, y, A.f, F);
+}
+
+// ------------------------------------------------------------- mixed cell update
+// Stage increment du = dt * L(u) of one cell (or a pair) in FP32: flux
+// divergence, gravity of both point masses, sinks, rotating-frame terms and
+// the outer buffer (problems/minidisk_scheme.cpp:337-352). pot returns
+// 1/sqrt(r^2 + rs^2), from which the cell-centre sound speed follows.
+template<typename T>
+__device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc[3], const T dfx[3], const T dfy[3],
+                                      const float bf[6], float dtf, T du[3], T& pot)
+{
+    const T uc[3] = {pc[0], vmul(pc[0], pc[1]), vmul(pc[0], pc[2])};
+    const T dx1 = vsub(x, bc<T>(bf[1])), dy1 = vsub(y, bc<T>(bf[2]));
+    const T dx2 = vsub(x, bc<T>(bf[4])), dy2 = vsub(y, bc<T>(bf[5]));
+    const T q1 = vfma(dx1, dx1, vmul(dy1, dy1)), q2 = vfma(dx2, dx2, vmul(dy2, dy2));
+    const T i1 = vrsqrt(vadd(q1, bc<T>(F.rs2))), i2 = vrsqrt(vadd(q2, bc<T>(F.rs2)));
+    const T g1 = vmul(vmul(vmul(bc<T>(-bf[0]), i1), i1), i1);
+    const T g2 = vmul(vmul(vmul(bc<T>(-bf[3]), i2), i2), i2);
+    const T sr1 = vmul(bc<T>(F.sink_rate), vexp(vmul(vmul(vmul(q1, q1), q1), bc<T>(-F.inv_s6))));
+    const T sr2 = vmul(bc<T>(F.sink_rate), vexp(vmul(vmul(vmul(q2, q2), q2), bc<T>(-F.inv_s6))));
+    const T r2 = vfma(x, x, vmul(y, y));
+    const T rinv = vrsqrt(r2);
+    const T rr = vmul(r2, rinv);
+    // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
+    const T br = vmul(bc<T>(F.buffer_rate),
+                      vrcp(vadd(bc<T>(1.0f), vexp(vmul(vsub(rr, bc<T>(F.R)), bc<T>(F.neg2_inv_buffer_scale))))));
+    pot = vrsqrt(vadd(r2, bc<T>(F.rs2)));
+    const T vp = vsub(vsqrt(pot), vmul(bc<T>(F.omega), rr));
+    const T ui[3] = {bc<T>(1.0f), vmul(vmul(vneg(vp), y), rinv), vmul(vmul(vp, x), rinv)};
+    T ax = vfma(g2, dx2, vmul(g1, dx1));
+    ax = vfma(bc<T>(F.omega2), x, ax);
+    ax = vfma(bc<T>(F.two_omega), pc[2], ax);
+    T ay = vfma(g2, dy2, vmul(g1, dy1));
+    ay = vfma(bc<T>(F.omega2), y, ay);
+    ay = vfma(bc<T>(-F.two_omega), pc[1], ay);
+    const T srs = vadd(sr1, sr2);
+    T src[3];
+    for (int k = 0; k < 3; ++k) src[k] = vfma(vsub(ui[k], uc[k]), br, vneg(vmul(uc[k], srs)));
+    src[1] = vfma(pc[0], ax, src[1]);
+    src[2] = vfma(pc[0], ay, src[2]);
+    for (int k = 0; k < 3; ++k)
+        du[k] = vmul(bc<T>(dtf), vfma(vadd(dfx[k], dfy[k]), bc<T>(-F.inv_dl), src[k]));
+}
+
+// Fastest wavespeed max(|vx|, |vy|) + cs of an FP64 state at a cell whose
+// 1/sqrt(r^2 + rs^2) is pot (iso2d::fastest_wavespeed, physics_iso2d.hpp:108-116).
+__device__ inline float cell_wavespeed(const FloatConsts& F, const double out[3], float pot)
+{
+    const float inv = rcp_fast(d2f(out[0]));
+    const float vx = vmul(d2f(out[1]), inv), vy = vmul(d2f(out[2]), inv);
+    const float cs = sqrt_fast(vmul(pot, F.inv_mach2));
+    return vadd(fmaxf(fabsf(vx), fabsf(vy)), cs);
+}
+
+// Store one cell's stage result: the FP32 increment (stage 1 of mixed RK2),
+// or the FP64 state u_in + du (with the RK2 average of the two increments in
+// stage 2), and fold its wavespeed into local_max.
+template<int KIND>
+__device__ inline void store_cell(const Args& A, float du[3], float pot, size_t idx, size_t NN, float& local_max)
+{
+    if (KIND == K_MIX1 && A.d_out)
+    {
+        for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
+        return;
+    }
+    double out[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        const float inc = KIND == K_MIX2 ? vmul(vadd(__ldg(A.d1 + k * NN + idx), du[k]), 0.5f) : du[k];
+        out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
+        A.u_out[k * NN + idx] = out[k];
+    }
+    if (A.amax) local_max = fmaxf(local_max, cell_wavespeed(A.f, out, pot));
+}
+
+template<int KIND>
+__device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
+                                  const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
+                                  float& local_max)
+{
+    float du[3], pot;
+    cell_increment<float>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, pot);
+    store_cell<KIND>(A, du, pot, idx, NN, local_max);
+}
+
+// The pair form: columns idx and idx + 1 of one row (idx even).
+template<int KIND>
+__device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const float2 pc[3], const float2 dfx[3],
+                                   const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
+                                   float& local_max)
+{
+    float2 du[3], pot;
+    cell_increment<float2>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, pot);
+    if (KIND == K_MIX1 && A.d_out)
+    {
+        for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(A.d_out + k * NN + idx) = du[k];
+        return;
+    }
+    double2 out[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        float2 inc = du[k];
+        if (KIND == K_MIX2) inc = vmul(vadd(__ldg(reinterpret_cast<const float2*>(A.d1 + k * NN + idx)), du[k]),
+                                       bc<float2>(0.5f));
+        const double2 u = __ldg(reinterpret_cast<const double2*>(A.u_in + k * NN + idx));
+        out[k] = make_double2(u.x + f2d(inc.x), u.y + f2d(inc.y));
+        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = out[k];
+    }
+    if (A.amax)
+    {
+        const double o0[3] = {out[0].x, out[1].x, out[2].x}, o1[3] = {out[0].y, out[1].y, out[2].y};
+        local_max = fmaxf(local_max, fmaxf(cell_wavespeed(A.f, o0, pot.x), cell_wavespeed(A.f, o1, pot.y)));
+    }
+}
+
+// ------------------------------------------------------------- warp-strip sweep (mixed path)
+// One warp updates a strip of SW_COLS columns (its 32 lanes hold columns
+// j0-2 .. j0+29: two halo columns each side) over A.sweep_rows rows, marching
+// along x. A three-row window of primitives, the x and y slopes of two rows
+// and the previous x-face flux stay in registers; y neighbours come from warp
+// shuffles. Every x face and y face of the strip is computed once, with no
+// shared memory and no barrier. Requires N >= 64 (halo wrap by one period).
+constexpr int SW_COLS = 28, SW_WARPS = 4;
+
+__device__ inline int wrap1(int g, int N) { return g < 0 ? g + N : (g >= N ? g - N : g); }
+
+// One row of this lane's column, raw: FP64 state (+ FP32 stage-1 increment).
+struct RawRow
+{
+    double u[3];
+    float d[3];
+};
+
+template<int KIND>
+__device__ inline void sweep_fetch(const Args& A, int row, int jg, size_t NN, RawRow& r)
+{
+    const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
+    for (int k = 0; k < 3; ++k) r.u[k] = __ldg(A.u_in + k * NN + idx);
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) r.d[k] = __ldg(A.d1 + k * NN + idx);
+}
+
+template<int KIND>
+__device__ inline void sweep_prim(const RawRow& r, float p[3])
+{
+    float s = d2f(r.u[0]), m1 = d2f(r.u[1]), m2 = d2f(r.u[2]);
+    if (KIND == K_MIX2)
+    {
+        s = vadd(s, r.d[0]);
+        m1 = vadd(m1, r.d[1]);
+        m2 = vadd(m2, r.d[2]);
+    }
+    const float inv = vrcp(s);
+    p[0] = s;
+    p[1] = vmul(m1, inv);
+    p[2] = vmul(m2, inv);
+}
+
+__device__ inline void slope_y(const float p[3], float theta, float g[3])
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        float l = __shfl_up_sync(0xffffffffu, p[k], 1);
+        float r = __shfl_down_sync(0xffffffffu, p[k], 1);
+        g[k] = plm(l, p[k], r, theta);
+    }
+}
+
+// Rows [i0, i1) of column strip sy of the mesh A describes: the body of a
+// sweep warp. Called with a warp-uniform (i0, i1, sy).
+template<int KIND>
+__device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int sy)
+{
+    const int lane = threadIdx.x & 31;
+    const int N = A.N;
+    const int jcol = sy * SW_COLS - 2 + lane;  // unwrapped column of this lane
+    const int jg = wrap1(jcol, N);
+    const bool interior = lane >= 2 && lane < 2 + SW_COLS && jcol < N;
+    const size_t NN = size_t(N) * N;
+    const FloatConsts& F = A.f;
+    const float theta = F.theta;
+
+    float bf[6];
+    double dt;
+    if (A.clock)
+    {
+        dt = A.clock->dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.clock->binary[A.stage][k]);
+    }
+    else
+    {
+        dt = A.dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.bin[k]);
+    }
+    const float dtf = d2f(dt);
+    const float yc = fmaf(float(jcol) + 0.5f, F.dl, -F.R);   // this lane's cell centre
+    const float yv = fmaf(float(jcol), F.dl, -F.R);          // face between lanes l-1 and l
+
+    // prologue: rows i0-2 .. i0+1, and the fetch of row i0+2
+    float pm2[3], pm1[3], p0[3], p1[3];
+    RawRow raw;
+    sweep_fetch<KIND>(A, i0 - 2, jg, NN, raw);
+    sweep_prim<KIND>(raw, pm2);
+    sweep_fetch<KIND>(A, i0 - 1, jg, NN, raw);
+    sweep_prim<KIND>(raw, pm1);
+    sweep_fetch<KIND>(A, i0, jg, NN, raw);
+    sweep_prim<KIND>(raw, p0);
+    sweep_fetch<KIND>(A, i0 + 1, jg, NN, raw);
+    sweep_prim<KIND>(raw, p1);
+    sweep_fetch<KIND>(A, i0 + 2, jg, NN, raw);
+    float gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        gxm1[k] = plm(pm2[k], pm1[k], p0[k], theta);
+        gx0[k] = plm(pm1[k], p0[k], p1[k], theta);
+    }
+    slope_y(pm1, theta, gym1);
+    slope_y(p0, theta, gy0);
+    face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
+
+    float local_max = 0.0f;
+    for (int i = i0; i < i1; ++i)
+    {
+        float p2[3], gx1[3], gy1[3], fxp[3];
+        sweep_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
+        sweep_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+        for (int k = 0; k < 3; ++k) gx1[k] = plm(p0[k], p1[k], p2[k], theta);
+        slope_y(p1, theta, gy1);
+        face_flux<0>(p0, p1, gx0, gx1, gy0, gy1, fmaf(float(i + 1), F.dl, -F.R), yc, A, fxp);
+
+        // y face on this lane's left side, from lane l-1 (row i)
+        float pl[3], gl[3], tl[3], fy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            pl[k] = __shfl_up_sync(0xffffffffu, p0[k], 1);
+            gl[k] = __shfl_up_sync(0xffffffffu, gy0[k], 1);
+            tl[k] = __shfl_up_sync(0xffffffffu, gx0[k], 1);
+        }
+        const float xc = fmaf(float(i) + 0.5f, F.dl, -F.R);
+        face_flux<1>(pl, p0, gl, gy0, tl, gx0, xc, yv, A, fy);
+        float dfx[3], dfy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            dfy[k] = vsub(__shfl_down_sync(0xffffffffu, fy[k], 1), fy[k]);
+            dfx[k] = vsub(fxp[k], fxm[k]);
+        }
+        if (interior)
+            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
+
+        for (int k = 0; k < 3; ++k)
+        {
+            p0[k] = p1[k];
+            p1[k] = p2[k];
+            gx0[k] = gx1[k];
+            gy0[k] = gy1[k];
+            fxm[k] = fxp[k];
+        }
+    }
+    if (A.amax)
+    {
+        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
+    }
+}
+
+// ------------------------------------------------------------- two-column sweep
+// Thread coarsening of the sweep: lane l holds the column pair
+// (j0 - 2 + 2l, j0 - 1 + 2l), so a warp covers 64 columns of which 60 are
+// interior (the 1-column sweep keeps 28 of 32): half the y-direction
+// shuffles per cell, a smaller share of halo lanes, and double2 / float2
+// loads and stores. The arithmetic is that of the 1-column sweep, so the
+// results are bit-identical. Requires an even N >= 64 and 16-byte aligned
+// state (8-byte aligned increments).
+constexpr int SW2_COLS = 60;
+
+struct RawRow2
+{
+    double2 u[3];
+    float2 d[3];
+};
+
+template<int KIND>
+__device__ inline void sweep2_fetch(const Args& A, int row, int jg, size_t NN, RawRow2& r)
+{
+    const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
+    for (int k = 0; k < 3; ++k) r.u[k] = __ldg(reinterpret_cast<const double2*>(A.u_in + k * NN + idx));
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) r.d[k] = __ldg(reinterpret_cast<const float2*>(A.d1 + k * NN + idx));
+}
+
+template<int KIND>
+__device__ inline void sweep2_prim(const RawRow2& r, float2 p[3])
+{
+    float2 s = make_float2(d2f(r.u[0].x), d2f(r.u[0].y));
+    float2 m1 = make_float2(d2f(r.u[1].x), d2f(r.u[1].y));
+    float2 m2 = make_float2(d2f(r.u[2].x), d2f(r.u[2].y));
+    if (KIND == K_MIX2)
+    {
+        s = vadd(s, r.d[0]);
+        m1 = vadd(m1, r.d[1]);
+        m2 = vadd(m2, r.d[2]);
+    }
+    const float2 inv = vrcp(s);
+    p[0] = s;
+    p[1] = vmul(m1, inv);
+    p[2] = vmul(m2, inv);
+}
+
+// y slopes of both columns: the left neighbour of the first column is lane
+// l-1's second column, the right neighbour of the second is lane l+1's first.
+__device__ inline void slope_y2(const float2 p[3], float theta, float2 g[3])
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        const float l = __shfl_up_sync(0xffffffffu, p[k].y, 1);
+        const float r = __shfl_down_sync(0xffffffffu, p[k].x, 1);
+        g[k] = vplm(make_float2(l, p[k].x), p[k], make_float2(p[k].y, r), theta);
+    }
+}
+
+template<int KIND>
+__device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy)
+{
+    const int lane = threadIdx.x & 31;
+    const int N = A.N;
+    const int jcol = sy * SW2_COLS - 2 + 2 * lane;    // unwrapped first column of this lane's pair
+    const int jg = wrap1(jcol, N);                      // N even: the pair stays adjacent after the wrap
+    const bool interior = lane >= 1 && lane < 1 + SW2_COLS / 2 && jcol < N;
+    const size_t NN = size_t(N) * N;
+    const FloatConsts& F = A.f;
+    const float theta = F.theta;
+
+    float bf[6];
+    double dt;
+    if (A.clock)
+    {
+        dt = A.clock->dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.clock->binary[A.stage][k]);
+    }
+    else
+    {
+        dt = A.dt;
+        for (int k = 0; k < 6; ++k) bf[k] = d2f(A.bin[k]);
+    }
+    const float dtf = d2f(dt);
+    // cell centres of the pair, and the faces on the left of each column
+    const float2 yc = make_float2(fmaf(float(jcol) + 0.5f, F.dl, -F.R), fmaf(float(jcol + 1) + 0.5f, F.dl, -F.R));
+    const float2 yv = make_float2(fmaf(float(jcol), F.dl, -F.R), fmaf(float(jcol + 1), F.dl, -F.R));
+
+    float2 pm2[3], pm1[3], p0[3], p1[3];
+    RawRow2 raw;
+    sweep2_fetch<KIND>(A, i0 - 2, jg, NN, raw);
+    sweep2_prim<KIND>(raw, pm2);
+    sweep2_fetch<KIND>(A, i0 - 1, jg, NN, raw);
+    sweep2_prim<KIND>(raw, pm1);
+    sweep2_fetch<KIND>(A, i0, jg, NN, raw);
+    sweep2_prim<KIND>(raw, p0);
+    sweep2_fetch<KIND>(A, i0 + 1, jg, NN, raw);
+    sweep2_prim<KIND>(raw, p1);
+    sweep2_fetch<KIND>(A, i0 + 2, jg, NN, raw);
+    float2 gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        gxm1[k] = vplm(pm2[k], pm1[k], p0[k], theta);
+        gx0[k] = vplm(pm1[k], p0[k], p1[k], theta);
+    }
+    slope_y2(pm1, theta, gym1);
+    slope_y2(p0, theta, gy0);
+    face_flux_f<0, float2>(pm1, p0, gxm1, gx0, gym1, gy0, bc<float2>(fmaf(float(i0), F.dl, -F.R)), yc, F, fxm);
+
+    float local_max = 0.0f;
+    for (int i = i0; i < i1; ++i)
+    {
+        float2 p2[3], gx1[3], gy1[3], fxp[3];
+        sweep2_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
+        sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+        for (int k = 0; k < 3; ++k) gx1[k] = vplm(p0[k], p1[k], p2[k], theta);
+        slope_y2(p1, theta, gy1);
+        face_flux_f<0, float2>(p0, p1, gx0, gx1, gy0, gy1, bc<float2>(fmaf(float(i + 1), F.dl, -F.R)), yc, F, fxp);
+
+        // y faces on the left of both columns (row i): the first from lane l-1's second column
+        float2 pa[3], ga[3], ta[3], fy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            pa[k] = make_float2(__shfl_up_sync(0xffffffffu, p0[k].y, 1), p0[k].x);
+            ga[k] = make_float2(__shfl_up_sync(0xffffffffu, gy0[k].y, 1), gy0[k].x);
+            ta[k] = make_float2(__shfl_up_sync(0xffffffffu, gx0[k].y, 1), gx0[k].x);
+        }
+        const float xc = fmaf(float(i) + 0.5f, F.dl, -F.R);
+        face_flux_f<1, float2>(pa, p0, ga, gy0, ta, gx0, bc<float2>(xc), yv, F, fy);
+        float2 dfx[3], dfy[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            const float right = __shfl_down_sync(0xffffffffu, fy[k].x, 1);
+            dfy[k] = vsub(make_float2(fy[k].y, right), fy[k]);
+            dfx[k] = vsub(fxp[k], fxm[k]);
+        }
+        if (interior)
+            mixed_cell2<KIND>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
+
+        for (int k = 0; k < 3; ++k)
+        {
+            p0[k] = p1[k];
+            p1[k] = p2[k];
+            gx0[k] = gx1[k];
+            gy0[k] = gy1[k];
+            fxm[k] = fxp[k];
+        }
+    }
+    if (A.amax)
+    {
+        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
+    }
+}
+
+// ------------------------------------------------------------- clock
+struct ClockArgs
+{
+    double R, dl, cfl, softening_length, mass_ratio, eccentricity, omega;
+    int dt_mode, rk_order;
+    int end_step;     // 1: finish the step that just ran (advance time, iteration)
+    int begin_step;   // 1: choose dt and stage binaries of the next step
+};
+
+__device__ inline void store_binary(double* dst, const Binary& b)
+{
+    dst[0] = b.m1; dst[1] = b.x1; dst[2] = b.y1; dst[3] = b.m2; dst[4] = b.x2; dst[5] = b.y2;
+}
+
+// One clock update: finish the step that just ran (RK2 time average,
+// iteration count) and/or choose the next dt and the stage binaries.
+__device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a)
+{
+    if (a.end_step)
+    {
+        double t = c->time, dt = c->dt;
+        if (a.rk_order == 2)
+        {
+            double t2 = (t + dt) + dt;
+            c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
+        }
+        else
+        {
+            c->time = t + dt;
+        }
+        c->iteration += 1;
+    }
+    if (a.begin_step)
+    {
+        double t = c->time, dt;
+        if (a.dt_mode == MARA_DT_FORMULA)
+        {
+            // problems/minidisk.cpp:204-206
+            double vmax = sqrt(1.0 * 0.5 / a.softening_length);
+            double cfl = a.cfl * fmin(1.0, 0.01 + t / 0.05);
+            dt = a.dl / vmax * cfl;
+        }
+        else
+        {
+            dt = a.cfl * a.dl / c->max_wavespeed;   // scheme_mhd_v1.cpp:287 form
+        }
+        c->dt = dt;
+        store_binary(c->binary[0], binary_state(a.mass_ratio, a.eccentricity, a.omega, t));
+        store_binary(c->binary[1], binary_state(a.mass_ratio, a.eccentricity, a.omega, t + dt));
+        c->max_wavespeed = 0.0;
+    }
+}
+
+// ------------------------------------------------------------- host helpers (minidisk.cu)
+int check_params(const mara_minidisk_params* sd);
+Args base_args(const mara_minidisk_params* sd);
+ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, int end_step, int begin_step);
+int grid_stage(Args A, int kind, cudaStream_t s);
+int clock_init(const mara_minidisk_params* sd, const double* u, double time, mara_minidisk_clock* clock,
+               int precision, cudaStream_t s);
+
+} // namespace md
+} // namespace mara

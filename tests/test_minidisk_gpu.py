@@ -192,3 +192,33 @@ def test_mass_conservation_full_size(md):
         run = md.Run(sd, u0.clone(), rk_order=2, precision=precision, dt_mode=md.DT_CFL)
         run.advance(2)
         assert abs(run.u[0].sum().item() - m0) < 1e-11 * m0
+
+
+@pytest.mark.parametrize("block_size,depth", [(64, 0), (66, 0), (96, 1), (100, 1), (64, 2), (80, 2)])
+def test_sweep_column_forms_bit_identical(md, block_size, depth):
+    """The 1-column sweep and the 2-column sweep (a column pair per lane)
+    give bit-identical states and clocks: the mixed path
+    rounds every operation explicitly. Meshes whose cell size is not a power
+    of two (96, 200, 320) catch any rewritten product; N = 66 leaves a
+    6-column last strip. (Odd N puts a cell centre on the origin, where the
+    reference's initial state divides by r = 0, so it is not a minidisk mesh.)"""
+    from mara3p_gb300._capi import lib
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    u0 = md.initial_conserved(sd, seed=5, amplitude=0.01)
+    out = []
+    try:
+        for cols in (1, 2):
+            assert lib.mara_minidisk_sweep_columns(cols) in (0, 1, 2)
+            for rk in (1, 2):
+                run = md.Run(sd, u0.clone(), rk_order=rk, precision=md.MIXED, dt_mode=md.DT_CFL)
+                run.advance(6 if rk == 2 else 3)
+                torch.cuda.synchronize()
+                out.append((cols, rk, run.u.clone(), run.clock_state()))
+    finally:
+        lib.mara_minidisk_sweep_columns(0)
+    for (c1, rk1, u1, k1), (c2, rk2, u2, k2) in zip(out[:2], out[2:]):
+        assert rk1 == rk2 and c1 == 1 and c2 == 2
+        assert torch.isfinite(u1).all()
+        assert torch.equal(u1, u2), (block_size, depth, rk1, float((u1 - u2).abs().max()))
+        assert (k1.time, k1.dt, k1.max_wavespeed, k1.iteration) == (k2.time, k2.dt, k2.max_wavespeed, k2.iteration)
+    assert lib.mara_minidisk_sweep_columns(3) == -1
