@@ -271,9 +271,12 @@ int enqueue_stages(mara_minidisk_ensemble* e, int phase, bool tuning, cudaStream
             const int dyn = e->config.chunks_per_warp > 1;
             unsigned* c = e->counters + 2 * st;
             const int v = e->config.register_variant, cols = e->config.cols_per_lane;
-            int r = st == 1
-                ? launch_sweep_variant<K_MIX2>(cols, v, e->grid_blocks, s, t, e->items, e->first, int(e->nchunks), dyn, c)
-                : launch_sweep_variant<K_MIX1>(cols, v, e->grid_blocks, s, t, e->items, e->first, int(e->nchunks), dyn, c);
+            int r = st == 1 ? launch_sweep_variant<K_MIX2>(cols, v, e->grid_blocks, s, t, e->items, e->first,
+                                                           int(e->nchunks), dyn, c)
+                  : stages == 2 ? launch_sweep_variant<K_MIXD>(cols, v, e->grid_blocks, s, t, e->items, e->first,
+                                                               int(e->nchunks), dyn, c)
+                                : launch_sweep_variant<K_MIX1>(cols, v, e->grid_blocks, s, t, e->items, e->first,
+                                                               int(e->nchunks), dyn, c);
             if (r) return r;
         }
         else
@@ -537,8 +540,16 @@ int mara_minidisk_ensemble_create(const mara_minidisk_params* params, int32_t co
         for (int v = 0; v < kRegVariants; ++v)
         {
             int o1 = 1, o2 = 1;
-            if (int r = sweep_occupancy<K_MIX1>(cols, v, &o1)) return fail_out(r);
-            if (int r = sweep_occupancy<K_MIX2>(cols, v, &o2)) return fail_out(r);
+            if (rk_order == 2)
+            {
+                if (int r = sweep_occupancy<K_MIXD>(cols, v, &o1)) return fail_out(r);
+                if (int r = sweep_occupancy<K_MIX2>(cols, v, &o2)) return fail_out(r);
+            }
+            else
+            {
+                if (int r = sweep_occupancy<K_MIX1>(cols, v, &o1)) return fail_out(r);
+                o2 = o1;
+            }
             e->occupancy[cols - 1][v] = std::min(o1, o2);
         }
     for (int m = 0; m < count; ++m) e->even = e->even && e->sizes[m] % 2 == 0;
@@ -729,8 +740,12 @@ int mara_minidisk_ensemble_stage_times(mara_minidisk_ensemble* e, int32_t reps, 
             unsigned* c = e->counters + 2 * st;
             const int v = e->config.register_variant;
             const int cols = e->config.cols_per_lane;
-            r = st == 1 ? launch_sweep_variant<K_MIX2>(cols, v, e->grid_blocks, s, tab, e->items, e->first, int(e->nchunks), dyn, c)
-                        : launch_sweep_variant<K_MIX1>(cols, v, e->grid_blocks, s, tab, e->items, e->first, int(e->nchunks), dyn, c);
+            r = st == 1 ? launch_sweep_variant<K_MIX2>(cols, v, e->grid_blocks, s, tab, e->items, e->first,
+                                                       int(e->nchunks), dyn, c)
+              : e->rk_order == 2 ? launch_sweep_variant<K_MIXD>(cols, v, e->grid_blocks, s, tab, e->items, e->first,
+                                                                int(e->nchunks), dyn, c)
+                                 : launch_sweep_variant<K_MIX1>(cols, v, e->grid_blocks, s, tab, e->items, e->first,
+                                                                int(e->nchunks), dyn, c);
         }
         cudaEventRecord(ev.back(), s);
         if (r == MARA_OK)

@@ -292,7 +292,9 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
             const float p3[3] = {float(pc[0]), float(pc[1]), float(pc[2])};
             const float fx3[3] = {float(dfx[0]), float(dfx[1]), float(dfx[2])};
             const float fy3[3] = {float(dfy[0]), float(dfy[1]), float(dfy[2])};
-            mixed_cell<KIND>(A, float(S.xc[i]), float(S.yc[j]), p3, fx3, fy3, bf, dtf, idx, NN, local_max_f);
+            CellIn<float> cin;
+            load_cell_in<KIND>(A, idx, NN, cin);
+            mixed_cell<KIND>(A, float(S.xc[i]), float(S.yc[j]), p3, fx3, fy3, bf, dtf, idx, NN, cin, local_max_f);
         }
     }
 
@@ -570,7 +572,7 @@ int launch_stage(const Args& A, int tiles, cudaStream_t s)
 
 int grid_stage(Args A, int kind, cudaStream_t s)
 {
-    if (A.N >= 64 && kind == K_MIX1) return launch_sweep_auto<K_MIX1>(A, s);
+    if (A.N >= 64 && kind == K_MIX1) return A.d_out ? launch_sweep_auto<K_MIXD>(A, s) : launch_sweep_auto<K_MIX1>(A, s);
     if (A.N >= 64 && kind == K_MIX2) return launch_sweep_auto<K_MIX2>(A, s);
     int tiles_x = (A.N + TX - 1) / TX;
     A.tiles_y = (A.N + TY - 1) / TY;

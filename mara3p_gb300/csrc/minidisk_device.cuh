@@ -17,7 +17,11 @@ constexpr int GX = TX + 2, GY = TY + 2;     // slope region
 constexpr int NFX = (TX + 1) * TY;          // x faces
 constexpr int NFY = TX * (TY + 1);          // y faces
 
-enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3 };
+// Stage kinds: plain FP64; mixed stage writing an FP64 state from its input
+// (forward Euler, or the tiled kernel's stage 1 of RK2 when d_out is set);
+// mixed stage 2 of RK2; the per-block drop-in; mixed stage 1 of RK2 writing
+// only the FP32 increment (the sweeps' form of it, with no state operands).
+enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3, K_MIXD = 4 };
 
 // Single-precision constants of the mixed path, prepared on the host so that
 // no FP64 instruction (GB300 runs FP64 at 1/64 of the FP32 rate) is issued
@@ -343,13 +347,16 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
 // ------------------------------------------------------------- mixed cell update
 // Stage increment du = dt * L(u) of one cell (or a pair) in FP32: flux
 // divergence, gravity of both point masses, sinks, rotating-frame terms and
-// the outer buffer (problems/minidisk_scheme.cpp:337-352). pot returns
+// the outer buffer (problems/minidisk_scheme.cpp:337-352). uc returns the
+// FP32 conserved state the increment was computed from, pot returns
 // 1/sqrt(r^2 + rs^2), from which the cell-centre sound speed follows.
 template<typename T>
 __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc[3], const T dfx[3], const T dfy[3],
-                                      const float bf[6], float dtf, T du[3], T& pot)
+                                      const float bf[6], float dtf, T du[3], T uc[3], T& pot)
 {
-    const T uc[3] = {pc[0], vmul(pc[0], pc[1]), vmul(pc[0], pc[2])};
+    uc[0] = pc[0];
+    uc[1] = vmul(pc[0], pc[1]);
+    uc[2] = vmul(pc[0], pc[2]);
     const T dx1 = vsub(x, bc<T>(bf[1])), dy1 = vsub(y, bc<T>(bf[2]));
     const T dx2 = vsub(x, bc<T>(bf[4])), dy2 = vsub(y, bc<T>(bf[5]));
     const T q1 = vfma(dx1, dx1, vmul(dy1, dy1)), q2 = vfma(dx2, dx2, vmul(dy2, dy2));
@@ -382,75 +389,97 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
         du[k] = vmul(bc<T>(dtf), vfma(vadd(dfx[k], dfy[k]), bc<T>(-F.inv_dl), src[k]));
 }
 
-// Fastest wavespeed max(|vx|, |vy|) + cs of an FP64 state at a cell whose
-// 1/sqrt(r^2 + rs^2) is pot (iso2d::fastest_wavespeed, physics_iso2d.hpp:108-116).
-__device__ inline float cell_wavespeed(const FloatConsts& F, const double out[3], float pot)
+// Operands of one cell's (or one pair's) FP64 store, loaded ahead of the
+// flux work so that their latency hides behind it: the stage-input state and,
+// in stage 2 of RK2, the stage-1 increment.
+template<typename T> struct CellIn;
+template<> struct CellIn<float> { double u[3]; float d[3]; };
+template<> struct CellIn<float2> { double2 u[3]; float2 d[3]; };
+
+// Stage 1 of mixed RK2 stores only the FP32 increment; every other mixed
+// stage writes an FP64 state.
+template<int KIND>
+__device__ inline bool writes_state(const Args& A) { return KIND != K_MIXD && !(KIND == K_MIX1 && A.d_out); }
+
+template<int KIND>
+__device__ inline void load_cell_in(const Args& A, size_t idx, size_t NN, CellIn<float>& c)
 {
-    const float inv = rcp_fast(d2f(out[0]));
-    const float vx = vmul(d2f(out[1]), inv), vy = vmul(d2f(out[2]), inv);
+    if (!writes_state<KIND>(A)) return;
+    for (int k = 0; k < 3; ++k) c.u[k] = __ldg(A.u_in + k * NN + idx);
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) c.d[k] = __ldg(A.d1 + k * NN + idx);
+}
+
+template<int KIND>
+__device__ inline void load_cell_in(const Args& A, size_t idx, size_t NN, CellIn<float2>& c)
+{
+    if (!writes_state<KIND>(A)) return;
+    for (int k = 0; k < 3; ++k) c.u[k] = __ldg(reinterpret_cast<const double2*>(A.u_in + k * NN + idx));
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) c.d[k] = __ldg(reinterpret_cast<const float2*>(A.d1 + k * NN + idx));
+}
+
+// Fastest wavespeed max(|vx|, |vy|) + cs (iso2d::fastest_wavespeed,
+// physics_iso2d.hpp:108-116) of an FP32 conserved state at a cell whose
+// 1/sqrt(r^2 + rs^2) is pot.
+__device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, float m2, float pot)
+{
+    const float inv = rcp_fast(s);
+    const float vx = vmul(m1, inv), vy = vmul(m2, inv);
     const float cs = sqrt_fast(vmul(pot, F.inv_mach2));
     return vadd(fmaxf(fabsf(vx), fabsf(vy)), cs);
 }
 
-// Store one cell's stage result: the FP32 increment (stage 1 of mixed RK2),
-// or the FP64 state u_in + du (with the RK2 average of the two increments in
-// stage 2), and fold its wavespeed into local_max.
+// One cell's stage result: the FP32 increment (stage 1 of mixed RK2), or the
+// FP64 state u_in + du (with the RK2 average of the two increments in stage
+// 2). The CFL wavespeed of the new state is taken from its FP32 image: the
+// stage input plus du (RK1), or u0 + (d1 + du)/2 = u1 + (du - d1)/2 (RK2).
 template<int KIND>
-__device__ inline void store_cell(const Args& A, float du[3], float pot, size_t idx, size_t NN, float& local_max)
+__device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
+                                  const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
+                                  const CellIn<float>& in, float& local_max)
 {
-    if (KIND == K_MIX1 && A.d_out)
+    float du[3], uc[3], pot;
+    cell_increment<float>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot);
+    if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
         return;
     }
-    double out[3];
+    float of[3];
     for (int k = 0; k < 3; ++k)
     {
-        const float inc = KIND == K_MIX2 ? vmul(vadd(__ldg(A.d1 + k * NN + idx), du[k]), 0.5f) : du[k];
-        out[k] = __ldg(A.u_in + k * NN + idx) + f2d(inc);
-        A.u_out[k * NN + idx] = out[k];
+        const float inc = KIND == K_MIX2 ? vmul(vadd(in.d[k], du[k]), 0.5f) : du[k];
+        A.u_out[k * NN + idx] = in.u[k] + f2d(inc);
+        of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), 0.5f, uc[k]) : vadd(uc[k], du[k]);
     }
-    if (A.amax) local_max = fmaxf(local_max, cell_wavespeed(A.f, out, pot));
-}
-
-template<int KIND>
-__device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
-                                  const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                  float& local_max)
-{
-    float du[3], pot;
-    cell_increment<float>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, pot);
-    store_cell<KIND>(A, du, pot, idx, NN, local_max);
+    if (A.amax) local_max = fmaxf(local_max, wavespeed_f(A.f, of[0], of[1], of[2], pot));
 }
 
 // The pair form: columns idx and idx + 1 of one row (idx even).
 template<int KIND>
 __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const float2 pc[3], const float2 dfx[3],
                                    const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                   float& local_max)
+                                   const CellIn<float2>& in, float& local_max)
 {
-    float2 du[3], pot;
-    cell_increment<float2>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, pot);
-    if (KIND == K_MIX1 && A.d_out)
+    float2 du[3], uc[3], pot;
+    cell_increment<float2>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot);
+    if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(A.d_out + k * NN + idx) = du[k];
         return;
     }
-    double2 out[3];
+    float2 of[3];
     for (int k = 0; k < 3; ++k)
     {
-        float2 inc = du[k];
-        if (KIND == K_MIX2) inc = vmul(vadd(__ldg(reinterpret_cast<const float2*>(A.d1 + k * NN + idx)), du[k]),
-                                       bc<float2>(0.5f));
-        const double2 u = __ldg(reinterpret_cast<const double2*>(A.u_in + k * NN + idx));
-        out[k] = make_double2(u.x + f2d(inc.x), u.y + f2d(inc.y));
-        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = out[k];
+        const float2 inc = KIND == K_MIX2 ? vmul(vadd(in.d[k], du[k]), bc<float2>(0.5f)) : du[k];
+        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = make_double2(in.u[k].x + f2d(inc.x),
+                                                                           in.u[k].y + f2d(inc.y));
+        of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), bc<float2>(0.5f), uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax)
-    {
-        const double o0[3] = {out[0].x, out[1].x, out[2].x}, o1[3] = {out[0].y, out[1].y, out[2].y};
-        local_max = fmaxf(local_max, fmaxf(cell_wavespeed(A.f, o0, pot.x), cell_wavespeed(A.f, o1, pot.y)));
-    }
+        local_max = fmaxf(local_max, fmaxf(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, pot.x),
+                                           wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, pot.y)));
 }
 
 // ------------------------------------------------------------- warp-strip sweep (mixed path)
@@ -564,6 +593,8 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
         float p2[3], gx1[3], gy1[3], fxp[3];
         sweep_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
         sweep_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+        CellIn<float> cin;
+        if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
         for (int k = 0; k < 3; ++k) gx1[k] = plm(p0[k], p1[k], p2[k], theta);
         slope_y(p1, theta, gy1);
         face_flux<0>(p0, p1, gx0, gx1, gy0, gy1, fmaf(float(i + 1), F.dl, -F.R), yc, A, fxp);
@@ -585,7 +616,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
+            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -714,6 +745,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         float2 p2[3], gx1[3], gy1[3], fxp[3];
         sweep2_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
         sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+        CellIn<float2> cin;
+        if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
         for (int k = 0; k < 3; ++k) gx1[k] = vplm(p0[k], p1[k], p2[k], theta);
         slope_y2(p1, theta, gy1);
         face_flux_f<0, float2>(p0, p1, gx0, gx1, gy0, gy1, bc<float2>(fmaf(float(i + 1), F.dl, -F.R)), yc, F, fxp);
@@ -736,7 +769,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell2<KIND>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, local_max);
+            mixed_cell2<KIND>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max);
 
         for (int k = 0; k < 3; ++k)
         {
