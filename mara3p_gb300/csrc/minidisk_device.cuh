@@ -57,23 +57,24 @@ struct Args
     FloatConsts f;
 };
 
-// double -> float (round to nearest even) and float -> double (exact) with
-// integer instructions only, so that the mixed path issues no FP64-pipe work
-// for them. Magnitudes below the smallest normal float (1.2e-38) become signed
-// zero; overflow gives infinity; NaN stays NaN.
+// double -> float and float -> double (exact) with integer instructions
+// only, so that the mixed path issues no FP64-pipe work for them.
+// d2f rounds to nearest with ties away from zero. For a double of biased
+// exponent e = 896 + ef in the float range, bits 28..0 of the 64-bit pattern
+// shifted left by 3 are e[7:0] and the top 23 mantissa bits, and e[7:0] is
+// ef with bit 7 flipped; bit 28 of the low word is the first bit rounded off
+// (a carry out of the mantissa correctly bumps the exponent). Magnitudes below
+// the smallest normal float (1.2e-38) become signed zero; magnitudes of 2^128
+// and beyond, infinities and NaNs become NaN.
 __device__ inline float d2f(double x)
 {
     const unsigned long long b = __double_as_longlong(x);
     const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
-    const unsigned sign = hi & 0x80000000u;
-    const unsigned e = (hi >> 20) & 0x7FFu;
-    unsigned f = sign | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const unsigned rest = lo & 0x1FFFFFFFu;
-    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
-    const bool nan = e == 0x7FFu && ((hi & 0xFFFFFu) | lo) != 0u;
-    f = e < 897u ? sign : f;
-    f = e > 1150u ? (sign | (nan ? 0x7FC00000u : 0x7F800000u)) : f;
-    return __uint_as_float(f);
+    const unsigned sign = hi & 0x80000000u, mag = hi & 0x7FFFFFFFu;
+    unsigned f = ((__funnelshift_l(lo, hi, 3) & 0x7FFFFFFFu) ^ 0x40000000u) + ((lo >> 28) & 1u);
+    f = mag < 0x38100000u ? 0u : f;
+    f = mag >= 0x47F00000u ? 0x7FC00000u : f;
+    return __uint_as_float(f | sign);
 }
 
 __device__ inline double f2d(float x)
