@@ -79,6 +79,12 @@ def parse():
     ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch", default=None,
+                    help="ensemble launch shape blocks_per_sm,chunks_per_warp,cols_per_lane,register_variant "
+                         "(default: tuned)")
+    ap.add_argument("--no-looped", action="store_true", help="ensemble: skip the looped single-mesh comparison")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip)")
     return ap.parse_args()
 
 
@@ -303,7 +309,7 @@ def run_ours(args):
     step_bytes = (STAGE_BYTES[(pname, 1)] + STAGE_BYTES[(pname, 2)]) * cells
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic,
-                "kernel": f"sweep_kernel<{dominant}>" if prec == md.MIXED else f"stage_kernel<double, 0> (stage {dominant})",
+                "kernel": f"sweep_kernel (stage {dominant})" if prec == md.MIXED else f"stage_kernel<double, 0> (stage {dominant})",
                 "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "peak_source": f"{peak_kind} hbm_gbs",
                 "stage_ms": [s1, s2],
                 "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
@@ -343,6 +349,21 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(WORKLOADS[args.workload], args.cpu_sample_seconds)
 
+    # Mixed-precision error: both paths advanced from the same state with the
+    # same (formula) time steps, relative L1 per component after S steps.
+    accuracy = None
+    if prec == md.MIXED and args.accuracy_steps > 0:
+        runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_FORMULA) for p in (md.FP64, md.MIXED)}
+        for r in runs.values():
+            r.advance(args.accuracy_steps)
+        torch.cuda.synchronize()
+        a, b = runs[md.MIXED].u, runs[md.FP64].u
+        rel = [float((a[k] - b[k]).abs().sum() / b[k].abs().sum()) for k in range(3)]
+        accuracy = {"steps": args.accuracy_steps, "dt": "formula (identical in both paths)",
+                    "rel_l1_vs_fp64": {"density": rel[0], "momentum_x": rel[1], "momentum_y": rel[2]},
+                    "time": runs[md.MIXED].time}
+        del runs, a, b
+
     if rank == 0:
         line = {
             "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
@@ -355,7 +376,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "l2": f"no flush: FP64 state {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
-            "clocks": sampler.summary(),
+            "clocks": sampler.summary(), "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -401,12 +422,27 @@ def run_mhd(args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
             "kernel": "whole RK2 step (prim, 3 x face, update per stage)", "peak_source": f"{kind} hbm_gbs"}
     c = run.clock.read()
+    accuracy = None
+    if prec == mh.MIXED and args.accuracy_steps > 0:
+        k = min(args.accuracy_steps, 50)
+        out = {}
+        for p in (mh.FP64, mh.MIXED):
+            r = mh.Run(mh.initial_state(cfg, seed=1 + rank, modes=24), precision=p)
+            r.advance(k)
+            torch.cuda.synchronize()
+            out[p] = (r.state, r.clock.read()["time"], r.max_div_b())
+        (sf, tf, _), (sm, tm, dbm) = out[mh.FP64], out[mh.MIXED]
+        rel = {name: float((a - b).abs().sum() / b.abs().sum())
+               for name, a, b in (("density", sm.uc[0], sf.uc[0]), ("energy", sm.uc[4], sf.uc[4]),
+                                  ("bx_faces", sm.bf[0], sf.bf[0]))}
+        accuracy = {"steps": k, "rel_l1_vs_fp64": rel, "time_mixed": tm, "time_fp64": tf,
+                    "dt": "CFL in each path (times differ by the FP32 wavespeed)", "max_div_b_mixed": dbm}
     line = _line(args, world, value, "cell-updates/s", ms / args.steps,
                  "f32 compute, f64 state" if prec == mh.MIXED else "f64",
                  {"workload": "mhd-128", "cells": cells, "scheme": "PLM(1.5)+HLLE+CT, RK2, CFL 0.3",
                   "precision": args.precision, "l2": "state 126 MB + intermediates > L2, no flush"}, roof,
                  {"max_div_b": run.max_div_b(), "failures": c["failures"], "time": c["time"],
-                  "clocks": sampler.summary(), "gpu_launches": 13 * args.steps})
+                  "clocks": sampler.summary(), "gpu_launches": 13 * args.steps, "accuracy": accuracy})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -485,7 +521,11 @@ def run_ensemble(args):
     u0 = [md.initial_conserved(sd, seed=100 + m, amplitude=0.01) for m, sd in enumerate(members)]
     stream = torch.cuda.current_stream()
     t0 = time.perf_counter()
-    e = en.Ensemble(members, [u.clone() for u in u0], precision=md.MIXED, dt_mode=md.DT_CFL, autotune=1)
+    e = en.Ensemble(members, [u.clone() for u in u0], precision=md.MIXED, dt_mode=md.DT_CFL,
+                    autotune=0 if args.launch else 1)
+    if args.launch:
+        b, c, k, v = (int(x) for x in args.launch.split(","))
+        e.set_config(blocks_per_sm=b, chunks_per_warp=c, cols_per_lane=k, register_variant=v)
     tune_s = time.perf_counter() - t0
 
     def timed(fn, steps):
@@ -511,13 +551,17 @@ def run_ensemble(args):
     gpu_launches = 1 + 3 * args.steps + (args.steps % 2)   # clock begin, per step 2 sweeps + clock, copy-back
 
     # the same members advanced one at a time through the single-mesh call
-    runs = [md.Run(sd, u.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL) for sd, u in zip(members, u0)]
+    looped_line = None
+    if not args.no_looped:
+        runs = [md.Run(sd, u.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL) for sd, u in zip(members, u0)]
 
-    def looped(k):
-        for r in runs:
-            r.advance(k)
-    ms_loop = timed(looped, args.steps)
-    value_loop = cells * args.steps * world / (ms_loop * 1e-3)
+        def looped(k):
+            for r in runs:
+                r.advance(k)
+        ms_loop = timed(looped, args.steps)
+        looped_line = {"value": cells * args.steps * world / (ms_loop * 1e-3), "ms_per_step": ms_loop / args.steps,
+                       "gpu_launches": len(members) * (1 + 3 * args.steps)}
+        del runs
 
     s1, s2 = e.stage_times(5)
     peak, kind = measured_peaks()
@@ -526,8 +570,14 @@ def run_ensemble(args):
     dom_bytes = STAGE_BYTES[("mixed", dominant)] * cells
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     step_bytes = (STAGE_BYTES[("mixed", 1)] + STAGE_BYTES[("mixed", 2)]) * cells
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        tk = json.loads(tfile.read_text()).get(f"{args.workload}/mixed/stage{dominant}")
+        if tk is not None:
+            traffic = float(tk["bytes_per_cell"]) * cells
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": f"ensemble_sweep_kernel<{dominant}>", "kernel_ms": dom_ms,
+            "traffic": traffic, "kernel": f"ensemble_sweep_kernel (stage {dominant})", "kernel_ms": dom_ms,
             "algorithmic_bytes": dom_bytes, "peak_source": f"{kind} hbm_gbs", "stage_ms": [s1, s2],
             "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
 
@@ -567,8 +617,7 @@ def run_ensemble(args):
                   "scheme": "PLM(theta=1.5)+HLLE+viscosity+gravity/sink/buffer sources, RK2, CFL 0.3 per member",
                   "launch": e.config, "tune_seconds": tune_s, "parallelism": f"replicas x{world}",
                   "l2": f"no flush: FP64 states {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
-                 roof, {"looped_single_mesh": {"value": value_loop, "ms_per_step": ms_loop / args.steps,
-                                               "gpu_launches": len(members) * (1 + 3 * args.steps)},
+                 roof, {"looped_single_mesh": looped_line,
                         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
                         "clocks": sampler.summary()})
     e.close()
