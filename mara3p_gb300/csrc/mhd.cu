@@ -30,6 +30,7 @@
 #include <cstring>
 #include <vector>
 #include "common.cuh"
+#include "mixed_math.cuh"
 
 namespace mara {
 namespace mhd {
@@ -188,10 +189,45 @@ __global__ void prim_kernel(const Args A)
     R* P = static_cast<R*>(A.P);
     const R gm = R(A.gamma);
     double m = 0.0;
+    float mf = 0.0f;
     unsigned long long bad = 0;
     for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
     {
         const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        if constexpr (sizeof(R) == sizeof(float))
+        {
+            // Mixed: the recovery in FP32 from the FP64 state (integer conversions,
+            // one reciprocal); only the energy difference E - kinetic - magnetic
+            // is taken in FP64.
+            const float b[3] = {
+                0.5f * (d2f(A.bf[0][fidx(N, 0, i, j, k)]) + d2f(A.bf[0][fidx(N, 0, i + 1, j, k)])),
+                0.5f * (d2f(A.bf[1][fidx(N, 1, i, j, k)]) + d2f(A.bf[1][fidx(N, 1, i, j + 1, k)])),
+                0.5f * (d2f(A.bf[2][fidx(N, 2, i, j, k)]) + d2f(A.bf[2][fidx(N, 2, i, j, k + 1)]))};
+            const double energy = A.uc[4 * A.ucs + c * A.uzs];
+            Prim<float> p;
+            p.d = d2f(A.uc[c * A.uzs]);
+            const float S[3] = {d2f(A.uc[A.ucs + c * A.uzs]), d2f(A.uc[2 * A.ucs + c * A.uzs]),
+                                d2f(A.uc[3 * A.ucs + c * A.uzs])};
+            const float inv = rcp_fast(p.d);
+            for (int q = 0; q < 3; ++q)
+            {
+                p.v[q] = S[q] * inv;
+                p.b[q] = b[q];
+            }
+            const float kin_mag = 0.5f * sum3(S, p.v) + 0.5f * sum3(b, b);
+            p.p = d2f(energy - f2d(kin_mag)) * (gm - 1.0f);
+            if (p.d < 0.0f || p.p < 0.0f) ++bad;
+            P[0 * NN + c] = p.d;
+            P[1 * NN + c] = p.v[0];
+            P[2 * NN + c] = p.v[1];
+            P[3 * NN + c] = p.v[2];
+            P[4 * NN + c] = p.p;
+            P[5 * NN + c] = p.b[0];
+            P[6 * NN + c] = p.b[1];
+            P[7 * NN + c] = p.b[2];
+            mf = fmaxf(mf, fastest_speed(p, gm));
+            continue;
+        }
         const double b1 = 0.5 * (A.bf[0][fidx(N, 0, i, j, k)] + A.bf[0][fidx(N, 0, i + 1, j, k)]);
         const double b2 = 0.5 * (A.bf[1][fidx(N, 1, i, j, k)] + A.bf[1][fidx(N, 1, i, j + 1, k)]);
         const double b3 = 0.5 * (A.bf[2][fidx(N, 2, i, j, k)] + A.bf[2][fidx(N, 2, i, j, k + 1)]);
@@ -222,6 +258,7 @@ __global__ void prim_kernel(const Args A)
         P[7 * NN + c] = p.b[2];
         m = fmax(m, double(fastest_speed(p, gm)));
     }
+    if (sizeof(R) == sizeof(float)) m = double(mf);
     for (int o = 16; o > 0; o >>= 1)
     {
         m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -304,24 +341,62 @@ __device__ inline double ef(const Args& A, int axis, int comp, int i, int j, int
 template<typename R>
 __device__ inline double ee(const Args& A, int axis, int i, int j, int k)
 {
+    // explicit rounding: every face sharing the edge must see the same double
+    auto avg = [](double x, double y) { return __dmul_rn(0.5, __dadd_rn(x, y)); };
     double a, b;
     if (axis == 0)
     {
-        a = 0.5 * (ef<R>(A, 1, 0, i, j, k - 1) + ef<R>(A, 1, 0, i, j, k));
-        b = 0.5 * (ef<R>(A, 2, 0, i, j - 1, k) + ef<R>(A, 2, 0, i, j, k));
+        a = avg(ef<R>(A, 1, 0, i, j, k - 1), ef<R>(A, 1, 0, i, j, k));
+        b = avg(ef<R>(A, 2, 0, i, j - 1, k), ef<R>(A, 2, 0, i, j, k));
     }
     else if (axis == 1)
     {
-        a = 0.5 * (ef<R>(A, 2, 1, i - 1, j, k) + ef<R>(A, 2, 1, i, j, k));
-        b = 0.5 * (ef<R>(A, 0, 1, i, j, k - 1) + ef<R>(A, 0, 1, i, j, k));
+        a = avg(ef<R>(A, 2, 1, i - 1, j, k), ef<R>(A, 2, 1, i, j, k));
+        b = avg(ef<R>(A, 0, 1, i, j, k - 1), ef<R>(A, 0, 1, i, j, k));
     }
     else
     {
-        a = 0.5 * (ef<R>(A, 0, 2, i, j - 1, k) + ef<R>(A, 0, 2, i, j, k));
-        b = 0.5 * (ef<R>(A, 1, 2, i - 1, j, k) + ef<R>(A, 1, 2, i, j, k));
+        a = avg(ef<R>(A, 0, 2, i, j - 1, k), ef<R>(A, 0, 2, i, j, k));
+        b = avg(ef<R>(A, 1, 2, i - 1, j, k), ef<R>(A, 1, 2, i, j, k));
     }
-    return 0.5 * (a + b);
+    return avg(a, b);
 }
+
+// The mixed form of ee: the same averages in FP32, every operation rounded
+// explicitly (no contraction), so each edge EMF is one fixed function of the
+// four face values around it and every face that shares the edge sees the
+// same float; differences of floats are exact in FP64.
+__device__ inline float ee_f(const Args& A, int axis, int i, int j, int k)
+{
+    auto e = [&](int ax, int comp, int a, int b, int c) {
+        const int N = A.N;
+        if (ax != 0) a = wrap(a, N);
+        if (ax != 1) b = wrap(b, N);
+        if (ax != 2) c = wrap(c, N);
+        const int slot = comp < ax ? comp : comp - 1;
+        return static_cast<const float*>(A.E[ax])[slot * nb(N, ax) + fidx(N, ax, a, b, c)];
+    };
+    auto avg = [](float x, float y) { return __fmul_rn(0.5f, __fadd_rn(x, y)); };
+    float a, b;
+    if (axis == 0)
+    {
+        a = avg(e(1, 0, i, j, k - 1), e(1, 0, i, j, k));
+        b = avg(e(2, 0, i, j - 1, k), e(2, 0, i, j, k));
+    }
+    else if (axis == 1)
+    {
+        a = avg(e(2, 1, i - 1, j, k), e(2, 1, i, j, k));
+        b = avg(e(0, 1, i, j, k - 1), e(0, 1, i, j, k));
+    }
+    else
+    {
+        a = avg(e(0, 2, i, j - 1, k), e(0, 2, i, j, k));
+        b = avg(e(1, 2, i - 1, j, k), e(1, 2, i, j, k));
+    }
+    return avg(a, b);
+}
+
+__device__ inline double fdiff(float a, float b) { return f2d(a) - f2d(b); }
 
 template<typename R>
 __global__ void update_kernel(const Args A)
@@ -330,7 +405,8 @@ __global__ void update_kernel(const Args A)
     const int64_t NN = int64_t(N) * N * N;
     const double dt = A.clock->dt[A.stage];
     const double dl = A.dl;
-    const float dt_over_dl = float(dt / dl);
+    const double dt_over_dl_d = dt / dl;
+    const float dt_over_dl = float(dt_over_dl_d);
     const int64_t nf0 = nb(N, 0), nf1 = nb(N, 1), nf2 = nb(N, 2);
     const int64_t total = NN + nf0 + nf1 + nf2;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x)
@@ -361,9 +437,11 @@ __global__ void update_kernel(const Args A)
                     const float dc = (float(F0[q * nf0 + x1]) - float(F0[q * nf0 + x0]))
                                    + (float(F1[q * nf1 + y1]) - float(F1[q * nf1 + y0]))
                                    + (float(F2[q * nf2 + z1]) - float(F2[q * nf2 + z0]));
-                    out = u - double(dc * dt_over_dl);
+                    out = u - f2d(dc * dt_over_dl);
                 }
-                if (A.uavg) out = A.uavg[q * NN + c] * 0.5 + out * (1 - 0.5);
+                // weighted_sum a*0.5 + b*(1-0.5): halving is exact, so (a + b)*0.5 is the same double
+                if (A.uavg) out = sizeof(R) == sizeof(float) ? (A.uavg[q * NN + c] + out) * 0.5
+                                                             : A.uavg[q * NN + c] * 0.5 + out * (1 - 0.5);
                 A.uc_out[q * NN + c] = out;
             }
             continue;
@@ -374,6 +452,20 @@ __global__ void update_kernel(const Args A)
         const int n1 = N + (axis == 1), n2 = N + (axis == 2);
         const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
         // solenoidal_difference (mesh_cartesian_3d.hpp:265-274)
+        if constexpr (sizeof(R) == sizeof(float))
+        {
+            double cf;
+            if (axis == 0)
+                cf = fdiff(ee_f(A, 2, i, j + 1, k), ee_f(A, 2, i, j, k)) - fdiff(ee_f(A, 1, i, j, k + 1), ee_f(A, 1, i, j, k));
+            else if (axis == 1)
+                cf = fdiff(ee_f(A, 0, i, j, k + 1), ee_f(A, 0, i, j, k)) - fdiff(ee_f(A, 2, i + 1, j, k), ee_f(A, 2, i, j, k));
+            else
+                cf = fdiff(ee_f(A, 1, i + 1, j, k), ee_f(A, 1, i, j, k)) - fdiff(ee_f(A, 0, i, j + 1, k), ee_f(A, 0, i, j, k));
+            double out = fma(-cf, dt_over_dl_d, A.bf[axis][f]);
+            if (A.bavg[axis]) out = (A.bavg[axis][f] + out) * 0.5;
+            A.bf_out[axis][f] = out;
+            continue;
+        }
         double cf;
         if (axis == 0)
             cf = (ee<R>(A, 2, i, j + 1, k) - ee<R>(A, 2, i, j, k)) - (ee<R>(A, 1, i, j, k + 1) - ee<R>(A, 1, i, j, k));

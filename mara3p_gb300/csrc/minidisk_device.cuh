@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "common.cuh"
+#include "mixed_math.cuh"
 
 namespace mara {
 namespace md {
@@ -56,69 +57,6 @@ struct Args
     unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
     FloatConsts f;
 };
-
-// double -> float and float -> double (exact) with integer instructions
-// only, so that the mixed path issues no FP64-pipe work for them.
-// d2f rounds to nearest with ties away from zero. For a double of biased
-// exponent e = 896 + ef in the float range, bits 28..0 of the 64-bit pattern
-// shifted left by 3 are e[7:0] and the top 23 mantissa bits, and e[7:0] is
-// ef with bit 7 flipped; bit 28 of the low word is the first bit rounded off
-// (a carry out of the mantissa correctly bumps the exponent). Magnitudes below
-// the smallest normal float (1.2e-38) become signed zero; magnitudes of 2^128
-// and beyond, infinities and NaNs become NaN.
-__device__ inline float d2f(double x)
-{
-    const unsigned long long b = __double_as_longlong(x);
-    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
-    const unsigned sign = hi & 0x80000000u, mag = hi & 0x7FFFFFFFu;
-    unsigned f = ((__funnelshift_l(lo, hi, 3) & 0x7FFFFFFFu) ^ 0x40000000u) + ((lo >> 28) & 1u);
-    f = mag < 0x38100000u ? 0u : f;
-    f = mag >= 0x47F00000u ? 0x7FC00000u : f;
-    return __uint_as_float(f | sign);
-}
-
-__device__ inline double f2d(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xFFu;
-    const unsigned m = b & 0x7FFFFFu;
-    const unsigned ee = e == 255u ? 2047u : e + 896u;
-    unsigned hi = (b & 0x80000000u) | (ee << 20) | (m >> 3);
-    unsigned lo = m << 29;
-    hi = e == 0u ? (b & 0x80000000u) : hi;
-    lo = e == 0u ? 0u : lo;
-    return __hiloint2double(int(hi), int(lo));
-}
-
-// Single-MUFU approximations for the mixed path (relative error ~1e-7,
-// well inside the FP32 budget of the fluxes; denormals flush to zero).
-__device__ inline float rcp_fast(float x)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float sqrt_fast(float x)
-{
-    float y;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float rsqrt_fast(float x)
-{
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ inline float exp_fast(float x)
-{
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
-    return y;
-}
 
 // ------------------------------------------------------------- geometry
 // vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
