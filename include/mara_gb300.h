@@ -373,7 +373,8 @@ int mara_srhd_mlp_infer(const void* weights, const float* features, int64_t n, f
  * control::advance_runge_kutta and zero-gradient boundaries. State u: SoA
  * [4][N][N] (D, S1, S2, tau), device. clock: mara_srhd_tube_clock_bytes()
  * bytes of device memory (time, dt, fastest speed, iteration, failed
- * recoveries, total FP64 Newton iterations). */
+ * recoveries, total FP64 Newton iterations, HLLC faces whose contact speed
+ * was rejected). */
 int64_t mara_srhd_tube_clock_bytes(void);
 int64_t mara_srhd_tube_workspace_bytes(int32_t N);
 /* Two states split by the line (x - 1/2) cos(angle) + (y - 1/2) sin(angle) = 0,
@@ -383,10 +384,22 @@ int mara_srhd_tube_initial(int32_t N, double angle, double rho_l, double p_l, do
 /* `steps` RK2 steps; dt = cfl / N / max outer wavespeed of each step's
  * initial state. guess: 0 = p = 0 (the reference's recovery, bit-identical),
  * 1 = the learned guess (mlp_weights), 2 = the previous stage's pressure;
- * refine32 FP32 Newton steps sharpen a guess before the FP64 polish. */
+ * refine32 FP32 Newton steps sharpen a guess before the FP64 polish.
+ * riemann_solver: 0 = HLLE, 1 = HLLC (a face whose HLLC contact speed the
+ * reference would reject gets the HLLE flux and is counted in the clock). */
 int mara_srhd_tube_advance(int32_t N, double* u, void* clock, int32_t steps, double cfl, double plm_theta,
                            double gamma_law_index, double temperature_floor, int32_t precision, int32_t guess,
-                           const void* mlp_weights, int32_t refine32, void* workspace, void* stream);
+                           const void* mlp_weights, int32_t refine32, int32_t riemann_solver, void* workspace,
+                           void* stream);
+
+/* srhd::riemann_solver at fixed faces (src/physics_srhd.hpp:377-487), FP64,
+ * the drop-in for its HLLE (solver 0) and HLLC (solver 1) modes: n faces,
+ * left/right primitives pl, pr AoS (rho, u1, u2, u3, p) per face, axis 1..3,
+ * fluxes f AoS 5 per face; status[i] (nullable) = 1 where the reference
+ * throws (HLLC contact speed NaN or beyond 1e3; f holds the HLLE flux
+ * there). Device buffers. */
+int mara_srhd_riemann(const double* pl, const double* pr, int64_t n, int32_t axis, double gamma_law_index,
+                      int32_t solver, double* f, int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -148,7 +148,9 @@ SIGNATURES.update({
     "mara_srhd_tube_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32]),
     "mara_srhd_tube_initial": (ctypes.c_int, [ctypes.c_int32] + [ctypes.c_double] * 6 + [_vp, _vp, _vp]),
     "mara_srhd_tube_advance": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, ctypes.c_int32] + [ctypes.c_double] * 4 +
-                               [ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp]),
+                               [ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp]),
+    "mara_srhd_riemann": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+                                         _vp, _vp, _vp]),
 })
 
 

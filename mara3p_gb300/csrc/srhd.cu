@@ -164,6 +164,31 @@ __global__ void seeded_zones_kernel(uint64_t seed, int64_t n, double rho_lo, dou
 
 using namespace mara;
 
+namespace mara {
+namespace srhd {
+
+// One fixed face per thread: the reference's riemann_solver in HLLE or HLLC mode.
+__global__ void riemann_kernel(const double* pl, const double* pr, int64_t n, int axis, double gm, int solver,
+                               double* f, int32_t* status)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        const double* a = pl + 5 * i;
+        const double* b = pr + 5 * i;
+        const SPrim<double> L{a[0], {a[1], a[2], a[3]}, a[4]};
+        const SPrim<double> R{b[0], {b[1], b[2], b[3]}, b[4]};
+        double F[5];
+        int bad = 0;
+        if (solver == 1) bad = hllc(L, R, axis, gm, F);
+        else hlle(L, R, axis, gm, F);
+        for (int k = 0; k < 5; ++k) f[5 * i + k] = F[k];
+        if (status) status[i] = bad;
+    }
+}
+
+} // namespace srhd
+} // namespace mara
+
 extern "C" {
 
 int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component_stride, int64_t zone_stride,
@@ -221,6 +246,20 @@ int mara_srhd_seeded_zones(uint64_t seed, int64_t n, double rho_lo, double rho_h
     srhd::seeded_zones_kernel<<<blocks, 256, 0, as_stream(stream)>>>(seed, n, rho_lo, rho_hi, p_lo, p_hi, w_hi,
                                                                      gamma_law_index, prim, cons);
     return launch_status("seeded_zones_kernel");
+}
+
+int mara_srhd_riemann(const double* pl, const double* pr, int64_t n, int32_t axis, double gamma_law_index,
+                      int32_t solver, double* f, int32_t* status, void* stream)
+{
+    MARA_REQUIRE(n >= 0, "mara_srhd_riemann: negative count");
+    MARA_REQUIRE(axis >= 1 && axis <= 3, "mara_srhd_riemann: axis must be 1, 2 or 3");
+    MARA_REQUIRE(solver == 0 || solver == 1, "mara_srhd_riemann: solver must be 0 (HLLE) or 1 (HLLC)");
+    if (n == 0) return MARA_OK;
+    MARA_REQUIRE(pl && pr && f, "mara_srhd_riemann: null buffer");
+    int blocks = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
+    srhd::riemann_kernel<<<blocks, 256, 0, as_stream(stream)>>>(pl, pr, n, axis - 1, gamma_law_index, solver, f,
+                                                                status);
+    return launch_status("riemann_kernel");
 }
 
 } // extern "C"

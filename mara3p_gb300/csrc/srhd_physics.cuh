@@ -110,43 +110,91 @@ __device__ inline void conserved_density(const double p[5], double gm, double u[
 template<typename R>
 struct SPrim { R rho, u[3], p; };
 
-template<typename R>
-__device__ inline R gamma_beta_squared(const SPrim<R>& p) { return p.u[0] * p.u[0] + p.u[1] * p.u[1] + p.u[2] * p.u[2]; }
+// Explicitly rounded arithmetic, no contraction: in FP64 the fluxes below
+// equal the reference's (compiled without FMA contraction) bit for bit; in
+// FP32 they are the mixed path's.
+__device__ inline double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ inline double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ inline double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ inline double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ inline double rsqrt_rn(double a) { return __dsqrt_rn(a); }
+__device__ inline float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ inline float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ inline float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ inline float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ inline float rsqrt_rn(float a) { return __fsqrt_rn(a); }
 
+// 0 + u1^2 + u2^2 + u3^2 (physics_srhd.hpp gamma_beta_squared)
+template<typename R>
+__device__ inline R gamma_beta_squared(const SPrim<R>& p)
+{
+    return radd(radd(radd(R(0), rmul(p.u[0], p.u[0])), rmul(p.u[1], p.u[1])), rmul(p.u[2], p.u[2]));
+}
+
+template<typename R>
+__device__ inline R lorentz_factor(const SPrim<R>& p) { return rsqrt_rn(radd(R(1), gamma_beta_squared(p))); }
+
+// rho c^2 + p (1 + 1/(gamma - 1))
+template<typename R>
+__device__ inline R enthalpy_density(const SPrim<R>& p, R gm)
+{
+    return radd(rmul(p.rho, R(1)), rmul(p.p, radd(R(1), rdiv(R(1), rsub(gm, R(1))))));
+}
+
+// conserved_density (physics_srhd.hpp:291-304)
 template<typename R>
 __device__ inline void cons_of(const SPrim<R>& p, R gm, R u[5])
 {
-    const R W = sqrt(R(1) + gamma_beta_squared(p));
-    const R D = p.rho * W;
-    const R h = (p.rho * R(1) + p.p * (R(1) + R(1) / (gm - R(1)))) / p.rho;
+    const R W = lorentz_factor(p);
+    const R D = rmul(p.rho, W);
+    const R h = rdiv(enthalpy_density(p, gm), p.rho);
     u[0] = D;
-    for (int k = 0; k < 3; ++k) u[1 + k] = D * h * p.u[k] / R(1);
-    u[4] = D * (h * W - R(1) * R(1)) - p.p;
+    for (int k = 0; k < 3; ++k) u[1 + k] = rdiv(rmul(rmul(D, h), p.u[k]), R(1));
+    u[4] = rsub(rmul(D, rsub(rmul(h, W), rmul(R(1), R(1)))), p.p);
 }
 
-// normal three-velocity along axis (0, 1, 2)
+// normal three-velocity 0 + n.v along axis (0, 1, 2); the terms of the other
+// two axes are exact zeros for finite velocities and are left out
 template<typename R>
 __device__ inline R normal_velocity(const SPrim<R>& p, int axis)
 {
-    const R W = sqrt(R(1) + gamma_beta_squared(p));
-    return R(1) * p.u[axis] / W;
+    return radd(R(0), rdiv(rmul(R(1), p.u[axis]), lorentz_factor(p)));
 }
 
+// flux (physics_srhd.hpp:310-324)
+template<typename R>
+__device__ inline void flux_of(const SPrim<R>& p, const R u[5], int axis, R f[5])
+{
+    const R vn = normal_velocity(p, axis);
+    const R pt[5] = {rmul(R(0), R(0)), rmul(p.p, R(axis == 0)), rmul(p.p, R(axis == 1)), rmul(p.p, R(axis == 2)),
+                     rmul(p.p, vn)};
+    for (int k = 0; k < 5; ++k) f[k] = radd(rmul(vn, u[k]), pt[k]);
+}
+
+// outer_wavespeeds (physics_srhd.hpp:182-195)
 template<typename R>
 __device__ inline void outer_speeds(const SPrim<R>& p, int axis, R gm, R& am, R& ap)
 {
-    const R H = p.rho * R(1) + p.p * (R(1) + R(1) / (gm - R(1)));
-    const R a2 = gm * R(1) * p.p / H / R(1);
+    const R a2 = rdiv(rdiv(rmul(rmul(gm, R(1)), p.p), enthalpy_density(p, gm)), R(1));
     const R uu = gamma_beta_squared(p);
     const R vn = normal_velocity(p, axis);
-    const R bn = vn / R(1);
-    const R bb = uu / (R(1) + uu);
-    const R b2 = bn * bn;
-    R disc = a2 * (R(1) - bb) * (R(1) - bb * a2 - b2 * (R(1) - a2));
+    const R bn = rdiv(vn, R(1));
+    const R bb = rdiv(uu, radd(R(1), uu));
+    const R b2 = rmul(bn, bn);
+    R disc = rmul(rmul(a2, rsub(R(1), bb)), rsub(rsub(R(1), rmul(bb, a2)), rmul(b2, rsub(R(1), a2))));
     if (sizeof(R) == sizeof(float)) disc = fmax(disc, R(0));   // FP32 rounding can dip below zero
-    const R k0 = sqrt(disc) * R(1);
-    am = (vn * (R(1) - a2) - k0) / (R(1) - bb * a2);
-    ap = (vn * (R(1) - a2) + k0) / (R(1) - bb * a2);
+    const R k0 = rmul(rsqrt_rn(disc), R(1));
+    const R den = rsub(R(1), rmul(bb, a2));
+    const R vna = rmul(vn, rsub(R(1), a2));
+    am = rdiv(rsub(vna, k0), den);
+    ap = rdiv(radd(vna, k0), den);
+}
+
+// (ar fl - al fr - (ul - ur) ar al) / (ar - al)
+template<typename R>
+__device__ inline R hll_average(R fl, R fr, R ul, R ur, R al, R ar)
+{
+    return rdiv(rsub(rsub(rmul(ar, fl), rmul(al, fr)), rmul(rmul(rsub(ul, ur), ar), al)), rsub(ar, al));
 }
 
 // riemann_hlle (fixed face, physics_srhd.hpp:395-400, 489-497) along axis
@@ -156,14 +204,8 @@ __device__ inline void hlle(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R 
     R ul[5], ur[5], fl[5], fr[5];
     cons_of(pl, gm, ul);
     cons_of(pr, gm, ur);
-    const R vl = normal_velocity(pl, axis), vr = normal_velocity(pr, axis);
-    for (int k = 0; k < 5; ++k)
-    {
-        const R ptl = k == 0 ? R(0) * R(0) : (k == 4 ? pl.p * vl : (k - 1 == axis ? pl.p : R(0)));
-        const R ptr = k == 0 ? R(0) * R(0) : (k == 4 ? pr.p * vr : (k - 1 == axis ? pr.p : R(0)));
-        fl[k] = vl * ul[k] + ptl;
-        fr[k] = vr * ur[k] + ptr;
-    }
+    flux_of(pl, ul, axis, fl);
+    flux_of(pr, ur, axis, fr);
     R alm, alp, arm, arp;
     outer_speeds(pl, axis, gm, alm, alp);
     outer_speeds(pr, axis, gm, arm, arp);
@@ -171,7 +213,75 @@ __device__ inline void hlle(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R 
     const R al = fmin(alm, arm);
     if (R(0) < al) { for (int k = 0; k < 5; ++k) F[k] = fl[k]; return; }
     if (R(0) > ar) { for (int k = 0; k < 5; ++k) F[k] = fr[k]; return; }
-    for (int k = 0; k < 5; ++k) F[k] = (ar * fl[k] - al * fr[k] - (ul[k] - ur[k]) * ar * al) / (ar - al);
+    for (int k = 0; k < 5; ++k) F[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
+}
+
+// riemann_hllc (fixed face, physics_srhd.hpp:401-487; Mignone & Bodo 2005)
+// along axis. Returns 1 where the reference throws (contact speed NaN or
+// beyond 1e3); F then holds the HLLE flux.
+template<typename R>
+__device__ inline int hllc(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R gm, R F[5])
+{
+    R ul[5], ur[5], fl[5], fr[5];
+    cons_of(pl, gm, ul);
+    cons_of(pr, gm, ur);
+    flux_of(pl, ul, axis, fl);
+    flux_of(pr, ur, axis, fr);
+    R alm, alp, arm, arp;
+    outer_speeds(pl, axis, gm, alm, alp);
+    outer_speeds(pr, axis, gm, arm, arp);
+    const R ar = fmax(alp, arp);
+    const R al = fmin(alm, arm);
+    R u_hll[5], f_hll[5];
+    for (int k = 0; k < 5; ++k)
+    {
+        u_hll[k] = rdiv(radd(rsub(rmul(ar, ur[k]), rmul(al, ul[k])), rsub(fl[k], fr[k])), rsub(ar, al));
+        f_hll[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
+    }
+    const R c2 = rmul(R(1), R(1));
+    const R n[3] = {R(axis == 0), R(axis == 1), R(axis == 2)};
+    const R ue_hll = radd(u_hll[4], rmul(u_hll[0], c2));
+    const R fe_hll = radd(f_hll[4], rmul(f_hll[0], c2));
+    const R um_hll = radd(radd(radd(R(0), rmul(u_hll[1], n[0])), rmul(u_hll[2], n[1])), rmul(u_hll[3], n[2]));
+    const R fm_hll = radd(radd(radd(R(0), rmul(f_hll[1], n[0])), rmul(f_hll[2], n[1])), rmul(f_hll[3], n[2]));
+    const R a = fe_hll;
+    const R b = rsub(-fm_hll, ue_hll);
+    const R c = um_hll;
+    const R d = rsub(rmul(b, b), rmul(rmul(R(4), a), c));
+    const R as = d < R(0) ? R(0)
+               : rmul(fabs(a) > R(1e-8) ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(R(2), a)) : rdiv(-c, b), c2);
+    if (isnan(as) || as < R(-1e3) || as > R(1e3))
+    {
+        for (int k = 0; k < 5; ++k) F[k] = f_hll[k];
+        if (R(0) < al) for (int k = 0; k < 5; ++k) F[k] = fl[k];
+        if (R(0) > ar) for (int k = 0; k < 5; ++k) F[k] = fr[k];
+        return 1;
+    }
+    const R ps = radd(rdiv(rmul(-fe_hll, as), c2), fm_hll);
+    auto star = [&](const R u[5], const R f[5], const SPrim<R>& p, R s) {
+        const R v = normal_velocity(p, axis);
+        const R e = radd(u[4], rmul(u[0], c2));
+        const R m = radd(radd(radd(R(0), rmul(u[1], n[0])), rmul(u[2], n[1])), rmul(u[3], n[2]));
+        const R sv = rsub(s, v), sa = rsub(s, as);
+        const R es = rdiv(rsub(radd(rmul(e, sv), rmul(ps, as)), rmul(p.p, v)), sa);
+        const R ms = rdiv(rsub(radd(rmul(m, sv), ps), p.p), sa);
+        const R Ds = rdiv(rmul(u[0], sv), sa);
+        R us[5];
+        us[0] = Ds;
+        for (int k = 0; k < 3; ++k)
+        {
+            const R nk = rsub(u[1 + k], rmul(m, n[k]));
+            const R ns = rdiv(rmul(nk, sv), sa);
+            us[1 + k] = radd(rmul(ms, n[k]), ns);
+        }
+        us[4] = rsub(es, rmul(Ds, c2));
+        for (int k = 0; k < 5; ++k) F[k] = rsub(radd(f[k], rmul(s, rsub(us[k], u[k]))), rmul(R(0), us[k]));
+    };
+    if (R(0) <= al) { for (int k = 0; k < 5; ++k) F[k] = fl[k]; return 0; }
+    if (R(0) >= ar) { for (int k = 0; k < 5; ++k) F[k] = fr[k]; return 0; }
+    if (R(0) <= as) star(ul, fl, pl, al);
+    else star(ur, fr, pr, ar);
+    return 0;
 }
 
 } // namespace srhd

@@ -38,6 +38,7 @@ struct Clock
     int64_t iteration;
     unsigned long long failures;  // zones whose recovery failed
     unsigned long long newton;    // FP64 Newton iterations summed over all recoveries
+    unsigned long long riemann;   // HLLC faces whose contact speed was rejected (HLLE flux used there)
 };
 
 enum Guess { GUESS_ZERO = 0, GUESS_MLP = 1, GUESS_PREVIOUS = 2 };
@@ -178,7 +179,7 @@ struct Flux
     const double* u_in;
     const double* u_avg;
     double* u_out;
-    const Clock* clock;
+    Clock* clock;
     int tiles_y;
 };
 
@@ -206,7 +207,8 @@ __device__ inline float plm(float yl, float y0, float yr, float theta)
     return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
 }
 
-template<typename R>
+// SOLVER: 0 HLLE, 1 HLLC (riemann_solver, physics_srhd.hpp:377-487)
+template<typename R, int SOLVER>
 __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
 {
     extern __shared__ __align__(16) unsigned char raw[];
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
     __syncthreads();
 
     // faces: x face (fi, j) between tile cells (fi-1, j) and (fi, j) -> halo (fi+1, j+2), (fi+2, j+2)
+    unsigned rejected = 0;
     for (int e = tid; e < (TX + 1) * TY + TX * (TY + 1); e += NT)
     {
         const bool xf = e < (TX + 1) * TY;
@@ -256,7 +259,8 @@ __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
         L = SPrim<R>{l[0], {l[1], l[2], l[3]}, l[4]};
         Rr = SPrim<R>{r[0], {r[1], r[2], r[3]}, r[4]};
         R F[5];
-        srhd::hlle(L, Rr, xf ? 0 : 1, gm, F);
+        if (SOLVER == 1) rejected += srhd::hllc(L, Rr, xf ? 0 : 1, gm, F);
+        else srhd::hlle(L, Rr, xf ? 0 : 1, gm, F);
         const int comp[4] = {0, 1, 2, 4};
         if (xf)
         {
@@ -269,6 +273,11 @@ __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
             const int i = q0 / (TY + 1), fj = q0 - (q0 / (TY + 1)) * (TY + 1);
             for (int q = 0; q < 4; ++q) S.fy[q][i][fj] = F[comp[q]];
         }
+    }
+    if (SOLVER == 1)
+    {
+        for (int o = 16; o > 0; o >>= 1) rejected += __shfl_xor_sync(0xffffffffu, rejected, o);
+        if ((tid & 31) == 0 && rejected) atomicAdd(&A.clock->riemann, (unsigned long long)rejected);
     }
     __syncthreads();
 
@@ -300,20 +309,27 @@ __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
     }
 }
 
-template<typename R>
+template<typename R, int SOLVER>
 int launch_flux(const Flux& F, cudaStream_t s)
 {
     static std::once_flag flags[64];
     int dev = 0;
     cudaGetDevice(&dev);
     std::call_once(flags[dev & 63], [] {
-        cudaFuncSetAttribute(tube_flux_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(TileSmem<R>)));
+        cudaFuncSetAttribute(tube_flux_kernel<R, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(sizeof(TileSmem<R>)));
     });
     Flux A = F;
     A.tiles_y = (A.N + TY - 1) / TY;
     const int tiles = ((A.N + TX - 1) / TX) * A.tiles_y;
-    tube_flux_kernel<R><<<tiles, NT, sizeof(TileSmem<R>), s>>>(A);
+    tube_flux_kernel<R, SOLVER><<<tiles, NT, sizeof(TileSmem<R>), s>>>(A);
     return launch_status("tube_flux_kernel");
+}
+
+int launch_flux(const Flux& F, int precision, int solver, cudaStream_t s)
+{
+    if (precision == MARA_MIXED) return solver ? launch_flux<float, 1>(F, s) : launch_flux<float, 0>(F, s);
+    return solver ? launch_flux<double, 1>(F, s) : launch_flux<double, 0>(F, s);
 }
 
 inline int blocks_for(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16)); }
@@ -372,9 +388,11 @@ int mara_srhd_tube_initial(int32_t N, double angle, double rho_l, double p_l, do
 
 int mara_srhd_tube_advance(int32_t N, double* u, void* clock, int32_t steps, double cfl, double plm_theta,
                            double gamma_law_index, double temperature_floor, int32_t precision, int32_t guess,
-                           const void* mlp_weights, int32_t refine32, void* workspace, void* stream)
+                           const void* mlp_weights, int32_t refine32, int32_t riemann_solver, void* workspace,
+                           void* stream)
 {
     MARA_REQUIRE(N >= 4 && u && clock && workspace, "mara_srhd_tube_advance: bad argument");
+    MARA_REQUIRE(riemann_solver == 0 || riemann_solver == 1, "mara_srhd_tube_advance: riemann_solver must be 0 or 1");
     MARA_REQUIRE(precision == MARA_FP64 || precision == MARA_MIXED, "mara_srhd_tube_advance: bad precision");
     MARA_REQUIRE(guess >= GUESS_ZERO && guess <= GUESS_PREVIOUS, "mara_srhd_tube_advance: bad guess kind");
     MARA_REQUIRE(guess != GUESS_MLP || mlp_weights, "mara_srhd_tube_advance: the learned guess needs weights");
@@ -425,10 +443,10 @@ int mara_srhd_tube_advance(int32_t N, double* u, void* clock, int32_t steps, dou
         dt_kernel<<<1, 32, 0, s>>>(c, cfl, dl, 0);
         if (int r = launch_status("tube dt_kernel")) return r;
         f.u_in = u; f.u_avg = nullptr; f.u_out = u1;
-        if (int r = precision == MARA_MIXED ? launch_flux<float>(f, s) : launch_flux<double>(f, s)) return r;
+        if (int r = launch_flux(f, precision, riemann_solver, s)) return r;
         if (int r = c2p(u1, 0)) return r;
         f.u_in = u1; f.u_avg = u; f.u_out = u;
-        if (int r = precision == MARA_MIXED ? launch_flux<float>(f, s) : launch_flux<double>(f, s)) return r;
+        if (int r = launch_flux(f, precision, riemann_solver, s)) return r;
         clock_end_kernel<<<1, 32, 0, s>>>(c);
         if (int r = launch_status("tube clock_end_kernel")) return r;
     }

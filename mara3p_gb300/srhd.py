@@ -120,14 +120,30 @@ class ShockTube:
                                          self.u.data_ptr(), self.clock.data_ptr(), _stream()), "tube initial")
 
     def advance(self, steps: int, precision: int = 0, guess: int = GUESS_ZERO, mlp: "PressureGuess | None" = None,
-                refine32: int = 0) -> None:
+                refine32: int = 0, riemann: str = "hlle") -> None:
+        """`steps` RK2 steps; riemann is "hlle" or "hllc" (riemann_solver, physics_srhd.hpp:377-487)."""
+        solver = {"hlle": 0, "hllc": 1}[riemann]
         check(lib.mara_srhd_tube_advance(self.N, self.u.data_ptr(), self.clock.data_ptr(), steps, self.cfl, self.theta,
                                          self.gamma, self.floor, precision, guess, mlp.weights.data_ptr() if mlp else None,
-                                         refine32, self.workspace.data_ptr(), _stream()), "tube advance")
+                                         refine32, solver, self.workspace.data_ptr(), _stream()), "tube advance")
 
     def clock_state(self) -> dict:
         raw = self.clock.cpu().numpy()
         d = raw.view("float64")
         q = raw.view("uint64")
         return {"time": float(d[0]), "dt": float(d[1]), "iteration": int(q[3]), "failures": int(q[4]),
-                "newton": int(q[5])}
+                "newton": int(q[5]), "riemann_rejected": int(q[6])}
+
+
+def riemann(pl: torch.Tensor, pr: torch.Tensor, axis: int, gamma_law_index: float = 4.0 / 3.0,
+            solver: str = "hlle") -> tuple[torch.Tensor, torch.Tensor]:
+    """srhd::riemann_solver at fixed faces (physics_srhd.hpp:377-487): left/right
+    primitives (n, 5) float64 CUDA, axis 1..3; returns fluxes (n, 5) and the
+    per-face status (1 where the reference throws)."""
+    pl, pr = pl.contiguous(), pr.contiguous()
+    n = pl.shape[0]
+    f = torch.empty_like(pl)
+    status = torch.empty(n, dtype=torch.int32, device=pl.device)
+    check(lib.mara_srhd_riemann(pl.data_ptr(), pr.data_ptr(), n, axis, gamma_law_index,
+                                {"hlle": 0, "hllc": 1}[solver], f.data_ptr(), status.data_ptr(), _stream()), "riemann")
+    return f, status

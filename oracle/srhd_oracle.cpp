@@ -212,7 +212,7 @@ inline void put(Prim& p, int k, double v)
 // (physics_srhd.hpp:489-497), u1 = u - (dFx + dFy) dt / dl. Zero-gradient
 // boundaries (ghost cells copy the edge cell). u, out: [4][N][N] (D, S1, S2, tau).
 int tube_stage(int N, const double* u, double* out, double dt, double dl, double theta, double gm, double floor_,
-               const double* avg, std::vector<Prim>& P)
+               const double* avg, std::vector<Prim>& P, bool hllc = false, int64_t* rejected = nullptr)
 {
     const size_t NN = size_t(N) * N;
     int bad = 0;
@@ -236,13 +236,19 @@ int tube_stage(int N, const double* u, double* out, double dt, double dl, double
         return s;
     };
     // face fluxes: x face (f, j) between cells (f-1, j) and (f, j), f in [0, N]
+    // HLLC faces whose contact speed the reference would reject take the HLLE flux
+    auto face = [&] (const Prim& l, const Prim& r, int axis, Cons& out_) {
+        if (hllc && riemann(l, r, axis, gm, true, out_) == 0) return;
+        if (hllc && rejected) ++*rejected;
+        riemann(l, r, axis, gm, false, out_);
+    };
     std::vector<Cons> fx(size_t(N + 1) * N), fy(size_t(N) * (N + 1));
     for (int f = 0; f <= N; ++f)
         for (int j = 0; j < N; ++j)
-            riemann(state(f - 1, j, 0, +1.0), state(f, j, 0, -1.0), 1, gm, false, fx[size_t(f) * N + j]);
+            face(state(f - 1, j, 0, +1.0), state(f, j, 0, -1.0), 1, fx[size_t(f) * N + j]);
     for (int i = 0; i < N; ++i)
         for (int f = 0; f <= N; ++f)
-            riemann(state(i, f - 1, 1, +1.0), state(i, f, 1, -1.0), 2, gm, false, fy[size_t(i) * (N + 1) + f]);
+            face(state(i, f - 1, 1, +1.0), state(i, f, 1, -1.0), 2, fy[size_t(i) * (N + 1) + f]);
     const int comp[4] = {0, 1, 2, 4};
     for (int i = 0; i < N; ++i)
         for (int j = 0; j < N; ++j)
@@ -309,24 +315,37 @@ void oracle_srhd_tube_initial(int32_t N, double angle, double rho_l, double p_l,
 // `steps` RK2 steps (advance_runge_kutta order 2); dt = cfl * dl / max speed
 // of the step's initial state. Returns the final time; *failures counts
 // zones whose recovery failed (status != 0).
-double oracle_srhd_tube_advance(int32_t N, double* u, double time, int32_t steps, double cfl, double theta,
-                                double gamma_law_index, double temperature_floor, int64_t* failures)
+// The same with the Riemann solver chosen: hllc = 0 HLLE, 1 HLLC; *rejected
+// (nullable) counts HLLC faces that fell back to HLLE.
+double oracle_srhd_tube_advance_solver(int32_t N, double* u, double time, int32_t steps, double cfl, double theta,
+                                       double gamma_law_index, double temperature_floor, int32_t hllc,
+                                       int64_t* failures, int64_t* rejected)
 {
     const size_t NN = size_t(N) * N;
     const double dl = 1.0 / N;
     std::vector<double> u1(4 * NN), u2(4 * NN);
     std::vector<Prim> P(NN);
     int64_t bad = 0;
+    if (rejected) *rejected = 0;
     for (int s = 0; s < steps; ++s)
     {
         const double dt = cfl * dl / tube_max_speed(N, u, gamma_law_index, temperature_floor);
-        bad += tube_stage(N, u, u1.data(), dt, dl, theta, gamma_law_index, temperature_floor, nullptr, P);
-        bad += tube_stage(N, u1.data(), u, dt, dl, theta, gamma_law_index, temperature_floor, u, P);
+        bad += tube_stage(N, u, u1.data(), dt, dl, theta, gamma_law_index, temperature_floor, nullptr, P, hllc != 0,
+                          rejected);
+        bad += tube_stage(N, u1.data(), u, dt, dl, theta, gamma_law_index, temperature_floor, u, P, hllc != 0,
+                          rejected);
         const double t2 = (time + dt) + dt;
         time = time * 0.5 + t2 * (1 - 0.5);
     }
     if (failures) *failures = bad;
     return time;
+}
+
+double oracle_srhd_tube_advance(int32_t N, double* u, double time, int32_t steps, double cfl, double theta,
+                                double gamma_law_index, double temperature_floor, int64_t* failures)
+{
+    return oracle_srhd_tube_advance_solver(N, u, time, steps, cfl, theta, gamma_law_index, temperature_floor, 0,
+                                           failures, nullptr);
 }
 
 // srhd::recover_primitive over n AoS zones (5 doubles each). p_start may be
