@@ -93,7 +93,8 @@ __global__ void c2p_refined_kernel(const C2PArgs a)
 __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
 {
     __shared__ mlp::Shared sm;
-    mlp::load_weights(*a.mlp, sm);
+    mlp::begin(*a.mlp, sm);
+    uint32_t phase = 0;
     for (int64_t base = int64_t(blockIdx.x) * mlp::kZones; base < a.n; base += int64_t(gridDim.x) * mlp::kZones)
     {
         __syncthreads();
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
             mlp::stage_features(sm, t, feat);
         }
         __syncthreads();
-        mlp::forward(sm);
+        mlp::forward(sm, phase);
         __syncthreads();
         for (int t = threadIdx.x; t < mlp::kZones; t += blockDim.x)
         {
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
             polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau));
         }
     }
+    mlp::end(sm);
 }
 
 __device__ inline double uniform01(uint64_t seed, uint64_t i)

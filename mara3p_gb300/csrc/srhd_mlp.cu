@@ -278,7 +278,8 @@ __global__ void export_bf16_kernel(Weights* w)
 __global__ void __launch_bounds__(kThreads) infer_kernel(const Weights* w, const float* feat, int64_t n, float* y)
 {
     __shared__ Shared sm;
-    load_weights(*w, sm);
+    begin(*w, sm);
+    uint32_t phase = 0;
     for (int64_t base = int64_t(blockIdx.x) * kZones; base < n; base += int64_t(gridDim.x) * kZones)
     {
         __syncthreads();
@@ -290,11 +291,12 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(const Weights* w, const
             stage_features(sm, t, f);
         }
         __syncthreads();
-        forward(sm);
+        forward(sm, phase);
         __syncthreads();
         for (int t = threadIdx.x; t < kZones; t += blockDim.x)
             if (base + t < n) y[base + t] = sm.out[t];
     }
+    end(sm);
 }
 
 int grad_launch(const Weights* w, const float* feat, const float* target, const int64_t* idx, int64_t begin,

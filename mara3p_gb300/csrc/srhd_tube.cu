@@ -123,7 +123,8 @@ __global__ void tube_c2p_kernel(const C2P a)
 __global__ void __launch_bounds__(mlp::kThreads) tube_c2p_mlp_kernel(const C2P a)
 {
     __shared__ mlp::Shared sm;
-    mlp::load_weights(*a.mlp, sm);
+    mlp::begin(*a.mlp, sm);
+    uint32_t phase = 0;
     const int64_t NN = int64_t(a.N) * a.N;
     double m = 0.0;
     unsigned long long bad = 0, its = 0;
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(mlp::kThreads) tube_c2p_mlp_kernel(const C2P a
             mlp::stage_features(sm, t, f);
         }
         __syncthreads();
-        mlp::forward(sm);
+        mlp::forward(sm, phase);
         __syncthreads();
         for (int t = threadIdx.x; t < mlp::kZones; t += blockDim.x)
         {
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(mlp::kThreads) tube_c2p_mlp_kernel(const C2P a
             finish_cell(a, c, z, mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau), m, bad, its);
         }
     }
+    mlp::end(sm);
     reduce_out(a, m, bad, its);
 }
 
