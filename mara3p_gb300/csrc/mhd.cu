@@ -74,8 +74,26 @@ __device__ inline int64_t fidx(int N, int axis, int i, int j, int k)
 
 __device__ inline int64_t cidx(int N, int i, int j, int k) { return (int64_t(i) * N + j) * N + k; }
 
+// (i, j, k) of linear index t of an n0 x n1 x n2 array, in 32-bit arithmetic
+// (every array here has fewer than 2^31 elements: N <= 1024 is checked on the host)
+__device__ inline void unflatten(int64_t t, int n1, int n2, int& i, int& j, int& k)
+{
+    const uint32_t u = uint32_t(t), plane = uint32_t(n1) * uint32_t(n2);
+    const uint32_t a = u / plane, r = u - a * plane, b = r / uint32_t(n2);
+    i = int(a);
+    j = int(b);
+    k = int(r - b * uint32_t(n2));
+}
+
 template<typename R>
 struct Prim { R d, v[3], p, b[3]; };
+
+// Division and square root: IEEE in FP64 (the reference's arithmetic), single
+// MUFU approximations in the mixed path's FP32 (relative error ~1e-7).
+__device__ inline double qdiv(double a, double b) { return a / b; }
+__device__ inline float qdiv(float a, float b) { return a * rcp_fast(b); }
+__device__ inline double qsqrt(double a) { return sqrt(a); }
+__device__ inline float qsqrt(float a) { return sqrt_fast(a); }
 
 template<typename R>
 __device__ inline R sum3(const R a[3], const R b[3]) { return ((R(0) + a[0] * b[0]) + a[1] * b[1]) + a[2] * b[2]; }
@@ -101,15 +119,15 @@ template<typename R>
 __device__ inline void outer_wavespeeds(const Prim<R>& p, int axis, R gm, R& am, R& ap)
 {
     const R n[3] = {R(axis == 0), R(axis == 1), R(axis == 2)};
-    const R cs2 = gm * p.p / p.d;
-    const R va2 = sum3(p.b, p.b) / p.d;
+    const R cs2 = qdiv(gm * p.p, p.d);
+    const R va2 = qdiv(sum3(p.b, p.b), p.d);
     const R bn = sum3(p.b, n);
-    const R van2 = (bn * bn) / p.d;
+    const R van2 = qdiv(bn * bn, p.d);
     const R cf2 = cs2 + va2;
     R disc = cf2 * cf2 - R(4) * cs2 * van2;
     if (sizeof(R) == sizeof(float)) disc = fmax(disc, R(0));   // FP32 rounding can dip below zero
-    const R cg2 = sqrt(disc);
-    const R cf = sqrt(R(0.5) * (cf2 + cg2));
+    const R cg2 = qsqrt(disc);
+    const R cf = qsqrt(R(0.5) * (cf2 + cg2));
     const R vn = sum3(n, p.v);
     am = vn - cf;
     ap = vn + cf;
@@ -131,7 +149,7 @@ __device__ inline void conserved(const Prim<R>& p, R gm, R u[5])
     u[1] = p.d * p.v[0];
     u[2] = p.d * p.v[1];
     u[3] = p.d * p.v[2];
-    u[4] = R(0.5) * p.d * sum3(p.v, p.v) + p.p / (gm - R(1)) + R(0.5) * sum3(p.b, p.b);
+    u[4] = R(0.5) * p.d * sum3(p.v, p.v) + qdiv(p.p, gm - R(1)) + R(0.5) * sum3(p.b, p.b);
 }
 
 // HLLE flux and E-field (physics_mhd.hpp:324-390), `axis` normal, bl the face B.
@@ -158,7 +176,7 @@ __device__ inline void riemann_hlle(Prim<R> pl, Prim<R> pr, R bl, R gm, R F[5], 
     outer_wavespeeds(pr, AXIS, gm, arm, arp);
     const R ap = fmax(R(0), fmax(alp, arp));
     const R am = fmin(R(0), fmin(alm, arm));
-    for (int k = 0; k < 5; ++k) F[k] = (ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am) / (ap - am);
+    for (int k = 0; k < 5; ++k) F[k] = qdiv(ap * fl[k] - am * fr[k] - (ul[k] - ur[k]) * ap * am, ap - am);
     // induction = n x E with E = -(v x B); E-field of the face = -(n x hll_induction)
     auto induction = [] (const Prim<R>& p, R I[3]) {
         const R e[3] = {-(p.v[1] * p.b[2] - p.v[2] * p.b[1]), -(p.v[2] * p.b[0] - p.v[0] * p.b[2]),
@@ -171,7 +189,7 @@ __device__ inline void riemann_hlle(Prim<R> pl, Prim<R> pr, R bl, R gm, R F[5], 
     R il[3], ir[3], hi[3];
     induction(pl, il);
     induction(pr, ir);
-    for (int k = 0; k < 3; ++k) hi[k] = (ap * il[k] - am * ir[k] - (pl.b[k] - pr.b[k]) * ap * am) / (ap - am);
+    for (int k = 0; k < 3; ++k) hi[k] = qdiv(ap * il[k] - am * ir[k] - (pl.b[k] - pr.b[k]) * ap * am, ap - am);
     const R n[3] = {R(AXIS == 0), R(AXIS == 1), R(AXIS == 2)};
     const R c[3] = {n[1] * hi[2] - n[2] * hi[1], n[2] * hi[0] - n[0] * hi[2], n[0] * hi[1] - n[1] * hi[0]};
     // transverse components in increasing axis order
@@ -193,7 +211,8 @@ __global__ void prim_kernel(const Args A)
     unsigned long long bad = 0;
     for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
     {
-        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        int i, j, k;
+        unflatten(c, N, N, i, j, k);
         if constexpr (sizeof(R) == sizeof(float))
         {
             // Mixed: the recovery in FP32 from the FP64 state (integer conversions,
@@ -299,7 +318,8 @@ __global__ void face_kernel(const Args A)
     const int di = AXIS == 0, dj = AXIS == 1, dk = AXIS == 2;
     for (int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; f < NF; f += int64_t(gridDim.x) * blockDim.x)
     {
-        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        int i, j, k;
+        unflatten(f, n1, n2, i, j, k);
         const int64_t cm2 = cidx(N, wrap(i - 2 * di, N), wrap(j - 2 * dj, N), wrap(k - 2 * dk, N));
         const int64_t cm1 = cidx(N, wrap(i - di, N), wrap(j - dj, N), wrap(k - dk, N));
         const int64_t c0 = cidx(N, wrap(i, N), wrap(j, N), wrap(k, N));
@@ -414,7 +434,8 @@ __global__ void update_kernel(const Args A)
         if (t < NN)
         {
             const int64_t c = t;
-            const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+            int i, j, k;
+        unflatten(c, N, N, i, j, k);
             const R* F0 = static_cast<const R*>(A.F[0]);
             const R* F1 = static_cast<const R*>(A.F[1]);
             const R* F2 = static_cast<const R*>(A.F[2]);
@@ -450,7 +471,8 @@ __global__ void update_kernel(const Args A)
         int axis = 0;
         if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
         const int n1 = N + (axis == 1), n2 = N + (axis == 2);
-        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        int i, j, k;
+        unflatten(f, n1, n2, i, j, k);
         // solenoidal_difference (mesh_cartesian_3d.hpp:265-274)
         if constexpr (sizeof(R) == sizeof(float))
         {
@@ -502,7 +524,8 @@ __global__ void div_b_kernel(int N, const double* b1, const double* b2, const do
     double m = 0.0;
     for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
     {
-        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        int i, j, k;
+        unflatten(c, N, N, i, j, k);
         const double d = (b1[fidx(N, 0, i + 1, j, k)] - b1[fidx(N, 0, i, j, k)])
                        + (b2[fidx(N, 1, i, j + 1, k)] - b2[fidx(N, 1, i, j, k)])
                        + (b3[fidx(N, 2, i, j, k + 1)] - b3[fidx(N, 2, i, j, k)]);
@@ -552,7 +575,8 @@ __global__ void init_faces_kernel(int N, const Mode* modes, int count, double a_
         int axis = 0;
         if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
         const int n1 = N + (axis == 1), n2 = N + (axis == 2);
-        const int i = int(f / (int64_t(n1) * n2)), j = int((f / n2) % n1), k = int(f % n2);
+        int i, j, k;
+        unflatten(f, n1, n2, i, j, k);
         auto ae = [&] (int ax, int a, int b, int c) { return edge_a(modes, count, a_amp, N, ax, a, b, c); };
         if (axis == 0)
             b1[f] = ((ae(2, i, j + 1, k) - ae(2, i, j, k)) - (ae(1, i, j, k + 1) - ae(1, i, j, k))) / da;
@@ -569,7 +593,8 @@ __global__ void init_cells_kernel(int N, const Mode* modes, int count, double v_
     const int64_t NN = int64_t(N) * N * N;
     for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
     {
-        const int i = int(c / (int64_t(N) * N)), j = int((c / N) % N), k = int(c % N);
+        int i, j, k;
+        unflatten(c, N, N, i, j, k);
         const double x[3] = {0.5 * (lin(i, N) + lin(i + 1, N)), 0.5 * (lin(j, N) + lin(j + 1, N)), 0.5 * (lin(k, N) + lin(k + 1, N))};
         Prim<double> p;
         p.d = 1.0;
