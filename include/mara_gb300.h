@@ -38,6 +38,8 @@ enum mara_precision {
 enum mara_dt_mode {
     MARA_DT_FORMULA = 0,     /* problems/minidisk.cpp:204-206 fixed formula with start-up ramp */
     MARA_DT_CFL = 1,         /* cfl * dl / max fastest wavespeed (reduction over the mesh) */
+    MARA_DT_FORMULA_HELD = 2,/* the formula at the start of each advance call, held for all its steps:
+                                the reference driver's fold batches (problems/minidisk.cpp:202-213) */
 };
 
 /* Field-for-field minidisk::solver_data_t (problems/minidisk.hpp:77-93), plus

@@ -68,6 +68,23 @@ def build_library(verbose: bool = False) -> Path:
     return LIB
 
 
+DRIVER_SRC = Path(__file__).resolve().parent / "driver" / "mara_minidisk.cpp"
+DRIVER = Path(__file__).resolve().parent / "mara_minidisk"
+
+
+def build_driver(verbose: bool = False) -> Path:
+    """The C++17 minidisk driver (problems/minidisk.cpp's main loop) on the C
+    ABI, linked against libmara_gb300.so next to it."""
+    if DRIVER.exists() and DRIVER.stat().st_mtime >= max(DRIVER_SRC.stat().st_mtime, LIB.stat().st_mtime,
+                                                         (ROOT / "include" / "mara_gb300.h").stat().st_mtime):
+        return DRIVER
+    _run([nvcc(), "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(DRIVER_SRC), "-L", str(LIB.parent),
+          "-lmara_gb300", "-lcudart", "-Xlinker", "-rpath,$ORIGIN", "-o", str(DRIVER)])
+    if verbose:
+        print(f"[build] {DRIVER.name}", flush=True)
+    return DRIVER
+
+
 def build_oracle(reference: bool = False) -> None:
     """Compile oracle/ (test infrastructure) with make; reference=True also
     builds oracle/_ref from the reference checkout when it is present."""
@@ -78,5 +95,6 @@ def build_oracle(reference: bool = False) -> None:
 
 if __name__ == "__main__":
     build_library(verbose=True)
+    build_driver(verbose=True)
     if "--oracle" in sys.argv:
         build_oracle(reference=True)

@@ -773,7 +773,7 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
     MARA_REQUIRE(steps >= 0, "mara_minidisk_advance: negative step count");
     MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_minidisk_advance: rk_order must be 1 or 2");
     MARA_REQUIRE(precision == MARA_FP64 || precision == MARA_MIXED, "mara_minidisk_advance: bad precision");
-    MARA_REQUIRE(dt_mode == MARA_DT_FORMULA || dt_mode == MARA_DT_CFL, "mara_minidisk_advance: bad dt_mode");
+    MARA_REQUIRE(dt_mode >= MARA_DT_FORMULA && dt_mode <= MARA_DT_FORMULA_HELD, "mara_minidisk_advance: bad dt_mode");
     if (steps == 0) return MARA_OK;
     cudaStream_t s = as_stream(stream);
     const int N = sd->block_size << sd->depth;
@@ -787,7 +787,9 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
     double* cur = u;
     double* alt = ws_state;
 
-    if (int r = clock_step(sd, clock, dt_mode, rk_order, 0, 1, s)) return r;
+    // a held formula dt is chosen by the call's first step
+    if (int r = clock_step(sd, clock, dt_mode == MARA_DT_FORMULA_HELD ? MARA_DT_FORMULA : dt_mode, rk_order, 0, 1, s))
+        return r;
     for (int step = 0; step < steps; ++step)
     {
         if (precision == MARA_FP64 && rk_order == 2)
@@ -899,7 +901,7 @@ int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clo
     if (int r = check_params(sd)) return r;
     MARA_REQUIRE(clock != nullptr, "mara_minidisk_clock_update: clock is null");
     MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_minidisk_clock_update: rk_order must be 1 or 2");
-    MARA_REQUIRE(dt_mode == MARA_DT_FORMULA || dt_mode == MARA_DT_CFL, "mara_minidisk_clock_update: bad dt_mode");
+    MARA_REQUIRE(dt_mode >= MARA_DT_FORMULA && dt_mode <= MARA_DT_FORMULA_HELD, "mara_minidisk_clock_update: bad dt_mode");
     return clock_step(sd, clock, dt_mode, rk_order, end_step != 0, begin_step != 0, as_stream(stream));
 }
 

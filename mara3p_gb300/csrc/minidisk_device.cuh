@@ -761,7 +761,11 @@ __device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a)
     if (a.begin_step)
     {
         double t = c->time, dt;
-        if (a.dt_mode == MARA_DT_FORMULA)
+        if (a.dt_mode == MARA_DT_FORMULA_HELD)
+        {
+            dt = c->dt;   // the batch's dt, chosen by its first step
+        }
+        else if (a.dt_mode == MARA_DT_FORMULA)
         {
             // problems/minidisk.cpp:204-206
             double vmax = sqrt(1.0 * 0.5 / a.softening_length);

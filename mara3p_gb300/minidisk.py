@@ -19,7 +19,7 @@ import torch
 from ._capi import MinidiskClock, MinidiskParams, check, lib
 
 FP64, MIXED = 0, 1
-DT_FORMULA, DT_CFL = 0, 1
+DT_FORMULA, DT_CFL, DT_FORMULA_HELD = 0, 1, 2
 
 
 @dataclass(frozen=True)
