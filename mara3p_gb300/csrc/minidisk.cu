@@ -19,7 +19,9 @@
 //          stays FP64 in HBM and is accumulated in FP64. RK2 keeps only the
 //          FP32 stage-1 increment d1 = dt*L(u0) between stages; stage 2 uses
 //          u1 = f32(u0) + d1 for its fluxes and writes u0 + (d1 + d2)/2 in FP64.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
@@ -34,29 +36,76 @@ namespace md {
 template<typename R>
 struct Smem
 {
-    R p[3][EX][EY];        // primitives of the halo tile
+    // primitives of the halo tile; in the FP64 path an interior tile's raw
+    // state lands here first, by one TMA copy (box 36 x 20 x 3 of [3][N][N])
+    __align__(128) R p[3][EX][EY];
     R gx[3][GX][GY];       // x slopes of halo-tile cells [1, TX+3) x [1, TY+3)
     R gy[3][GX][GY];       // y slopes, same cells
     R fx[3][TX + 1][TY];   // x-face fluxes
     R fy[3][TX][TY + 1];   // y-face fluxes
     R xv[TX + 1], xc[TX], yv[TY + 1], yc[TY];
     double wmax[NT / 32];
+    unsigned long long tma_bar;   // completion barrier of the tile copy
 };
+
+// Bounded wait on the tile copy's barrier (phase 0): false if it timed out.
+__device__ inline bool tile_copy_wait(unsigned long long* bar)
+{
+    const uint32_t addr = uint32_t(__cvta_generic_to_shared(bar));
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it)
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(addr), "r"(0));
+    return done != 0;
+}
 
 template<typename R>
 __device__ inline R to_r(double v) { return R(v); }
 
 // ------------------------------------------------------------- stage kernel
+// tmap: the state [3][N][N] as a 3D tensor (columns, rows, components) with a
+// 36 x 20 x 3 box, used by FP64 tiles that need no periodic wrap (A.use_tma).
 template<typename R, int KIND>
-__global__ void __launch_bounds__(NT) stage_kernel(const Args A)
+__global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_constant__ CUtensorMap tmap)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<R>& S = *reinterpret_cast<Smem<R>*>(smem_raw);
     const int tid = threadIdx.x;
     const int tx = blockIdx.x / A.tiles_y, ty = blockIdx.x % A.tiles_y;
     const int gx0 = tx * TX, gy0 = ty * TY;
     const int N = A.N;
     const size_t NN = size_t(N) * N;
+
+    // FP64 interior tile: one bulk tensor copy of the raw halo tile into S.p,
+    // issued first so that it runs while the coordinates are computed. The
+    // box's first coordinate (gy0 - 2 doubles) is a multiple of 16 bytes.
+    bool tma = false;
+    if constexpr (KIND == K_FP64)
+    {
+        tma = A.use_tma && gx0 >= 2 && gx0 + TX + 2 <= N && gy0 >= 2 && gy0 + TY + 2 <= N &&
+              (__cvta_generic_to_shared(&S.p[0][0][0]) & 127) == 0;
+        if (tma)
+        {
+            const uint32_t bar = uint32_t(__cvta_generic_to_shared(&S.tma_bar));
+            if (tid == 0)
+            {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(1));
+                asm volatile("fence.mbarrier_init.release.cluster;");
+            }
+            __syncthreads();
+            if (tid == 0)
+            {
+                const uint32_t dst = uint32_t(__cvta_generic_to_shared(&S.p[0][0][0]));
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                             :: "r"(bar), "r"(uint32_t(sizeof(S.p))));
+                asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                             " [%0], [%1, {%2, %3, %4}], [%5];"
+                             :: "r"(dst), "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(gy0 - 2), "r"(gx0 - 2), "r"(0),
+                                "r"(bar)
+                             : "memory");
+            }
+        }
+    }
 
     // coordinates of this tile's vertices and centres: the reference's
     // per-block linspace in FP64 for the FP64 path, x = -R + i*dl in FP32 for
@@ -102,7 +151,18 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A)
         }
     }
 
-    // phase 1: halo tile -> primitives
+    // phase 1: halo tile -> primitives (in place after the tile copy)
+    if (tma && tile_copy_wait(&S.tma_bar))
+    {
+        for (int e = tid; e < EX * EY; e += NT)
+        {
+            const int ei = e / EY, ej = e - (e / EY) * EY;
+            const double s = S.p[0][ei][ej], m1 = S.p[1][ei][ej], m2 = S.p[2][ei][ej];
+            S.p[1][ei][ej] = R(m1 / s);
+            S.p[2][ei][ej] = R(m2 / s);
+        }
+    }
+    else
     for (int e = tid; e < EX * EY; e += NT)
     {
         int ei = e / EY, ej = e - (e / EY) * EY;
@@ -557,6 +617,37 @@ void set_binary(Args& A, const mara_minidisk_params* sd, double t)
     std::memcpy(A.bin, v, sizeof v);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null if the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The [3][N][N] FP64 state as a 3D tensor with the halo tile's 36 x 20 x 3
+// box; false (and the per-thread tile loads) where TMA cannot address it:
+// N odd (row stride not a multiple of 16 bytes) or an unaligned state.
+bool state_tensor_map(const double* u, int N, CUtensorMap* map)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode || N % 2 != 0 || (reinterpret_cast<uintptr_t>(u) & 15) != 0) return false;
+    const cuuint64_t dims[3] = {cuuint64_t(N), cuuint64_t(N), 3};
+    const cuuint64_t strides[2] = {cuuint64_t(N) * sizeof(double), cuuint64_t(N) * N * sizeof(double)};
+    const cuuint32_t box[3] = {EY, EX, 3};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(u), dims, strides, box, elem,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template<typename R, int KIND>
 int launch_stage(const Args& A, int tiles, cudaStream_t s)
 {
@@ -566,7 +657,11 @@ int launch_stage(const Args& A, int tiles, cudaStream_t s)
     std::call_once(flags[dev & 63], [] {
         cudaFuncSetAttribute(stage_kernel<R, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(Smem<R>)));
     });
-    stage_kernel<R, KIND><<<tiles, NT, sizeof(Smem<R>), s>>>(A);
+    Args a = A;
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    a.use_tma = KIND == K_FP64 && A.N >= TX + 4 && state_tensor_map(A.u_in, A.N, &map);
+    stage_kernel<R, KIND><<<tiles, NT, sizeof(Smem<R>), s>>>(a, map);
     return launch_status("minidisk stage kernel");
 }
 

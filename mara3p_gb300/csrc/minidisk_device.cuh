@@ -40,6 +40,7 @@ struct Args
     int level;             // block level (2^level blocks per side)
     int tiles_y;
     int sweep_rows;        // mixed sweep: rows per warp
+    int use_tma;           // FP64 tiles: interior halo tiles by one TMA copy
     uint64_t bi, bj;       // K_BLOCK: block coordinates
     double R, dl;
     double rs2;            // softening_length^2 (std::pow(rs, 2.0) on the host)
