@@ -243,26 +243,19 @@ __device__ inline void face_flux_f(const T pa[3], const T pb[3], const T ga[3], 
     fr[2] = AXIS == 0 ? vmul(vr, ur[2]) : vfma(vr, ur[2], pgr);
     const T ap = vmax(bc<T>(0.0f), vadd(vmax(vl, vr), cs));
     const T am = vmin(bc<T>(0.0f), vsub(vmin(vl, vr), cs));
+    // (ap fl - am fr - (ul - ur) ap am) / (ap - am) = a fl + b fr + c (ur - ul)
     const T inv = vrcp(vsub(ap, am));
-    const T apam = vmul(ap, am);
-    const T nam = vneg(am);
-    for (int k = 0; k < 3; ++k)
-    {
-        // (ap*fl - am*fr - (ul - ur)*ap*am) / (ap - am)
-        T t = vmul(ap, fl[k]);
-        t = vfma(nam, fr[k], t);
-        t = vfma(vsub(ur[k], ul[k]), apam, t);
-        out[k] = vmul(t, inv);
-    }
+    const T ca = vmul(ap, inv), cb = vmul(vneg(am), inv), cc = vmul(vmul(ap, am), inv);
+    for (int k = 0; k < 3; ++k) out[k] = vfma(cc, vsub(ur[k], ul[k]), vfma(cb, fr[k], vmul(ca, fl[k])));
     if (F.half_nu != 0.0f)
     {
-        const T h = bc<T>(F.half_inv_dl);
-        const T mu = vmul(bc<T>(F.half_nu), vadd(Rr[0], L[0]));
+        // mu = nu (Sigma_l + Sigma_r) / 2 carries the 1/(2 dl) of the averaged slopes
+        const T mu = vmul(vmul(bc<T>(F.half_nu), vadd(Rr[0], L[0])), bc<T>(F.half_inv_dl));
         const T nmu = vneg(mu);
-        const T vx_long = vmul(vadd(ga[1], gb[1]), h);
-        const T vy_long = vmul(vadd(ga[2], gb[2]), h);
-        const T vx_tran = vmul(vadd(ta[1], tb[1]), h);
-        const T vy_tran = vmul(vadd(ta[2], tb[2]), h);
+        const T vx_long = vadd(ga[1], gb[1]);
+        const T vy_long = vadd(ga[2], gb[2]);
+        const T vx_tran = vadd(ta[1], tb[1]);
+        const T vy_tran = vadd(ta[2], tb[2]);
         if (AXIS == 0)
         {
             out[1] = vfma(nmu, vsub(vx_long, vy_tran), out[1]);

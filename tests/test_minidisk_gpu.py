@@ -222,3 +222,21 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
         assert torch.equal(u1, u2), (block_size, depth, rk1, float((u1 - u2).abs().max()))
         assert (k1.time, k1.dt, k1.max_wavespeed, k1.iteration) == (k2.time, k2.dt, k2.max_wavespeed, k2.iteration)
     assert lib.mara_minidisk_sweep_columns(3) == -1
+
+
+@pytest.mark.parametrize("block_size,depth", [(20, 2), (50, 1), (40, 3), (130, 0)])
+def test_ragged_meshes_fp64_rk2_and_mixed(md, oracle, block_size, depth):
+    """Meshes whose size is not a multiple of the 16 x 32 tiles or the 28/60
+    column strips (80, 100, 320, 130): FP64 RK2 against the oracle, and the
+    mixed path within its error budget of the FP64 path. 320 and 130 also
+    contain TMA-loaded interior tiles next to wrapped boundary tiles."""
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    u0 = md.initial_conserved(sd, seed=4, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    a = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)
+    a.advance(3)
+    oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 3, 2, 0, 8)
+    assert rel_l1_components(a.u.cpu().numpy(), ref) < FP64_ONE_STEP
+    b = md.Run(sd, u0.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_FORMULA)
+    b.advance(3)
+    assert rel_l1_components(b.u.cpu().numpy(), a.u.cpu().numpy()) < 1e-6
