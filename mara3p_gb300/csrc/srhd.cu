@@ -67,10 +67,10 @@ __device__ inline void polish(const C2PArgs& a, int64_t i, const Zone& z, double
     if (a.refine32 > 0) guess = refine_fp32(z, a.gamma, guess, a.refine32);
     double prim[5] = {0, 0, 0, 0, 0};
     int it = 0, it2 = 0;
-    int st = newton(z, a.gamma, a.floor, guess, a.seeded_budget, prim, it);
+    int st = newton_fast(z, a.gamma, a.floor, guess, a.seeded_budget, prim, it);
     if (st != 0)
     {
-        // fall back to the reference's start and budget
+        // fall back to the reference's start, budget and arithmetic
         st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it2);
         it += it2;
     }

@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include "mixed_math.cuh"
 
 namespace mara {
 namespace srhd {
@@ -64,6 +65,86 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     prim[1] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S1), Et), 1.0);
     prim[2] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S2), Et), 1.0);
     prim[3] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S3), Et), 1.0);
+    prim[4] = p;
+    return 0;
+}
+
+// FP64 reciprocal and inverse square root for the seeded polish: an FP32
+// seed (relative error ~2^-22) and two Newton-Raphson steps, each of which
+// squares the relative error (y <- y + y (1 - b y); y <- y (3/2 - x y^2 / 2)),
+// so the result is within a few ulp of the exact value. Arguments must lie in
+// the FP32 normal range, as the polish's quantities do; anything else gives
+// NaN or infinity and the zone falls back to the exact iteration.
+__device__ inline double rcp_nr(double b)
+{
+    double y = f2d(rcp_fast(d2f(b)));
+    y = fma(y, fma(-b, y, 1.0), y);
+    y = fma(y, fma(-b, y, 1.0), y);
+    return y;
+}
+
+__device__ inline double rsqrt_nr(double x)
+{
+    const double h = 0.5 * x;
+    double y = f2d(rsqrt_fast(d2f(x)));
+    y = y * fma(-h * y, y, 1.5);
+    y = y * fma(-h * y, y, 1.5);
+    return y;
+}
+
+// The Newton iteration of newton() from a seeded pressure with the same
+// stopping rule (|f| < 1e-12, 1e-8 on the last allowed iteration) and the
+// same final primitives, its update rearranged to three reciprocals and one
+// inverse square root per iteration instead of eight divisions and a square
+// root. The seeded paths use it; the reference's own start (newton) keeps the
+// reference's arithmetic bit for bit.
+__device__ inline int newton_fast(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
+                                  double prim[5], int& iterations)
+{
+    const double tol = 1e-12;
+    const double D = z.D, tau = z.tau;
+    const double SS = z.S1 * z.S1 + z.S2 * z.S2 + z.S3 * z.S3;
+    const double iD = rcp_nr(D);
+    const double gm1 = gm - 1.0;
+    const double b2max = 1.0 - 1e-10;
+    bool found = false;
+    int iteration = 0;
+    double W0 = 1.0;
+    double p = p_start;
+    while (iteration <= iter_max)
+    {
+        const double Et = (tau + p) + D;
+        const double iE = rcp_nr(Et);
+        const double b2 = fmin(SS * iE * iE, b2max);
+        const double ib = 1.0 - b2;
+        const double W = rsqrt_nr(ib);                 // 1 / sqrt(1 - b2)
+        const double W2 = W * W;
+        const double iW = ib * W;                      // sqrt(1 - b2)
+        const double e = ((tau + D * (1.0 - W)) + p * (1.0 - W2)) * iW * iD;
+        const double d = D * iW;
+        const double pWD = p * W * iD;                 // p / d
+        const double h = (1.0 + e) + pWD;
+        const double a2 = gm * pWD * rcp_nr(h);        // gm p / (d h)
+        const double f = d * e * gm1 - p;
+        const double g = b2 * a2 - 1.0;
+        p = fma(-f, rcp_nr(g), p);
+        if (fabs(f) < tol || (fabs(f) < tol * 1e4 && iteration == iter_max))
+        {
+            W0 = W;
+            found = true;
+            break;
+        }
+        ++iteration;
+    }
+    iterations = found ? iteration + 1 : iteration;
+    if (temperature_floor > 0.0) p = fmax(p, temperature_floor * D);
+    if (!found) return 1;
+    if (temperature_floor <= 0.0 && p <= 0.0) return 2;
+    const double Et = __dadd_rn(__dadd_rn(tau, D), p);
+    prim[0] = __ddiv_rn(D, W0);
+    prim[1] = __ddiv_rn(__dmul_rn(W0, z.S1), Et);
+    prim[2] = __ddiv_rn(__dmul_rn(W0, z.S2), Et);
+    prim[3] = __ddiv_rn(__dmul_rn(W0, z.S3), Et);
     prim[4] = p;
     return 0;
 }

@@ -67,7 +67,7 @@ __device__ inline void finish_cell(const C2P& a, int64_t c, const srhd::Zone& z,
     else
     {
         if (a.refine32 > 0) guess = srhd::refine_fp32(z, a.gamma, guess, a.refine32);
-        st = srhd::newton(z, a.gamma, a.floor, guess, a.budget, prim, it);
+        st = srhd::newton_fast(z, a.gamma, a.floor, guess, a.budget, prim, it);
         if (st != 0)
         {
             st = srhd::newton(z, a.gamma, a.floor, 0.0, 50, prim, it2);
