@@ -21,8 +21,12 @@
 //
 // FP64: reference evaluation order. MIXED: P, F and E in FP32; u and B stay
 // FP64 and are accumulated in FP64; the curl of the FP32 edge EMFs is formed
-// exactly in FP64 (differences of floats are exact doubles), so div B is
-// preserved to FP64 rounding as in the FP64 path.
+// from exact float-pair differences and rounded once to FP64, so div B is
+// preserved to FP64 rounding as in the FP64 path. The mixed RK2 keeps stage
+// 1's cell change as an FP32 increment (the minidisk's scheme), so that the
+// cells of both stages take one FP64 addition per component per step; FP64
+// runs at a small fraction of the FP32 rate on this part, and the update
+// kernel was bound by its FP64 pipe.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -59,7 +63,15 @@ struct Args
     void* E[3];                                  // [2][face count]: the two transverse components
     Clock* clock;
     int stage;
+    float* dinc;                                 // [5][N^3] mixed RK2 stage-1 increments
 };
+
+// Cell updates of the mixed path (a template argument of the prim and update
+// kernels): MIX_PLAIN writes u_out = u - du; MIX_INCREMENT (RK2 stage 1)
+// writes only dinc = -du as floats; MIX_FROM_INCREMENT (stage 2) takes u0 from
+// uc and u1 = u0 + dinc, and writes u_out = u0 + (dinc - du) / 2. Faces are
+// updated in FP64 in every mode.
+enum { MIX_PLAIN = 0, MIX_INCREMENT = 1, MIX_FROM_INCREMENT = 2 };
 
 __host__ __device__ inline int64_t nb(int N, int axis) { return int64_t(N + (axis == 0)) * (N + (axis == 1)) * (N + (axis == 2)); }
 
@@ -198,8 +210,8 @@ __device__ inline void riemann_hlle(Prim<R> pl, Prim<R> pr, R bl, R gm, R F[5], 
 }
 
 // ---------------------------------------------------------------- kernels
-template<typename R>
-__global__ void prim_kernel(const Args A)
+template<typename R, int MODE>
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_kernel(const Args A)
 {
     __shared__ double wmax[8];
     const int N = A.N;
@@ -225,8 +237,15 @@ __global__ void prim_kernel(const Args A)
             const double energy = A.uc[4 * A.ucs + c * A.uzs];
             Prim<float> p;
             p.d = d2f(A.uc[c * A.uzs]);
-            const float S[3] = {d2f(A.uc[A.ucs + c * A.uzs]), d2f(A.uc[2 * A.ucs + c * A.uzs]),
-                                d2f(A.uc[3 * A.ucs + c * A.uzs])};
+            float S[3] = {d2f(A.uc[A.ucs + c * A.uzs]), d2f(A.uc[2 * A.ucs + c * A.uzs]),
+                          d2f(A.uc[3 * A.ucs + c * A.uzs])};
+            float de = 0.0f;   // energy increment, folded into the FP64 difference below
+            if (MODE == MIX_FROM_INCREMENT)
+            {
+                p.d = __fadd_rn(p.d, A.dinc[c]);
+                for (int q = 0; q < 3; ++q) S[q] = __fadd_rn(S[q], A.dinc[(q + 1) * NN + c]);
+                de = A.dinc[4 * NN + c];
+            }
             const float inv = rcp_fast(p.d);
             for (int q = 0; q < 3; ++q)
             {
@@ -234,7 +253,7 @@ __global__ void prim_kernel(const Args A)
                 p.b[q] = b[q];
             }
             const float kin_mag = 0.5f * sum3(S, p.v) + 0.5f * sum3(b, b);
-            p.p = d2f(energy - f2d(kin_mag)) * (gm - 1.0f);
+            p.p = d2f(energy - f2d(__fsub_rn(kin_mag, de))) * (gm - 1.0f);
             if (p.d < 0.0f || p.p < 0.0f) ++bad;
             P[0 * NN + c] = p.d;
             P[1 * NN + c] = p.v[0];
@@ -416,17 +435,59 @@ __device__ inline float ee_f(const Args& A, int axis, int i, int j, int k)
     return avg(a, b);
 }
 
-__device__ inline double fdiff(float a, float b) { return f2d(a) - f2d(b); }
+// a - b as the unrounded pair s + e of floats (Knuth's TwoSum, 6 operations,
+// each rounded explicitly so the compiler can neither contract nor reorder)
+__device__ inline void two_diff(float a, float b, float& s, float& e)
+{
+    s = __fsub_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(-b, bb));
+}
 
-template<typename R>
-__global__ void update_kernel(const Args A)
+// (a - b) - (c - d) of four floats, as a double: the three differences are
+// exact float pairs; only the sum of the three rounding terms rounds (in
+// FP32, at 2^-24 of the terms, themselves at most half an ulp of a - b and
+// c - d), then hi + lo is one FP64 addition. Equal to the FP64 curl of the
+// float EMFs up to rounding far below the FP64 rounding of the face update.
+__device__ inline double curl_f(float a, float b, float c, float d)
+{
+    float s1, e1, s2, e2, s3, e3;
+    two_diff(a, b, s1, e1);
+    two_diff(c, d, s2, e2);
+    two_diff(s1, s2, s3, e3);
+    return f2d(s3) + f2d(__fadd_rn(__fsub_rn(e1, e2), e3));
+}
+
+// x / 2 by decrementing the exponent: exact, and equal to x * 0.5, for every
+// normal x above the smallest normal double times 2; zero, subnormals, the
+// two smallest binades, infinities and NaN are returned unchanged (an error
+// below 4.5e-308 for the tiny ones). Integer instructions only.
+__device__ inline double half_exact(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const unsigned e = unsigned(b >> 52) & 0x7FFu;
+    return e >= 2u && e <= 0x7FEu ? __longlong_as_double(b - (1LL << 52)) : x;
+}
+
+template<typename R, int MODE>
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) update_kernel(const Args A)
 {
     const int N = A.N;
     const int64_t NN = int64_t(N) * N * N;
     const double dt = A.clock->dt[A.stage];
     const double dl = A.dl;
-    const double dt_over_dl_d = dt / dl;
-    const float dt_over_dl = float(dt_over_dl_d);
+    // dt / dl once per block: an FP64 division and conversion per thread
+    // would cost more FP64-pipe issue than the update itself
+    __shared__ double s_dtdl;
+    __shared__ float s_dtdl_f;
+    if (threadIdx.x == 0)
+    {
+        s_dtdl = dt / dl;
+        s_dtdl_f = float(s_dtdl);
+    }
+    __syncthreads();
+    const double dt_over_dl_d = s_dtdl;
+    const float dt_over_dl = s_dtdl_f;
     const int64_t nf0 = nb(N, 0), nf1 = nb(N, 1), nf2 = nb(N, 2);
     const int64_t total = NN + nf0 + nf1 + nf2;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x)
@@ -444,10 +505,10 @@ __global__ void update_kernel(const Args A)
             const int64_t z0 = fidx(N, 2, i, j, k), z1 = fidx(N, 2, i, j, k + 1);
             for (int q = 0; q < 5; ++q)
             {
-                double u = A.uc[q * A.ucs + c * A.uzs];
                 double out;
                 if (sizeof(R) == sizeof(double))
                 {
+                    const double u = A.uc[q * A.ucs + c * A.uzs];
                     const double dc = (double(F0[q * nf0 + x1]) - double(F0[q * nf0 + x0]))
                                     + (double(F1[q * nf1 + y1]) - double(F1[q * nf1 + y0]))
                                     + (double(F2[q * nf2 + z1]) - double(F2[q * nf2 + z0]));
@@ -458,10 +519,20 @@ __global__ void update_kernel(const Args A)
                     const float dc = (float(F0[q * nf0 + x1]) - float(F0[q * nf0 + x0]))
                                    + (float(F1[q * nf1 + y1]) - float(F1[q * nf1 + y0]))
                                    + (float(F2[q * nf2 + z1]) - float(F2[q * nf2 + z0]));
-                    out = u - f2d(dc * dt_over_dl);
+                    const float du = __fmul_rn(dc, dt_over_dl);
+                    if (MODE == MIX_INCREMENT)
+                    {
+                        A.dinc[q * NN + c] = -du;
+                        continue;
+                    }
+                    const double u = A.uc[q * A.ucs + c * A.uzs];
+                    if (MODE == MIX_FROM_INCREMENT)
+                        out = u + f2d(__fmul_rn(0.5f, __fsub_rn(A.dinc[q * NN + c], du)));
+                    else
+                        out = u - f2d(du);
                 }
                 // weighted_sum a*0.5 + b*(1-0.5): halving is exact, so (a + b)*0.5 is the same double
-                if (A.uavg) out = sizeof(R) == sizeof(float) ? (A.uavg[q * NN + c] + out) * 0.5
+                if (A.uavg) out = sizeof(R) == sizeof(float) ? half_exact(A.uavg[q * NN + c] + out)
                                                              : A.uavg[q * NN + c] * 0.5 + out * (1 - 0.5);
                 A.uc_out[q * NN + c] = out;
             }
@@ -478,13 +549,13 @@ __global__ void update_kernel(const Args A)
         {
             double cf;
             if (axis == 0)
-                cf = fdiff(ee_f(A, 2, i, j + 1, k), ee_f(A, 2, i, j, k)) - fdiff(ee_f(A, 1, i, j, k + 1), ee_f(A, 1, i, j, k));
+                cf = curl_f(ee_f(A, 2, i, j + 1, k), ee_f(A, 2, i, j, k), ee_f(A, 1, i, j, k + 1), ee_f(A, 1, i, j, k));
             else if (axis == 1)
-                cf = fdiff(ee_f(A, 0, i, j, k + 1), ee_f(A, 0, i, j, k)) - fdiff(ee_f(A, 2, i + 1, j, k), ee_f(A, 2, i, j, k));
+                cf = curl_f(ee_f(A, 0, i, j, k + 1), ee_f(A, 0, i, j, k), ee_f(A, 2, i + 1, j, k), ee_f(A, 2, i, j, k));
             else
-                cf = fdiff(ee_f(A, 1, i + 1, j, k), ee_f(A, 1, i, j, k)) - fdiff(ee_f(A, 0, i, j + 1, k), ee_f(A, 0, i, j, k));
+                cf = curl_f(ee_f(A, 1, i + 1, j, k), ee_f(A, 1, i, j, k), ee_f(A, 0, i, j + 1, k), ee_f(A, 0, i, j, k));
             double out = fma(-cf, dt_over_dl_d, A.bf[axis][f]);
-            if (A.bavg[axis]) out = (A.bavg[axis][f] + out) * 0.5;
+            if (A.bavg[axis]) out = half_exact(A.bavg[axis][f] + out);
             A.bf_out[axis][f] = out;
             continue;
         }
@@ -664,7 +735,8 @@ inline int blocks_for(int64_t n) { return int(std::min<int64_t>((n + 255) / 256,
 template<typename R>
 int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
           const double* u_in, int64_t ucs, int64_t uzs, const double* const b_in[3],
-          const double* uavg, const double* const bavg[3], double* u_out, double* const b_out[3], cudaStream_t s)
+          const double* uavg, const double* const bavg[3], double* u_out, double* const b_out[3],
+          int mixed_mode, cudaStream_t s)
 {
     const int N = mp->N;
     const int64_t NN = int64_t(N) * N * N;
@@ -691,7 +763,14 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     A.P = w.P;
     A.clock = clock;
     A.stage = st;
-    prim_kernel<R><<<blocks_for(NN), 256, 0, s>>>(A);
+    A.dinc = reinterpret_cast<float*>(w.u1);   // the FP32 increments reuse the stage-1 state region
+    if constexpr (sizeof(R) == sizeof(float))
+    {
+        if (mixed_mode == MIX_INCREMENT) prim_kernel<R, MIX_INCREMENT><<<blocks_for(NN), 256, 0, s>>>(A);
+        else if (mixed_mode == MIX_FROM_INCREMENT) prim_kernel<R, MIX_FROM_INCREMENT><<<blocks_for(NN), 256, 0, s>>>(A);
+        else prim_kernel<R, MIX_PLAIN><<<blocks_for(NN), 256, 0, s>>>(A);
+    }
+    else prim_kernel<R, MIX_PLAIN><<<blocks_for(NN), 256, 0, s>>>(A);
     if (int r = launch_status("mhd prim_kernel")) return r;
     dt_kernel<<<1, 32, 0, s>>>(clock, st, mp->cfl, A.dl, 0);
     if (int r = launch_status("mhd dt_kernel")) return r;
@@ -699,7 +778,14 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     face_kernel<R, 1><<<blocks_for(nb(N, 1)), 256, 0, s>>>(A);
     face_kernel<R, 2><<<blocks_for(nb(N, 2)), 256, 0, s>>>(A);
     if (int r = launch_status("mhd face_kernel")) return r;
-    update_kernel<R><<<blocks_for(NN + nb(N, 0) + nb(N, 1) + nb(N, 2)), 256, 0, s>>>(A);
+    const int ub = blocks_for(NN + nb(N, 0) + nb(N, 1) + nb(N, 2));
+    if constexpr (sizeof(R) == sizeof(float))
+    {
+        if (mixed_mode == MIX_INCREMENT) update_kernel<R, MIX_INCREMENT><<<ub, 256, 0, s>>>(A);
+        else if (mixed_mode == MIX_FROM_INCREMENT) update_kernel<R, MIX_FROM_INCREMENT><<<ub, 256, 0, s>>>(A);
+        else update_kernel<R, MIX_PLAIN><<<ub, 256, 0, s>>>(A);
+    }
+    else update_kernel<R, MIX_PLAIN><<<ub, 256, 0, s>>>(A);
     return launch_status("mhd update_kernel");
 }
 
@@ -708,8 +794,8 @@ int run_stage(int precision, const mara_mhd_params* mp, const Workspace& w, Cloc
               const double* const bavg[3], double* u_out, double* const b_out[3], cudaStream_t s)
 {
     if (precision == MARA_MIXED)
-        return stage<float>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, s);
-    return stage<double>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, s);
+        return stage<float>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, MIX_PLAIN, s);
+    return stage<double>(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out, MIX_PLAIN, s);
 }
 
 } // namespace mhd
@@ -784,10 +870,24 @@ int mara_mhd_advance(const mara_mhd_params* mp, double* uc, double* bf1, double*
     {
         dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);
         if (int r = launch_status("mhd dt_kernel")) return r;
-        // stage 1: (u1, b1) = advance_mhd_ct(u0, b0) with its own dt
-        if (int r = run_stage(precision, mp, w, c, 0, uc, NN, 1, b0c, nullptr, nullptr, w.u1, w.b1, s)) return r;
-        // stage 2: u0 <- u0/2 + advance_mhd_ct(u1, b1)/2, in place (each element reads its own u0)
-        if (int r = run_stage(precision, mp, w, c, 1, w.u1, NN, 1, b1c, uc, b0c, uc, b0, s)) return r;
+        if (precision == MARA_MIXED)
+        {
+            // stage 1: b1 = advance(b0) in FP64; the cells keep only the FP32
+            // increment d1 = u1 - u0. Stage 2 reads u1 as u0 + d1 and writes
+            // u0 + (d1 + d2) / 2, which is u0/2 + (u1 + d2)/2 to FP32 rounding
+            // of the increments.
+            if (int r = stage<float>(mp, w, c, 0, uc, NN, 1, b0c, nullptr, nullptr, nullptr, w.b1, MIX_INCREMENT, s))
+                return r;
+            if (int r = stage<float>(mp, w, c, 1, uc, NN, 1, b1c, nullptr, b0c, uc, b0, MIX_FROM_INCREMENT, s))
+                return r;
+        }
+        else
+        {
+            // stage 1: (u1, b1) = advance_mhd_ct(u0, b0) with its own dt
+            if (int r = run_stage(precision, mp, w, c, 0, uc, NN, 1, b0c, nullptr, nullptr, w.u1, w.b1, s)) return r;
+            // stage 2: u0 <- u0/2 + advance_mhd_ct(u1, b1)/2, in place (each element reads its own u0)
+            if (int r = run_stage(precision, mp, w, c, 1, w.u1, NN, 1, b1c, uc, b0c, uc, b0, s)) return r;
+        }
         clock_end_kernel<<<1, 32, 0, s>>>(c, 2);
         if (int r = launch_status("mhd clock_end_kernel")) return r;
     }
