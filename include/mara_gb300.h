@@ -196,6 +196,67 @@ int mara_minidisk_advance_noalloc(const mara_minidisk_params* sd, double* u, mar
                                   int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
                                   void* stream);
 
+/* ---------------------------------------------------------------- minidisk time series */
+/* Diagnostics of a minidisk run: the time series of forces, work and orbital
+ * element evolution that the reference driver lists as to do
+ * (problems/minidisk.cpp:69) and schedules as a side effect without writing
+ * it (schedule_t::time_series, problems/minidisk.hpp:64-68). One rate vector
+ * holds sums over all cells of the cell area times:
+ *    0, 1   mass removal rate of sink 1, 2: Sigma sr_k, with sr_k the sink
+ *           rate field (problems/minidisk_scheme.cpp:57-65)
+ *    2..5   momentum removal rate of sink 1 (x, y), then of sink 2: (Sigma vx, Sigma vy) sr_k
+ *    6..9   gravitational force of the gas on body 1 (x, y), then on body 2:
+ *           -Sigma g_k, with g_k = two_body::gravitational_acceleration
+ *           (src/physics_two_body.hpp:209-218) of body k at the cell
+ *    10     mass source rate of the outer buffer: (Sigma_init - Sigma) br
+ *           (buffer_rate_field, problems/minidisk_scheme.cpp:47-55)
+ *    11     disk mass: Sigma
+ *    12     disk angular momentum about the origin: x Sigma vy - y Sigma vx
+ * and, from the force sums and the binary at the stage time,
+ *    13, 14 gravitational torque on body 1, 2: x_k F_ky - y_k F_kx
+ *    15     power of the gas's gravity on the binary: F_1 . v_1 + F_2 . v_2.
+ * Positions, velocities and forces are in the rotating frame (the binary's
+ * velocities rotated with its positions, as two_body::rotate does), so the
+ * power equals the inertial-frame power. Sums 0-12 are reductions fused into
+ * the mixed-precision stage kernels (FP32 per thread, FP64 across warps); the
+ * FP64 path reduces the stage input in FP64 with one extra kernel per stage. */
+#define MARA_DIAG_COUNT 16
+typedef struct mara_minidisk_diagnostics {
+    double rate[2][MARA_DIAG_COUNT];   /* the last step's stage inputs: stage 1 at t, stage 2 at t + dt (RK1: rate[0]) */
+    double integral[MARA_DIAG_COUNT];  /* time integrals over completed steps with the update's RK weights:
+                                          dt (rate[0] + rate[1]) / 2 (RK2), dt rate[0] (RK1); entries 11 and 12
+                                          hold the values at the start of the last completed step instead */
+    int64_t steps;                     /* completed steps in the integrals */
+} mara_minidisk_diagnostics;
+
+/* Zero a device mara_minidisk_diagnostics (stream-ordered). */
+int mara_minidisk_diagnostics_reset(mara_minidisk_diagnostics* diag, void* stream);
+
+/* mara_minidisk_advance that also accumulates the diagnostics of every step
+ * into diag (device memory; NULL gives mara_minidisk_advance). */
+int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                               int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                               void* workspace, mara_minidisk_diagnostics* diag, void* stream);
+
+/* The rate vector of one state at one time, in FP64: u (device, SoA), plus
+ * the FP32 increment d1 when not NULL (u + d1, a mixed RK2 stage-2 input);
+ * the binary at `time` from two_body::orbital_state + rotate. out: device,
+ * MARA_DIAG_COUNT doubles. */
+int mara_minidisk_rates(const mara_minidisk_params* sd, const double* u, const float* d1, double time,
+                        double* out, void* stream);
+
+/* two_body::recover_orbital_elements (src/physics_two_body.hpp:284-379), host
+ * FP64, G = 1: state = {m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2} at time t
+ * -> out = {a, M, q, e, x_cm, y_cm, vx_cm, vy_cm, pomega, tau}. An unbound
+ * state (E >= 0) returns MARA_ERR_ARGUMENT, as the reference throws. */
+int mara_two_body_elements(const double* state, double time, double* out);
+
+/* Rates of change of (a, M, q, e) implied by a rate vector (entries 0-9)
+ * acting on the binary state: dm_k/dt = sink mass rate k, d(m_k v_k)/dt =
+ * gas force + sink momentum rate k, positions fixed; central difference of
+ * mara_two_body_elements. Host FP64. out: 4 doubles. */
+int mara_two_body_element_rates(const double* state, double time, const double* rates, double* out);
+
 /* Columns per thread of the mixed-precision sweep kernels, process-wide:
  * 0 = automatic (two wherever N is even and the buffers are 16-byte aligned;
  * else one), 1 or 2 to force a form (2 still falls back to 1 where it cannot

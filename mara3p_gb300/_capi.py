@@ -49,6 +49,20 @@ class MinidiskClock(ctypes.Structure):
     ]
 
 
+DIAG_COUNT = 16
+
+
+class MinidiskDiagnostics(ctypes.Structure):
+    """mara_minidisk_diagnostics: per-stage rate vectors of the last step,
+    their time integrals over the completed steps, and the step count."""
+
+    _fields_ = [
+        ("rate", (ctypes.c_double * DIAG_COUNT) * 2),
+        ("integral", ctypes.c_double * DIAG_COUNT),
+        ("steps", ctypes.c_int64),
+    ]
+
+
 # (name, restype, argtypes) for every exported entry point of include/mara_gb300.h.
 _vp = ctypes.c_void_p
 _MP = ctypes.POINTER(MinidiskParams)
@@ -76,6 +90,12 @@ SIGNATURES = {
     "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp]),
     "mara_minidisk_sweep_columns": (ctypes.c_int, [ctypes.c_int32]),
+    "mara_minidisk_diagnostics_reset": (ctypes.c_int, [_vp, _vp]),
+    "mara_minidisk_advance_diag": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                  ctypes.c_int32, _vp, _vp, _vp]),
+    "mara_minidisk_rates": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_double, _vp, _vp]),
+    "mara_two_body_elements": (ctypes.c_int, [c_double_p, ctypes.c_double, c_double_p]),
+    "mara_two_body_element_rates": (ctypes.c_int, [c_double_p, ctypes.c_double, c_double_p, c_double_p]),
     "mara_minidisk_advance_noalloc": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                      ctypes.c_int32, _vp]),
     "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,

@@ -374,21 +374,21 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
 }
 
 // ------------------------------------------------------------- warp-strip sweep (mixed path)
-template<int KIND, int COLS>
+template<int KIND, int COLS, bool DIAG>
 __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A)
 {
     const int warp = blockIdx.x * SW_WARPS + (threadIdx.x >> 5);
     const int sx = warp / A.tiles_y, sy = warp - sx * A.tiles_y;
     const int i0 = sx * A.sweep_rows;
     if (i0 >= A.N) return;                    // uniform per warp
-    if (COLS == 2) sweep_strip2<KIND>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
-    else sweep_strip<KIND>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
+    if (COLS == 2) sweep_strip2<KIND, DIAG>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
+    else sweep_strip<KIND, DIAG>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
 }
 
 // Rows per warp: enough segments along x that all strips run as one wave of
 // resident warps (no half-empty tail wave), but never fewer than 32 rows so
 // the two halo rows stay a small overhead.
-template<int KIND, int COLS>
+template<int KIND, int COLS, bool DIAG>
 int launch_sweep(Args A, cudaStream_t s)
 {
     static int blocks_per_sm[64] = {};
@@ -398,7 +398,7 @@ int launch_sweep(Args A, cudaStream_t s)
     if (blocks_per_sm[dev & 63] == 0)
     {
         int b = 0, n = 0;
-        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS>, SW_WARPS * 32, 0));
+        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS, DIAG>, SW_WARPS * 32, 0));
         MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
         sm_count[dev & 63] = n;
         blocks_per_sm[dev & 63] = b > 0 ? b : 1;
@@ -410,7 +410,7 @@ int launch_sweep(Args A, cudaStream_t s)
     A.sweep_rows = std::max(32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
     const int warps = strips_x * A.tiles_y;
-    sweep_kernel<KIND, COLS><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
+    sweep_kernel<KIND, COLS, DIAG><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
     return launch_status("minidisk sweep kernel");
 }
 
@@ -428,7 +428,87 @@ template<int KIND>
 int launch_sweep_auto(const Args& A, cudaStream_t s)
 {
     const bool two = g_sweep_columns != 1 && two_column_ok(A);
-    return two ? launch_sweep<KIND, 2>(A, s) : launch_sweep<KIND, 1>(A, s);
+    if (A.diag) return two ? launch_sweep<KIND, 2, true>(A, s) : launch_sweep<KIND, 1, true>(A, s);
+    return two ? launch_sweep<KIND, 2, false>(A, s) : launch_sweep<KIND, 1, false>(A, s);
+}
+
+// ------------------------------------------------------------- diagnostics (FP64)
+// The rate-vector sums 0..12 of a state u (+ the FP32 increment d1) in FP64,
+// the source-term fields as problems/minidisk_scheme.cpp:47-76 and
+// src/physics_two_body.hpp:200-218 define them. The binary comes from the
+// clock row A.stage, or A.bin when A.clock is null.
+__global__ void __launch_bounds__(256) rates_kernel(const Args A, const double* u, const float* d1, double* out)
+{
+    __shared__ double part[DIAG_SUMS][8];
+    const int N = A.N;
+    const int64_t NN = int64_t(N) * N;
+    const double* bin = A.clock ? A.clock->binary[A.stage] : A.bin;
+    const double m1 = bin[0], x1 = bin[1], y1 = bin[2], m2 = bin[3], x2 = bin[4], y2 = bin[5];
+    double acc[DIAG_SUMS] = {};
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(c / N), j = int(c - int64_t(i) * N);
+        // cell centres: adjacent_mean of the block's vertex linspace
+        const int ki = i % A.n, kj = j % A.n;
+        const uint64_t bi = uint64_t(i / A.n), bj = uint64_t(j / A.n);
+        const double x = 0.5 * (vertex(A.R, A.n, A.level, bi, ki) + vertex(A.R, A.n, A.level, bi, ki + 1));
+        const double y = 0.5 * (vertex(A.R, A.n, A.level, bj, kj) + vertex(A.R, A.n, A.level, bj, kj + 1));
+        double w[3];
+        for (int k = 0; k < 3; ++k) w[k] = u[k * NN + c] + (d1 ? double(d1[k * NN + c]) : 0.0);
+        auto sink = [&](double px, double py) {
+            const double dx = x - px, dy = y - py;
+            return A.sink_rate * exp(-pow(0.0 + dx * dx + dy * dy, 3.0) / A.s6);
+        };
+        auto accel = [&](double m, double px, double py, double& ax, double& ay) {
+            const double dx = x - px, dy = y - py;
+            const double g = -1.0 * m / pow(dx * dx + dy * dy + A.rs2, 1.5);
+            ax = g * dx;
+            ay = g * dy;
+        };
+        const double sr1 = sink(x1, y1), sr2 = sink(x2, y2);
+        double a1x, a1y, a2x, a2y;
+        accel(m1, x1, y1, a1x, a1y);
+        accel(m2, x2, y2, a2x, a2y);
+        const double rr = sqrt(0.0 + x * x + y * y);
+        const double br = 0.5 * A.buffer_rate * (1.0 + tanh((rr - A.R) / A.buffer_scale));
+        const double v[DIAG_SUMS] = {
+            w[0] * sr1, w[0] * sr2, w[1] * sr1, w[2] * sr1, w[1] * sr2, w[2] * sr2,
+            -w[0] * a1x, -w[0] * a1y, -w[0] * a2x, -w[0] * a2y,
+            (1.0 - w[0]) * br, w[0], x * w[2] - y * w[1]};
+        for (int k = 0; k < DIAG_SUMS; ++k) acc[k] += v[k];
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; k < DIAG_SUMS; ++k)
+    {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) part[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < DIAG_SUMS)
+    {
+        double v = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) v += part[threadIdx.x][w];
+        atomicAdd(out + threadIdx.x, v * (A.dl * A.dl));
+    }
+}
+
+// Entries 13..15 of a rate row from its force sums and the binary (position
+// and velocity) at the row's time.
+__global__ void rates_finish_kernel(double* r, Binary b)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    r[13] = b.x1 * r[7] - b.y1 * r[6];
+    r[14] = b.x2 * r[9] - b.y2 * r[8];
+    r[15] = (r[6] * b.vx1 + r[7] * b.vy1) + (r[8] * b.vx2 + r[9] * b.vy2);
+}
+
+int launch_rates(const Args& A, const double* u, const float* d1, double* out, cudaStream_t s)
+{
+    const int64_t NN = int64_t(A.N) * A.N;
+    const int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
+    rates_kernel<<<blocks, 256, 0, s>>>(A, u, d1, out);
+    return launch_status("minidisk rates_kernel");
 }
 
 // ------------------------------------------------------------- clock kernel
@@ -669,6 +749,12 @@ int grid_stage(Args A, int kind, cudaStream_t s)
 {
     if (A.N >= 64 && kind == K_MIX1) return A.d_out ? launch_sweep_auto<K_MIXD>(A, s) : launch_sweep_auto<K_MIX1>(A, s);
     if (A.N >= 64 && kind == K_MIX2) return launch_sweep_auto<K_MIX2>(A, s);
+    if (A.diag)
+    {
+        // no fused sums outside the mixed sweeps: reduce the stage input first
+        if (int r = launch_rates(A, A.u_in, kind == K_MIX2 ? A.d1 : nullptr, A.diag, s)) return r;
+        A.diag = nullptr;
+    }
     int tiles_x = (A.N + TX - 1) / TX;
     A.tiles_y = (A.N + TY - 1) / TY;
     int tiles = tiles_x * A.tiles_y;
@@ -684,6 +770,7 @@ int grid_stage(Args A, int kind, cudaStream_t s)
 ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, int end_step, int begin_step)
 {
     ClockArgs a;
+    a.diag = nullptr;
     a.R = sd->domain_radius;
     a.dl = cell_size(sd, sd->depth);
     a.cfl = sd->cfl;
@@ -699,9 +786,11 @@ ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, 
 }
 
 int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
-               int end_step, int begin_step, cudaStream_t s)
+               int end_step, int begin_step, cudaStream_t s, mara_minidisk_diagnostics* diag = nullptr)
 {
-    clock_kernel<<<1, 32, 0, s>>>(clock, clock_args(sd, dt_mode, rk_order, end_step, begin_step));
+    ClockArgs a = clock_args(sd, dt_mode, rk_order, end_step, begin_step);
+    a.diag = diag;
+    clock_kernel<<<1, 32, 0, s>>>(clock, a);
     return launch_status("minidisk clock kernel");
 }
 
@@ -863,6 +952,13 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
                           int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
                           void* workspace, void* stream)
 {
+    return mara_minidisk_advance_diag(sd, u, clock, steps, rk_order, precision, dt_mode, workspace, nullptr, stream);
+}
+
+int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
+                               int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
+                               void* workspace, mara_minidisk_diagnostics* diag, void* stream)
+{
     if (int r = check_params(sd)) return r;
     MARA_REQUIRE(u && clock && workspace, "mara_minidisk_advance: null buffer");
     MARA_REQUIRE(steps >= 0, "mara_minidisk_advance: negative step count");
@@ -882,39 +978,45 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
     double* cur = u;
     double* alt = ws_state;
 
+    double* rate0 = diag ? diag->rate[0] : nullptr;
+    double* rate1 = diag ? diag->rate[1] : nullptr;
+
     // a held formula dt is chosen by the call's first step
-    if (int r = clock_step(sd, clock, dt_mode == MARA_DT_FORMULA_HELD ? MARA_DT_FORMULA : dt_mode, rk_order, 0, 1, s))
+    if (int r = clock_step(sd, clock, dt_mode == MARA_DT_FORMULA_HELD ? MARA_DT_FORMULA : dt_mode, rk_order, 0, 1, s,
+                           diag))
         return r;
     for (int step = 0; step < steps; ++step)
     {
         if (precision == MARA_FP64 && rk_order == 2)
         {
-            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = ws_state;
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = ws_state; a1.diag = rate0;
             if (int r = grid_stage(a1, K_FP64, s)) return r;
             Args a2 = A; a2.stage = 1; a2.u_in = ws_state; a2.u_avg = cur; a2.u_out = cur; a2.amax = amax;
+            a2.diag = rate1;
             if (int r = grid_stage(a2, K_FP64, s)) return r;
         }
         else if (precision == MARA_FP64)
         {
-            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax;
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax; a1.diag = rate0;
             if (int r = grid_stage(a1, K_FP64, s)) return r;
             std::swap(cur, alt);
         }
         else if (rk_order == 2)
         {
-            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1;
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1; a1.diag = rate0;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = alt; a2.amax = amax;
+            a2.diag = rate1;
             if (int r = grid_stage(a2, K_MIX2, s)) return r;
             std::swap(cur, alt);
         }
         else
         {
-            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax;
+            Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax; a1.diag = rate0;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             std::swap(cur, alt);
         }
-        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s)) return r;
+        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag)) return r;
     }
     if (cur != u)
         MARA_CUDA(cudaMemcpyAsync(u, cur, 3 * NN * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -998,6 +1100,27 @@ int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clo
     MARA_REQUIRE(rk_order == 1 || rk_order == 2, "mara_minidisk_clock_update: rk_order must be 1 or 2");
     MARA_REQUIRE(dt_mode >= MARA_DT_FORMULA && dt_mode <= MARA_DT_FORMULA_HELD, "mara_minidisk_clock_update: bad dt_mode");
     return clock_step(sd, clock, dt_mode, rk_order, end_step != 0, begin_step != 0, as_stream(stream));
+}
+
+int mara_minidisk_diagnostics_reset(mara_minidisk_diagnostics* diag, void* stream)
+{
+    MARA_REQUIRE(diag != nullptr, "mara_minidisk_diagnostics_reset: diag is null");
+    MARA_CUDA(cudaMemsetAsync(diag, 0, sizeof *diag, as_stream(stream)));
+    return MARA_OK;
+}
+
+int mara_minidisk_rates(const mara_minidisk_params* sd, const double* u, const float* d1, double time,
+                        double* out, void* stream)
+{
+    if (int r = check_params(sd)) return r;
+    MARA_REQUIRE(u && out, "mara_minidisk_rates: null buffer");
+    cudaStream_t s = as_stream(stream);
+    Args A = base_args(sd);
+    set_binary(A, sd, time);
+    MARA_CUDA(cudaMemsetAsync(out, 0, MARA_DIAG_COUNT * sizeof(double), s));
+    if (int r = launch_rates(A, u, d1, out, s)) return r;
+    rates_finish_kernel<<<1, 32, 0, s>>>(out, binary_state(sd->mass_ratio, sd->eccentricity, sd->omega_frame, time));
+    return launch_status("minidisk rates_finish_kernel");
 }
 
 } // extern "C"

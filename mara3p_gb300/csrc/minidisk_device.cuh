@@ -56,8 +56,13 @@ struct Args
     float* d_out;          // K_MIX1 + RK2: increment out
     const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
     unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
+    double* diag;          // optional: rate row of this stage (diagnostic sums 0..12 of the stage input)
     FloatConsts f;
 };
+
+// Diagnostic sums taken per cell (the rate-vector entries 0..12 of
+// mara_minidisk_diagnostics); 13..15 follow from them in the clock kernel.
+constexpr int DIAG_SUMS = 13;
 
 // ------------------------------------------------------------- geometry
 // vertex_positions (problems/minidisk_scheme.cpp:101-116): linspace of block b
@@ -283,9 +288,12 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
 // the outer buffer (problems/minidisk_scheme.cpp:337-352). uc returns the
 // FP32 conserved state the increment was computed from, pot returns
 // 1/sqrt(r^2 + rs^2), from which the cell-centre sound speed follows.
-template<typename T>
+__device__ __forceinline__ void diag_add(float& a, float v) { a += v; }
+__device__ __forceinline__ void diag_add(float& a, float2 v) { a += v.x + v.y; }
+
+template<typename T, bool DIAG = false>
 __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc[3], const T dfx[3], const T dfy[3],
-                                      const float bf[6], float dtf, T du[3], T uc[3], T& pot)
+                                      const float bf[6], float dtf, T du[3], T uc[3], T& pot, float* acc = nullptr)
 {
     uc[0] = pc[0];
     uc[1] = vmul(pc[0], pc[1]);
@@ -314,6 +322,24 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
     ay = vfma(bc<T>(F.omega2), y, ay);
     ay = vfma(bc<T>(-F.two_omega), pc[1], ay);
     const T srs = vadd(sr1, sr2);
+    if constexpr (DIAG)
+    {
+        // the rate-vector sums of this cell (times the cell area on the flush)
+        const T sg1 = vmul(pc[0], g1), sg2 = vmul(pc[0], g2);
+        diag_add(acc[0], vmul(pc[0], sr1));
+        diag_add(acc[1], vmul(pc[0], sr2));
+        diag_add(acc[2], vmul(uc[1], sr1));
+        diag_add(acc[3], vmul(uc[2], sr1));
+        diag_add(acc[4], vmul(uc[1], sr2));
+        diag_add(acc[5], vmul(uc[2], sr2));
+        diag_add(acc[6], vneg(vmul(sg1, dx1)));
+        diag_add(acc[7], vneg(vmul(sg1, dy1)));
+        diag_add(acc[8], vneg(vmul(sg2, dx2)));
+        diag_add(acc[9], vneg(vmul(sg2, dy2)));
+        diag_add(acc[10], vmul(vsub(bc<T>(1.0f), pc[0]), br));
+        diag_add(acc[11], pc[0]);
+        diag_add(acc[12], vsub(vmul(x, uc[2]), vmul(y, uc[1])));
+    }
     T src[3];
     for (int k = 0; k < 3; ++k) src[k] = vfma(vsub(ui[k], uc[k]), br, vneg(vmul(uc[k], srs)));
     src[1] = vfma(pc[0], ax, src[1]);
@@ -367,13 +393,13 @@ __device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, flo
 // FP64 state u_in + du (with the RK2 average of the two increments in stage
 // 2). The CFL wavespeed of the new state is taken from its FP32 image: the
 // stage input plus du (RK1), or u0 + (d1 + du)/2 = u1 + (du - d1)/2 (RK2).
-template<int KIND>
+template<int KIND, bool DIAG = false>
 __device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
                                   const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                  const CellIn<float>& in, float& local_max)
+                                  const CellIn<float>& in, float& local_max, float* acc = nullptr)
 {
     float du[3], uc[3], pot;
-    cell_increment<float>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot);
+    cell_increment<float, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
     if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
@@ -390,13 +416,13 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
 }
 
 // The pair form: columns idx and idx + 1 of one row (idx even).
-template<int KIND>
+template<int KIND, bool DIAG = false>
 __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const float2 pc[3], const float2 dfx[3],
                                    const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                   const CellIn<float2>& in, float& local_max)
+                                   const CellIn<float2>& in, float& local_max, float* acc = nullptr)
 {
     float2 du[3], uc[3], pot;
-    cell_increment<float2>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot);
+    cell_increment<float2, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
     if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(A.d_out + k * NN + idx) = du[k];
@@ -413,6 +439,19 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
     if (A.amax)
         local_max = fmaxf(local_max, fmaxf(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, pot.x),
                                            wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, pot.y)));
+}
+
+// A warp's diagnostic sums into the stage's rate row: FP32 per lane, a
+// shuffle reduction, then FP64 atomics scaled by the cell area.
+__device__ inline void diag_flush(const Args& A, const float* acc)
+{
+    const double da = A.dl * A.dl;
+    for (int k = 0; k < DIAG_SUMS; ++k)
+    {
+        float v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(A.diag + k, double(v) * da);
+    }
 }
 
 // ------------------------------------------------------------- warp-strip sweep (mixed path)
@@ -470,7 +509,7 @@ __device__ inline void slope_y(const float p[3], float theta, float g[3])
 
 // Rows [i0, i1) of column strip sy of the mesh A describes: the body of a
 // sweep warp. Called with a warp-uniform (i0, i1, sy).
-template<int KIND>
+template<int KIND, bool DIAG = false>
 __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int sy)
 {
     const int lane = threadIdx.x & 31;
@@ -521,6 +560,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
     face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
 
     float local_max = 0.0f;
+    float acc[DIAG ? DIAG_SUMS : 1] = {};
     for (int i = i0; i < i1; ++i)
     {
         float p2[3], gx1[3], gy1[3], fxp[3];
@@ -549,7 +589,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell<KIND>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max);
+            mixed_cell<KIND, DIAG>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -560,6 +600,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
             fxm[k] = fxp[k];
         }
     }
+    if constexpr (DIAG) diag_flush(A, acc);
     if (A.amax)
     {
         for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
@@ -622,7 +663,7 @@ __device__ inline void slope_y2(const float2 p[3], float theta, float2 g[3])
     }
 }
 
-template<int KIND>
+template<int KIND, bool DIAG = false>
 __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy)
 {
     const int lane = threadIdx.x & 31;
@@ -673,6 +714,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     face_flux_f<0, float2>(pm1, p0, gxm1, gx0, gym1, gy0, bc<float2>(fmaf(float(i0), F.dl, -F.R)), yc, F, fxm);
 
     float local_max = 0.0f;
+    float acc[DIAG ? DIAG_SUMS : 1] = {};
     for (int i = i0; i < i1; ++i)
     {
         float2 p2[3], gx1[3], gy1[3], fxp[3];
@@ -702,7 +744,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell2<KIND>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max);
+            mixed_cell2<KIND, DIAG>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin,
+                                    local_max, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -713,6 +756,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             fxm[k] = fxp[k];
         }
     }
+    if constexpr (DIAG) diag_flush(A, acc);
     if (A.amax)
     {
         for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
@@ -727,7 +771,33 @@ struct ClockArgs
     int dt_mode, rk_order;
     int end_step;     // 1: finish the step that just ran (advance time, iteration)
     int begin_step;   // 1: choose dt and stage binaries of the next step
+    mara_minidisk_diagnostics* diag;   // optional: integrate the step's rates (end), clear them (begin)
 };
+
+// Complete the rate rows of the step that ran (torques and power from the
+// force sums and the binary at each stage time) and add them to the time
+// integrals with the RK weights of the update.
+__device__ inline void finish_diagnostics(const mara_minidisk_clock* c, const ClockArgs& a)
+{
+    mara_minidisk_diagnostics* d = a.diag;
+    const double t = c->time, dt = c->dt;
+    for (int s = 0; s < a.rk_order; ++s)
+    {
+        double* r = d->rate[s];
+        const Binary b = binary_state(a.mass_ratio, a.eccentricity, a.omega, s == 0 ? t : t + dt);
+        r[13] = b.x1 * r[7] - b.y1 * r[6];
+        r[14] = b.x2 * r[9] - b.y2 * r[8];
+        r[15] = (r[6] * b.vx1 + r[7] * b.vy1) + (r[8] * b.vx2 + r[9] * b.vy2);
+    }
+    for (int k = 0; k < MARA_DIAG_COUNT; ++k)
+    {
+        if (k == 11 || k == 12)
+            d->integral[k] = d->rate[0][k];
+        else
+            d->integral[k] += a.rk_order == 2 ? dt * (0.5 * (d->rate[0][k] + d->rate[1][k])) : dt * d->rate[0][k];
+    }
+    d->steps += 1;
+}
 
 __device__ inline void store_binary(double* dst, const Binary& b)
 {
@@ -738,6 +808,7 @@ __device__ inline void store_binary(double* dst, const Binary& b)
 // iteration count) and/or choose the next dt and the stage binaries.
 __device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a)
 {
+    if (a.end_step && a.diag) finish_diagnostics(c, a);
     if (a.end_step)
     {
         double t = c->time, dt = c->dt;
@@ -774,6 +845,8 @@ __device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a)
         store_binary(c->binary[0], binary_state(a.mass_ratio, a.eccentricity, a.omega, t));
         store_binary(c->binary[1], binary_state(a.mass_ratio, a.eccentricity, a.omega, t + dt));
         c->max_wavespeed = 0.0;
+        if (a.diag)
+            for (int k = 0; k < 2 * MARA_DIAG_COUNT; ++k) a.diag->rate[k / MARA_DIAG_COUNT][k % MARA_DIAG_COUNT] = 0.0;
     }
 }
 

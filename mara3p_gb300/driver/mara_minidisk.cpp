@@ -21,8 +21,17 @@
 // Extensions (not in the reference): plm_theta (the reference hard-codes 2),
 // rk (the reference's driver is forward Euler), precision fp64|mixed,
 // dt formula|cfl, seed / perturbation (seeded density perturbation of the
-// initial state), graph (replay each fold batch from a CUDA graph), and
-// dry (print the configuration and exit without touching the GPU).
+// initial state), graph (replay each fold batch from a CUDA graph), dry
+// (print the configuration and exit without touching the GPU), and tsi:
+// every tsi orbits the time_series side effect (the schedule entry the
+// reference keeps but never writes, problems/minidisk.hpp:64-68; listed as
+// to do at problems/minidisk.cpp:69) appends one row to time_series.dat:
+// time, iteration, the time integrals of the diagnostics rate vector
+// (mara_minidisk_diagnostics, accumulated on the device every step), the
+// last step's mean rates, the binary's semi-major axis and eccentricity
+// (two_body::recover_orbital_elements) and the rates of (a, M, q, e) that
+// the gas's forces and accretion imply. Checkpoints carry the integrals
+// (time_series.json), so a restart continues them.
 #include <cuda_runtime.h>
 #include <chrono>
 #include <cmath>
@@ -81,6 +90,7 @@ std::vector<Item> config_template()
         {"perturbation", "double", "0.0", "relative amplitude of the initial density perturbation"},
         {"graph", "int", "1", "replay each fold batch from a CUDA graph"},
         {"dry", "int", "0", "print the configuration and exit"},
+        {"tsi", "double", "0.0", "number of orbits between time-series samples (0: none)"},
     };
 }
 
@@ -347,10 +357,12 @@ struct Run
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_fold = 0;
+    mara_minidisk_diagnostics* diag = nullptr;   // device; with the time series only
 
     ~Run()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (diag) cudaFree(diag);
         if (u) cudaFree(u);
         if (clock) cudaFree(clock);
         if (workspace) cudaFree(workspace);
@@ -370,7 +382,8 @@ struct Run
     {
         if (!use_graph)
         {
-            mara_check(mara_minidisk_advance(&p, u, clock, fold, rk, precision, dt_mode, workspace, stream), "advance");
+            mara_check(mara_minidisk_advance_diag(&p, u, clock, fold, rk, precision, dt_mode, workspace, diag, stream),
+                       "advance");
             return;
         }
         if (!graph || graph_fold != fold)
@@ -379,7 +392,7 @@ struct Run
             graph = nullptr;
             cudaGraph_t g = nullptr;
             cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed), "begin capture");
-            const int r = mara_minidisk_advance(&p, u, clock, fold, rk, precision, dt_mode, workspace, stream);
+            const int r = mara_minidisk_advance_diag(&p, u, clock, fold, rk, precision, dt_mode, workspace, diag, stream);
             const cudaError_t e = cudaStreamEndCapture(stream, &g);
             mara_check(r, "advance (capture)");
             cuda_check(e, "end capture");
@@ -388,6 +401,14 @@ struct Run
             graph_fold = fold;
         }
         cuda_check(cudaGraphLaunch(graph, stream), "graph launch");
+    }
+
+    mara_minidisk_diagnostics read_diagnostics() const
+    {
+        mara_minidisk_diagnostics d;
+        cuda_check(cudaMemcpyAsync(&d, diag, sizeof d, cudaMemcpyDeviceToHost, stream), "read diagnostics");
+        cuda_check(cudaStreamSynchronize(stream), "read diagnostics");
+        return d;
     }
 };
 
@@ -417,6 +438,15 @@ void write_checkpoint(const fs::path& dir, const Config& cfg, const Schedule& sc
                json_number(sch.time_series_next_due) + ", \"count\": " + std::to_string(sch.time_series_count) + "}\n}\n");
     write_file(tmp / "solution.json", "{\n  \"iteration\": " + std::to_string(c.iteration) + ",\n  \"time\": " +
                                       json_number(c.time) + "\n}\n");
+    if (run.diag)
+    {
+        const mara_minidisk_diagnostics d = run.read_diagnostics();
+        // the integrals keyed by their entry number (the reader knows objects, not arrays)
+        std::string ts = "{\n  \"steps\": " + std::to_string(d.steps) + ",\n  \"integral\": {";
+        for (int k = 0; k < MARA_DIAG_COUNT; ++k)
+            ts += "\"" + std::to_string(k) + "\": " + json_number(d.integral[k]) + (k + 1 < MARA_DIAG_COUNT ? ", " : "");
+        write_file(tmp / "time_series.json", ts + "}\n}\n");
+    }
     // every block's conserved tuples (n, n, 3), the reference's nd::shared_array layout
     std::string block(size_t(n) * n * 3 * sizeof(double), '\0');
     for (long bi = 0; bi < nb; ++bi)
@@ -460,6 +490,20 @@ Schedule read_schedule(const fs::path& dir)
 }
 
 // the solution of a checkpoint into the device state; returns (iteration, time)
+// The diagnostics integrals of a checkpoint (zero if it has none) into run.diag.
+void read_time_series(const fs::path& dir, Run& run)
+{
+    mara_minidisk_diagnostics d;
+    std::memset(&d, 0, sizeof d);
+    if (fs::exists(dir / "time_series.json"))
+    {
+        const Json j = JsonReader(read_file(dir / "time_series.json")).parse();
+        d.steps = int64_t(j.at("steps").number);
+        for (int k = 0; k < MARA_DIAG_COUNT; ++k) d.integral[k] = j.at("integral").at(std::to_string(k)).number;
+    }
+    cuda_check(cudaMemcpy(run.diag, &d, sizeof d, cudaMemcpyHostToDevice), "restore diagnostics");
+}
+
 std::pair<long, double> read_solution(const fs::path& dir, Run& run)
 {
     const Json j = JsonReader(read_file(dir / "solution.json")).parse();
@@ -521,6 +565,13 @@ int main_impl(int argc, const char* argv[])
     const int64_t ws = mara_minidisk_workspace_bytes(&run.p, run.rk, run.precision);
     if (ws < 0) mara_check(MARA_ERR_ARGUMENT, "workspace");
     cuda_check(cudaMalloc(&run.workspace, size_t(std::max<int64_t>(ws, 256))), "workspace");
+    const double tsi = cfg.get_double("tsi");
+    if (tsi < 0.0) throw std::invalid_argument("tsi must not be negative");
+    if (tsi > 0.0)
+    {
+        cuda_check(cudaMalloc(&run.diag, sizeof(mara_minidisk_diagnostics)), "diagnostics");
+        mara_check(mara_minidisk_diagnostics_reset(run.diag, run.stream), "diagnostics");
+    }
 
     Schedule schedule;
     const std::string restart = cfg.str("restart");
@@ -530,6 +581,7 @@ int main_impl(int argc, const char* argv[])
     {
         schedule = read_schedule(restart);
         std::tie(iteration, time) = read_solution(restart, run);
+        if (run.diag) read_time_series(restart, run);
     }
     else
     {
@@ -548,7 +600,48 @@ int main_impl(int argc, const char* argv[])
     const int fold = cfg.get_int("fold");
     const bool use_graph = cfg.get_int("graph") != 0;
     const fs::path outdir = cfg.str("outdir");
+    const fs::path ts_file = outdir / "time_series.dat";
+    if (run.diag) fs::create_directories(outdir);
+    if (run.diag && restart.empty())
+    {
+        std::ofstream f(ts_file, std::ios::trunc);
+        f << "# time iteration integral[0..15] rate[0..15] a e da/dt dM/dt dq/dt de/dt\n"
+             "# rate entries: sink mass 1, 2; sink momentum x1 y1 x2 y2; gas force x1 y1 x2 y2; buffer mass;\n"
+             "#   disk mass; disk angular momentum; torque 1, 2; power (integrals of disk mass and angular\n"
+             "#   momentum hold their values at the start of the last step)\n";
+    }
+    auto time_series = [&](double t) {
+        const mara_minidisk_diagnostics d = run.read_diagnostics();
+        const mara_minidisk_clock c = run.read_clock();
+        double mean[MARA_DIAG_COUNT];
+        for (int k = 0; k < MARA_DIAG_COUNT; ++k)
+            mean[k] = run.rk == 2 ? 0.5 * (d.rate[0][k] + d.rate[1][k]) : d.rate[0][k];
+        if (d.steps == 0)
+            for (double& m : mean) m = 0.0;
+        double b[10], el[10], er[4];
+        mara_check(mara_minidisk_binary(&run.p, t, b), "binary");
+        mara_check(mara_two_body_elements(b, t, el), "orbital elements");
+        mara_check(mara_two_body_element_rates(b, t, mean, er), "element rates");
+        std::ofstream f(ts_file, std::ios::app);
+        if (!f) throw std::runtime_error("cannot append to " + ts_file.string());
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%.17g %lld", t, (long long)c.iteration);
+        f << buf;
+        auto put = [&](double x) { std::snprintf(buf, sizeof buf, " %.17g", x); f << buf; };
+        for (double x : d.integral) put(x);
+        for (double x : mean) put(x);
+        put(el[0]);
+        put(el[3]);
+        for (double x : er) put(x);
+        f << "\n";
+    };
     auto side_effects = [&](double t) {
+        if (run.diag && t >= schedule.time_series_next_due)
+        {
+            schedule.time_series_next_due += tsi * binary_period;
+            schedule.time_series_count += 1;
+            time_series(t);
+        }
         if (t >= schedule.checkpoint_next_due)
         {
             char name[32];

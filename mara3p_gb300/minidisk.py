@@ -16,7 +16,7 @@ from dataclasses import dataclass, fields, replace
 
 import torch
 
-from ._capi import MinidiskClock, MinidiskParams, check, lib
+from ._capi import DIAG_COUNT, MinidiskClock, MinidiskDiagnostics, MinidiskParams, check, lib
 
 FP64, MIXED = 0, 1
 DT_FORMULA, DT_CFL, DT_FORMULA_HELD = 0, 1, 2
@@ -74,6 +74,14 @@ def _ptr(t: torch.Tensor | None) -> int | None:
         return None
     if not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
         raise TypeError("expected a contiguous CUDA float64 tensor")
+    return t.data_ptr()
+
+
+def _any_ptr(t: torch.Tensor | None) -> int | None:
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise TypeError("expected a contiguous CUDA tensor")
     return t.data_ptr()
 
 
@@ -146,14 +154,51 @@ def substep(sd: SolverData, u: torch.Tensor, time: float, dt: float, u_avg: torc
     return out
 
 
+# Names of the rate-vector entries (mara_minidisk_diagnostics).
+DIAG_NAMES = ("sink_mass_1", "sink_mass_2", "sink_px_1", "sink_py_1", "sink_px_2", "sink_py_2",
+              "force_x_1", "force_y_1", "force_x_2", "force_y_2", "buffer_mass", "disk_mass",
+              "disk_angular_momentum", "torque_1", "torque_2", "power")
+assert len(DIAG_NAMES) == DIAG_COUNT
+
+
+def rates(sd: SolverData, u: torch.Tensor, time: float, d1: torch.Tensor | None = None) -> dict[str, float]:
+    """The time-series rate vector of the SoA state u (+ FP32 increment d1)
+    at `time`, reduced on the GPU in FP64."""
+    out = torch.zeros(DIAG_COUNT, dtype=torch.float64, device=u.device)
+    check(lib.mara_minidisk_rates(ctypes.byref(sd.to_c()), _ptr(u), _any_ptr(d1), time, _ptr(out), _stream()),
+          "mara_minidisk_rates")
+    return dict(zip(DIAG_NAMES, out.tolist()))
+
+
+def two_body_elements(state: list[float], time: float) -> dict[str, float]:
+    """two_body::recover_orbital_elements (src/physics_two_body.hpp:284-379) of
+    {m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2}; raises MaraError if unbound."""
+    s = (ctypes.c_double * 10)(*state)
+    out = (ctypes.c_double * 10)()
+    check(lib.mara_two_body_elements(s, time, out), "mara_two_body_elements")
+    return dict(zip(("a", "M", "q", "e", "x_cm", "y_cm", "vx_cm", "vy_cm", "pomega", "tau"), out))
+
+
+def element_rates(state: list[float], time: float, rate: list[float] | dict[str, float]) -> dict[str, float]:
+    """d(a, M, q, e)/dt implied by a rate vector acting on the binary state."""
+    r = [rate[k] for k in DIAG_NAMES] if isinstance(rate, dict) else list(rate)
+    s = (ctypes.c_double * 10)(*state)
+    rv = (ctypes.c_double * DIAG_COUNT)(*r)
+    out = (ctypes.c_double * 4)()
+    check(lib.mara_two_body_element_rates(s, time, rv, out), "mara_two_body_element_rates")
+    return dict(zip(("a", "M", "q", "e"), out))
+
+
 class Run:
     """A minidisk run resident on one GPU: SoA state, device clock and workspace.
 
     advance() enqueues whole RK steps; time, dt and the binary position are
-    computed on the device, so steps need no host round trip."""
+    computed on the device, so steps need no host round trip. With
+    diagnostics=True every step also accumulates the time-series rates
+    (mara_minidisk_diagnostics), read back by diagnostics()."""
 
     def __init__(self, sd: SolverData, u: torch.Tensor, time: float = 0.0, rk_order: int = 2,
-                 precision: int = FP64, dt_mode: int = DT_FORMULA):
+                 precision: int = FP64, dt_mode: int = DT_FORMULA, diagnostics: bool = False):
         self.sd = sd
         self.c = sd.to_c()
         self.u = u
@@ -167,11 +212,27 @@ class Run:
         self.clock = torch.zeros(ctypes.sizeof(MinidiskClock), dtype=torch.uint8, device=u.device)
         check(lib.mara_minidisk_clock_init(ctypes.byref(self.c), _ptr(u), time, self.clock.data_ptr(), _stream()),
               "clock_init")
+        self.diag = None
+        if diagnostics:
+            self.diag = torch.zeros(ctypes.sizeof(MinidiskDiagnostics), dtype=torch.uint8, device=u.device)
 
     def advance(self, steps: int) -> None:
-        check(lib.mara_minidisk_advance(ctypes.byref(self.c), _ptr(self.u), self.clock.data_ptr(), steps,
-                                        self.rk_order, self.precision, self.dt_mode,
-                                        self.workspace.data_ptr(), _stream()), "advance")
+        check(lib.mara_minidisk_advance_diag(ctypes.byref(self.c), _ptr(self.u), self.clock.data_ptr(), steps,
+                                             self.rk_order, self.precision, self.dt_mode,
+                                             self.workspace.data_ptr(), _any_ptr(self.diag), _stream()), "advance")
+
+    def diagnostics(self) -> dict:
+        """rate (per stage of the last step), integral and steps of the
+        run's diagnostics, entries named by DIAG_NAMES."""
+        if self.diag is None:
+            raise ValueError("this Run was made without diagnostics")
+        d = MinidiskDiagnostics.from_buffer_copy(self.diag.cpu().numpy().tobytes())
+        return {"rate": [dict(zip(DIAG_NAMES, list(d.rate[s]))) for s in range(2)],
+                "integral": dict(zip(DIAG_NAMES, list(d.integral))), "steps": d.steps}
+
+    def reset_diagnostics(self) -> None:
+        if self.diag is not None:
+            check(lib.mara_minidisk_diagnostics_reset(self.diag.data_ptr(), _stream()), "diagnostics_reset")
 
     def clock_state(self) -> MinidiskClock:
         raw = self.clock.cpu().numpy().tobytes()

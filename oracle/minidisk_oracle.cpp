@@ -510,6 +510,53 @@ void oracle_minidisk_substep_blocks(const oracle_minidisk_params* sd, const doub
 // the stage-1 time t+dt, then u = u0*b + u2*(1-b) with b = 1/2, and
 // t = t0*b + t2*(1-b). dt_mode 0: fixed formula; 1: CFL reduction.
 // Returns the final time; u is updated in place.
+// The time-series rate vector of a state at time t (the sums that the
+// minidisk driver lists as to do, problems/minidisk.cpp:69): the source-term
+// fields of updated_conserved (problems/minidisk_scheme.cpp:47-76, 337-352;
+// src/physics_two_body.hpp:200-218), each summed over all cells times the
+// cell area. out[16]: sink mass rates (2), sink momentum rates (4), gas force
+// on each body (4), buffer mass rate, disk mass, disk angular momentum,
+// torques on each body (2) and power on the binary.
+void oracle_minidisk_rates(const oracle_minidisk_params* sd, const double* u, double t, double* out)
+{
+    const int n = sd->block_size, nb = 1 << sd->depth, N = n * nb;
+    const double R = sd->domain_radius;
+    const double dl = cell_size(*sd, sd->depth);
+    PointMass s1, s2;
+    binary_state(*sd, t, s1, s2);
+    const double s6 = std::pow(sd->sink_radius, 6.0);
+    double acc[13] = {};
+    for (long i = 0; i < N; ++i)
+    {
+        for (long j = 0; j < N; ++j)
+        {
+            const double x = center(R, n, sd->depth, i / n, int(i % n));
+            const double y = center(R, n, sd->depth, j / n, int(j % n));
+            const double w[3] = {u[soa(N, 0, i, j)], u[soa(N, 1, i, j)], u[soa(N, 2, i, j)]};
+            auto sink = [&] (const PointMass& s) {
+                double dx = x - s.x, dy = y - s.y;
+                double r6 = std::pow(0.0 + dx * dx + dy * dy, 3.0);
+                return sd->sink_rate * std::exp(-r6 / s6);
+            };
+            const double sr1 = sink(s1), sr2 = sink(s2);
+            double a1x, a1y, a2x, a2y;
+            gravitational_acceleration(s1, x, y, sd->softening_length, a1x, a1y);
+            gravitational_acceleration(s2, x, y, sd->softening_length, a2x, a2y);
+            const double rr = std::sqrt(0.0 + x * x + y * y);
+            const double br = 0.5 * sd->buffer_rate * (1.0 + std::tanh((rr - R) / sd->buffer_scale));
+            const double v[13] = {
+                w[0] * sr1, w[0] * sr2, w[1] * sr1, w[2] * sr1, w[1] * sr2, w[2] * sr2,
+                -w[0] * a1x, -w[0] * a1y, -w[0] * a2x, -w[0] * a2y,
+                (1.0 - w[0]) * br, w[0], x * w[2] - y * w[1]};
+            for (int k = 0; k < 13; ++k) acc[k] += v[k];
+        }
+    }
+    for (int k = 0; k < 13; ++k) out[k] = acc[k] * (dl * dl);
+    out[13] = s1.x * out[7] - s1.y * out[6];
+    out[14] = s2.x * out[9] - s2.y * out[8];
+    out[15] = (out[6] * s1.vx + out[7] * s1.vy) + (out[8] * s2.vx + out[9] * s2.vy);
+}
+
 double oracle_minidisk_advance(const oracle_minidisk_params* sd, double* u, double t, int32_t steps,
                                int32_t rk_order, int32_t dt_mode, int32_t threads)
 {

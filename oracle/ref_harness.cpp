@@ -329,4 +329,43 @@ double ref_mhd_advance_ct(int32_t N, double time, const double* uc, const double
     }
 }
 
+// two_body::recover_orbital_elements (physics_two_body.hpp:284-379) of a
+// state {m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2} at time t:
+// out = {a, M, q, e, x_cm, y_cm, vx_cm, vy_cm, pomega, tau}; 1 if unbound.
+int ref_two_body_elements(const double* s, double t, double* out)
+{
+    using namespace two_body;
+    using namespace dimensional;
+    point_mass_t c1{unit_mass(s[0]), unit_length(s[1]), unit_length(s[2]), unit_velocity(s[3]), unit_velocity(s[4])};
+    point_mass_t c2{unit_mass(s[5]), unit_length(s[6]), unit_length(s[7]), unit_velocity(s[8]), unit_velocity(s[9])};
+    try
+    {
+        auto p = recover_orbital_elements(orbital_state_t{c1, c2}, unit_time(t));
+        auto el = numeric::get<0>(p);
+        auto o = numeric::get<1>(p);
+        double v[10] = {semimajor_axis(el).value, total_mass(el).value, mass_ratio(el).value, eccentricity(el).value,
+                        numeric::get<0>(o).value, numeric::get<1>(o).value, numeric::get<2>(o).value,
+                        numeric::get<3>(o).value, numeric::get<4>(o).value, numeric::get<5>(o).value};
+        std::memcpy(out, v, sizeof v);
+        return 0;
+    }
+    catch (const std::invalid_argument&)
+    {
+        return 1;
+    }
+}
+
+// two_body::orbital_state (physics_two_body.hpp:128-157) for elements
+// (a, M, q, e) at time t: out = {m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2}.
+void ref_two_body_state(double a, double M, double q, double e, double t, double* out)
+{
+    using namespace two_body;
+    auto s = orbital_state(orbital_elements(a, M, q, e), dimensional::unit_time(t));
+    double v[10] = {s.first.mass.value, s.first.position_x.value, s.first.position_y.value,
+                    s.first.velocity_x.value, s.first.velocity_y.value,
+                    s.second.mass.value, s.second.position_x.value, s.second.position_y.value,
+                    s.second.velocity_x.value, s.second.velocity_y.value};
+    std::memcpy(out, v, sizeof v);
+}
+
 } // extern "C"

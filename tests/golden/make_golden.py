@@ -122,6 +122,41 @@ def binary_fixture(r) -> dict[str, np.ndarray]:
     return {"binary/cases": cases, "binary/times": times, "binary/state": res}
 
 
+def two_body_fixture(r) -> dict[str, np.ndarray]:
+    """two_body::orbital_state and recover_orbital_elements of the reference on
+    on-orbit states, states moved off the orbit (shifted, boosted, rescaled
+    velocities) and unbound states."""
+    rng = np.random.default_rng(17)
+    elements = np.array([[1.0, 1.0, 1.0, 0.0], [1.0, 1.0, 1.0, 0.5], [1.0, 1.0, 0.5, 0.1], [2.0, 1.5, 0.3, 0.7]])
+    times = np.array([0.0, 0.37, 2.3, 17.0])
+    states, ts = [], []
+    for el in elements:
+        for t in times:
+            buf = np.zeros(10)
+            r.ref_two_body_state(*[ctypes.c_double(v) for v in el], ctypes.c_double(t), dptr(buf))
+            states.append(buf.copy())
+            ts.append(t)
+            off = buf.copy()
+            off[[1, 6]] += rng.uniform(-0.3, 0.3)
+            off[[2, 7]] += rng.uniform(-0.3, 0.3)
+            off[[3, 8]] += rng.uniform(-0.2, 0.2)
+            off[[4, 9]] += rng.uniform(-0.2, 0.2)
+            off[[3, 4, 8, 9]] *= rng.uniform(0.9, 1.1)
+            states.append(off)
+            ts.append(t)
+    unbound = states[0].copy()
+    unbound[[3, 4, 8, 9]] *= 2.0
+    states.append(unbound)
+    ts.append(0.0)
+    states = np.array(states)
+    out = np.zeros_like(states)
+    status = np.zeros(len(states), np.int32)
+    for i, (st, t) in enumerate(zip(states, ts)):
+        status[i] = r.ref_two_body_elements(dptr(st), ctypes.c_double(t), dptr(out[i]))
+    return {"two_body/elements": elements, "two_body/times": times, "two_body/state": states,
+            "two_body/t": np.array(ts), "two_body/recovered": out, "two_body/status": status}
+
+
 def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
     g = 4.0 / 3.0
     n = 4096
@@ -229,6 +264,7 @@ def main() -> None:
     np.savez_compressed(HERE / "minidisk_golden.npz", **fixtures)
     np.savez_compressed(HERE / "srhd_golden.npz", **srhd_fixtures(o, r))
     np.savez_compressed(HERE / "mhd_golden.npz", **mhd_fixtures(o, r))
+    np.savez_compressed(HERE / "two_body_golden.npz", **two_body_fixture(r))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size, "bytes")
 

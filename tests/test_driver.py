@@ -126,3 +126,51 @@ def test_graph_replay_equals_direct_launches(tmp_path):
     g = checkpoint.read(tmp_path / "g" / "chkpt.0001")
     d = checkpoint.read(tmp_path / "d" / "chkpt.0001")
     assert np.array_equal(g["conserved"], d["conserved"]) and g["time"] == d["time"]
+
+
+def read_time_series(path):
+    rows = [list(map(float, line.split())) for line in open(path) if not line.startswith("#")]
+    return np.array(rows)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_time_series_rows_and_mass_balance(tmp_path, precision):
+    # tsi = cpi: a sample (and a checkpoint) at t = 0 and every 0.001 orbits
+    args = [*SMALL, "fold=2", "orbits=0.003", "cpi=0.001", "tsi=0.001", f"precision={precision}", "rk=2",
+            "perturbation=0.01", "seed=3", f"outdir={tmp_path}"]
+    run_driver(*args)
+    ts = read_time_series(tmp_path / "time_series.dat")
+    assert ts.shape[1] == 2 + 16 + 16 + 2 + 4
+    assert len(ts) >= 3 and np.all(np.diff(ts[:, 0]) > 0)
+    assert np.all(ts[0, 2:34] == 0.0)                      # nothing integrated at t = 0
+    # a = 1, e = 0 (e is a square root of a rounding-level difference, so ~1e-8)
+    assert np.allclose(ts[:, 34], 1.0, rtol=1e-12) and np.allclose(ts[:, 35], 0.0, atol=1e-7)
+    # the disk mass changes by the integrated buffer and sink rates
+    ck = sorted(p.name for p in tmp_path.iterdir() if p.name.startswith("chkpt."))
+    first, last = checkpoint.read(tmp_path / ck[0]), checkpoint.read(tmp_path / ck[-2])
+    N = first["conserved"].shape[1]
+    dl = 2 * 4.0 / N
+    row = ts[np.argmin(np.abs(ts[:, 0] - last["time"]))]
+    assert row[0] == last["time"]
+    I = row[2:18]
+    dm = (last["conserved"][0].sum() - first["conserved"][0].sum()) * dl * dl
+    scale = abs(I[10]) + abs(I[0]) + abs(I[1])
+    assert abs(dm - (I[10] - I[0] - I[1])) <= (1e-9 if precision == "fp64" else 1e-4) * scale
+
+
+@pytest.mark.gpu
+def test_time_series_continues_across_restart(tmp_path):
+    args = [*SMALL, "fold=2", "orbits=0.003", "cpi=0.0015", "tsi=0.0005", "precision=mixed", "rk=2"]
+    run_driver(*args, f"outdir={tmp_path / 'a'}")
+    ckpts = sorted(p.name for p in (tmp_path / "a").iterdir() if p.name.startswith("chkpt."))
+    run_driver(f"restart={tmp_path / 'a' / ckpts[1]}", f"outdir={tmp_path / 'b'}")
+    a = read_time_series(tmp_path / "a" / "time_series.dat")
+    b = read_time_series(tmp_path / "b" / "time_series.dat")
+    # the restarted run writes the samples after its checkpoint: the same times and
+    # iterations as the straight run's, and the same integrals up to the order of the
+    # device's FP64 atomic sums
+    assert len(b) >= 1
+    tail = a[-len(b):]
+    assert np.array_equal(tail[:, :2], b[:, :2])
+    assert np.allclose(tail[:, 2:], b[:, 2:], rtol=1e-10, atol=1e-14)
