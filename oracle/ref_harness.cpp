@@ -8,6 +8,7 @@
 // nd::shared_array / numeric::tuple_t types, plus the reference's driver loop
 // restated where the original translation unit cannot be built here
 // (problems/minidisk.cpp needs HDF5 and MPI).
+#include <array>
 #include <cstdint>
 #include <cstring>
 #include <utility>
@@ -18,6 +19,7 @@
 #include "physics_two_body.hpp"
 #include "scheme_mhd_v1.hpp"
 #include "scheme_plm_gradient.hpp"
+#include "scheme_sedov2d.hpp"
 
 namespace {
 
@@ -367,5 +369,139 @@ void ref_two_body_state(double a, double M, double q, double e, double t, double
                     s.second.velocity_x.value, s.second.velocity_y.value};
     std::memcpy(out, v, sizeof v);
 }
+
+// ---------------------------------------------------------------- sedov2d
+// A set of T radial tracks as flat buffers: ncells[j] cells on track j,
+// theta[2j], theta[2j+1] its polar bounds, radii the concatenated face radii
+// (ncells[j] + 1 per track), u the concatenated conserved tuples (5 per cell:
+// D, S1, S2, S3, tau, the conserved volume integrals the reference holds).
+namespace {
+
+struct FlatTracks
+{
+    nd::shared_array<sedov::radial_track_t, 1> tracks;
+    nd::shared_array<nd::shared_array<srhd::conserved_t, 1>, 1> u;
+};
+
+FlatTracks load_tracks(int32_t T, const int64_t* ncells, const double* theta, const double* radii, const double* u)
+{
+    auto tr = nd::make_unique_array<sedov::radial_track_t>(nd::uivec(T));
+    auto uc = nd::make_unique_array<nd::shared_array<srhd::conserved_t, 1>>(nd::uivec(T));
+    for (int32_t j = 0; j < T; ++j)
+    {
+        auto rf = nd::make_unique_array<dimensional::unit_length>(nd::uivec(ncells[j] + 1));
+        for (int64_t i = 0; i <= ncells[j]; ++i) rf(i) = *radii++;
+        auto c = nd::make_unique_array<srhd::conserved_t>(nd::uivec(ncells[j]));
+        for (int64_t i = 0; i < ncells[j]; ++i, u += 5) c(i) = to_tuple<srhd::conserved_t>(u);
+        tr(j) = sedov::radial_track_t{nd::make_shared_array(std::move(rf)), theta[2 * j], theta[2 * j + 1]};
+        uc(j) = nd::make_shared_array(std::move(c));
+    }
+    return {nd::make_shared_array(std::move(tr)), nd::make_shared_array(std::move(uc))};
+}
+
+// problems/sedov2d.cpp:563-587 with the boundary primitive states given per
+// track (the driver takes them from its wind profile at the track's ends)
+sedov::radial_godunov_data_t inner_bc(const srhd::primitive_t& ghost, const nd::shared_array<srhd::primitive_t, 1>& pc)
+{
+    auto vel = std::min(srhd::velocity_1(front(pc)), dimensional::unit_velocity(0.0));
+    auto mode = srhd::riemann_solver_mode_hllc_fluxes_moving_face_t{vel};
+    return std::pair(srhd::riemann_solver(ghost, front(pc), geometric::unit_vector_on(1), 4. / 3, mode), vel);
+}
+
+sedov::radial_godunov_data_t outer_bc(const srhd::primitive_t& ghost, const nd::shared_array<srhd::primitive_t, 1>& pc)
+{
+    auto vel = srhd::velocity_1(ghost);
+    auto mode = srhd::riemann_solver_mode_hllc_fluxes_moving_face_t{vel};
+    return std::pair(srhd::riemann_solver(back(pc), ghost, geometric::unit_vector_on(1), 4. / 3, mode), vel);
+}
+
+} // namespace
+
+// The forward-Euler advance of problems/sedov2d.cpp:608-660 (the driver's own
+// translation unit needs HDF5, so its glue is restated here around the
+// reference's sedov:: scheme functions): recover_primitive, radial_gradient,
+// radial_godunov_data with the inner/outer boundary Riemann data,
+// polar_godunov_data between neighbouring tracks (empty track data beyond
+// the poles), delta_conserved and delta_face_positions. Writes the new radii
+// and conserved tuples in the input layout; optional outputs (may be null):
+// prim and grad (5 per cell), radial (6 per face: flux, contact speed), and
+// polar (8 per transverse face: flux, area, il, ir; for each interface
+// j = 0..T-2 the ncells[j] + ncells[j+1] + 1 faces of transverse_faces).
+// Returns 1 if the reference threw.
+int ref_sedov_advance(int32_t T, const int64_t* ncells, const double* theta, const double* radii, const double* u,
+                      const double* ghost_in, const double* ghost_out, double dt, int32_t use_plm,
+                      double* radii_out, double* u_out, double* prim, double* grad, double* radial, double* polar)
+{
+    try
+    {
+        auto in = load_tracks(T, ncells, theta, radii, u);
+        auto t0 = in.tracks;
+        auto uc = in.u;
+        std::vector<nd::shared_array<srhd::primitive_t, 1>> pc(T);
+        std::vector<nd::shared_array<sedov::primitive_per_length_t, 1>> dc(T);
+        std::vector<nd::shared_array<sedov::radial_godunov_data_t, 1>> ff(T);
+        for (int32_t j = 0; j < T; ++j)
+        {
+            pc[j] = sedov::recover_primitive(t0(j), uc(j));
+            dc[j] = sedov::radial_gradient(t0(j), pc[j], use_plm != 0);
+            auto gi = to_tuple<srhd::primitive_t>(ghost_in + 5 * j);
+            auto go = to_tuple<srhd::primitive_t>(ghost_out + 5 * j);
+            ff[j] = sedov::radial_godunov_data(t0(j), pc[j], dc[j], inner_bc(gi, pc[j]), outer_bc(go, pc[j]));
+        }
+        auto td = [&] (int32_t j) -> sedov::track_data_t {
+            if (j < 0 || j >= T) return sedov::track_data_t();
+            return sedov::track_data_t{t0(j), pc[j], dc[j]};
+        };
+        std::vector<nd::shared_array<sedov::polar_godunov_data_t, 1>> gf(T + 1);
+        for (int32_t j = 0; j + 1 < T; ++j)
+            gf[j + 1] = sedov::polar_godunov_data(td(j - 1), td(j), td(j + 1), td(j + 2), use_plm != 0);
+        for (int32_t j = 0; j < T; ++j)
+        {
+            auto du = sedov::delta_conserved(t0(j), pc[j], ff[j], gf[j], gf[j + 1], dimensional::unit_time(dt));
+            auto dr = sedov::delta_face_positions(ff[j], dimensional::unit_time(dt));
+            for (std::size_t i = 0; i < size(uc(j)); ++i, u_out += 5) from_tuple(uc(j)(i) + du(i), u_out);
+            for (std::size_t i = 0; i < size(t0(j).face_radii); ++i) *radii_out++ = (t0(j).face_radii(i) + dr(i)).value;
+            for (std::size_t i = 0; prim && i < size(pc[j]); ++i, prim += 5) from_tuple(pc[j](i), prim);
+            for (std::size_t i = 0; grad && i < size(dc[j]); ++i, grad += 5) from_tuple(dc[j](i), grad);
+            for (std::size_t i = 0; radial && i < size(ff[j]); ++i, radial += 6)
+            {
+                from_tuple(std::get<0>(ff[j](i)), radial);
+                radial[5] = std::get<1>(ff[j](i)).value;
+            }
+        }
+        for (int32_t j = 0; polar && j + 1 < T; ++j)
+        {
+            for (std::size_t n = 0; n < size(gf[j + 1]); ++n, polar += 8)
+            {
+                auto [f, da, il, ir] = gf[j + 1](n);
+                from_tuple(f, polar);
+                polar[5] = da.value;
+                polar[6] = double(il);
+                polar[7] = double(ir);
+            }
+        }
+        return 0;
+    }
+    catch (const std::exception&)
+    {
+        return 1;
+    }
+}
+
+// sedov::generate_radial_track (scheme_sedov2d.cpp:108-129): the face radii
+// of a log-spaced track; returns the number of faces (written if radii is
+// non-null and capacity suffices).
+int64_t ref_sedov_generate_track(double r0, double r1, double theta0, double theta1, double aspect, double* radii,
+                                 int64_t capacity)
+{
+    auto t = sedov::generate_radial_track(r0, r1, theta0, theta1, aspect);
+    const int64_t n = int64_t(size(t.face_radii));
+    for (int64_t i = 0; radii && i < n && i < capacity; ++i) radii[i] = t.face_radii(i).value;
+    return n;
+}
+
+// sedov::cell_volume and sedov::face_area (scheme_sedov2d.cpp:40-62)
+double ref_sedov_cell_volume(double r0, double r1, double t0, double t1) { return sedov::cell_volume(r0, r1, t0, t1).value; }
+double ref_sedov_face_area(double r0, double r1, double t0, double t1) { return sedov::face_area(r0, r1, t0, t1).value; }
 
 } // extern "C"

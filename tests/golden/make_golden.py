@@ -157,6 +157,123 @@ def two_body_fixture(r) -> dict[str, np.ndarray]:
             "two_body/t": np.array(ts), "two_body/recovered": out, "two_body/status": status}
 
 
+SEDOV_CASES = {
+    # name: (track count, polar focus, radial aspect, outer radius, u3 amplitude, use_plm, seed)
+    "uniform_plm": (6, 0.0, 0.5, 6.0, 0.0, 1, 31),
+    "focused_swirl": (7, 0.5, 0.4, 5.0, 0.05, 1, 32),
+    "focused_pcm": (5, 0.3, 0.6, 4.0, 0.0, 0, 33),
+}
+
+
+def sedov_case(o, r, name):
+    """Tracks from the reference's generate_radial_track over polar bounds
+    spaced as the driver's "focus" option spaces them, a seeded blast in a
+    wind (primitives at the cell centres, conserved volume integrals), and
+    ghost primitives for the boundary Riemann problems of three RK stages."""
+    T, focus, aspect, r1, u3amp, use_plm, seed = SEDOV_CASES[name]
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, T + 1)
+    theta = np.pi * (x + focus * (x - 1) * x) / (1 + 2 * focus * (x - 1) * x)
+    r.ref_sedov_generate_track.restype = ctypes.c_int64
+    r.ref_sedov_cell_volume.restype = ctypes.c_double
+    radii, ncells = [], []
+    for j in range(T):
+        a = (ctypes.c_double(1.0), ctypes.c_double(r1), ctypes.c_double(theta[j]), ctypes.c_double(theta[j + 1]),
+             ctypes.c_double(aspect))
+        n = r.ref_sedov_generate_track(*a, None, ctypes.c_int64(0))
+        buf = np.zeros(n)
+        r.ref_sedov_generate_track(*a, dptr(buf), ctypes.c_int64(n))
+        radii.append(buf)
+        ncells.append(n - 1)
+    cons = []
+    for j in range(T):
+        rf = radii[j]
+        rc = 0.5 * (rf[:-1] + rf[1:])
+        qc = 0.5 * (theta[j] + theta[j + 1])
+        n = len(rc)
+        pr = np.zeros((n, 5))
+        pr[:, 0] = rc ** -2 * (1 + 0.05 * rng.uniform(-1, 1, n))
+        pr[:, 1] = 0.5 + 0.3 * np.sin(3 * qc) + 0.05 * rng.uniform(-1, 1, n)
+        pr[:, 2] = 0.02 * rng.uniform(-1, 1, n)
+        pr[:, 3] = u3amp * rng.uniform(-1, 1, n)
+        pr[:, 4] = 1e-3 * pr[:, 0] * (1 + 0.1 * rng.uniform(0, 1, n)) + np.where(rc < 2.0, 0.5, 0.0)
+        uc = np.zeros(5 * n)
+        o.oracle_srhd_conserved_density(dptr(np.ascontiguousarray(pr.ravel())), ctypes.c_int64(n),
+                                        ctypes.c_double(4.0 / 3.0), dptr(uc))
+        dv = np.array([r.ref_sedov_cell_volume(ctypes.c_double(rf[i]), ctypes.c_double(rf[i + 1]),
+                                               ctypes.c_double(theta[j]), ctypes.c_double(theta[j + 1]))
+                       for i in range(n)])
+        cons.append((uc.reshape(n, 5) * dv[:, None]).ravel())
+    stages = 3
+    gin = np.zeros((stages, T, 5))
+    gout = np.zeros((stages, T, 5))
+    for s in range(stages):
+        gin[s] = [2.0 + 0.1 * s, 1.0, 0.0, 0.0, 0.1]
+        gout[s] = [0.01, 0.1 + 0.01 * s, 0.0, 0.0, 1e-4]
+    return {"T": np.array([T]), "ncells": np.array(ncells, np.int64), "theta": np.repeat(theta, 2)[1:-1].copy(),
+            "radii": np.concatenate(radii), "u": np.concatenate(cons), "ghost_in": gin.ravel(),
+            "ghost_out": gout.ravel(), "use_plm": np.array([use_plm])}
+
+
+def sedov_dt(c) -> float:
+    """0.3 of the smallest radial spacing (the driver's cfl * min spacing / c)."""
+    nc = c["ncells"]
+    off = np.concatenate([[0], np.cumsum(nc + 1)])
+    return 0.3 * min(np.diff(c["radii"][off[j]:off[j + 1]]).min() for j in range(len(nc)))
+
+
+def sedov_fixtures(o, r) -> dict[str, np.ndarray]:
+    """One forward-Euler advance of every case through the reference's sedov::
+    functions (with its intermediate arrays), and RK2 / RK3 runs of three
+    steps composed with the reference's weighted_sum semantics."""
+    out = {}
+    for name in SEDOV_CASES:
+        c = sedov_case(o, r, name)
+        T = int(c["T"][0])
+        nc = c["ncells"]
+        C = int(nc.sum())
+        F = C + T
+        NP = int(sum(nc[j] + nc[j + 1] + 1 for j in range(T - 1)))
+        dt = sedov_dt(c)
+        plm = ctypes.c_int32(int(c["use_plm"][0]))
+        args = (ctypes.c_int32(T), nc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(c["theta"]))
+        T5 = 5 * T
+
+        def step(rad, u, s, parts=None):
+            ro_, uo_ = np.zeros(F), np.zeros(5 * C)
+            gi = np.ascontiguousarray(c["ghost_in"][T5 * s: T5 * (s + 1)])
+            go = np.ascontiguousarray(c["ghost_out"][T5 * s: T5 * (s + 1)])
+            extra = [dptr(x) for x in parts] if parts else [None] * 4
+            assert r.ref_sedov_advance(*args, dptr(rad), dptr(u), dptr(gi), dptr(go), ctypes.c_double(dt), plm,
+                                       dptr(ro_), dptr(uo_), *extra) == 0
+            return ro_, uo_
+
+        parts = [np.zeros(5 * C), np.zeros(5 * C), np.zeros(6 * F), np.zeros(8 * NP)]
+        ro, uo = step(c["radii"], c["u"], 0, parts)
+        for k, v in c.items():
+            out[f"sedov/{name}/{k}"] = v
+        out[f"sedov/{name}/dt"] = np.array([dt])
+        out[f"sedov/{name}/euler/radii"] = ro
+        out[f"sedov/{name}/euler/u"] = uo
+        for k, v in zip(("prim", "grad", "radial", "polar"), parts):
+            out[f"sedov/{name}/euler/{k}"] = v
+        for rk in (2, 3):
+            rad, u = c["radii"].copy(), c["u"].copy()
+            for _ in range(3):
+                r0, u0 = rad, u
+                r1_, u1 = step(r0, u0, 0)
+                r2_, u2 = step(r1_, u1, 1)
+                if rk == 2:
+                    rad, u = r0 * (1 / 2) + r2_ * (1 / 2), u0 * (1 / 2) + u2 * (1 / 2)
+                else:
+                    r2_, u2 = r0 * (3 / 4) + r2_ * (1 / 4), u0 * (3 / 4) + u2 * (1 / 4)
+                    r3_, u3 = step(r2_, u2, 2)
+                    rad, u = r0 * (1 / 3) + r3_ * (2 / 3), u0 * (1 / 3) + u3 * (2 / 3)
+            out[f"sedov/{name}/rk{rk}_3/radii"] = rad
+            out[f"sedov/{name}/rk{rk}_3/u"] = u
+    return out
+
+
 def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
     g = 4.0 / 3.0
     n = 4096
@@ -265,6 +382,7 @@ def main() -> None:
     np.savez_compressed(HERE / "srhd_golden.npz", **srhd_fixtures(o, r))
     np.savez_compressed(HERE / "mhd_golden.npz", **mhd_fixtures(o, r))
     np.savez_compressed(HERE / "two_body_golden.npz", **two_body_fixture(r))
+    np.savez_compressed(HERE / "sedov_golden.npz", **sedov_fixtures(o, r))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size, "bytes")
 
