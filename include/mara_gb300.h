@@ -464,6 +464,49 @@ int mara_srhd_tube_advance(int32_t N, double* u, void* clock, int32_t steps, dou
 int mara_srhd_riemann(const double* pl, const double* pr, int64_t n, int32_t axis, double gamma_law_index,
                       int32_t solver, double* f, int32_t* status, void* stream);
 
+/* ---------------------------------------------------------------- spherical tracks (sedov2d) */
+/* The moving radial-track SRHD scheme of src/scheme_sedov2d.cpp (driven by
+ * problems/sedov2d.cpp), gamma 4/3, temperature floor 1e-6. Device buffers:
+ *   cell_offset[track_count + 1] (int64): track j holds cells
+ *     [cell_offset[j], cell_offset[j+1]) (at least 2), cells = cell_offset[track_count];
+ *   theta[2 * track_count]: polar bounds (theta0, theta1) of each track;
+ *   radii[cells + track_count]: face radii, track j's n_j + 1 faces from
+ *     cell_offset[j] + j (the reference's radial_track_t::face_radii);
+ *   u[5][cells]: SoA conserved volume integrals (D, S1, S2, S3, tau);
+ *   ghost_in / ghost_out: primitives (rho, u1, u2, u3, p) beyond each
+ *     track's inner / outer face, [stage][track][5] (problems/sedov2d.cpp:563-587
+ *     takes them from its wind profile at the stage time);
+ *   failures (nullable, int32): incremented where the reference throws
+ *     (a recovery fails, an HLLC contact speed is NaN or beyond 1e3). */
+int64_t mara_sedov_workspace_bytes(int32_t track_count, int64_t cells);
+
+/* One forward-Euler advance of every track: sedov::recover_primitive,
+ * radial_gradient, radial_godunov_data with the driver's inner_bc/outer_bc,
+ * polar_godunov_data between neighbouring tracks, delta_conserved and
+ * delta_face_positions (src/scheme_sedov2d.cpp:150-356,
+ * problems/sedov2d.cpp:608-660). Optional outputs for parity checks (NULL
+ * to skip): prim [5][cells], grad [5][cells], radial [6][cells + track_count]
+ * (HLLC flux, contact or face speed), polar [6][2 cells + track_count] (flux,
+ * area of each transverse face; interface j's faces start at
+ * cell_offset[j] + cell_offset[j+1] - cell_offset[1] + j, invalid ones zero)
+ * and polar_index [2][2 cells + track_count] (int32 il, ir merge counters). */
+int mara_sedov_stage(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                     const double* radii, const double* u, const double* ghost_in, const double* ghost_out, double dt,
+                     int32_t use_plm, double* radii_out, double* u_out, double* prim, double* grad, double* radial,
+                     double* polar, int32_t* polar_index, void* workspace, int32_t* failures, void* stream);
+
+/* control::advance_runge_kutta (src/app_control.hpp:169-195) of that advance,
+ * rk_order 1, 2 or 3, radii and u combined by weighted_sum; in place. ghost
+ * arrays hold rk_order stages. */
+int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                       double* radii, double* u, const double* ghost_in, const double* ghost_out, double dt,
+                       int32_t rk_order, int32_t use_plm, void* workspace, int32_t* failures, void* stream);
+
+/* sedov::minimum_spacing over all tracks (scheme_sedov2d.cpp:66-69, the
+ * driver's dt = cfl * min spacing / c): out is one device double. */
+int mara_sedov_min_spacing(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* radii,
+                           double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,695 @@
+// Spherical-track SRHD (the sedov2d scheme) on the GPU: the per-stage
+// functions of src/scheme_sedov2d.cpp:150-356 over a set of radial tracks,
+// with the boundary Riemann data of problems/sedov2d.cpp:563-587 and the RK
+// combinations of src/app_control.hpp:169-195 (weighted_sum of radii and
+// conserved, problems/sedov2d.cpp:127-152). gamma = 4/3, temperature floor 1e-6.
+//
+// Layout (device): T tracks in CSR form. cell_offset[T+1] (int64) gives the
+// first cell of each track; track j has n_j = cell_offset[j+1] - cell_offset[j]
+// cells and n_j + 1 face radii starting at radii[cell_offset[j] + j];
+// theta[2j], theta[2j+1] bound it in the polar angle. Conserved volume
+// integrals are SoA u[5][C] (D, S1, S2, S3, tau). The transverse (polar)
+// faces of the interface between tracks j and j+1 are the n_j + n_{j+1} + 1
+// adjacent pairs of the merged face radii of both tracks
+// (mesh::transverse_faces, src/mesh_sliding.hpp:122-172); interface j's
+// faces start at po(j) = co[j] + co[j+1] - co[1] + j.
+//
+// One stage = four kernels, one thread per item:
+//   prim_kernel    cell: volume, u / dV, SRHD Newton recovery
+//   radial_kernel  face: PLM slopes of both neighbours on the cell-centre
+//                  radii, HLLC flux across the contact and the contact speed;
+//                  boundary faces: moving-face HLLC against the ghost states;
+//                  moves the face by speed * dt (and the RK combination)
+//   polar_kernel   transverse face: merge-path position in the two tracks'
+//                  radii, samples, PLM in theta, fixed-face HLLC, face area
+//   update_kernel  cell: radial flux differences, the polar fluxes binned on
+//                  the cell in face order, spherical source terms, u + du
+//                  (and the RK combination)
+// Radial slopes are recomputed by the faces that need them (two per cell)
+// and by the polar samples, so no gradient array is stored.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include "common.cuh"
+#include "srhd_physics.cuh"
+
+namespace mara {
+namespace sedov {
+
+using srhd::SPrim;
+
+constexpr double kGamma = 4. / 3;
+constexpr double kFloor = 1e-6;
+
+struct Tracks
+{
+    int T;
+    int64_t C;
+    const int64_t* co;
+    const double* theta;
+};
+
+struct Stage
+{
+    Tracks t;
+    const double* r;        // input radii [C + T]
+    const double* u;        // input conserved [5][C]
+    const double* gin;      // ghost primitives inside / outside [T][5]
+    const double* gout;
+    double dt;
+    int use_plm;
+    // RK combination: out = base * b + (in + du) * (1 - b); base null: out = in + du
+    const double* r_base;
+    const double* u_base;
+    double b, b1;
+    double* r_out;
+    double* u_out;
+    // workspace
+    double* P;              // [5][C] primitives
+    double* rf;             // [6][F] radial flux and contact speed
+    double* pf;             // [6][NPmax] polar flux and area
+    int32_t* pil;           // [NPmax] merge counters
+    int32_t* pir;
+    int64_t np_max;
+    int* failures;
+    // optional copies for parity checks
+    double* grad_out;       // [5][C]
+};
+
+__device__ inline int64_t track_of(const int64_t* off, int T, int64_t x)
+{
+    // largest j with off[j] <= x
+    int lo = 0, hi = T - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ inline int64_t face_offset(const Tracks& t, int j) { return t.co[j] + j; }
+__device__ inline int64_t polar_offset(const Tracks& t, int j) { return t.co[j] + t.co[j + 1] - t.co[1] + j; }
+
+// sedov::cell_volume / face_area (scheme_sedov2d.cpp:40-62)
+__device__ inline double cell_volume(double r0, double r1, double t0, double t1)
+{
+    const double dcost = -(cos(t1) - cos(t0));
+    return 2.0 * M_PI * (r1 * r1 * r1 - r0 * r0 * r0) / 3.0 * dcost;
+}
+
+__device__ inline double face_area(double r0, double r1, double t0, double t1)
+{
+    const double R0 = r0 * sin(t0), R1 = r1 * sin(t1);
+    const double z0 = r0 * cos(t0), z1 = r1 * cos(t1);
+    const double dR = R1 - R0, dz = z1 - z0;
+    return M_PI * (R0 + R1) * pow(dR * dR + dz * dz, 0.5);
+}
+
+// plm_gradient_scalar_t on coordinates (scheme_plm_gradient.hpp:44-67)
+__device__ inline double plm_x(double xl, double x0, double xr, double yl, double y0, double yr, double theta)
+{
+    const double a = (y0 - yl) / (x0 - xl) * theta;
+    const double b = (yr - yl) / (xr - xl);
+    const double c = (yr - y0) / (xr - x0) * theta;
+    const double sa = copysign(1.0, a), sb = copysign(1.0, b), sc = copysign(1.0, c);
+    return 0.25 * fabs(sa + sb) * (sa + sc) * fmin(fmin(fabs(a), fabs(b)), fabs(c));
+}
+
+__device__ inline double comp(const SPrim<double>& p, int k) { return k == 0 ? p.rho : (k == 4 ? p.p : p.u[k - 1]); }
+__device__ inline void set_comp(SPrim<double>& p, int k, double v)
+{
+    if (k == 0) p.rho = v; else if (k == 4) p.p = v; else p.u[k - 1] = v;
+}
+
+__device__ inline SPrim<double> load_prim(const double* P, int64_t C, int64_t c)
+{
+    SPrim<double> p;
+    for (int k = 0; k < 5; ++k) set_comp(p, k, P[k * C + c]);
+    return p;
+}
+
+__device__ inline SPrim<double> load_ghost(const double* g, int j)
+{
+    SPrim<double> p;
+    for (int k = 0; k < 5; ++k) set_comp(p, k, g[5 * j + k]);
+    return p;
+}
+
+// the radial slope of cell i (local) of track j: zero at both ends
+__device__ inline void radial_slope(const Stage& S, int j, int64_t i, int64_t n, double g[5])
+{
+    for (int k = 0; k < 5; ++k) g[k] = 0.0;
+    if (i <= 0 || i + 1 >= n) return;
+    const int64_t c = S.t.co[j] + i, f = face_offset(S.t, j) + i;
+    const double* r = S.r + f;
+    const double xl = 0.5 * (r[-1] + r[0]), x0 = 0.5 * (r[0] + r[1]), xr = 0.5 * (r[1] + r[2]);
+    const double th = S.use_plm ? 1.0 : 0.0;
+    const int64_t C = S.t.C;
+    for (int k = 0; k < 5; ++k)
+        g[k] = plm_x(xl, x0, xr, S.P[k * C + c - 1], S.P[k * C + c], S.P[k * C + c + 1], th);
+}
+
+// The HLLC modes of riemann_solver (physics_srhd.hpp:351-487) along axis:
+// FIXED (face speed 0), MOVING (face speed w), ACROSS (the left star flux
+// with the contact speed, which is returned in *contact). Returns 1 where the
+// reference throws (NaN contact speed or beyond 1e3).
+enum { FIXED = 0, MOVING = 1, ACROSS = 2 };
+
+__device__ inline int hllc_mode(const SPrim<double>& pl, const SPrim<double>& pr, int axis, int mode, double w,
+                                double F[5], double* contact)
+{
+    using namespace srhd;
+    const double gm = kGamma;
+    double ul[5], ur[5], fl[5], fr[5];
+    cons_of(pl, gm, ul);
+    cons_of(pr, gm, ur);
+    flux_of(pl, ul, axis, fl);
+    flux_of(pr, ur, axis, fr);
+    double alm, alp, arm, arp;
+    outer_speeds(pl, axis, gm, alm, alp);
+    outer_speeds(pr, axis, gm, arm, arp);
+    const double ar = fmax(alp, arp);
+    const double al = fmin(alm, arm);
+    double u_hll[5], f_hll[5];
+    for (int k = 0; k < 5; ++k)
+    {
+        u_hll[k] = rdiv(radd(rsub(rmul(ar, ur[k]), rmul(al, ul[k])), rsub(fl[k], fr[k])), rsub(ar, al));
+        f_hll[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
+    }
+    const double c2 = 1.0;
+    const double n[3] = {double(axis == 0), double(axis == 1), double(axis == 2)};
+    const double ue_hll = radd(u_hll[4], rmul(u_hll[0], c2));
+    const double fe_hll = radd(f_hll[4], rmul(f_hll[0], c2));
+    const double um_hll = radd(radd(radd(0.0, rmul(u_hll[1], n[0])), rmul(u_hll[2], n[1])), rmul(u_hll[3], n[2]));
+    const double fm_hll = radd(radd(radd(0.0, rmul(f_hll[1], n[0])), rmul(f_hll[2], n[1])), rmul(f_hll[3], n[2]));
+    const double a = fe_hll;
+    const double b = rsub(-fm_hll, ue_hll);
+    const double c = um_hll;
+    const double d = rsub(rmul(b, b), rmul(rmul(4.0, a), c));
+    const double as = d < 0.0 ? 0.0
+                    : rmul(fabs(a) > 1e-8 ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(2.0, a)) : rdiv(-c, b), c2);
+    if (isnan(as) || as < -1e3 || as > 1e3)
+    {
+        for (int k = 0; k < 5; ++k) F[k] = 0.0;
+        if (contact) *contact = 0.0;
+        return 1;
+    }
+    const double ps = radd(rdiv(rmul(-fe_hll, as), c2), fm_hll);
+    auto star = [&](const double u[5], const double f[5], const SPrim<double>& p, double s, double face) {
+        const double v = normal_velocity(p, axis);
+        const double e = radd(u[4], rmul(u[0], c2));
+        const double m = radd(radd(radd(0.0, rmul(u[1], n[0])), rmul(u[2], n[1])), rmul(u[3], n[2]));
+        const double sv = rsub(s, v), sa = rsub(s, as);
+        const double es = rdiv(rsub(radd(rmul(e, sv), rmul(ps, as)), rmul(p.p, v)), sa);
+        const double ms = rdiv(rsub(radd(rmul(m, sv), ps), p.p), sa);
+        const double Ds = rdiv(rmul(u[0], sv), sa);
+        double us[5];
+        us[0] = Ds;
+        for (int k = 0; k < 3; ++k)
+        {
+            const double nk = rsub(u[1 + k], rmul(m, n[k]));
+            const double ns = rdiv(rmul(nk, sv), sa);
+            us[1 + k] = radd(rmul(ms, n[k]), ns);
+        }
+        us[4] = rsub(es, rmul(Ds, c2));
+        for (int k = 0; k < 5; ++k) F[k] = rsub(radd(f[k], rmul(s, rsub(us[k], u[k]))), rmul(face, us[k]));
+    };
+    if (mode == ACROSS)
+    {
+        star(ul, fl, pl, al, as);
+        if (contact) *contact = as;
+        return 0;
+    }
+    if (mode == MOVING)
+    {
+        if (w <= al) { for (int k = 0; k < 5; ++k) F[k] = rsub(fl[k], rmul(w, ul[k])); return 0; }
+        if (w >= ar) { for (int k = 0; k < 5; ++k) F[k] = rsub(fr[k], rmul(w, ur[k])); return 0; }
+        if (w <= as) star(ul, fl, pl, al, w);
+        else star(ur, fr, pr, ar, w);
+        return 0;
+    }
+    if (0.0 <= al) { for (int k = 0; k < 5; ++k) F[k] = fl[k]; return 0; }
+    if (0.0 >= ar) { for (int k = 0; k < 5; ++k) F[k] = fr[k]; return 0; }
+    if (0.0 <= as) star(ul, fl, pl, al, 0.0);
+    else star(ur, fr, pr, ar, 0.0);
+    return 0;
+}
+
+__device__ inline void count_failure(const Stage& S, int bad)
+{
+    if (bad && S.failures) atomicAdd(S.failures, bad);
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void __launch_bounds__(256) prim_kernel(const Stage S)
+{
+    const int64_t C = S.t.C;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < C; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int j = int(track_of(S.t.co, S.t.T, c));
+        const int64_t i = c - S.t.co[j];
+        const double* r = S.r + face_offset(S.t, j) + i;
+        const double dv = cell_volume(r[0], r[1], S.t.theta[2 * j], S.t.theta[2 * j + 1]);
+        srhd::Zone z{S.u[c] / dv, S.u[C + c] / dv, S.u[2 * C + c] / dv, S.u[3 * C + c] / dv, S.u[4 * C + c] / dv};
+        double prim[5] = {0, 0, 0, 0, 0};
+        int it = 0;
+        const int st = srhd::newton(z, kGamma, kFloor, 0.0, 50, prim, it);
+        if (st != 0)
+            for (int k = 0; k < 5; ++k) prim[k] = 0.0;
+        count_failure(S, st != 0);
+        for (int k = 0; k < 5; ++k) S.P[k * C + c] = prim[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) radial_kernel(const Stage S)
+{
+    const int64_t C = S.t.C, F = C + S.t.T;
+    for (int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; f < F; f += int64_t(gridDim.x) * blockDim.x)
+    {
+        // faces of track j: [co[j] + j, co[j+1] + j], i.e. face offsets co[j] + j
+        int lo = 0, hi = S.t.T - 1;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.t.co[mid] + mid <= f) lo = mid; else hi = mid - 1;
+        }
+        const int j = lo;
+        const int64_t n = S.t.co[j + 1] - S.t.co[j];
+        const int64_t i = f - face_offset(S.t, j);
+        const int64_t c0 = S.t.co[j];
+        double flux[5], speed = 0.0;
+        int bad = 0;
+        if (i == 0)
+        {
+            // inner_bc (problems/sedov2d.cpp:563-574)
+            const SPrim<double> front = load_prim(S.P, C, c0);
+            speed = fmin(1.0 * front.u[0] / srhd::lorentz_factor(front), 0.0);
+            bad = hllc_mode(load_ghost(S.gin, j), front, 0, MOVING, speed, flux, nullptr);
+        }
+        else if (i == n)
+        {
+            // outer_bc (problems/sedov2d.cpp:576-587)
+            const SPrim<double> ghost = load_ghost(S.gout, j);
+            speed = 1.0 * ghost.u[0] / srhd::lorentz_factor(ghost);
+            bad = hllc_mode(load_prim(S.P, C, c0 + n - 1), ghost, 0, MOVING, speed, flux, nullptr);
+        }
+        else
+        {
+            // radial_godunov_data (scheme_sedov2d.cpp:208-230)
+            double gl[5], gr[5];
+            radial_slope(S, j, i - 1, n, gl);
+            radial_slope(S, j, i, n, gr);
+            const double drl = S.r[f] - S.r[f - 1], drr = S.r[f + 1] - S.r[f];
+            SPrim<double> pl = load_prim(S.P, C, c0 + i - 1), pr = load_prim(S.P, C, c0 + i);
+            for (int k = 0; k < 5; ++k)
+            {
+                set_comp(pl, k, comp(pl, k) + 0.5 * gl[k] * drl);
+                set_comp(pr, k, comp(pr, k) - 0.5 * gr[k] * drr);
+            }
+            bad = hllc_mode(pl, pr, 0, ACROSS, 0.0, flux, &speed);
+        }
+        count_failure(S, bad);
+        for (int k = 0; k < 5; ++k) S.rf[k * F + f] = flux[k];
+        S.rf[5 * F + f] = speed;
+        // delta_face_positions + the RK combination
+        const double moved = S.r[f] + speed * S.dt;
+        S.r_out[f] = S.r_base ? S.r_base[f] * S.b + moved * S.b1 : moved;
+        if (S.grad_out && i < n)
+        {
+            double g[5];
+            radial_slope(S, j, i, n, g);
+            for (int k = 0; k < 5; ++k) S.grad_out[k * C + c0 + i] = g[k];
+        }
+    }
+}
+
+// sedov::sample (scheme_sedov2d.cpp:235-253) on track j (or the fallback)
+__device__ inline SPrim<double> sample(const Stage& S, int j, double r, int64_t index, const SPrim<double>& fallback)
+{
+    const int64_t n = S.t.co[j + 1] - S.t.co[j];
+    const double* rf = S.r + face_offset(S.t, j);
+    if (r <= rf[0] || r >= rf[n]) return fallback;
+    index = min(index, n);
+    // the walk of the reference from the hint; r lies strictly inside the
+    // track, so it ends within [0, n - 1]; the bound only guards bad input
+    for (int64_t guard = 0; guard <= n && r < rf[index]; ++guard) --index;
+    for (int64_t guard = 0; guard <= n && r > rf[index + 1]; ++guard) ++index;
+    index = max(int64_t(0), min(index, n - 1));
+    const double rc = 0.5 * (rf[index] + rf[index + 1]);
+    double g[5];
+    radial_slope(S, j, index, n, g);
+    const int64_t c = S.t.co[j] + index;
+    SPrim<double> out;
+    for (int k = 0; k < 5; ++k) set_comp(out, k, S.P[k * S.t.C + c] + g[k] * (r - rc));
+    return out;
+}
+
+__global__ void __launch_bounds__(256) polar_kernel(const Stage S)
+{
+    const int T = S.t.T;
+    if (T < 2) return;
+    const int64_t NP = polar_offset(S.t, T - 1);
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < NP; p += int64_t(gridDim.x) * blockDim.x)
+    {
+        int lo = 0, hi = T - 2;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (polar_offset(S.t, mid) <= p) lo = mid; else hi = mid - 1;
+        }
+        const int j = lo;
+        const int64_t m = p - polar_offset(S.t, j);           // face m of interface j | j + 1
+        const double* L = S.r + face_offset(S.t, j);
+        const double* R = S.r + face_offset(S.t, j + 1);
+        const int64_t nl = S.t.co[j + 1] - S.t.co[j] + 1, nr = S.t.co[j + 2] - S.t.co[j + 1] + 1;
+        // merge path: a = how many of L are among the first m + 1 merged radii (L first on ties)
+        const int64_t d = m + 1;
+        int64_t a = max(int64_t(0), d - nr), b = min(d, nl);
+        while (a < b)
+        {
+            const int64_t mid = (a + b) >> 1;
+            if (L[mid] <= R[d - mid - 1]) a = mid + 1; else b = mid;
+        }
+        const int64_t il = a - 1, ir = m - a;
+        const double trailing = fmax(il >= 0 ? L[il] : -INFINITY, ir >= 0 ? R[ir] : -INFINITY);
+        const double leading = fmin(a < nl ? L[a] : INFINITY, m + 1 - a < nr ? R[m + 1 - a] : INFINITY);
+        S.pil[p] = int32_t(il);
+        S.pir[p] = int32_t(ir);
+        const bool valid = il >= 0 && il + 1 < nl && ir >= 0 && ir + 1 < nr;
+        double flux[5] = {0, 0, 0, 0, 0}, da = 0.0;
+        if (valid)
+        {
+            const double ql = S.t.theta[2 * j + 1], qr = S.t.theta[2 * (j + 1)];
+            const double rf = 0.5 * (trailing + leading);
+            const SPrim<double> none{0.0, {0.0, 0.0, 0.0}, 0.0};
+            SPrim<double> pl, pr;
+            if (!S.use_plm || j == 0 || j + 2 >= T)
+            {
+                pl = sample(S, j, rf, il, none);
+                pr = sample(S, j + 1, rf, ir, none);
+            }
+            else
+            {
+                auto qc = [&](int k) { return 0.5 * (S.t.theta[2 * k] + S.t.theta[2 * k + 1]); };
+                const double q0 = qc(j - 1), q1 = qc(j), q2 = qc(j + 1), q3 = qc(j + 2);
+                const SPrim<double> p1 = sample(S, j, rf, il, none);
+                const SPrim<double> p2 = sample(S, j + 1, rf, ir, none);
+                const SPrim<double> p0 = sample(S, j - 1, rf, il, p1);
+                const SPrim<double> p3 = sample(S, j + 2, rf, ir, p2);
+                for (int k = 0; k < 5; ++k)
+                {
+                    const double cl = plm_x(q0, q1, q2, comp(p0, k), comp(p1, k), comp(p2, k), 1.0);
+                    const double cr = plm_x(q1, q2, q3, comp(p1, k), comp(p2, k), comp(p3, k), 1.0);
+                    set_comp(pl, k, comp(p1, k) + (ql - q1) * cl);
+                    set_comp(pr, k, comp(p2, k) + (qr - q2) * cr);
+                }
+            }
+            count_failure(S, hllc_mode(pl, pr, 1, FIXED, 0.0, flux, nullptr));
+            da = face_area(trailing, leading, ql, qr);
+        }
+        for (int k = 0; k < 5; ++k) S.pf[k * S.np_max + p] = flux[k];
+        S.pf[5 * S.np_max + p] = da;
+    }
+}
+
+// first index in [lo, hi) whose counter is >= v (counters are nondecreasing)
+__device__ inline int64_t lower_bound(const int32_t* a, int64_t lo, int64_t hi, int64_t v)
+{
+    while (lo < hi)
+    {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) update_kernel(const Stage S)
+{
+    const int64_t C = S.t.C, F = C + S.t.T;
+    const int T = S.t.T;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < C; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int j = int(track_of(S.t.co, T, c));
+        const int64_t n = S.t.co[j + 1] - S.t.co[j];
+        const int64_t i = c - S.t.co[j];
+        const int64_t f = face_offset(S.t, j) + i;
+        const double t0 = S.t.theta[2 * j], t1 = S.t.theta[2 * j + 1];
+        const double r0 = S.r[f], r1 = S.r[f + 1];
+        const double da0 = face_area(r0, r0, t0, t1), da1 = face_area(r1, r1, t0, t1);
+        const double dv = cell_volume(r0, r1, t0, t1);
+        // polar fluxes binned on this cell, in face order (mesh::bin_values)
+        double gl[5] = {0, 0, 0, 0, 0}, gr[5] = {0, 0, 0, 0, 0};
+        if (j > 0)
+        {
+            // interface j-1 | j: this track is the right side, binned by ir
+            const int64_t p0 = polar_offset(S.t, j - 1), p1 = polar_offset(S.t, j);
+            const int64_t nl = S.t.co[j] - S.t.co[j - 1] + 1;
+            for (int64_t p = lower_bound(S.pir, p0, p1, i); p < p1 && S.pir[p] == i; ++p)
+            {
+                const int64_t il = S.pil[p];
+                if (il < 0 || il + 1 >= nl) continue;
+                const double da = S.pf[5 * S.np_max + p];
+                for (int k = 0; k < 5; ++k) gl[k] = gl[k] + S.pf[k * S.np_max + p] * da;
+            }
+        }
+        if (j + 1 < T)
+        {
+            // interface j | j+1: this track is the left side, binned by il
+            const int64_t p0 = polar_offset(S.t, j), p1 = polar_offset(S.t, j + 1);
+            const int64_t nr = S.t.co[j + 2] - S.t.co[j + 1] + 1;
+            for (int64_t p = lower_bound(S.pil, p0, p1, i); p < p1 && S.pil[p] == i; ++p)
+            {
+                const int64_t ir = S.pir[p];
+                if (ir < 0 || ir + 1 >= nr) continue;
+                const double da = S.pf[5 * S.np_max + p];
+                for (int k = 0; k < 5; ++k) gr[k] = gr[k] + S.pf[k * S.np_max + p] * da;
+            }
+        }
+        // spherical_geometry_source_terms (physics_srhd.hpp:330-345)
+        const SPrim<double> p = load_prim(S.P, C, c);
+        const double rc = 0.5 * (r0 + r1);
+        const double qc = 0.5 * (t0 + t1);
+        const double cotq = tan(M_PI_2 - qc);
+        const double ur = p.u[0], uq = p.u[1], up = p.u[2], pg = p.p;
+        const double H0 = srhd::enthalpy_density(p, kGamma);
+        const double src[5] = {0.0 / 1.0, (2.0 * pg + H0 * (uq * uq + up * up)) / rc,
+                               (cotq * pg + H0 * (up * up * cotq - ur * uq)) / rc, -up * H0 * (ur + uq * cotq) / rc,
+                               0.0 / 1.0};
+        for (int k = 0; k < 5; ++k)
+        {
+            const double df = S.rf[k * F + f + 1] * da1 - S.rf[k * F + f] * da0;
+            const double dg = gr[k] - gl[k];
+            const double sc = src[k] * dv;
+            const double out = S.u[k * C + c] + (-(df + dg) + sc) * S.dt;
+            S.u_out[k * C + c] = S.u_base ? S.u_base[k * C + c] * S.b + out * S.b1 : out;
+        }
+        (void)n;
+    }
+}
+
+__global__ void min_spacing_kernel(Tracks t, const double* r, unsigned long long* out)
+{
+    double m = INFINITY;
+    const int64_t C = t.C;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < C; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int j = int(track_of(t.co, t.T, c));
+        const int64_t f = c + j;
+        m = fmin(m, r[f + 1] - r[f]);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    // positive doubles order as their bit patterns
+    if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMin(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// ---------------------------------------------------------------- host
+struct Workspace
+{
+    double* P;
+    double* rf;
+    double* pf;
+    int32_t* pil;
+    int32_t* pir;
+    double* r_stage[2];
+    double* u_stage[2];
+    int* failures;
+    int64_t np_max;
+};
+
+int64_t np_bound(int T, int64_t C) { return 2 * C + T; }
+
+int64_t workspace_bytes(int T, int64_t C)
+{
+    const int64_t F = C + T, NP = np_bound(T, C);
+    auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
+    return al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) + 256 + 256;
+}
+
+Workspace carve(void* base, int T, int64_t C)
+{
+    const int64_t F = C + T, NP = np_bound(T, C);
+    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + 255) & ~uintptr_t(255));
+    auto take = [&](int64_t bytes) { char* q = p; p += (bytes + 255) / 256 * 256; return q; };
+    Workspace w;
+    w.P = reinterpret_cast<double*>(take(5 * C * 8));
+    w.rf = reinterpret_cast<double*>(take(6 * F * 8));
+    w.pf = reinterpret_cast<double*>(take(6 * NP * 8));
+    w.pil = reinterpret_cast<int32_t*>(take(NP * 4));
+    w.pir = reinterpret_cast<int32_t*>(take(NP * 4));
+    for (int s = 0; s < 2; ++s) w.r_stage[s] = reinterpret_cast<double*>(take(F * 8));
+    for (int s = 0; s < 2; ++s) w.u_stage[s] = reinterpret_cast<double*>(take(5 * C * 8));
+    w.failures = reinterpret_cast<int*>(take(256));
+    w.np_max = NP;
+    return w;
+}
+
+inline int blocks_for(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16))); }
+
+int run_stage(Stage S, cudaStream_t s)
+{
+    const int64_t C = S.t.C, F = C + S.t.T;
+    prim_kernel<<<blocks_for(C), 256, 0, s>>>(S);
+    if (int r = launch_status("sedov prim_kernel")) return r;
+    radial_kernel<<<blocks_for(F), 256, 0, s>>>(S);
+    if (int r = launch_status("sedov radial_kernel")) return r;
+    polar_kernel<<<blocks_for(S.np_max), 256, 0, s>>>(S);
+    if (int r = launch_status("sedov polar_kernel")) return r;
+    update_kernel<<<blocks_for(C), 256, 0, s>>>(S);
+    return launch_status("sedov update_kernel");
+}
+
+int check_tracks(int T, int64_t C, const int64_t* co, const double* theta)
+{
+    MARA_REQUIRE(T >= 1 && T <= (1 << 24), "sedov: track_count must be in [1, 2^24]");
+    MARA_REQUIRE(C >= 2 * int64_t(T) && C + T < (int64_t(1) << 31) / 3,
+                 "sedov: cells must be at least 2 per track and fewer than 2^31/3 - track_count");
+    MARA_REQUIRE(co && theta, "sedov: null track buffer");
+    return MARA_OK;
+}
+
+} // namespace sedov
+} // namespace mara
+
+using namespace mara;
+using namespace mara::sedov;
+
+extern "C" {
+
+int64_t mara_sedov_workspace_bytes(int32_t track_count, int64_t cells)
+{
+    if (track_count < 1 || cells < 2 * int64_t(track_count)) return -1;
+    return workspace_bytes(track_count, cells);
+}
+
+int mara_sedov_stage(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                     const double* radii, const double* u, const double* ghost_in, const double* ghost_out, double dt,
+                     int32_t use_plm, double* radii_out, double* u_out, double* prim, double* grad, double* radial,
+                     double* polar, int32_t* polar_index, void* workspace, int32_t* failures, void* stream)
+{
+    if (int r = check_tracks(track_count, cells, cell_offset, theta)) return r;
+    MARA_REQUIRE(radii && u && ghost_in && ghost_out && radii_out && u_out && workspace, "mara_sedov_stage: null buffer");
+    MARA_REQUIRE(radii_out != radii && u_out != u, "mara_sedov_stage: outputs must not alias inputs");
+    cudaStream_t s = as_stream(stream);
+    Workspace w = carve(workspace, track_count, cells);
+    Stage S{};
+    S.t = Tracks{track_count, cells, cell_offset, theta};
+    S.r = radii;
+    S.u = u;
+    S.gin = ghost_in;
+    S.gout = ghost_out;
+    S.dt = dt;
+    S.use_plm = use_plm != 0;
+    S.r_out = radii_out;
+    S.u_out = u_out;
+    S.P = prim ? prim : w.P;
+    S.rf = radial ? radial : w.rf;
+    S.pf = polar ? polar : w.pf;
+    S.pil = polar_index ? polar_index : w.pil;
+    S.pir = polar_index ? polar_index + w.np_max : w.pir;
+    S.np_max = w.np_max;
+    S.failures = failures;
+    S.grad_out = grad;
+    return run_stage(S, s);
+}
+
+int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                       double* radii, double* u, const double* ghost_in, const double* ghost_out, double dt,
+                       int32_t rk_order, int32_t use_plm, void* workspace, int32_t* failures, void* stream)
+{
+    if (int r = check_tracks(track_count, cells, cell_offset, theta)) return r;
+    MARA_REQUIRE(radii && u && ghost_in && ghost_out && workspace, "mara_sedov_advance: null buffer");
+    MARA_REQUIRE(rk_order >= 1 && rk_order <= 3, "mara_sedov_advance: rk_order must be 1, 2 or 3");
+    cudaStream_t s = as_stream(stream);
+    const int T = track_count;
+    Workspace w = carve(workspace, T, cells);
+    Stage base{};
+    base.t = Tracks{T, cells, cell_offset, theta};
+    base.dt = dt;
+    base.use_plm = use_plm != 0;
+    base.P = w.P;
+    base.rf = w.rf;
+    base.pf = w.pf;
+    base.pil = w.pil;
+    base.pir = w.pir;
+    base.np_max = w.np_max;
+    base.failures = failures;
+    auto stage = [&](int k, const double* rin, const double* uin, double* rout, double* uout, const double* rb,
+                     const double* ub, double b, double b1) {
+        Stage S = base;
+        S.r = rin;
+        S.u = uin;
+        S.gin = ghost_in + 5 * int64_t(T) * k;
+        S.gout = ghost_out + 5 * int64_t(T) * k;
+        S.r_out = rout;
+        S.u_out = uout;
+        S.r_base = rb;
+        S.u_base = ub;
+        S.b = b;
+        S.b1 = b1;
+        return run_stage(S, s);
+    };
+    double* ra = w.r_stage[0];
+    double* ua = w.u_stage[0];
+    double* rb = w.r_stage[1];
+    double* ub = w.u_stage[1];
+    const int64_t F = cells + T;
+    if (rk_order == 1)
+    {
+        if (int r = stage(0, radii, u, ra, ua, nullptr, nullptr, 0, 0)) return r;
+    }
+    else if (rk_order == 2)
+    {
+        // u1 = L(u0); u = u0 / 2 + L(u1) / 2 (app_control.hpp:178-183)
+        if (int r = stage(0, radii, u, ra, ua, nullptr, nullptr, 0, 0)) return r;
+        if (int r = stage(1, ra, ua, rb, ub, radii, u, 1.0 / 2, 1.0 / 2)) return r;
+        ra = rb;
+        ua = ub;
+    }
+    else
+    {
+        // u1 = L(u0); u2 = 3/4 u0 + 1/4 L(u1); u = 1/3 u0 + 2/3 L(u2) (app_control.hpp:184-190)
+        if (int r = stage(0, radii, u, ra, ua, nullptr, nullptr, 0, 0)) return r;
+        if (int r = stage(1, ra, ua, rb, ub, radii, u, 3.0 / 4, 1.0 / 4)) return r;
+        if (int r = stage(2, rb, ub, ra, ua, radii, u, 1.0 / 3, 2.0 / 3)) return r;
+    }
+    MARA_CUDA(cudaMemcpyAsync(radii, ra, F * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    MARA_CUDA(cudaMemcpyAsync(u, ua, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return MARA_OK;
+}
+
+int mara_sedov_min_spacing(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* radii,
+                           double* out, void* stream)
+{
+    MARA_REQUIRE(track_count >= 1 && cells >= 1 && cell_offset && radii && out, "mara_sedov_min_spacing: bad argument");
+    cudaStream_t s = as_stream(stream);
+    const double inf = INFINITY;
+    MARA_CUDA(cudaMemcpyAsync(out, &inf, sizeof inf, cudaMemcpyHostToDevice, s));
+    MARA_CUDA(cudaStreamSynchronize(s));   // the host value lives on this stack frame
+    min_spacing_kernel<<<blocks_for(cells), 256, 0, s>>>(Tracks{track_count, cells, cell_offset, nullptr}, radii,
+                                                         reinterpret_cast<unsigned long long*>(out));
+    return launch_status("sedov min_spacing_kernel");
+}
+
+} // extern "C"

@@ -1,0 +1,124 @@
+"""Host-side mirror of the reference's spherical-track SRHD scheme
+(src/scheme_sedov2d.hpp, driven by problems/sedov2d.cpp).
+
+`Tracks` holds a set of radial tracks resident on one GPU in CSR form (see
+include/mara_gb300.h): face radii, polar bounds and conserved volume
+integrals. `advance` is the driver's RK step (control::advance_runge_kutta of
+the forward-Euler advance); `stage` runs one forward-Euler advance and can
+return the scheme's intermediate arrays (sedov::recover_primitive,
+radial_gradient, radial_godunov_data, polar_godunov_data) for parity checks.
+`generate_radial_track` is sedov::generate_radial_track. Every call goes
+through libmara_gb300.so; errors raise MaraError.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from ._capi import check, lib
+
+GAMMA = 4.0 / 3.0
+
+
+def generate_radial_track(r0: float, r1: float, theta0: float, theta1: float, aspect: float) -> np.ndarray:
+    """Face radii of a log-spaced track (scheme_sedov2d.cpp:108-129):
+    int(pi / (theta1 - theta0) / aspect) faces from r0 to r1."""
+    n = int(math.pi / (theta1 - theta0) / aspect)
+    a, b = math.log10(r0), math.log10(r1)
+    return np.array([10.0 ** (a + (b - a) * float(i) / float(n - 1)) for i in range(n)])
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Tracks:
+    """Radial tracks on the GPU. ncells[j] cells on track j, theta (T, 2)
+    polar bounds, radii the concatenated face radii, u the conserved volume
+    integrals as (cells, 5) tuples (the reference's layout) or (5, cells)."""
+
+    def __init__(self, ncells, theta, radii, u, device="cuda"):
+        ncells = np.asarray(ncells, dtype=np.int64)
+        self.T = len(ncells)
+        self.cells = int(ncells.sum())
+        if np.any(ncells < 2):
+            raise ValueError("every track needs at least 2 cells")
+        co = np.concatenate([[0], np.cumsum(ncells)]).astype(np.int64)
+        self.ncells = ncells
+        self.co = torch.from_numpy(co).to(device)
+        self.theta = torch.from_numpy(np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))).to(device)
+        radii = np.asarray(radii, dtype=np.float64)
+        if radii.size != self.cells + self.T:
+            raise ValueError("radii must hold ncells[j] + 1 faces per track")
+        self.radii = torch.from_numpy(radii.copy()).to(device)
+        u = np.asarray(u, dtype=np.float64)
+        soa = u.reshape(self.cells, 5).T if u.shape != (5, self.cells) else u
+        self.u = torch.from_numpy(np.ascontiguousarray(soa)).to(device)
+        nbytes = lib.mara_sedov_workspace_bytes(self.T, self.cells)
+        if nbytes < 0:
+            check(1, "mara_sedov_workspace_bytes")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        self.failures = torch.zeros(1, dtype=torch.int32, device=device)
+
+    @property
+    def polar_capacity(self) -> int:
+        return 2 * self.cells + self.T
+
+    def polar_offsets(self) -> list[int]:
+        """First transverse face of each interface j | j+1, and the total."""
+        co = self.co.cpu().numpy()
+        return [int(co[j] + co[j + 1] - co[1] + j) for j in range(self.T)]
+
+    def _ghosts(self, ghost, stages):
+        g = torch.as_tensor(np.asarray(ghost, dtype=np.float64), device=self.u.device)
+        g = g.reshape(-1, self.T, 5)
+        if g.shape[0] < stages:
+            raise ValueError(f"ghost states for {stages} stages are needed")
+        return g.contiguous()
+
+    def advance(self, dt: float, ghost_in, ghost_out, rk_order: int = 1, use_plm: bool = True) -> None:
+        """control::advance_runge_kutta of the forward-Euler advance, in place;
+        ghost_in / ghost_out: (stages, T, 5) boundary primitives."""
+        gi, go = self._ghosts(ghost_in, rk_order), self._ghosts(ghost_out, rk_order)
+        check(lib.mara_sedov_advance(self.T, self.cells, self.co.data_ptr(), self.theta.data_ptr(),
+                                     self.radii.data_ptr(), self.u.data_ptr(), gi.data_ptr(), go.data_ptr(), dt,
+                                     rk_order, int(use_plm), self.workspace.data_ptr(), self.failures.data_ptr(),
+                                     _stream()), "mara_sedov_advance")
+
+    def stage(self, dt: float, ghost_in, ghost_out, use_plm: bool = True) -> dict:
+        """One forward-Euler advance into new arrays, with the intermediate
+        arrays; the tracks themselves are unchanged."""
+        dev = self.u.device
+        C, F, NP = self.cells, self.cells + self.T, self.polar_capacity
+        out = {"radii": torch.empty(F, dtype=torch.float64, device=dev),
+               "u": torch.empty(5, C, dtype=torch.float64, device=dev),
+               "prim": torch.empty(5, C, dtype=torch.float64, device=dev),
+               "grad": torch.empty(5, C, dtype=torch.float64, device=dev),
+               "radial": torch.empty(6, F, dtype=torch.float64, device=dev),
+               "polar": torch.empty(6, NP, dtype=torch.float64, device=dev),
+               "polar_index": torch.empty(2, NP, dtype=torch.int32, device=dev)}
+        gi, go = self._ghosts(ghost_in, 1), self._ghosts(ghost_out, 1)
+        check(lib.mara_sedov_stage(self.T, C, self.co.data_ptr(), self.theta.data_ptr(), self.radii.data_ptr(),
+                                   self.u.data_ptr(), gi.data_ptr(), go.data_ptr(), dt, int(use_plm),
+                                   out["radii"].data_ptr(), out["u"].data_ptr(), out["prim"].data_ptr(),
+                                   out["grad"].data_ptr(), out["radial"].data_ptr(), out["polar"].data_ptr(),
+                                   out["polar_index"].data_ptr(), self.workspace.data_ptr(),
+                                   self.failures.data_ptr(), _stream()), "mara_sedov_stage")
+        return out
+
+    def min_spacing(self) -> float:
+        """sedov::minimum_spacing over every track."""
+        out = torch.empty(1, dtype=torch.float64, device=self.u.device)
+        check(lib.mara_sedov_min_spacing(self.T, self.cells, self.co.data_ptr(), self.radii.data_ptr(),
+                                         out.data_ptr(), _stream()), "mara_sedov_min_spacing")
+        return float(out.item())
+
+    def failure_count(self) -> int:
+        return int(self.failures.item())
+
+    def host_state(self) -> tuple[np.ndarray, np.ndarray]:
+        """(radii, u as (cells, 5) tuples) on the host."""
+        return self.radii.cpu().numpy(), self.u.cpu().numpy().T.copy()
