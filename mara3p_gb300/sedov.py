@@ -31,6 +31,54 @@ def generate_radial_track(r0: float, r1: float, theta0: float, theta1: float, as
     return np.array([10.0 ** (a + (b - a) * float(i) / float(n - 1)) for i in range(n)])
 
 
+def conserved_density(prim: np.ndarray, gamma: float = GAMMA) -> np.ndarray:
+    """srhd::conserved_density (src/physics_srhd.hpp:291-304), c = 1, of
+    (n, 5) primitives (rho, u1, u2, u3, p) with four-velocity components."""
+    rho, uu, p = prim[:, 0], prim[:, 1:4], prim[:, 4]
+    W = np.sqrt(1.0 + (uu ** 2).sum(1))
+    D = rho * W
+    h = (rho + p * (1.0 + 1.0 / (gamma - 1.0))) / rho
+    out = np.empty_like(prim)
+    out[:, 0] = D
+    out[:, 1:4] = (D * h)[:, None] * uu
+    out[:, 4] = D * (h * W - 1.0) - p
+    return out
+
+
+def cell_volumes(radii: np.ndarray, theta0: float, theta1: float) -> np.ndarray:
+    """sedov::cell_volume of consecutive faces of one track."""
+    dcost = -(math.cos(theta1) - math.cos(theta0))
+    return 2.0 * math.pi * (radii[1:] ** 3 - radii[:-1] ** 3) / 3.0 * dcost
+
+
+def seeded_tracks(track_count: int, aspect: float = 2.0, r0: float = 1.0, r1: float = 1.8, seed: int = 0,
+                  focus: float = 0.0):
+    """Tracks laid out as problems/sedov2d.cpp:528-561 lays them out (polar
+    bounds from its "focus" spacing, each track from generate_radial_track
+    between r0 and r1) holding a seeded relativistic wind with a hot core:
+    rho ~ r^-2 (+-5%), radial four-velocity 0.4 (+-0.02), polar 0 (+-0.01),
+    pressure 1e-3 rho plus 0.3 inside r < (r0 + r1) / 2.
+    Returns (ncells, theta (T, 2), radii, u (cells, 5))."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, track_count + 1)
+    theta = np.pi * (x + focus * (x - 1) * x) / (1 + 2 * focus * (x - 1) * x)
+    ncells, radii, cons = [], [], []
+    for j in range(track_count):
+        rf = generate_radial_track(r0, r1, theta[j], theta[j + 1], aspect)
+        rc = 0.5 * (rf[:-1] + rf[1:])
+        n = len(rc)
+        pr = np.zeros((n, 5))
+        pr[:, 0] = rc ** -2 * (1 + 0.05 * rng.uniform(-1, 1, n))
+        pr[:, 1] = 0.4 + 0.02 * rng.uniform(-1, 1, n)
+        pr[:, 2] = 0.01 * rng.uniform(-1, 1, n)
+        pr[:, 4] = 1e-3 * pr[:, 0] + np.where(rc < 0.5 * (r0 + r1), 0.3, 0.0)
+        cons.append(conserved_density(pr) * cell_volumes(rf, theta[j], theta[j + 1])[:, None])
+        ncells.append(n)
+        radii.append(rf)
+    return (np.array(ncells, np.int64), np.stack([theta[:-1], theta[1:]], 1), np.concatenate(radii),
+            np.concatenate(cons))
+
+
 def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
