@@ -715,9 +715,9 @@ def run_sedov(args):
     peak, kind = measured_peaks()
     achieved = (80.0 * C + 16.0 * F) * rk / (ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "whole step (prim, radial, polar, update kernels; bound by FP64 recovery and "
+            "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels; bound by FP64 recovery and "
                                        "HLLC arithmetic, not by HBM)", "peak_source": f"{kind} hbm_gbs"}
-    extra = {"gpu_launches": 4 * rk * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
+    extra = {"gpu_launches": 5 * rk * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
     if not args.no_e2e:
         # through the public call with host buffers: state to the GPU, one
         # step, state back, every step

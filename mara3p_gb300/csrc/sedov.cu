@@ -14,10 +14,11 @@
 // (mesh::transverse_faces, src/mesh_sliding.hpp:122-172); interface j's
 // faces start at po(j) = co[j] + co[j+1] - co[1] + j.
 //
-// One stage = four kernels, one thread per item:
+// One stage = five kernels, one thread per item:
 //   prim_kernel    cell: volume, u / dV, SRHD Newton recovery
-//   radial_kernel  face: PLM slopes of both neighbours on the cell-centre
-//                  radii, HLLC flux across the contact and the contact speed;
+//   grad_kernel    cell: PLM slope on the cell-centre radii (zero at both ends)
+//   radial_kernel  face: faces states from both neighbours' slopes, HLLC flux
+//                  across the contact and the contact speed;
 //                  boundary faces: moving-face HLLC against the ghost states;
 //                  moves the face by speed * dt (and the RK combination)
 //   polar_kernel   transverse face: merge-path position in the two tracks'
@@ -25,8 +26,9 @@
 //   update_kernel  cell: radial flux differences, the polar fluxes binned on
 //                  the cell in face order, spherical source terms, u + du
 //                  (and the RK combination)
-// Radial slopes are recomputed by the faces that need them (two per cell)
-// and by the polar samples, so no gradient array is stored.
+// The slopes are stored once per cell: every radial face reads two and every
+// transverse face samples up to four (each slope costs 15 FP64 divisions,
+// and FP64 runs at a small fraction of the FP32 rate on this part).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -67,14 +69,13 @@ struct Stage
     double* u_out;
     // workspace
     double* P;              // [5][C] primitives
+    double* G;              // [5][C] radial slopes
     double* rf;             // [6][F] radial flux and contact speed
     double* pf;             // [6][NPmax] polar flux and area
     int32_t* pil;           // [NPmax] merge counters
     int32_t* pir;
     int64_t np_max;
     int* failures;
-    // optional copies for parity checks
-    double* grad_out;       // [5][C]
 };
 
 __device__ inline int64_t track_of(const int64_t* off, int T, int64_t x)
@@ -138,6 +139,11 @@ __device__ inline SPrim<double> load_ghost(const double* g, int j)
 }
 
 // the radial slope of cell i (local) of track j: zero at both ends
+__device__ inline void load_slope(const Stage& S, int64_t c, double g[5])
+{
+    for (int k = 0; k < 5; ++k) g[k] = S.G[k * S.t.C + c];
+}
+
 __device__ inline void radial_slope(const Stage& S, int j, int64_t i, int64_t n, double g[5])
 {
     for (int k = 0; k < 5; ++k) g[k] = 0.0;
@@ -263,6 +269,19 @@ __global__ void __launch_bounds__(256) prim_kernel(const Stage S)
     }
 }
 
+// radial_gradient (scheme_sedov2d.cpp:188-203)
+__global__ void __launch_bounds__(256) grad_kernel(const Stage S)
+{
+    const int64_t C = S.t.C;
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < C; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        const int j = int(track_of(S.t.co, S.t.T, c));
+        double g[5];
+        radial_slope(S, j, c - S.t.co[j], S.t.co[j + 1] - S.t.co[j], g);
+        for (int k = 0; k < 5; ++k) S.G[k * C + c] = g[k];
+    }
+}
+
 __global__ void __launch_bounds__(256) radial_kernel(const Stage S)
 {
     const int64_t C = S.t.C, F = C + S.t.T;
@@ -299,8 +318,8 @@ __global__ void __launch_bounds__(256) radial_kernel(const Stage S)
         {
             // radial_godunov_data (scheme_sedov2d.cpp:208-230)
             double gl[5], gr[5];
-            radial_slope(S, j, i - 1, n, gl);
-            radial_slope(S, j, i, n, gr);
+            load_slope(S, c0 + i - 1, gl);
+            load_slope(S, c0 + i, gr);
             const double drl = S.r[f] - S.r[f - 1], drr = S.r[f + 1] - S.r[f];
             SPrim<double> pl = load_prim(S.P, C, c0 + i - 1), pr = load_prim(S.P, C, c0 + i);
             for (int k = 0; k < 5; ++k)
@@ -316,12 +335,6 @@ __global__ void __launch_bounds__(256) radial_kernel(const Stage S)
         // delta_face_positions + the RK combination
         const double moved = S.r[f] + speed * S.dt;
         S.r_out[f] = S.r_base ? S.r_base[f] * S.b + moved * S.b1 : moved;
-        if (S.grad_out && i < n)
-        {
-            double g[5];
-            radial_slope(S, j, i, n, g);
-            for (int k = 0; k < 5; ++k) S.grad_out[k * C + c0 + i] = g[k];
-        }
     }
 }
 
@@ -338,9 +351,9 @@ __device__ inline SPrim<double> sample(const Stage& S, int j, double r, int64_t 
     for (int64_t guard = 0; guard <= n && r > rf[index + 1]; ++guard) ++index;
     index = max(int64_t(0), min(index, n - 1));
     const double rc = 0.5 * (rf[index] + rf[index + 1]);
-    double g[5];
-    radial_slope(S, j, index, n, g);
     const int64_t c = S.t.co[j] + index;
+    double g[5];
+    load_slope(S, c, g);
     SPrim<double> out;
     for (int k = 0; k < 5; ++k) set_comp(out, k, S.P[k * S.t.C + c] + g[k] * (r - rc));
     return out;
@@ -508,6 +521,7 @@ __global__ void min_spacing_kernel(Tracks t, const double* r, unsigned long long
 struct Workspace
 {
     double* P;
+    double* G;
     double* rf;
     double* pf;
     int32_t* pil;
@@ -524,7 +538,7 @@ int64_t workspace_bytes(int T, int64_t C)
 {
     const int64_t F = C + T, NP = np_bound(T, C);
     auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
-    return al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) + 256 + 256;
+    return 2 * al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) + 256 + 256;
 }
 
 Workspace carve(void* base, int T, int64_t C)
@@ -534,6 +548,7 @@ Workspace carve(void* base, int T, int64_t C)
     auto take = [&](int64_t bytes) { char* q = p; p += (bytes + 255) / 256 * 256; return q; };
     Workspace w;
     w.P = reinterpret_cast<double*>(take(5 * C * 8));
+    w.G = reinterpret_cast<double*>(take(5 * C * 8));
     w.rf = reinterpret_cast<double*>(take(6 * F * 8));
     w.pf = reinterpret_cast<double*>(take(6 * NP * 8));
     w.pil = reinterpret_cast<int32_t*>(take(NP * 4));
@@ -552,6 +567,8 @@ int run_stage(Stage S, cudaStream_t s)
     const int64_t C = S.t.C, F = C + S.t.T;
     prim_kernel<<<blocks_for(C), 256, 0, s>>>(S);
     if (int r = launch_status("sedov prim_kernel")) return r;
+    grad_kernel<<<blocks_for(C), 256, 0, s>>>(S);
+    if (int r = launch_status("sedov grad_kernel")) return r;
     radial_kernel<<<blocks_for(F), 256, 0, s>>>(S);
     if (int r = launch_status("sedov radial_kernel")) return r;
     polar_kernel<<<blocks_for(S.np_max), 256, 0, s>>>(S);
@@ -604,13 +621,13 @@ int mara_sedov_stage(int32_t track_count, int64_t cells, const int64_t* cell_off
     S.r_out = radii_out;
     S.u_out = u_out;
     S.P = prim ? prim : w.P;
+    S.G = grad ? grad : w.G;
     S.rf = radial ? radial : w.rf;
     S.pf = polar ? polar : w.pf;
     S.pil = polar_index ? polar_index : w.pil;
     S.pir = polar_index ? polar_index + w.np_max : w.pir;
     S.np_max = w.np_max;
     S.failures = failures;
-    S.grad_out = grad;
     return run_stage(S, s);
 }
 
@@ -629,6 +646,7 @@ int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_o
     base.dt = dt;
     base.use_plm = use_plm != 0;
     base.P = w.P;
+    base.G = w.G;
     base.rf = w.rf;
     base.pf = w.pf;
     base.pil = w.pil;
