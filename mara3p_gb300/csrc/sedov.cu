@@ -184,10 +184,9 @@ __device__ inline int hllc_mode(const SPrim<double>& pl, const SPrim<double>& pr
         u_hll[k] = rdiv(radd(rsub(rmul(ar, ur[k]), rmul(al, ul[k])), rsub(fl[k], fr[k])), rsub(ar, al));
         f_hll[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
     }
-    const double c2 = 1.0;
     const double n[3] = {double(axis == 0), double(axis == 1), double(axis == 2)};
-    const double ue_hll = radd(u_hll[4], rmul(u_hll[0], c2));
-    const double fe_hll = radd(f_hll[4], rmul(f_hll[0], c2));
+    const double ue_hll = radd(u_hll[4], u_hll[0]);
+    const double fe_hll = radd(f_hll[4], f_hll[0]);
     const double um_hll = radd(radd(radd(0.0, rmul(u_hll[1], n[0])), rmul(u_hll[2], n[1])), rmul(u_hll[3], n[2]));
     const double fm_hll = radd(radd(radd(0.0, rmul(f_hll[1], n[0])), rmul(f_hll[2], n[1])), rmul(f_hll[3], n[2]));
     const double a = fe_hll;
@@ -195,17 +194,17 @@ __device__ inline int hllc_mode(const SPrim<double>& pl, const SPrim<double>& pr
     const double c = um_hll;
     const double d = rsub(rmul(b, b), rmul(rmul(4.0, a), c));
     const double as = d < 0.0 ? 0.0
-                    : rmul(fabs(a) > 1e-8 ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(2.0, a)) : rdiv(-c, b), c2);
+                    : (fabs(a) > 1e-8 ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(2.0, a)) : rdiv(-c, b));
     if (isnan(as) || as < -1e3 || as > 1e3)
     {
         for (int k = 0; k < 5; ++k) F[k] = 0.0;
         if (contact) *contact = 0.0;
         return 1;
     }
-    const double ps = radd(rdiv(rmul(-fe_hll, as), c2), fm_hll);
+    const double ps = radd(rmul(-fe_hll, as), fm_hll);
     auto star = [&](const double u[5], const double f[5], const SPrim<double>& p, double s, double face) {
         const double v = normal_velocity(p, axis);
-        const double e = radd(u[4], rmul(u[0], c2));
+        const double e = radd(u[4], u[0]);
         const double m = radd(radd(radd(0.0, rmul(u[1], n[0])), rmul(u[2], n[1])), rmul(u[3], n[2]));
         const double sv = rsub(s, v), sa = rsub(s, as);
         const double es = rdiv(rsub(radd(rmul(e, sv), rmul(ps, as)), rmul(p.p, v)), sa);
@@ -219,7 +218,7 @@ __device__ inline int hllc_mode(const SPrim<double>& pl, const SPrim<double>& pr
             const double ns = rdiv(rmul(nk, sv), sa);
             us[1 + k] = radd(rmul(ms, n[k]), ns);
         }
-        us[4] = rsub(es, rmul(Ds, c2));
+        us[4] = rsub(es, Ds);
         for (int k = 0; k < 5; ++k) F[k] = rsub(radd(f[k], rmul(s, rsub(us[k], u[k]))), rmul(face, us[k]));
     };
     if (mode == ACROSS)

@@ -23,7 +23,7 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     const double D = z.D, tau = z.tau;
     const double SS = __dadd_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(z.S1, z.S1)), __dmul_rn(z.S2, z.S2)),
                                 __dmul_rn(z.S3, z.S3));
-    const double Dc2 = __dmul_rn(D, c2);
+    const double Dc2 = D;   // D * c^2
     const double gm1 = __dadd_rn(gm, -1.0);
     const double b2max = 1.0 - 1e-10;
     bool found = false;
@@ -34,7 +34,7 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     while (iteration <= iter_max)
     {
         double Et = __dadd_rn(__dadd_rn(tau, p), Dc2);
-        double b2 = fmin(__ddiv_rn(__ddiv_rn(__dmul_rn(SS, c2), Et), Et), b2max);
+        double b2 = fmin(__ddiv_rn(__ddiv_rn(SS, Et), Et), b2max);
         double W2 = __ddiv_rn(1.0, __dadd_rn(1.0, -b2));
         double W = __dsqrt_rn(W2);
         double e = __ddiv_rn(__dadd_rn(__dadd_rn(tau, __dmul_rn(Dc2, __dadd_rn(1.0, -W))), __dmul_rn(p, __dadd_rn(1.0, -W2))),
@@ -57,14 +57,14 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     }
     iterations = found ? iteration + 1 : iteration;
     if (temperature_floor > 0.0)
-        p = fmax(p, __dmul_rn(__dmul_rn(temperature_floor, D), c2));
+        p = fmax(p, __dmul_rn(temperature_floor, D));
     if (!found) return 1;
     if (temperature_floor <= 0.0 && p <= 0.0) return 2;
     double Et = __dadd_rn(__dadd_rn(tau, Dc2), p);
     prim[0] = __ddiv_rn(D, W0);
-    prim[1] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S1), Et), 1.0);
-    prim[2] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S2), Et), 1.0);
-    prim[3] = __dmul_rn(__ddiv_rn(__dmul_rn(W0, z.S3), Et), 1.0);
+    prim[1] = __ddiv_rn(__dmul_rn(W0, z.S1), Et);   // the reference's trailing * c is a * 1
+    prim[2] = __ddiv_rn(__dmul_rn(W0, z.S2), Et);
+    prim[3] = __ddiv_rn(__dmul_rn(W0, z.S3), Et);
     prim[4] = p;
     return 0;
 }
@@ -193,7 +193,8 @@ struct SPrim { R rho, u[3], p; };
 
 // Explicitly rounded arithmetic, no contraction: in FP64 the fluxes below
 // equal the reference's (compiled without FMA contraction) bit for bit; in
-// FP32 they are the mixed path's.
+// FP32 they are the mixed path's. The reference's factors and divisors of
+// c = 1 (x * 1, x / 1, 1 * 1) are exact identities and are left out.
 __device__ inline double rmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ inline double radd(double a, double b) { return __dadd_rn(a, b); }
 __device__ inline double rsub(double a, double b) { return __dsub_rn(a, b); }
@@ -219,7 +220,7 @@ __device__ inline R lorentz_factor(const SPrim<R>& p) { return rsqrt_rn(radd(R(1
 template<typename R>
 __device__ inline R enthalpy_density(const SPrim<R>& p, R gm)
 {
-    return radd(rmul(p.rho, R(1)), rmul(p.p, radd(R(1), rdiv(R(1), rsub(gm, R(1))))));
+    return radd(p.rho, rmul(p.p, radd(R(1), rdiv(R(1), rsub(gm, R(1))))));
 }
 
 // conserved_density (physics_srhd.hpp:291-304)
@@ -230,8 +231,8 @@ __device__ inline void cons_of(const SPrim<R>& p, R gm, R u[5])
     const R D = rmul(p.rho, W);
     const R h = rdiv(enthalpy_density(p, gm), p.rho);
     u[0] = D;
-    for (int k = 0; k < 3; ++k) u[1 + k] = rdiv(rmul(rmul(D, h), p.u[k]), R(1));
-    u[4] = rsub(rmul(D, rsub(rmul(h, W), rmul(R(1), R(1)))), p.p);
+    for (int k = 0; k < 3; ++k) u[1 + k] = rmul(rmul(D, h), p.u[k]);
+    u[4] = rsub(rmul(D, rsub(rmul(h, W), R(1))), p.p);
 }
 
 // normal three-velocity 0 + n.v along axis (0, 1, 2); the terms of the other
@@ -239,7 +240,7 @@ __device__ inline void cons_of(const SPrim<R>& p, R gm, R u[5])
 template<typename R>
 __device__ inline R normal_velocity(const SPrim<R>& p, int axis)
 {
-    return radd(R(0), rdiv(rmul(R(1), p.u[axis]), lorentz_factor(p)));
+    return radd(R(0), rdiv(p.u[axis], lorentz_factor(p)));
 }
 
 // flux (physics_srhd.hpp:310-324)
@@ -247,7 +248,7 @@ template<typename R>
 __device__ inline void flux_of(const SPrim<R>& p, const R u[5], int axis, R f[5])
 {
     const R vn = normal_velocity(p, axis);
-    const R pt[5] = {rmul(R(0), R(0)), rmul(p.p, R(axis == 0)), rmul(p.p, R(axis == 1)), rmul(p.p, R(axis == 2)),
+    const R pt[5] = {R(0), rmul(p.p, R(axis == 0)), rmul(p.p, R(axis == 1)), rmul(p.p, R(axis == 2)),
                      rmul(p.p, vn)};
     for (int k = 0; k < 5; ++k) f[k] = radd(rmul(vn, u[k]), pt[k]);
 }
@@ -256,15 +257,15 @@ __device__ inline void flux_of(const SPrim<R>& p, const R u[5], int axis, R f[5]
 template<typename R>
 __device__ inline void outer_speeds(const SPrim<R>& p, int axis, R gm, R& am, R& ap)
 {
-    const R a2 = rdiv(rdiv(rmul(rmul(gm, R(1)), p.p), enthalpy_density(p, gm)), R(1));
+    const R a2 = rdiv(rmul(gm, p.p), enthalpy_density(p, gm));
     const R uu = gamma_beta_squared(p);
     const R vn = normal_velocity(p, axis);
-    const R bn = rdiv(vn, R(1));
+    const R bn = vn;
     const R bb = rdiv(uu, radd(R(1), uu));
     const R b2 = rmul(bn, bn);
     R disc = rmul(rmul(a2, rsub(R(1), bb)), rsub(rsub(R(1), rmul(bb, a2)), rmul(b2, rsub(R(1), a2))));
     if (sizeof(R) == sizeof(float)) disc = fmax(disc, R(0));   // FP32 rounding can dip below zero
-    const R k0 = rmul(rsqrt_rn(disc), R(1));
+    const R k0 = rsqrt_rn(disc);
     const R den = rsub(R(1), rmul(bb, a2));
     const R vna = rmul(vn, rsub(R(1), a2));
     am = rdiv(rsub(vna, k0), den);
@@ -319,10 +320,9 @@ __device__ inline int hllc(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R g
         u_hll[k] = rdiv(radd(rsub(rmul(ar, ur[k]), rmul(al, ul[k])), rsub(fl[k], fr[k])), rsub(ar, al));
         f_hll[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
     }
-    const R c2 = rmul(R(1), R(1));
     const R n[3] = {R(axis == 0), R(axis == 1), R(axis == 2)};
-    const R ue_hll = radd(u_hll[4], rmul(u_hll[0], c2));
-    const R fe_hll = radd(f_hll[4], rmul(f_hll[0], c2));
+    const R ue_hll = radd(u_hll[4], u_hll[0]);
+    const R fe_hll = radd(f_hll[4], f_hll[0]);
     const R um_hll = radd(radd(radd(R(0), rmul(u_hll[1], n[0])), rmul(u_hll[2], n[1])), rmul(u_hll[3], n[2]));
     const R fm_hll = radd(radd(radd(R(0), rmul(f_hll[1], n[0])), rmul(f_hll[2], n[1])), rmul(f_hll[3], n[2]));
     const R a = fe_hll;
@@ -330,7 +330,7 @@ __device__ inline int hllc(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R g
     const R c = um_hll;
     const R d = rsub(rmul(b, b), rmul(rmul(R(4), a), c));
     const R as = d < R(0) ? R(0)
-               : rmul(fabs(a) > R(1e-8) ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(R(2), a)) : rdiv(-c, b), c2);
+               : (fabs(a) > R(1e-8) ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(R(2), a)) : rdiv(-c, b));
     if (isnan(as) || as < R(-1e3) || as > R(1e3))
     {
         for (int k = 0; k < 5; ++k) F[k] = f_hll[k];
@@ -338,10 +338,10 @@ __device__ inline int hllc(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R g
         if (R(0) > ar) for (int k = 0; k < 5; ++k) F[k] = fr[k];
         return 1;
     }
-    const R ps = radd(rdiv(rmul(-fe_hll, as), c2), fm_hll);
+    const R ps = radd(rmul(-fe_hll, as), fm_hll);
     auto star = [&](const R u[5], const R f[5], const SPrim<R>& p, R s) {
         const R v = normal_velocity(p, axis);
-        const R e = radd(u[4], rmul(u[0], c2));
+        const R e = radd(u[4], u[0]);
         const R m = radd(radd(radd(R(0), rmul(u[1], n[0])), rmul(u[2], n[1])), rmul(u[3], n[2]));
         const R sv = rsub(s, v), sa = rsub(s, as);
         const R es = rdiv(rsub(radd(rmul(e, sv), rmul(ps, as)), rmul(p.p, v)), sa);
@@ -355,7 +355,7 @@ __device__ inline int hllc(const SPrim<R>& pl, const SPrim<R>& pr, int axis, R g
             const R ns = rdiv(rmul(nk, sv), sa);
             us[1 + k] = radd(rmul(ms, n[k]), ns);
         }
-        us[4] = rsub(es, rmul(Ds, c2));
+        us[4] = rsub(es, Ds);
         for (int k = 0; k < 5; ++k) F[k] = rsub(radd(f[k], rmul(s, rsub(us[k], u[k]))), rmul(R(0), us[k]));
     };
     if (R(0) <= al) { for (int k = 0; k < 5; ++k) F[k] = fl[k]; return 0; }
