@@ -377,11 +377,17 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
 template<int KIND, int COLS, bool DIAG>
 __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A)
 {
+    extern __shared__ __align__(16) unsigned char ring_smem[];   // two-column form: RING_WARP_BYTES per warp
     const int warp = blockIdx.x * SW_WARPS + (threadIdx.x >> 5);
     const int sx = warp / A.tiles_y, sy = warp - sx * A.tiles_y;
     const int i0 = sx * A.sweep_rows;
     if (i0 >= A.N) return;                    // uniform per warp
-    if (COLS == 2) sweep_strip2<KIND, DIAG>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
+    if constexpr (COLS == 2)
+    {
+        unsigned char* base = ring_smem + (threadIdx.x >> 5) * RING_WARP_BYTES;
+        const Ring2 ring{reinterpret_cast<double2*>(base), reinterpret_cast<float2*>(base + RING_U_BYTES)};
+        sweep_strip2<KIND, DIAG, true>(A, i0, min(i0 + A.sweep_rows, A.N), sy, ring);
+    }
     else sweep_strip<KIND, DIAG>(A, i0, min(i0 + A.sweep_rows, A.N), sy);
 }
 
@@ -393,12 +399,13 @@ int launch_sweep(Args A, cudaStream_t s)
 {
     static int blocks_per_sm[64] = {};
     static int sm_count[64] = {};
+    const size_t smem = COLS == 2 ? size_t(SW_WARPS) * RING_WARP_BYTES : 0;
     int dev = 0;
     MARA_CUDA(cudaGetDevice(&dev));
     if (blocks_per_sm[dev & 63] == 0)
     {
         int b = 0, n = 0;
-        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS, DIAG>, SW_WARPS * 32, 0));
+        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS, DIAG>, SW_WARPS * 32, smem));
         MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
         sm_count[dev & 63] = n;
         blocks_per_sm[dev & 63] = b > 0 ? b : 1;
@@ -410,7 +417,7 @@ int launch_sweep(Args A, cudaStream_t s)
     A.sweep_rows = std::max(32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
     const int warps = strips_x * A.tiles_y;
-    sweep_kernel<KIND, COLS, DIAG><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, 0, s>>>(A);
+    sweep_kernel<KIND, COLS, DIAG><<<(warps + SW_WARPS - 1) / SW_WARPS, SW_WARPS * 32, smem, s>>>(A);
     return launch_status("minidisk sweep kernel");
 }
 

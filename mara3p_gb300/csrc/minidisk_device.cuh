@@ -651,6 +651,57 @@ __device__ inline void sweep2_prim(const RawRow2& r, float2 p[3])
     p[2] = vmul(m2, inv);
 }
 
+// Per-warp ring of four rows in shared memory, filled by per-lane
+// asynchronous copies (cp.async): the row being recovered (i+2), the row in
+// flight (i+3), and the rows whose stage results are written (i, i+1), which
+// then need no second global load. Each lane copies and reads only its own
+// two columns, so no lane waits on another. Ring slot of row r: r & 3.
+constexpr int RING_ROWS = 4;
+constexpr int RING_U_BYTES = RING_ROWS * 3 * 32 * 16;     // double2 per lane and component
+constexpr int RING_D_BYTES = RING_ROWS * 3 * 32 * 8;      // float2 per lane and component
+constexpr int RING_WARP_BYTES = RING_U_BYTES + RING_D_BYTES;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+struct Ring2
+{
+    double2* u;    // [row slot][component][lane]
+    float2* d;
+};
+
+template<int KIND>
+__device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int jg, size_t NN, int lane)
+{
+    const int slot = row & (RING_ROWS - 1);
+    const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
+    for (int k = 0; k < 3; ++k) cp_async16(&R.u[(slot * 3 + k) * 32 + lane], A.u_in + k * NN + idx);
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) cp_async8(&R.d[(slot * 3 + k) * 32 + lane], A.d1 + k * NN + idx);
+    cp_async_commit();
+}
+
+template<int KIND>
+__device__ inline void ring2_row(const Ring2& R, int row, int lane, RawRow2& r)
+{
+    const int slot = row & (RING_ROWS - 1);
+    for (int k = 0; k < 3; ++k) r.u[k] = R.u[(slot * 3 + k) * 32 + lane];
+    if (KIND == K_MIX2)
+        for (int k = 0; k < 3; ++k) r.d[k] = R.d[(slot * 3 + k) * 32 + lane];
+}
+
 // y slopes of both columns: the left neighbour of the first column is lane
 // l-1's second column, the right neighbour of the second is lane l+1's first.
 __device__ inline void slope_y2(const float2 p[3], float theta, float2 g[3])
@@ -663,8 +714,8 @@ __device__ inline void slope_y2(const float2 p[3], float theta, float2 g[3])
     }
 }
 
-template<int KIND, bool DIAG = false>
-__device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy)
+template<int KIND, bool DIAG = false, bool RING = false>
+__device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy, Ring2 ring = Ring2{})
 {
     const int lane = threadIdx.x & 31;
     const int N = A.N;
@@ -694,15 +745,32 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
 
     float2 pm2[3], pm1[3], p0[3], p1[3];
     RawRow2 raw;
-    sweep2_fetch<KIND>(A, i0 - 2, jg, NN, raw);
-    sweep2_prim<KIND>(raw, pm2);
-    sweep2_fetch<KIND>(A, i0 - 1, jg, NN, raw);
-    sweep2_prim<KIND>(raw, pm1);
-    sweep2_fetch<KIND>(A, i0, jg, NN, raw);
-    sweep2_prim<KIND>(raw, p0);
-    sweep2_fetch<KIND>(A, i0 + 1, jg, NN, raw);
-    sweep2_prim<KIND>(raw, p1);
-    sweep2_fetch<KIND>(A, i0 + 2, jg, NN, raw);
+    if constexpr (RING)
+    {
+        for (int r = i0 - 2; r <= i0 + 1; ++r) ring2_fetch<KIND>(A, ring, r, jg, NN, lane);
+        cp_async_wait_all();
+        ring2_row<KIND>(ring, i0 - 2, lane, raw);
+        sweep2_prim<KIND>(raw, pm2);
+        ring2_row<KIND>(ring, i0 - 1, lane, raw);
+        sweep2_prim<KIND>(raw, pm1);
+        ring2_row<KIND>(ring, i0, lane, raw);
+        sweep2_prim<KIND>(raw, p0);
+        ring2_row<KIND>(ring, i0 + 1, lane, raw);
+        sweep2_prim<KIND>(raw, p1);
+        ring2_fetch<KIND>(A, ring, i0 + 2, jg, NN, lane);     // into the slot of row i0 - 2
+    }
+    else
+    {
+        sweep2_fetch<KIND>(A, i0 - 2, jg, NN, raw);
+        sweep2_prim<KIND>(raw, pm2);
+        sweep2_fetch<KIND>(A, i0 - 1, jg, NN, raw);
+        sweep2_prim<KIND>(raw, pm1);
+        sweep2_fetch<KIND>(A, i0, jg, NN, raw);
+        sweep2_prim<KIND>(raw, p0);
+        sweep2_fetch<KIND>(A, i0 + 1, jg, NN, raw);
+        sweep2_prim<KIND>(raw, p1);
+        sweep2_fetch<KIND>(A, i0 + 2, jg, NN, raw);
+    }
     float2 gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
     for (int k = 0; k < 3; ++k)
     {
@@ -718,10 +786,20 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     for (int i = i0; i < i1; ++i)
     {
         float2 p2[3], gx1[3], gy1[3], fxp[3];
-        sweep2_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
-        sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
         CellIn<float2> cin;
-        if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
+        if constexpr (RING)
+        {
+            cp_async_wait_all();                              // row i+2, issued last iteration
+            ring2_row<KIND>(ring, i + 2, lane, raw);
+            sweep2_prim<KIND>(raw, p2);
+            ring2_fetch<KIND>(A, ring, i + 3, jg, NN, lane);  // into the slot of row i-1
+        }
+        else
+        {
+            sweep2_prim<KIND>(raw, p2);                       // row i+2, fetched last iteration
+            sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
+            if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
+        }
         for (int k = 0; k < 3; ++k) gx1[k] = vplm(p0[k], p1[k], p2[k], theta);
         slope_y2(p1, theta, gy1);
         face_flux_f<0, float2>(p0, p1, gx0, gx1, gy0, gy1, bc<float2>(fmaf(float(i + 1), F.dl, -F.R)), yc, F, fxp);
@@ -742,6 +820,19 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             const float right = __shfl_down_sync(0xffffffffu, fy[k].x, 1);
             dfy[k] = vsub(make_float2(fy[k].y, right), fy[k]);
             dfx[k] = vsub(fxp[k], fxm[k]);
+        }
+        if constexpr (RING)
+        {
+            if (interior && writes_state<KIND>(A))
+            {
+                RawRow2 own;
+                ring2_row<KIND>(ring, i, lane, own);
+                for (int k = 0; k < 3; ++k)
+                {
+                    cin.u[k] = own.u[k];
+                    cin.d[k] = own.d[k];
+                }
+            }
         }
         if (interior)
             mixed_cell2<KIND, DIAG>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin,
