@@ -651,12 +651,13 @@ __device__ inline void sweep2_prim(const RawRow2& r, float2 p[3])
     p[2] = vmul(m2, inv);
 }
 
-// Per-warp ring of four rows in shared memory, filled by per-lane
-// asynchronous copies (cp.async): the row being recovered (i+2), the row in
-// flight (i+3), and the rows whose stage results are written (i, i+1), which
-// then need no second global load. Each lane copies and reads only its own
-// two columns, so no lane waits on another. Ring slot of row r: r & 3.
-constexpr int RING_ROWS = 4;
+// Per-warp ring of five rows in shared memory, filled by per-lane
+// asynchronous copies (cp.async): the row being recovered (i+2), two rows in
+// flight (i+3, i+4), and the rows whose stage results are written (i, i+1),
+// which then need no second global load. Each lane copies and reads only its
+// own two columns, so no lane waits on another. Ring slot of row r >= -2:
+// (r + 5) mod 5.
+constexpr int RING_ROWS = 5;
 constexpr int RING_U_BYTES = RING_ROWS * 3 * 32 * 16;     // double2 per lane and component
 constexpr int RING_D_BYTES = RING_ROWS * 3 * 32 * 8;      // float2 per lane and component
 constexpr int RING_WARP_BYTES = RING_U_BYTES + RING_D_BYTES;
@@ -675,6 +676,8 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ int ring_slot(int row) { return (row + RING_ROWS) % RING_ROWS; }
 
 struct Ring2
 {
@@ -685,7 +688,7 @@ struct Ring2
 template<int KIND>
 __device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int jg, size_t NN, int lane)
 {
-    const int slot = row & (RING_ROWS - 1);
+    const int slot = ring_slot(row);
     const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
     for (int k = 0; k < 3; ++k) cp_async16(&R.u[(slot * 3 + k) * 32 + lane], A.u_in + k * NN + idx);
     if (KIND == K_MIX2)
@@ -696,7 +699,7 @@ __device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int j
 template<int KIND>
 __device__ inline void ring2_row(const Ring2& R, int row, int lane, RawRow2& r)
 {
-    const int slot = row & (RING_ROWS - 1);
+    const int slot = ring_slot(row);
     for (int k = 0; k < 3; ++k) r.u[k] = R.u[(slot * 3 + k) * 32 + lane];
     if (KIND == K_MIX2)
         for (int k = 0; k < 3; ++k) r.d[k] = R.d[(slot * 3 + k) * 32 + lane];
@@ -757,7 +760,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         sweep2_prim<KIND>(raw, p0);
         ring2_row<KIND>(ring, i0 + 1, lane, raw);
         sweep2_prim<KIND>(raw, p1);
-        ring2_fetch<KIND>(A, ring, i0 + 2, jg, NN, lane);     // into the slot of row i0 - 2
+        ring2_fetch<KIND>(A, ring, i0 + 2, jg, NN, lane);     // into the slots of rows i0 - 2, i0 - 1
+        ring2_fetch<KIND>(A, ring, i0 + 3, jg, NN, lane);
     }
     else
     {
@@ -789,10 +793,10 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         CellIn<float2> cin;
         if constexpr (RING)
         {
-            cp_async_wait_all();                              // row i+2, issued last iteration
+            cp_async_wait_one();                              // row i+2 (row i+3 may stay in flight)
             ring2_row<KIND>(ring, i + 2, lane, raw);
             sweep2_prim<KIND>(raw, p2);
-            ring2_fetch<KIND>(A, ring, i + 3, jg, NN, lane);  // into the slot of row i-1
+            ring2_fetch<KIND>(A, ring, i + 4, jg, NN, lane);  // into the slot of row i-1
         }
         else
         {
@@ -847,6 +851,9 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             fxm[k] = fxp[k];
         }
     }
+    // the rows fetched beyond the strip are never read, but no copy may land
+    // in shared memory after the warp is gone
+    if constexpr (RING) cp_async_wait_all();
     if constexpr (DIAG) diag_flush(A, acc);
     if (A.amax)
     {
