@@ -87,9 +87,12 @@ __global__ void __launch_bounds__(SW_WARPS * 32, MINB)
 ensemble_sweep_kernel(const Args* __restrict__ table, const int4* __restrict__ items,
                       const int* __restrict__ first, int nchunks, int dynamic, unsigned* counter)
 {
+    extern __shared__ __align__(16) unsigned char ring_smem[];   // two-column form: RING_WARP_BYTES per warp
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * SW_WARPS + (threadIdx.x >> 5);
     const int warps = gridDim.x * SW_WARPS;
+    unsigned char* ring_base = ring_smem + (threadIdx.x >> 5) * RING_WARP_BYTES;
+    const Ring2 ring{reinterpret_cast<double2*>(ring_base), reinterpret_cast<float2*>(ring_base + RING_U_BYTES)};
     int chunk = dynamic ? claim_chunk(counter, lane) : warp;
     while (chunk < nchunks)
     {
@@ -98,7 +101,7 @@ ensemble_sweep_kernel(const Args* __restrict__ table, const int4* __restrict__ i
         {
             const int4 w = __ldg(items + it);
             const Args A = table[w.x];
-            if (COLS == 2) sweep_strip2<KIND>(A, w.z, w.w, w.y);
+            if constexpr (COLS == 2) sweep_strip2<KIND, false, true>(A, w.z, w.w, w.y, ring);
             else sweep_strip<KIND>(A, w.z, w.w, w.y);
         }
         chunk = dynamic ? claim_chunk(counter, lane) : chunk + warps;
@@ -170,18 +173,23 @@ auto sweep_function(int cols, int v)
     return cols == 2 ? sweep_variant<KIND, 2>(v) : sweep_variant<KIND, 1>(v);
 }
 
+// shared memory of the two-column sweep's row rings (one per warp)
+inline size_t ring_bytes(int cols) { return cols == 2 ? size_t(SW_WARPS) * RING_WARP_BYTES : 0; }
+
 template<int KIND>
 int launch_sweep_variant(int cols, int variant, int blocks, cudaStream_t s, const Args* table, const int4* items,
                          const int* first, int nchunks, int dynamic, unsigned* counter)
 {
-    sweep_function<KIND>(cols, variant)<<<blocks, SW_WARPS * 32, 0, s>>>(table, items, first, nchunks, dynamic, counter);
+    sweep_function<KIND>(cols, variant)<<<blocks, SW_WARPS * 32, ring_bytes(cols), s>>>(table, items, first, nchunks,
+                                                                                      dynamic, counter);
     return launch_status("ensemble sweep kernel");
 }
 
 template<int KIND>
 int sweep_occupancy(int cols, int variant, int* blocks)
 {
-    MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, sweep_function<KIND>(cols, variant), SW_WARPS * 32, 0));
+    MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, sweep_function<KIND>(cols, variant), SW_WARPS * 32,
+                                                             ring_bytes(cols)));
     if (*blocks < 1) *blocks = 1;
     return MARA_OK;
 }
