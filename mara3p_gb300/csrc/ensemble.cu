@@ -118,13 +118,14 @@ ensemble_sweep_kernel(const Args* __restrict__ table, const int4* __restrict__ i
 }
 
 __global__ void ensemble_clock_kernel(mara_minidisk_clock* clocks, const ClockArgs* args, int count,
-                                      int end_step, int begin_step)
+                                      int end_step, int begin_step, int key_state)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= count) return;
     ClockArgs a = args[m];
     a.end_step = end_step;
     a.begin_step = begin_step;
+    a.key_state = key_state;
     advance_clock(clocks + m, a);
 }
 
@@ -296,9 +297,13 @@ int enqueue_stages(mara_minidisk_ensemble* e, int phase, bool tuning, cudaStream
     return MARA_OK;
 }
 
-int enqueue_clock(mara_minidisk_ensemble* e, int end_step, int begin_step, cudaStream_t s)
+// phase: the buffer phase of the step that just ran; the mixed CFL
+// conversion reads the step's result, the other buffer when steps flip
+int enqueue_clock(mara_minidisk_ensemble* e, int end_step, int begin_step, int phase, cudaStream_t s)
 {
-    ensemble_clock_kernel<<<(e->count + 63) / 64, 64, 0, s>>>(e->clocks, e->clock_args, e->count, end_step, begin_step);
+    const int key_state = e->flips ? 1 - phase : 0;
+    ensemble_clock_kernel<<<(e->count + 63) / 64, 64, 0, s>>>(e->clocks, e->clock_args, e->count, end_step, begin_step,
+                                                              key_state);
     return launch_status("ensemble clock kernel");
 }
 
@@ -328,16 +333,16 @@ int capture_graph(mara_minidisk_ensemble* e, cudaGraphExec_t* out, F&& body)
 int build_graphs(mara_minidisk_ensemble* e)
 {
     release_graphs(e);
-    if (int r = capture_graph(e, &e->g_begin, [&](cudaStream_t s) { return enqueue_clock(e, 0, 1, s); })) return r;
+    if (int r = capture_graph(e, &e->g_begin, [&](cudaStream_t s) { return enqueue_clock(e, 0, 1, 0, s); })) return r;
     for (int p = 0; p < (e->flips ? 2 : 1); ++p)
     {
         if (int r = capture_graph(e, &e->g_step[p], [&](cudaStream_t s) {
                 if (int q = enqueue_stages(e, p, false, s)) return q;
-                return enqueue_clock(e, 1, 1, s);
+                return enqueue_clock(e, 1, 1, p, s);
             })) return r;
         if (int r = capture_graph(e, &e->g_last[p], [&](cudaStream_t s) {
                 if (int q = enqueue_stages(e, p, false, s)) return q;
-                if (int q = enqueue_clock(e, 1, 0, s)) return q;
+                if (int q = enqueue_clock(e, 1, 0, p, s)) return q;
                 return e->flips && p == 0 ? enqueue_copy_back(e, s) : MARA_OK;
             })) return r;
     }
@@ -608,10 +613,12 @@ int mara_minidisk_ensemble_create(const mara_minidisk_params* params, int32_t co
             {
                 a1.u_in = buf[p]; a1.d_out = e->d1[m];
                 a2.u_in = buf[p]; a2.d1 = e->d1[m]; a2.u_out = buf[1 - p]; a2.amax = reduce;
+                a2.amax_key = 1;
             }
             else
             {
                 a1.u_in = buf[p]; a1.u_out = buf[1 - p]; a1.amax = reduce;
+                a1.amax_key = precision == MARA_MIXED;
             }
             e->host_table[size_t(p * 2 + 0) * count + m] = a1;
             e->host_table[size_t(p * 2 + 1) * count + m] = a2;
@@ -624,6 +631,12 @@ int mara_minidisk_ensemble_create(const mara_minidisk_params* params, int32_t co
             }
         }
         cargs[m] = clock_args(params + m, dt_mode, rk_order, 1, 1);
+        if (precision == MARA_MIXED && dt_mode == MARA_DT_CFL)
+        {
+            cargs[m].wavespeed_key = 1;
+            cargs[m].u_key[0] = buf[0];
+            cargs[m].u_key[1] = buf[1];
+        }
         jobs[m] = CopyJob{e->alt[m], e->states[m], (long long)(3 * size_t(e->sizes[m]) * e->sizes[m])};
     }
     auto upload = [&](void** dst, const void* src, size_t n) -> int {

@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
         for (int k = 0; k < 6; ++k) b6[k] = A.bin[k];
     }
     double local_max = 0.0;
-    float local_max_f = 0.0f;
+    unsigned long long local_key = 0ull;   // mixed kinds
     float bf[6];
     for (int k = 0; k < 6; ++k) bf[k] = d2f(b6[k]);
     const float dtf = d2f(dt);
@@ -354,13 +354,16 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
             const float fy3[3] = {float(dfy[0]), float(dfy[1]), float(dfy[2])};
             CellIn<float> cin;
             load_cell_in<KIND>(A, idx, NN, cin);
-            mixed_cell<KIND>(A, float(S.xc[i]), float(S.yc[j]), p3, fx3, fy3, bf, dtf, idx, NN, cin, local_max_f);
+            mixed_cell<KIND>(A, float(S.xc[i]), float(S.yc[j]), p3, fx3, fy3, bf, dtf, idx, NN, cin, local_key);
         }
     }
 
-    if (A.amax)
+    if (A.amax && sizeof(R) == sizeof(float))
     {
-        if (sizeof(R) == sizeof(float)) local_max = double(local_max_f);
+        flush_speed_key(A, local_key);
+    }
+    else if (A.amax)
+    {
         for (int o = 16; o > 0; o >>= 1) local_max = fmax(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
         if ((tid & 31) == 0) S.wmax[tid >> 5] = local_max;
         __syncthreads();
@@ -521,8 +524,9 @@ int launch_rates(const Args& A, const double* u, const float* d1, double* out, c
 // ------------------------------------------------------------- clock kernel
 __global__ void clock_kernel(mara_minidisk_clock* c, const ClockArgs a)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    advance_clock(c, a);
+    // two lanes: the stage binaries (FP64 Kepler solves) run side by side
+    if (threadIdx.x >= 2 || blockIdx.x != 0) return;
+    advance_clock(c, a, int(threadIdx.x), 2);
 }
 
 // ------------------------------------------------------------- small kernels
@@ -564,31 +568,6 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
 
 // Fastest wavespeed of a state in FP32 (mixed-precision runs): the same
 // estimate as the fused reduction of the mixed stage kernels.
-__global__ void wavespeed_f32_kernel(int N, FloatConsts F, const double* u, unsigned long long* amax)
-{
-    __shared__ float wm[NT / 32];
-    size_t NN = size_t(N) * N;
-    float m = 0.0f;
-    for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
-    {
-        int i = int(c / N), j = int(c % N);
-        float x = fmaf(float(i) + 0.5f, F.dl, -F.R), y = fmaf(float(j) + 0.5f, F.dl, -F.R);
-        float cs = sqrt_fast(rsqrt_fast(fmaf(x, x, y * y) + F.rs2) * F.inv_mach2);
-        float inv = rcp_fast(d2f(u[c]));
-        float vx = d2f(u[NN + c]) * inv, vy = d2f(u[2 * NN + c]) * inv;
-        m = fmaxf(m, fmaxf(fabsf(vx), fabsf(vy)) + cs);
-    }
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        float r = 0.0f;
-        for (int w = 0; w < int(blockDim.x / 32); ++w) r = fmaxf(r, wm[w]);
-        atomicMax(amax, (unsigned long long)__double_as_longlong(double(r)));
-    }
-}
-
 // Fastest wavespeed of a state (for the first CFL step), FP64.
 __global__ void wavespeed_kernel(int N, int n, int level, double R, double rs2, double mach,
                                  const double* u, unsigned long long* amax)
@@ -597,16 +576,7 @@ __global__ void wavespeed_kernel(int N, int n, int level, double R, double rs2, 
     size_t NN = size_t(N) * N;
     double m = 0.0;
     for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
-    {
-        int i = int(c / N), j = int(c % N);
-        uint64_t bi = uint64_t(i / n), bj = uint64_t(j / n);
-        int ki = i - int(bi) * n, kj = j - int(bj) * n;
-        double x = 0.5 * (vertex(R, n, level, bi, ki) + vertex(R, n, level, bi, ki + 1));
-        double y = 0.5 * (vertex(R, n, level, bj, kj) + vertex(R, n, level, bj, kj + 1));
-        double cs = sqrt(-(-1.0 / sqrt((x * x + y * y) + rs2)) / mach / mach);
-        double vx = u[NN + c] / u[c], vy = u[2 * NN + c] / u[c];
-        m = fmax(m, fmax(fmax(fabs(vx - cs), fabs(vx + cs)), fmax(fabs(vy - cs), fabs(vy + cs))));
-    }
+        m = fmax(m, cell_wavespeed(u, NN, N, n, level, R, rs2, mach, c));
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
     __syncthreads();
@@ -778,6 +748,14 @@ ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, 
 {
     ClockArgs a;
     a.diag = nullptr;
+    a.wavespeed_key = 0;
+    a.key_state = 0;
+    a.u_key[0] = a.u_key[1] = nullptr;
+    a.N = sd->block_size << sd->depth;
+    a.n = sd->block_size;
+    a.level = sd->depth;
+    a.rs2 = std::pow(sd->softening_length, 2.0);
+    a.mach = sd->mach_number;
     a.R = sd->domain_radius;
     a.dl = cell_size(sd, sd->depth);
     a.cfl = sd->cfl;
@@ -793,10 +771,16 @@ ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, 
 }
 
 int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
-               int end_step, int begin_step, cudaStream_t s, mara_minidisk_diagnostics* diag = nullptr)
+               int end_step, int begin_step, cudaStream_t s, mara_minidisk_diagnostics* diag = nullptr,
+               const double* key_state = nullptr)
 {
     ClockArgs a = clock_args(sd, dt_mode, rk_order, end_step, begin_step);
     a.diag = diag;
+    if (key_state)
+    {
+        a.wavespeed_key = 1;
+        a.u_key[0] = key_state;
+    }
     clock_kernel<<<1, 32, 0, s>>>(clock, a);
     return launch_status("minidisk clock kernel");
 }
@@ -932,11 +916,8 @@ int clock_init(const mara_minidisk_params* sd, const double* u, double time, mar
     const int64_t NN = int64_t(N) * N;
     const int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
     auto* amax = reinterpret_cast<unsigned long long*>(&clock->max_wavespeed);
-    if (precision == MARA_MIXED)
-    {
-        wavespeed_f32_kernel<<<blocks, NT, 0, s>>>(N, base_args(sd).f, u, amax);
-        return launch_status("wavespeed_f32_kernel");
-    }
+    // FP64 in both precisions: the CFL dt is an FP64 quantity
+    (void)precision;
     wavespeed_kernel<<<blocks, NT, 0, s>>>(N, sd->block_size, sd->depth, sd->domain_radius,
         std::pow(sd->softening_length, 2.0), sd->mach_number, u, amax);
     return launch_status("wavespeed_kernel");
@@ -1013,6 +994,7 @@ int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_m
             Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1; a1.diag = rate0;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = alt; a2.amax = amax;
+            a2.amax_key = 1;
             a2.diag = rate1;
             if (int r = grid_stage(a2, K_MIX2, s)) return r;
             std::swap(cur, alt);
@@ -1020,10 +1002,13 @@ int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_m
         else
         {
             Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.u_out = alt; a1.amax = amax; a1.diag = rate0;
+            a1.amax_key = 1;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             std::swap(cur, alt);
         }
-        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag)) return r;
+        // mixed CFL: the reduction named the fastest cell of the new state cur
+        const double* key_state = precision == MARA_MIXED && amax ? cur : nullptr;
+        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag, key_state)) return r;
     }
     if (cur != u)
         MARA_CUDA(cudaMemcpyAsync(u, cur, 3 * NN * sizeof(double), cudaMemcpyDeviceToDevice, s));

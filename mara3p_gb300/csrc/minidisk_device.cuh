@@ -56,6 +56,7 @@ struct Args
     float* d_out;          // K_MIX1 + RK2: increment out
     const double* pe;      // K_BLOCK: (n+4)^2 AoS primitives
     unsigned long long* amax;  // optional: max fastest wavespeed of u_out (double bits)
+    int amax_key;          // mixed kinds: 1 = write the speed key of the fastest cell (speed_key) instead
     double* diag;          // optional: rate row of this stage (diagnostic sums 0..12 of the stage input)
     FloatConsts f;
 };
@@ -378,6 +379,30 @@ __device__ inline void load_cell_in(const Args& A, size_t idx, size_t NN, CellIn
         for (int k = 0; k < 3; ++k) c.d[k] = __ldg(reinterpret_cast<const float2*>(A.d1 + k * NN + idx));
 }
 
+// The mixed path's CFL reduction: the FP32 wavespeed's bits in the high word
+// and the cell index in the low word. The maximum key names the fastest cell
+// (ties go to the larger index, whatever the launch shape); the clock then
+// evaluates that cell's wavespeed in FP64 from the FP64 state, so the CFL dt
+// is an FP64 quantity as in the FP64 path.
+__device__ __forceinline__ unsigned long long speed_key(float v, size_t idx)
+{
+    return (static_cast<unsigned long long>(__float_as_uint(v)) << 32) | static_cast<unsigned>(idx);
+}
+
+__device__ __forceinline__ unsigned long long key_max(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
+// The end of a warp's CFL reduction: the key, or the FP32 maximum as double
+// bits where the caller asked for the wavespeed itself.
+__device__ inline void flush_speed_key(const Args& A, unsigned long long key)
+{
+    for (int o = 16; o > 0; o >>= 1) key = key_max(key, __shfl_xor_sync(0xffffffffu, key, o));
+    if ((threadIdx.x & 31) == 0)
+    {
+        const float v = __uint_as_float(unsigned(key >> 32));
+        atomicMax(A.amax, A.amax_key ? key : (unsigned long long)__double_as_longlong(double(v)));
+    }
+}
+
 // Fastest wavespeed max(|vx|, |vy|) + cs (iso2d::fastest_wavespeed,
 // physics_iso2d.hpp:108-116) of an FP32 conserved state at a cell whose
 // 1/sqrt(r^2 + rs^2) is pot.
@@ -396,7 +421,7 @@ __device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, flo
 template<int KIND, bool DIAG = false>
 __device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
                                   const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                  const CellIn<float>& in, float& local_max, float* acc = nullptr)
+                                  const CellIn<float>& in, unsigned long long& local_key, float* acc = nullptr)
 {
     float du[3], uc[3], pot;
     cell_increment<float, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
@@ -412,14 +437,14 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
         A.u_out[k * NN + idx] = in.u[k] + f2d(inc);
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), 0.5f, uc[k]) : vadd(uc[k], du[k]);
     }
-    if (A.amax) local_max = fmaxf(local_max, wavespeed_f(A.f, of[0], of[1], of[2], pot));
+    if (A.amax) local_key = key_max(local_key, speed_key(wavespeed_f(A.f, of[0], of[1], of[2], pot), idx));
 }
 
 // The pair form: columns idx and idx + 1 of one row (idx even).
 template<int KIND, bool DIAG = false>
 __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const float2 pc[3], const float2 dfx[3],
                                    const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                   const CellIn<float2>& in, float& local_max, float* acc = nullptr)
+                                   const CellIn<float2>& in, unsigned long long& local_key, float* acc = nullptr)
 {
     float2 du[3], uc[3], pot;
     cell_increment<float2, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
@@ -437,8 +462,8 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), bc<float2>(0.5f), uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax)
-        local_max = fmaxf(local_max, fmaxf(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, pot.x),
-                                           wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, pot.y)));
+        local_key = key_max(local_key, key_max(speed_key(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, pot.x), idx),
+                                               speed_key(wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, pot.y), idx + 1)));
 }
 
 // A warp's diagnostic sums into the stage's rate row: FP32 per lane, a
@@ -559,7 +584,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
     slope_y(p0, theta, gy0);
     face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
 
-    float local_max = 0.0f;
+    unsigned long long local_key = 0ull;
     float acc[DIAG ? DIAG_SUMS : 1] = {};
     for (int i = i0; i < i1; ++i)
     {
@@ -589,7 +614,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell<KIND, DIAG>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max, acc);
+            mixed_cell<KIND, DIAG>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_key, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -601,11 +626,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
         }
     }
     if constexpr (DIAG) diag_flush(A, acc);
-    if (A.amax)
-    {
-        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
-        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
-    }
+    if (A.amax) flush_speed_key(A, local_key);
 }
 
 // ------------------------------------------------------------- two-column sweep
@@ -785,7 +806,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     slope_y2(p0, theta, gy0);
     face_flux_f<0, float2>(pm1, p0, gxm1, gx0, gym1, gy0, bc<float2>(fmaf(float(i0), F.dl, -F.R)), yc, F, fxm);
 
-    float local_max = 0.0f;
+    unsigned long long local_key = 0ull;
     float acc[DIAG ? DIAG_SUMS : 1] = {};
     for (int i = i0; i < i1; ++i)
     {
@@ -840,7 +861,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         }
         if (interior)
             mixed_cell2<KIND, DIAG>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin,
-                                    local_max, acc);
+                                    local_key, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -855,11 +876,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     // in shared memory after the warp is gone
     if constexpr (RING) cp_async_wait_all();
     if constexpr (DIAG) diag_flush(A, acc);
-    if (A.amax)
-    {
-        for (int o = 16; o > 0; o >>= 1) local_max = fmaxf(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
-        if (lane == 0) atomicMax(A.amax, (unsigned long long)__double_as_longlong(double(local_max)));
-    }
+    if (A.amax) flush_speed_key(A, local_key);
 }
 
 // ------------------------------------------------------------- clock
@@ -870,7 +887,29 @@ struct ClockArgs
     int end_step;     // 1: finish the step that just ran (advance time, iteration)
     int begin_step;   // 1: choose dt and stage binaries of the next step
     mara_minidisk_diagnostics* diag;   // optional: integrate the step's rates (end), clear them (begin)
+    // mixed CFL mode: the reduction left the fastest cell's speed key in
+    // max_wavespeed; at the end of a step it becomes that cell's FP64 wavespeed
+    // in the state u_key[key_state] (the step's result)
+    int wavespeed_key, key_state;
+    const double* u_key[2];
+    int N, n, level;
+    double rs2, mach;
 };
+
+// iso2d::fastest_wavespeed at the cell-centre sound speed, FP64, of cell c of
+// the SoA state u (the form of the FP64 stage kernels' reduction)
+__device__ inline double cell_wavespeed(const double* u, size_t NN, int N, int n, int level, double R, double rs2,
+                                        double mach, size_t c)
+{
+    const int i = int(c / N), j = int(c % N);
+    const uint64_t bi = uint64_t(i / n), bj = uint64_t(j / n);
+    const int ki = i - int(bi) * n, kj = j - int(bj) * n;
+    const double x = 0.5 * (vertex(R, n, level, bi, ki) + vertex(R, n, level, bi, ki + 1));
+    const double y = 0.5 * (vertex(R, n, level, bj, kj) + vertex(R, n, level, bj, kj + 1));
+    const double cs = sqrt(-(-1.0 / sqrt((x * x + y * y) + rs2)) / mach / mach);
+    const double vx = u[NN + c] / u[c], vy = u[2 * NN + c] / u[c];
+    return fmax(fmax(fabs(vx - cs), fabs(vx + cs)), fmax(fabs(vy - cs), fabs(vy + cs)));
+}
 
 // Complete the rate rows of the step that ran (torques and power from the
 // force sums and the binary at each stage time) and add them to the time
@@ -904,47 +943,72 @@ __device__ inline void store_binary(double* dst, const Binary& b)
 
 // One clock update: finish the step that just ran (RK2 time average,
 // iteration count) and/or choose the next dt and the stage binaries.
-__device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a)
+// The parts of one clock update. `lanes` threads of one warp may share the
+// begin-step work: lane 0 does everything else, lane 1 (when present)
+// computes the second stage's binary while lane 0 computes the first.
+__device__ inline void clock_end_step(mara_minidisk_clock* c, const ClockArgs& a)
 {
-    if (a.end_step && a.diag) finish_diagnostics(c, a);
-    if (a.end_step)
+    if (a.diag) finish_diagnostics(c, a);
+    if (a.wavespeed_key)
     {
-        double t = c->time, dt = c->dt;
-        if (a.rk_order == 2)
+        const unsigned long long key = __double_as_longlong(c->max_wavespeed);
+        if (key != 0ull)
         {
-            double t2 = (t + dt) + dt;
-            c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
+            const size_t NN = size_t(a.N) * a.N;
+            c->max_wavespeed = cell_wavespeed(a.u_key[a.key_state], NN, a.N, a.n, a.level, a.R, a.rs2, a.mach,
+                                              size_t(unsigned(key)));
         }
-        else
-        {
-            c->time = t + dt;
-        }
-        c->iteration += 1;
     }
+    double t = c->time, dt = c->dt;
+    if (a.rk_order == 2)
+    {
+        double t2 = (t + dt) + dt;
+        c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
+    }
+    else
+    {
+        c->time = t + dt;
+    }
+    c->iteration += 1;
+}
+
+__device__ inline double clock_choose_dt(const mara_minidisk_clock* c, const ClockArgs& a)
+{
+    const double t = c->time;
+    if (a.dt_mode == MARA_DT_FORMULA_HELD) return c->dt;   // the batch's dt, chosen by its first step
+    if (a.dt_mode == MARA_DT_FORMULA)
+    {
+        // problems/minidisk.cpp:204-206
+        double vmax = sqrt(1.0 * 0.5 / a.softening_length);
+        double cfl = a.cfl * fmin(1.0, 0.01 + t / 0.05);
+        return a.dl / vmax * cfl;
+    }
+    return a.cfl * a.dl / c->max_wavespeed;   // scheme_mhd_v1.cpp:287 form
+}
+
+// One clock update: finish the step that just ran (RK2 time average,
+// iteration count) and/or choose the next dt and the stage binaries.
+// Call from `lanes` (1 or 2) consecutive threads of one warp, lane = 0, 1.
+__device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a, int lane = 0, int lanes = 1)
+{
+    if (lane == 0)
+    {
+        if (a.end_step) clock_end_step(c, a);
+        if (a.begin_step) c->dt = clock_choose_dt(c, a);
+    }
+    if (lanes > 1) __syncwarp(0x3u);
     if (a.begin_step)
     {
-        double t = c->time, dt;
-        if (a.dt_mode == MARA_DT_FORMULA_HELD)
+        const double t = c->time, dt = c->dt;
+        for (int s = lane; s < 2; s += lanes)
+            store_binary(c->binary[s], binary_state(a.mass_ratio, a.eccentricity, a.omega, s == 0 ? t : t + dt));
+        if (lanes > 1) __syncwarp(0x3u);
+        if (lane == 0)
         {
-            dt = c->dt;   // the batch's dt, chosen by its first step
+            c->max_wavespeed = 0.0;
+            if (a.diag)
+                for (int k = 0; k < 2 * MARA_DIAG_COUNT; ++k) a.diag->rate[k / MARA_DIAG_COUNT][k % MARA_DIAG_COUNT] = 0.0;
         }
-        else if (a.dt_mode == MARA_DT_FORMULA)
-        {
-            // problems/minidisk.cpp:204-206
-            double vmax = sqrt(1.0 * 0.5 / a.softening_length);
-            double cfl = a.cfl * fmin(1.0, 0.01 + t / 0.05);
-            dt = a.dl / vmax * cfl;
-        }
-        else
-        {
-            dt = a.cfl * a.dl / c->max_wavespeed;   // scheme_mhd_v1.cpp:287 form
-        }
-        c->dt = dt;
-        store_binary(c->binary[0], binary_state(a.mass_ratio, a.eccentricity, a.omega, t));
-        store_binary(c->binary[1], binary_state(a.mass_ratio, a.eccentricity, a.omega, t + dt));
-        c->max_wavespeed = 0.0;
-        if (a.diag)
-            for (int k = 0; k < 2 * MARA_DIAG_COUNT; ++k) a.diag->rate[k / MARA_DIAG_COUNT][k % MARA_DIAG_COUNT] = 0.0;
     }
 }
 
