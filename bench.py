@@ -83,8 +83,9 @@ def parse():
                     help="ensemble launch shape blocks_per_sm,chunks_per_warp,cols_per_lane,register_variant "
                          "(default: tuned)")
     ap.add_argument("--no-looped", action="store_true", help="ensemble: skip the looped single-mesh comparison")
-    ap.add_argument("--accuracy-steps", type=int, default=200,
-                    help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip)")
+    ap.add_argument("--accuracy-steps", type=int, default=2000,
+                    help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip); the "
+                         "4096^2 configuration's own 2000 by default")
     return ap.parse_args()
 
 
@@ -349,19 +350,24 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(WORKLOADS[args.workload], args.cpu_sample_seconds)
 
-    # Mixed-precision error: both paths advanced from the same state with the
-    # same (formula) time steps, relative L1 per component after S steps.
+    # Mixed-precision error: both paths advanced from the same state, each
+    # with its own CFL time step (an FP64 evaluation in both: the mixed path's
+    # reduction names the fastest cell and the clock evaluates it in FP64),
+    # relative L1 per component after S steps. (The reference's fixed-formula
+    # dt lets this configuration develop negative densities after ~600 steps
+    # in both precisions, so the CFL dt is used.)
     accuracy = None
     if prec == md.MIXED and args.accuracy_steps > 0:
-        runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_FORMULA) for p in (md.FP64, md.MIXED)}
+        runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_CFL) for p in (md.FP64, md.MIXED)}
         for r in runs.values():
             r.advance(args.accuracy_steps)
         torch.cuda.synchronize()
         a, b = runs[md.MIXED].u, runs[md.FP64].u
         rel = [float((a[k] - b[k]).abs().sum() / b[k].abs().sum()) for k in range(3)]
-        accuracy = {"steps": args.accuracy_steps, "dt": "formula (identical in both paths)",
+        accuracy = {"steps": args.accuracy_steps, "dt": "CFL 0.3, FP64 in each path",
                     "rel_l1_vs_fp64": {"density": rel[0], "momentum_x": rel[1], "momentum_y": rel[2]},
-                    "time": runs[md.MIXED].time}
+                    "time": runs[md.MIXED].time, "time_fp64": runs[md.FP64].time,
+                    "finite": bool(torch.isfinite(a).all().item() and torch.isfinite(b).all().item())}
         del runs, a, b
 
     if rank == 0:
