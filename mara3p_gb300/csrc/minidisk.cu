@@ -568,6 +568,42 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
 
 // Fastest wavespeed of a state in FP32 (mixed-precision runs): the same
 // estimate as the fused reduction of the mixed stage kernels.
+// The mixed path's CFL clock init: the FP32 wavespeed of every cell reduced
+// to the speed key of the fastest cell (as the stage kernels do), then that
+// cell's FP64 wavespeed (key_to_wavespeed_kernel). An FP64 reduction over
+// every cell costs FP64 divisions per cell, which GB300 runs slowly.
+__global__ void wavespeed_key_kernel(int N, FloatConsts F, const double* u, unsigned long long* key_out)
+{
+    __shared__ unsigned long long wk[NT / 32];
+    const size_t NN = size_t(N) * N;
+    unsigned long long key = 0ull;
+    for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < NN; c += size_t(gridDim.x) * blockDim.x)
+    {
+        const int i = int(c / N), j = int(c % N);
+        const float x = fmaf(float(i) + 0.5f, F.dl, -F.R), y = fmaf(float(j) + 0.5f, F.dl, -F.R);
+        const float pot = rsqrt_fast(fmaf(x, x, y * y) + F.rs2);
+        key = key_max(key, speed_key(wavespeed_f(F, d2f(u[c]), d2f(u[NN + c]), d2f(u[2 * NN + c]), pot), c));
+    }
+    for (int o = 16; o > 0; o >>= 1) key = key_max(key, __shfl_xor_sync(0xffffffffu, key, o));
+    if ((threadIdx.x & 31) == 0) wk[threadIdx.x >> 5] = key;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned long long r = 0ull;
+        for (int w = 0; w < int(blockDim.x / 32); ++w) r = key_max(r, wk[w]);
+        atomicMax(key_out, r);
+    }
+}
+
+__global__ void key_to_wavespeed_kernel(mara_minidisk_clock* clock, const ClockArgs a, const double* u)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const unsigned long long key = __double_as_longlong(clock->max_wavespeed);
+    if (key != 0ull)
+        clock->max_wavespeed = cell_wavespeed(u, size_t(a.N) * a.N, a.N, a.n, a.level, a.R, a.rs2, a.mach,
+                                              size_t(unsigned(key)));
+}
+
 // Fastest wavespeed of a state (for the first CFL step), FP64.
 __global__ void wavespeed_kernel(int N, int n, int level, double R, double rs2, double mach,
                                  const double* u, unsigned long long* amax)
@@ -916,8 +952,14 @@ int clock_init(const mara_minidisk_params* sd, const double* u, double time, mar
     const int64_t NN = int64_t(N) * N;
     const int blocks = int(std::min<int64_t>((NN + 255) / 256, 152 * 8));
     auto* amax = reinterpret_cast<unsigned long long*>(&clock->max_wavespeed);
-    // FP64 in both precisions: the CFL dt is an FP64 quantity
-    (void)precision;
+    if (precision == MARA_MIXED)
+    {
+        // the CFL dt stays an FP64 quantity: the fastest cell's FP64 wavespeed
+        wavespeed_key_kernel<<<blocks, NT, 0, s>>>(N, base_args(sd).f, u, amax);
+        if (int r = launch_status("wavespeed_key_kernel")) return r;
+        key_to_wavespeed_kernel<<<1, 32, 0, s>>>(clock, clock_args(sd, MARA_DT_CFL, 2, 0, 0), u);
+        return launch_status("key_to_wavespeed_kernel");
+    }
     wavespeed_kernel<<<blocks, NT, 0, s>>>(N, sd->block_size, sd->depth, sd->domain_radius,
         std::pow(sd->softening_length, 2.0), sd->mach_number, u, amax);
     return launch_status("wavespeed_kernel");
