@@ -160,7 +160,9 @@ int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_i
  *   1  mixed 1: d_out = dt*L(u_in) (FP32); with d_out NULL: u_out = u_in + dt*L(u_in)
  *   2  mixed 2: u_out = u_in + (d1 + dt*L(f32(u_in) + d1))/2
  * reduce_wavespeed != 0 also folds the fastest wavespeed of u_out into
- * clock->max_wavespeed. u_out must not alias u_in (kind 0 may alias u_avg). */
+ * clock->max_wavespeed (mixed kinds: from u_out's FP32 image, as a double;
+ * mara_minidisk_advance instead re-evaluates the fastest cell in FP64).
+ * u_out must not alias u_in (kind 0 may alias u_avg). */
 int mara_minidisk_stage(const mara_minidisk_params* sd, int32_t kind, const double* u_in, const float* d1,
                         const double* u_avg, double* u_out, float* d_out, mara_minidisk_clock* clock,
                         int32_t stage, int32_t reduce_wavespeed, void* stream);
