@@ -500,6 +500,27 @@ int64_t ref_sedov_generate_track(double r0, double r1, double theta0, double the
     return n;
 }
 
+// sedov::remesh of one track (scheme_sedov2d.cpp:362-412): returns the new
+// cell count (-1 if the reference threw); radii_out / u_out get the new
+// track (capacity ncells + 1 cells).
+int64_t ref_sedov_remesh(int64_t ncells, double theta0, double theta1, const double* radii, const double* u,
+                         double max_aspect, double min_aspect, double inner_radius, double* radii_out, double* u_out)
+{
+    try
+    {
+        const double th[2] = {theta0, theta1};
+        auto in = load_tracks(1, &ncells, th, radii, u);
+        auto [t, c] = sedov::remesh(in.tracks(0), in.u(0), max_aspect, min_aspect, inner_radius);
+        for (std::size_t i = 0; i < size(t.face_radii); ++i) radii_out[i] = t.face_radii(i).value;
+        for (std::size_t i = 0; i < size(c); ++i) from_tuple(c(i), u_out + 5 * i);
+        return int64_t(size(c));
+    }
+    catch (const std::exception&)
+    {
+        return -1;
+    }
+}
+
 // sedov::cell_volume and sedov::face_area (scheme_sedov2d.cpp:40-62)
 double ref_sedov_cell_volume(double r0, double r1, double t0, double t1) { return sedov::cell_volume(r0, r1, t0, t1).value; }
 double ref_sedov_face_area(double r0, double r1, double t0, double t1) { return sedov::face_area(r0, r1, t0, t1).value; }

@@ -377,6 +377,82 @@ int oracle_sedov_advance_rk(int32_t T, const int64_t* ncells, const double* thet
     return bad;
 }
 
+// sedov::remesh (scheme_sedov2d.cpp:362-412) of one track, in place on
+// radii (capacity ncells + 2) and u (capacity 5 (ncells + 1)): drop the
+// first cell while the inner face lies inside inner_radius, split the cell
+// of largest aspect dr / (r_c dtheta) if above the maximum (and stop), merge
+// the cell of smallest aspect with its smaller-aspect neighbour if below the
+// minimum. The reference recurses after a drop or a merge with the two
+// aspect bounds passed in swapped order (make_track calls remesh(..., min,
+// max, ...) into parameters (max, min)), so each further level runs with
+// the bounds exchanged; that is restated. Returns the new cell count, or -1
+// where the reference throws (a merge on a one-cell track).
+int64_t oracle_sedov_remesh(int64_t ncells, double theta0, double theta1, double* radii, double* u,
+                            double max_aspect, double min_aspect, double inner_radius)
+{
+    std::vector<double> rf(radii, radii + ncells + 1), uc(u, u + 5 * ncells);
+    double amax_bound = max_aspect, amin_bound = min_aspect;
+    for (;;)
+    {
+        const int64_t n = int64_t(rf.size()) - 1;
+        if (n < 1) return -1;
+        std::vector<double> aspect(n);
+        for (int64_t i = 0; i < n; ++i)
+        {
+            const double dr = rf[i + 1] - rf[i];
+            const double rc = 0.5 * (rf[i] + rf[i + 1]);
+            aspect[i] = dr / (rc * (theta1 - theta0));
+        }
+        // nd::argmin / argmax: the first index holding the min / max
+        const double mn = *std::min_element(aspect.begin(), aspect.end());
+        const double mx = *std::max_element(aspect.begin(), aspect.end());
+        int64_t imin = 0, imax = 0;
+        while (!(aspect[imin] == mn)) ++imin;
+        while (!(aspect[imax] == mx)) ++imax;
+        auto remove = [&] (int64_t e) -> bool {
+            if (e == 0 || e + 1 >= int64_t(rf.size())) return false;
+            rf.erase(rf.begin() + e);
+            for (int k = 0; k < 5; ++k) uc[5 * (e - 1) + k] = uc[5 * (e - 1) + k] + uc[5 * e + k];
+            uc.erase(uc.begin() + 5 * e, uc.begin() + 5 * e + 5);
+            return true;
+        };
+        if (rf.front() < inner_radius)
+        {
+            if (n < 2) return -1;   // the reference would drop into an empty track
+            rf.erase(rf.begin());
+            uc.erase(uc.begin(), uc.begin() + 5);
+            std::swap(amax_bound, amin_bound);
+            continue;
+        }
+        if (aspect[imax] > amax_bound)
+        {
+            const double mid = 0.5 * (rf[imax] + rf[imax + 1]);
+            rf.insert(rf.begin() + imax + 1, mid);
+            double half[5];
+            for (int k = 0; k < 5; ++k) half[k] = 0.5 * uc[5 * imax + k];
+            for (int k = 0; k < 5; ++k) uc[5 * imax + k] = half[k];
+            uc.insert(uc.begin() + 5 * (imax + 1), half, half + 5);
+            break;
+        }
+        if (aspect[imin] < amin_bound)
+        {
+            int64_t e = -1;
+            if (imin == 0) e = 1;
+            else if (imin + 1 == n) e = imin;
+            else if (aspect[imin - 1] <= aspect[imin + 1]) e = imin;
+            else if (aspect[imin - 1] >= aspect[imin + 1]) e = imin + 1;
+            if (e < 0) break;
+            if (!remove(e)) return -1;
+            std::swap(amax_bound, amin_bound);
+            continue;
+        }
+        break;
+    }
+    std::copy(rf.begin(), rf.end(), radii);
+    std::copy(uc.begin(), uc.end(), u);
+    return int64_t(rf.size()) - 1;
+}
+
 // sedov::cell_volume / face_area
 double oracle_sedov_cell_volume(double r0, double r1, double t0, double t1) { return cell_volume(r0, r1, t0, t1); }
 double oracle_sedov_face_area(double r0, double r1, double t0, double t1) { return face_area(r0, r1, t0, t1); }

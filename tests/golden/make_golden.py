@@ -274,6 +274,50 @@ def sedov_fixtures(o, r) -> dict[str, np.ndarray]:
     return out
 
 
+def sedov_remesh_cases(r):
+    """Tracks shaped to take each branch of sedov::remesh: a split of the most
+    elongated cell, merges at the start, the end and inside (either
+    neighbour), the inner-boundary drop (after which the reference recurses
+    with the aspect bounds exchanged), and a track left alone."""
+    rng = np.random.default_rng(77)
+    dth = np.pi / 24
+    # geometric radii of aspect dr / (r_c dtheta) = 1 everywhere
+    q = (2 + dth) / (2 - dth)
+    base = 1.0 * q ** np.arange(30)
+    cases = []
+    def add(name, rf, inner=1.0, amax=2.0, amin=0.5):
+        cells = len(rf) - 1
+        u = rng.uniform(0.5, 2.0, (cells, 5))
+        cases.append((name, rf, u.ravel(), inner, amax, amin))
+    add("unchanged", base.copy())
+    rf = base.copy(); rf[5] = 0.5 * (rf[4] + rf[6]) + 0.45 * (rf[6] - rf[4]); add("split", rf, amax=1.6)
+    rf = base.copy(); rf[1] = rf[0] + 0.1 * (rf[2] - rf[0]); add("merge_first", rf)
+    rf = base.copy(); rf[-2] = rf[-1] - 0.1 * (rf[-1] - rf[-3]); add("merge_last", rf)
+    rf = base.copy(); rf[7] = rf[6] + 0.05 * (rf[8] - rf[6]); add("merge_inner_left", rf)
+    rf = base.copy(); rf[7] = rf[8] - 0.05 * (rf[8] - rf[6]); add("merge_inner_right", rf)
+    rf = base.copy(); add("inner_drop", rf, inner=0.5 * (rf[1] + rf[2]))
+    rf = base.copy(); add("inner_drop_wide_bounds", rf, inner=0.5 * (rf[0] + rf[1]), amax=50.0, amin=0.01)
+    return cases
+
+
+def sedov_remesh_fixture(r) -> dict[str, np.ndarray]:
+    out = {}
+    for name, rf, u, inner, amax, amin in sedov_remesh_cases(r):
+        cells = len(rf) - 1
+        ro, uo = np.zeros(cells + 2), np.zeros(5 * (cells + 1))
+        m = r.ref_sedov_remesh.restype = ctypes.c_int64
+        m = r.ref_sedov_remesh(ctypes.c_int64(cells), ctypes.c_double(0.3), ctypes.c_double(0.3 + np.pi / 24),
+                               dptr(rf), dptr(u), ctypes.c_double(amax), ctypes.c_double(amin), ctypes.c_double(inner),
+                               dptr(ro), dptr(uo))
+        out[f"remesh/{name}/radii"] = rf
+        out[f"remesh/{name}/u"] = u
+        out[f"remesh/{name}/bounds"] = np.array([amax, amin, inner, 0.3, 0.3 + np.pi / 24])
+        out[f"remesh/{name}/cells_out"] = np.array([m])
+        out[f"remesh/{name}/radii_out"] = ro[:m + 1]
+        out[f"remesh/{name}/u_out"] = uo[:5 * m]
+    return out
+
+
 def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
     g = 4.0 / 3.0
     n = 4096
@@ -382,7 +426,7 @@ def main() -> None:
     np.savez_compressed(HERE / "srhd_golden.npz", **srhd_fixtures(o, r))
     np.savez_compressed(HERE / "mhd_golden.npz", **mhd_fixtures(o, r))
     np.savez_compressed(HERE / "two_body_golden.npz", **two_body_fixture(r))
-    np.savez_compressed(HERE / "sedov_golden.npz", **sedov_fixtures(o, r))
+    np.savez_compressed(HERE / "sedov_golden.npz", **sedov_fixtures(o, r), **sedov_remesh_fixture(r))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size, "bytes")
 

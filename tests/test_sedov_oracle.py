@@ -80,3 +80,30 @@ def test_geometry_matches_reference(oracle, sedov_golden):
         a = [ctypes.c_double(v) for v in (r0, r1, t0, t1)]
         assert oracle.oracle_sedov_cell_volume(*a) == r.ref_sedov_cell_volume(*a)
         assert oracle.oracle_sedov_face_area(*a) == r.ref_sedov_face_area(*a)
+
+
+def remesh_cases(g):
+    return sorted({k.split("/")[1] for k in g if k.startswith("remesh/")})
+
+
+def test_remesh_matches_reference(oracle, sedov_golden):
+    """sedov::remesh on tracks shaped for each branch (split, merges at the
+    start, end and inside, inner-boundary drop, no change), bit for bit; the
+    reference's recursion with exchanged aspect bounds included."""
+    oracle.oracle_sedov_remesh.restype = ctypes.c_int64
+    names = remesh_cases(sedov_golden)
+    assert len(names) == 8
+    for nm in names:
+        k = lambda s: sedov_golden[f"remesh/{nm}/{s}"]  # noqa: E731
+        rf, u = k("radii"), k("u")
+        cells = len(rf) - 1
+        amax, amin, inner, t0, t1 = k("bounds")
+        ro = np.zeros(cells + 2)
+        ro[:cells + 1] = rf
+        uo = np.zeros(5 * (cells + 1))
+        uo[:5 * cells] = u
+        m = oracle.oracle_sedov_remesh(ctypes.c_int64(cells), ctypes.c_double(t0), ctypes.c_double(t1), dptr(ro),
+                                       dptr(uo), ctypes.c_double(amax), ctypes.c_double(amin), ctypes.c_double(inner))
+        assert m == int(k("cells_out")[0]), nm
+        assert np.array_equal(ro[:m + 1], k("radii_out")), nm
+        assert np.array_equal(uo[:5 * m], k("u_out")), nm
