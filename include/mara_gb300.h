@@ -504,6 +504,22 @@ int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_o
                        double* radii, double* u, const double* ghost_in, const double* ghost_out, double dt,
                        int32_t rk_order, int32_t use_plm, void* workspace, int32_t* failures, void* stream);
 
+/* sedov::remesh (src/scheme_sedov2d.cpp:362-412) of every track: drop the
+ * first cell while the inner face lies inside inner_radius, split the cell of
+ * largest aspect dr / (r_c dtheta) above max_aspect, merge the cell of
+ * smallest aspect below min_aspect with its neighbour of smaller aspect. As in
+ * the reference, the recursion after a drop or a merge runs with the two
+ * aspect bounds exchanged. New tracks go to separate buffers of capacity
+ * cells + track_count cells: cell_offset_out[track_count + 1] (device),
+ * radii_out, u_out (SoA with the new cell count as its stride); the new cell
+ * count is written to *cells_out (host; the call synchronizes the stream).
+ * failures counts tracks where the reference would throw. */
+int64_t mara_sedov_remesh_workspace_bytes(int32_t track_count, int64_t cells);
+int mara_sedov_remesh(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                      const double* radii, const double* u, double max_aspect, double min_aspect, double inner_radius,
+                      int64_t* cell_offset_out, double* radii_out, double* u_out, int64_t* cells_out, void* workspace,
+                      int32_t* failures, void* stream);
+
 /* sedov::minimum_spacing over all tracks (scheme_sedov2d.cpp:66-69, the
  * driver's dt = cfl * min spacing / c): out is one device double. */
 int mara_sedov_min_spacing(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* radii,

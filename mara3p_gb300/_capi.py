@@ -96,6 +96,10 @@ SIGNATURES = {
     "mara_sedov_advance": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp,
                                           ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp]),
     "mara_sedov_min_spacing": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, _vp, _vp, _vp, _vp]),
+    "mara_sedov_remesh_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int64]),
+    "mara_sedov_remesh": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, _vp, _vp, _vp,
+                                         ctypes.POINTER(ctypes.c_int64), _vp, _vp, _vp]),
     "mara_minidisk_diagnostics_reset": (ctypes.c_int, [_vp, _vp]),
     "mara_minidisk_advance_diag": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp, _vp, _vp]),

@@ -516,6 +516,188 @@ __global__ void min_spacing_kernel(Tracks t, const double* r, unsigned long long
     if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMin(out, (unsigned long long)__double_as_longlong(m));
 }
 
+// ---------------------------------------------------------------- remesh
+// sedov::remesh (scheme_sedov2d.cpp:362-412) of every track: one warp per
+// track edits a scratch copy (drop the first cell, merge two cells, split a
+// cell) with warp-wide shifts, then the new tracks are packed by an offset
+// scan. The reference recurses after a drop or a merge with the two aspect
+// bounds passed in exchanged order, so each further level runs with them
+// exchanged; that is kept.
+struct Remesh
+{
+    int T;
+    int64_t C;
+    const int64_t* co;
+    const double* theta;
+    const double* r;
+    const double* u;
+    double* rs;            // scratch radii: track j at co[j] + 2j, capacity n + 2
+    double* us;            // scratch cells: [5][C + T], track j at co[j] + j, capacity n + 1
+    int64_t* counts;       // [T] new cell counts
+    int64_t* co_out;       // [T + 1]
+    double* r_out;
+    double* u_out;
+    double max_aspect, min_aspect, inner;
+    int* failures;
+};
+
+// a[k - 1] = a[k] for k in [from, end), ascending chunks of one warp
+__device__ inline void warp_shift_left(double* a, int64_t from, int64_t end, int lane)
+{
+    for (int64_t base = from; base < end; base += 32)
+    {
+        const int64_t k = base + lane;
+        const double v = k < end ? a[k] : 0.0;
+        __syncwarp();
+        if (k < end) a[k - 1] = v;
+        __syncwarp();
+    }
+}
+
+// a[k + 1] = a[k] for k in [from, end), descending chunks of one warp
+__device__ inline void warp_shift_right(double* a, int64_t from, int64_t end, int lane)
+{
+    for (int64_t top = end; top > from; top -= 32)
+    {
+        const int64_t k = top - 1 - lane;
+        const double v = k >= from ? a[k] : 0.0;
+        __syncwarp();
+        if (k >= from) a[k + 1] = v;
+        __syncwarp();
+    }
+}
+
+__global__ void remesh_track_kernel(const Remesh M)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t j = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (j >= M.T) return;                                     // uniform per warp
+    const int64_t S5 = M.C + M.T;
+    int64_t n = M.co[j + 1] - M.co[j];
+    double* rf = M.rs + M.co[j] + 2 * j;
+    double* uc[5];
+    for (int q = 0; q < 5; ++q) uc[q] = M.us + q * S5 + M.co[j] + j;
+    for (int64_t k = lane; k <= n; k += 32) rf[k] = M.r[M.co[j] + j + k];
+    for (int64_t k = lane; k < n; k += 32)
+        for (int q = 0; q < 5; ++q) uc[q][k] = M.u[q * M.C + M.co[j] + k];
+    __syncwarp();
+    const double dth = M.theta[2 * j + 1] - M.theta[2 * j];
+    double amax_b = M.max_aspect, amin_b = M.min_aspect;
+    int bad = 0;
+    for (int64_t guard = 0; guard < 2 * n + 4; ++guard)
+    {
+        // aspect dr / (r_c dtheta); nd::argmin / argmax take the first index
+        double mn = INFINITY, mx = -INFINITY;
+        int64_t imn = 0, imx = 0;
+        for (int64_t k = lane; k < n; k += 32)
+        {
+            const double a = (rf[k + 1] - rf[k]) / ((0.5 * (rf[k] + rf[k + 1])) * dth);
+            if (a < mn) { mn = a; imn = k; }
+            if (a > mx) { mx = a; imx = k; }
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            const double omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+            const int64_t oimn = __shfl_xor_sync(0xffffffffu, imn, o), oimx = __shfl_xor_sync(0xffffffffu, imx, o);
+            if (omn < mn || (omn == mn && oimn < imn)) { mn = omn; imn = oimn; }
+            if (omx > mx || (omx == mx && oimx < imx)) { mx = omx; imx = oimx; }
+        }
+        if (rf[0] < M.inner)
+        {
+            if (n < 2) { bad = 1; break; }
+            warp_shift_left(rf, 1, n + 1, lane);
+            for (int q = 0; q < 5; ++q) warp_shift_left(uc[q], 1, n, lane);
+            n -= 1;
+            const double t = amax_b; amax_b = amin_b; amin_b = t;
+            continue;
+        }
+        if (mx > amax_b)
+        {
+            const double mid = 0.5 * (rf[imx] + rf[imx + 1]);
+            double half[5];
+            for (int q = 0; q < 5; ++q) half[q] = 0.5 * uc[q][imx];
+            __syncwarp();
+            warp_shift_right(rf, imx + 1, n + 1, lane);
+            for (int q = 0; q < 5; ++q) warp_shift_right(uc[q], imx + 1, n, lane);
+            if (lane == 0)
+            {
+                rf[imx + 1] = mid;
+                for (int q = 0; q < 5; ++q) uc[q][imx] = uc[q][imx + 1] = half[q];
+            }
+            __syncwarp();
+            n += 1;
+            break;
+        }
+        if (mn < amin_b)
+        {
+            int64_t e = -1;
+            if (imn == 0) e = 1;
+            else if (imn + 1 == n) e = imn;
+            else
+            {
+                const double al = (rf[imn] - rf[imn - 1]) / ((0.5 * (rf[imn - 1] + rf[imn])) * dth);
+                const double ar = (rf[imn + 2] - rf[imn + 1]) / ((0.5 * (rf[imn + 1] + rf[imn + 2])) * dth);
+                if (al <= ar) e = imn;
+                else if (al >= ar) e = imn + 1;
+            }
+            if (e < 0) break;
+            if (e + 1 >= n + 1) { bad = 1; break; }
+            double merged[5];
+            for (int q = 0; q < 5; ++q) merged[q] = uc[q][e - 1] + uc[q][e];
+            __syncwarp();
+            if (lane == 0)
+                for (int q = 0; q < 5; ++q) uc[q][e - 1] = merged[q];
+            __syncwarp();
+            for (int q = 0; q < 5; ++q) warp_shift_left(uc[q], e + 1, n, lane);
+            warp_shift_left(rf, e + 1, n + 1, lane);
+            n -= 1;
+            const double t = amax_b; amax_b = amin_b; amin_b = t;
+            continue;
+        }
+        break;
+    }
+    if (lane == 0)
+    {
+        M.counts[j] = n;
+        if (bad && M.failures) atomicAdd(M.failures, 1);
+    }
+}
+
+// exclusive scan of the new counts into co_out (one block)
+__global__ void remesh_scan_kernel(const Remesh M)
+{
+    __shared__ int64_t part[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int64_t per = (M.T + nt - 1) / nt;
+    const int64_t a = t * per, b = min(int64_t(M.T), a + per);
+    int64_t sum = 0;
+    for (int64_t k = a; k < b; ++k) sum += M.counts[k];
+    part[t] = sum;
+    __syncthreads();
+    if (t == 0)
+    {
+        int64_t run = 0;
+        for (int k = 0; k < nt; ++k) { const int64_t v = part[k]; part[k] = run; run += v; }
+        M.co_out[M.T] = run;
+    }
+    __syncthreads();
+    int64_t run = part[t];
+    for (int64_t k = a; k < b; ++k) { M.co_out[k] = run; run += M.counts[k]; }
+}
+
+__global__ void remesh_pack_kernel(const Remesh M)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t j = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (j >= M.T) return;
+    const int64_t S5 = M.C + M.T, Cn = M.co_out[M.T];
+    const int64_t n = M.co_out[j + 1] - M.co_out[j];
+    const double* rf = M.rs + M.co[j] + 2 * j;
+    for (int64_t k = lane; k <= n; k += 32) M.r_out[M.co_out[j] + j + k] = rf[k];
+    for (int64_t k = lane; k < n; k += 32)
+        for (int q = 0; q < 5; ++q) M.u_out[q * Cn + M.co_out[j] + k] = M.us[q * S5 + M.co[j] + j + k];
+}
+
 // ---------------------------------------------------------------- host
 struct Workspace
 {
@@ -693,6 +875,58 @@ int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_o
     }
     MARA_CUDA(cudaMemcpyAsync(radii, ra, F * sizeof(double), cudaMemcpyDeviceToDevice, s));
     MARA_CUDA(cudaMemcpyAsync(u, ua, 5 * cells * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return MARA_OK;
+}
+
+int64_t mara_sedov_remesh_workspace_bytes(int32_t track_count, int64_t cells)
+{
+    if (track_count < 1 || cells < 2 * int64_t(track_count)) return -1;
+    const int64_t T = track_count;
+    return (cells + 2 * T) * 8 + 5 * (cells + T) * 8 + T * 8 + 3 * 256;
+}
+
+int mara_sedov_remesh(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* theta,
+                      const double* radii, const double* u, double max_aspect, double min_aspect, double inner_radius,
+                      int64_t* cell_offset_out, double* radii_out, double* u_out, int64_t* cells_out, void* workspace,
+                      int32_t* failures, void* stream)
+{
+    if (int r = check_tracks(track_count, cells, cell_offset, theta)) return r;
+    MARA_REQUIRE(radii && u && cell_offset_out && radii_out && u_out && cells_out && workspace,
+                 "mara_sedov_remesh: null buffer");
+    MARA_REQUIRE(radii_out != radii && u_out != u && cell_offset_out != cell_offset,
+                 "mara_sedov_remesh: outputs must not alias inputs");
+    cudaStream_t s = as_stream(stream);
+    const int64_t T = track_count;
+    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    Remesh M{};
+    M.T = track_count;
+    M.C = cells;
+    M.co = cell_offset;
+    M.theta = theta;
+    M.r = radii;
+    M.u = u;
+    M.rs = reinterpret_cast<double*>(p);
+    p += ((cells + 2 * T) * 8 + 255) / 256 * 256;
+    M.us = reinterpret_cast<double*>(p);
+    p += (5 * (cells + T) * 8 + 255) / 256 * 256;
+    M.counts = reinterpret_cast<int64_t*>(p);
+    M.co_out = cell_offset_out;
+    M.r_out = radii_out;
+    M.u_out = u_out;
+    M.max_aspect = max_aspect;
+    M.min_aspect = min_aspect;
+    M.inner = inner_radius;
+    M.failures = failures;
+    const int warps_per_block = 8;
+    const int blocks = int((T + warps_per_block - 1) / warps_per_block);
+    remesh_track_kernel<<<blocks, warps_per_block * 32, 0, s>>>(M);
+    if (int r = launch_status("sedov remesh_track_kernel")) return r;
+    remesh_scan_kernel<<<1, 1024, 0, s>>>(M);
+    if (int r = launch_status("sedov remesh_scan_kernel")) return r;
+    remesh_pack_kernel<<<blocks, warps_per_block * 32, 0, s>>>(M);
+    if (int r = launch_status("sedov remesh_pack_kernel")) return r;
+    MARA_CUDA(cudaMemcpyAsync(cells_out, cell_offset_out + T, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MARA_CUDA(cudaStreamSynchronize(s));
     return MARA_OK;
 }
 

@@ -157,6 +157,32 @@ class Tracks:
                                    self.failures.data_ptr(), _stream()), "mara_sedov_stage")
         return out
 
+    def remesh(self, max_aspect: float = 2.0, min_aspect: float = 0.5, inner_radius: float = 1.0) -> int:
+        """sedov::remesh of every track (the driver's defaults: max_aspect 2,
+        min_aspect 0.5, inner radius 1); the tracks move to new arrays.
+        Returns the new cell count."""
+        dev = self.u.device
+        cap = self.cells + self.T
+        co = torch.empty(self.T + 1, dtype=torch.int64, device=dev)
+        radii = torch.empty(cap + self.T, dtype=torch.float64, device=dev)
+        u = torch.empty(5 * cap, dtype=torch.float64, device=dev)
+        nbytes = lib.mara_sedov_remesh_workspace_bytes(self.T, self.cells)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        cells = ctypes.c_int64()
+        check(lib.mara_sedov_remesh(self.T, self.cells, self.co.data_ptr(), self.theta.data_ptr(),
+                                    self.radii.data_ptr(), self.u.data_ptr(), max_aspect, min_aspect, inner_radius,
+                                    co.data_ptr(), radii.data_ptr(), u.data_ptr(), ctypes.byref(cells),
+                                    ws.data_ptr(), self.failures.data_ptr(), _stream()), "mara_sedov_remesh")
+        self.cells = int(cells.value)
+        self.co = co
+        self.radii = radii[: self.cells + self.T]
+        self.u = u[: 5 * self.cells].view(5, self.cells)
+        self.ncells = (co[1:] - co[:-1]).cpu().numpy()
+        nbytes = lib.mara_sedov_workspace_bytes(self.T, self.cells)
+        if self.workspace.numel() < nbytes:
+            self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        return self.cells
+
     def min_spacing(self) -> float:
         """sedov::minimum_spacing over every track."""
         out = torch.empty(1, dtype=torch.float64, device=self.u.device)

@@ -209,3 +209,82 @@ def test_bad_arguments(sd):
     tr = sd.Tracks([2, 2], [0.0, 1.5, 1.5, np.pi], np.tile([1.0, 1.5, 2.0], 2), np.ones(20))
     with pytest.raises(MaraError, match="rk_order"):
         tr.advance(1e-3, np.zeros(40), np.zeros(40), rk_order=4)
+
+
+def oracle_remesh_all(oracle, ncells, th, radii, u, amax, amin, inner):
+    """sedov::remesh of every track through the oracle; new (ncells, radii, u)."""
+    oracle.oracle_sedov_remesh.restype = ctypes.c_int64
+    out_n, out_r, out_u = [], [], []
+    fo = np.concatenate([[0], np.cumsum(ncells + 1)])
+    co = np.concatenate([[0], np.cumsum(ncells)])
+    for j, n in enumerate(ncells):
+        rf = np.zeros(n + 2)
+        rf[:n + 1] = radii[fo[j]:fo[j + 1]]
+        uc = np.zeros(5 * (n + 1))
+        uc[:5 * n] = u[5 * co[j]:5 * co[j + 1]]
+        m = oracle.oracle_sedov_remesh(ctypes.c_int64(n), ctypes.c_double(th[2 * j]), ctypes.c_double(th[2 * j + 1]),
+                                       dptr(rf), dptr(uc), ctypes.c_double(amax), ctypes.c_double(amin),
+                                       ctypes.c_double(inner))
+        assert m > 0
+        out_n.append(m)
+        out_r.append(rf[:m + 1])
+        out_u.append(uc[:5 * m])
+    return np.array(out_n, np.int64), np.concatenate(out_r), np.concatenate(out_u)
+
+
+def test_remesh_matches_reference_fixtures(sd, sedov_golden):
+    names = sorted({k.split("/")[1] for k in sedov_golden if k.startswith("remesh/")})
+    for nm in names:
+        k = lambda s: sedov_golden[f"remesh/{nm}/{s}"]  # noqa: E731
+        rf, u = k("radii"), k("u")
+        amax, amin, inner, t0, t1 = k("bounds")
+        tr = sd.Tracks([len(rf) - 1], [t0, t1], rf, u)
+        m = tr.remesh(amax, amin, inner)
+        assert m == int(k("cells_out")[0]), nm
+        radii, uu = tr.host_state()
+        assert np.array_equal(radii, k("radii_out")), nm
+        assert np.array_equal(uu.ravel(), k("u_out")), nm
+        assert tr.failure_count() == 0
+
+
+def test_remesh_many_tracks_match_oracle(sd, oracle):
+    ncells, th, radii, u, gin, gout = make_tracks(sd, oracle, 40, 0.5, 3.0, 12)
+    rng = np.random.default_rng(3)
+    fo = np.concatenate([[0], np.cumsum(ncells + 1)])
+    radii = radii.copy()
+    for j in range(40):
+        # squeeze or stretch one interior face of most tracks
+        n = ncells[j]
+        if j % 5 == 4:
+            continue
+        f = fo[j] + rng.integers(2, n - 1)
+        lo, hi = radii[f - 1], radii[f + 1]
+        radii[f] = lo + (hi - lo) * rng.choice([0.03, 0.97, 0.5])
+    tr = sd.Tracks(ncells, th, radii, u)
+    m = tr.remesh(2.0, 0.5, 1.0)
+    ref_n, ref_r, ref_u = oracle_remesh_all(oracle, ncells, th, radii, u, 2.0, 0.5, 1.0)
+    assert m == ref_n.sum()
+    assert np.array_equal(tr.ncells, ref_n)
+    r_gpu, u_gpu = tr.host_state()
+    assert np.array_equal(r_gpu, ref_r) and np.array_equal(u_gpu.ravel(), ref_u)
+
+
+def test_advance_and_remesh_loop_matches_oracle(sd, oracle):
+    """The driver's loop (problems/sedov2d.cpp:700-712): an RK2 advance, then
+    remesh of every track, for 15 steps; tracks change length as their faces
+    move."""
+    ncells, th, radii, u, gin, gout = make_tracks(sd, oracle, 24, 0.4, 3.0, 21)
+    tr = sd.Tracks(ncells, th, radii, u)
+    dt = 0.3 * tr.min_spacing()
+    nc, rr, uu = ncells.copy(), radii.copy(), u.copy()
+    for _ in range(15):
+        tr.advance(dt, gin, gout, rk_order=2)
+        tr.remesh(2.0, 0.5, 1.0)
+        rr, uu = oracle_run(oracle, nc, th, rr, uu, gin, gout, dt, 2, True, 1)
+        nc, rr, uu = oracle_remesh_all(oracle, nc, th, rr, uu, 2.0, 0.5, 1.0)
+        assert np.array_equal(tr.ncells, nc)
+    r_gpu, u_gpu = tr.host_state()
+    assert tr.failure_count() == 0
+    assert rel_l1(r_gpu, rr) < 1e-12
+    assert rel_l1(u_gpu, uu.reshape(-1, 5)) < 1e-9
+    assert nc.sum() != ncells.sum() or not np.array_equal(nc, ncells)   # the loop did remesh
