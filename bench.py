@@ -687,8 +687,10 @@ def run_sedov(args):
     [0, pi], each from generate_radial_track(1, 1.8, aspect 2) as
     problems/sedov2d.cpp lays them out (its default is 128 tracks; 1024 gives
     522,919 cells), a seeded wind with a hot core, forward Euler (the
-    driver's default rk = 1), dt = 0.5 * min spacing. One step = recovery,
-    radial and transverse HLLC fluxes, update and face motion of every cell."""
+    driver's default rk = 1), dt = 0.5 * min spacing. One step is the
+    driver's (problems/sedov2d.cpp:700-712): recovery, radial and transverse
+    HLLC fluxes, update and face motion of every cell, then sedov::remesh of
+    every track (max aspect 2, min 0.5, inner radius 1)."""
     import torch
 
     import mara3p_gb300.sedov as sv
@@ -703,61 +705,92 @@ def run_sedov(args):
     gin = np.tile(wind(1.0), (rk, T, 1))
     gout = np.tile(wind(1.8), (rk, T, 1))
     dt = 0.5 * tracks.min_spacing()
-    for _ in range(max(args.warmup, 1)):
+
+    def step():
         tracks.advance(dt, gin, gout, rk_order=rk)
+        tracks.remesh(2.0, 0.5, 1.0)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
     torch.cuda.synchronize()
+    C, F = tracks.cells, tracks.cells + T
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cells_done = 0
     with ClockSampler(local) as sampler:
         e0.record(stream)
         for _ in range(args.steps):
-            tracks.advance(dt, gin, gout, rk_order=rk)
+            cells_done += tracks.cells
+            step()
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
-    value = C / (ms * 1e-3) * world
+    value = cells_done / args.steps / (ms * 1e-3) * world
     # algorithmic bytes per cell and stage: conserved in and out (2 x 40 B),
     # face radii in and out (2 x 8 B per face)
     peak, kind = measured_peaks()
-    achieved = (80.0 * C + 16.0 * F) * rk / (ms * 1e-3) / 1e9
+    Cm = cells_done / args.steps
+    achieved = (80.0 * Cm + 16.0 * (Cm + T)) * rk / (ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels; bound by FP64 recovery and "
+            "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels, then remesh; bound by FP64 recovery and "
                                        "HLLC arithmetic, not by HBM)", "peak_source": f"{kind} hbm_gbs"}
-    extra = {"gpu_launches": 5 * rk * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
+    extra = {"gpu_launches": (5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
     if not args.no_e2e:
-        # through the public call with host buffers: state to the GPU, one
-        # step, state back, every step
-        hu = torch.empty((5, C), dtype=torch.float64).pin_memory()
-        hr = torch.empty(F, dtype=torch.float64).pin_memory()
-        hu.copy_(tracks.u.cpu())
-        hr.copy_(tracks.radii.cpu())
+        # through the public calls with host buffers: the tracks' state to the
+        # GPU, one driver step, the (remeshed) state back, every step
+        cap = tracks.cells + (args.steps + 1) * T
+        hu = torch.empty(5 * cap, dtype=torch.float64).pin_memory()
+        hr = torch.empty(cap + T, dtype=torch.float64).pin_memory()
+        n0 = tracks.cells
+        hu[: 5 * n0].copy_(tracks.u.reshape(-1).cpu())
+        hr[: n0 + T].copy_(tracks.radii.cpu())
         torch.cuda.synchronize()
+        h2d = d2h = e2e_cells = 0
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            tracks.u.copy_(hu, non_blocking=True)
-            tracks.radii.copy_(hr, non_blocking=True)
-            tracks.advance(dt, gin, gout, rk_order=rk)
-            hu.copy_(tracks.u, non_blocking=True)
-            hr.copy_(tracks.radii, non_blocking=True)
+            n = tracks.cells
+            e2e_cells += n
+            tracks.u.reshape(-1).copy_(hu[: 5 * n], non_blocking=True)
+            tracks.radii.copy_(hr[: n + T], non_blocking=True)
+            step()
+            m = tracks.cells
+            hu[: 5 * m].copy_(tracks.u.reshape(-1), non_blocking=True)
+            hr[: m + T].copy_(tracks.radii, non_blocking=True)
+            h2d += 48 * n + 8 * T
+            d2h += 48 * m + 8 * T
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
-        extra["e2e"] = {"value": C / e2e_s * world, "unit": "cell-updates/s",
-                        "h2d_bytes_per_step": 40 * C + 8 * F, "d2h_bytes_per_step": 40 * C + 8 * F}
+        extra["e2e"] = {"value": e2e_cells / args.steps / e2e_s * world, "unit": "cell-updates/s",
+                        "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps}
     if rank == 0 and not args.no_cpu_baseline:
         from oracle.oracle import dptr, load_oracle
         o = load_oracle()
         ru, rr = tracks.u.cpu().numpy().T.copy().ravel(), tracks.radii.cpu().numpy().copy()
         th = np.ascontiguousarray(theta.ravel())
-        nc = np.ascontiguousarray(ncells, dtype=np.int64)
+        nc = np.ascontiguousarray(tracks.ncells, dtype=np.int64)
+        Cb = tracks.cells
         g_in, g_out = np.ascontiguousarray(gin.ravel()), np.ascontiguousarray(gout.ravel())
+        o.oracle_sedov_remesh.restype = ctypes.c_int64
         t0 = time.perf_counter()
         o.oracle_sedov_advance_rk(ctypes.c_int32(T), nc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(th),
                                   dptr(rr), dptr(ru), dptr(g_in), dptr(g_out), ctypes.c_double(dt), ctypes.c_int32(rk),
                                   ctypes.c_int32(1))
+        # sedov::remesh track by track, each in a buffer with room for a split
+        c0 = 0
+        for j in range(T):
+            n = int(nc[j])
+            rj = np.zeros(n + 2)
+            rj[: n + 1] = rr[c0 + j: c0 + j + n + 1]
+            uj = np.zeros(5 * (n + 1))
+            uj[: 5 * n] = ru[5 * c0: 5 * (c0 + n)]
+            o.oracle_sedov_remesh(ctypes.c_int64(n), ctypes.c_double(th[2 * j]), ctypes.c_double(th[2 * j + 1]),
+                                  dptr(rj), dptr(uj), ctypes.c_double(2.0), ctypes.c_double(0.5), ctypes.c_double(1.0))
+            c0 += n
         el = time.perf_counter() - t0
-        extra["cpu_baseline"] = {"value": C / el, "unit": "cell-updates/s", "cores": 1, "kind": "port",
-                                 "sample": f"one forward-Euler step of all {T} tracks ({C} cells), {el:.2f} s, "
-                                           "one thread (the reference's sedov:: functions restated)"}
+        extra["cpu_baseline"] = {"value": Cb / el, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                                 "sample": f"one driver step (forward Euler, then remesh of every track) of all {T} "
+                                           f"tracks ({Cb} cells), {el:.2f} s, one thread (the reference's sedov:: "
+                                           "functions restated)"}
     line = _line(args, world, value, "cell-updates/s", ms, "f64",
                  {"workload": "sedov-tracks-1024", "tracks": T, "cells": C, "rk": rk,
                   "scheme": "PLM(1) + HLLC across contacts, moving radial faces, theta PLM + HLLC on transverse "

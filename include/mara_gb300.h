@@ -266,6 +266,11 @@ int mara_two_body_element_rates(const double* state, double time, const double* 
  * says why). */
 int mara_minidisk_sweep_columns(int32_t columns);
 
+/* Launch shape of the single-mesh mixed sweep: warps per block (1, 2 or 4;
+ * 0 = 4) and how many waves of resident warps its strip segments fill
+ * (0 = 2). Results do not depend on it. Returns 0, or -1 on bad arguments. */
+int mara_minidisk_sweep_shape(int32_t block_warps, int32_t waves);
+
 /* ---------------------------------------------------------------- minidisk ensemble */
 
 /* Many independent minidisk meshes (members, each with its own parameters

@@ -90,6 +90,7 @@ SIGNATURES = {
     "mara_minidisk_clock_update": (ctypes.c_int, [_MP, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.c_int32, _vp]),
     "mara_minidisk_sweep_columns": (ctypes.c_int, [ctypes.c_int32]),
+    "mara_minidisk_sweep_shape": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
     "mara_sedov_workspace_bytes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int64]),
     "mara_sedov_stage": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double,
                                         ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

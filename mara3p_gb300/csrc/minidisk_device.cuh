@@ -29,8 +29,11 @@ enum Kind { K_FP64 = 0, K_MIX1 = 1, K_MIX2 = 2, K_BLOCK = 3, K_MIXD = 4 };
 // for them on the device.
 struct FloatConsts
 {
-    float rs2, inv_mach2, half_nu, half_inv_dl, inv_dl, theta, R, dl;
+    float rs2, inv_mach2, half_nu, half_inv_dl, quarter_inv_dl, inv_dl, theta, two_theta, R, dl;
     float sink_rate, inv_s6, buffer_rate, neg2_inv_buffer_scale, omega, omega2, two_omega;
+    float visc_mu;          // nu / 2 / (4 dl): the viscous coefficient per (Sigma_l + Sigma_r) of doubled slopes
+    float sink_ex2;         // -log2(e) / s^6: sink rate = sink_rate 2^(q^3 sink_ex2), q = |x - x_body|^2
+    float buffer_ex2;       // -2 log2(e) / buffer_scale
 };
 
 struct Args
@@ -136,6 +139,12 @@ __device__ __forceinline__ float ex2_fast(float x)
     return y;
 }
 template<typename T>
+__device__ __forceinline__ T vex2(T a)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return ex2_fast(a);
+    else return make_float2(ex2_fast(a.x), ex2_fast(a.y));
+}
+template<typename T>
 __device__ __forceinline__ T vexp(T a)
 {
     const T t = vmul(a, bc<T>(1.4426950408889634f));
@@ -147,24 +156,38 @@ __device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float2 vmax(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 __device__ __forceinline__ float2 vmin(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
 
-__device__ __forceinline__ float minmod_select(float a, float b, float c)
+// The FP32 slopes are kept DOUBLED: for a = y0 - yl, b = yr - yl, c = yr - y0,
+// 2 minmod(theta a, b / 2, theta c) = sign x min(2 theta min(|a|, |c|), |b|)
+// (plm_gradient_scalar_t, scheme_plm_gradient.hpp:44-67). Scaling by two and
+// taking minima commute with rounding, so this is exactly twice the slope of
+// the three-multiply form, in one multiply; consumers take a quarter of it
+// for the face values.
+__device__ __forceinline__ float minmod2(float a, float b, float c, float two_theta)
 {
-    const float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
+    const float m = fminf(vmul(two_theta, fminf(fabsf(a), fabsf(c))), fabsf(b));
     const int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
     return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
 }
 
 template<typename T>
-__device__ __forceinline__ T vplm(T yl, T y0, T yr, float theta)
+__device__ __forceinline__ T vplm2(T yl, T y0, T yr, float two_theta)
 {
-    const T a = vmul(vsub(y0, yl), bc<T>(theta));
-    const T b = vmul(vsub(yr, yl), bc<T>(0.5f));
-    const T c = vmul(vsub(yr, y0), bc<T>(theta));
-    if constexpr (sizeof(T) == sizeof(float)) return minmod_select(a, b, c);
-    else return make_float2(minmod_select(a.x, b.x, c.x), minmod_select(a.y, b.y, c.y));
+    const T a = vsub(y0, yl), b = vsub(yr, yl), c = vsub(yr, y0);
+    if constexpr (sizeof(T) == sizeof(float)) return minmod2(a, b, c, two_theta);
+    else return make_float2(minmod2(a.x, b.x, c.x, two_theta), minmod2(a.y, b.y, c.y, two_theta));
 }
 
-__device__ inline float plm(float yl, float y0, float yr, float theta) { return vplm(yl, y0, yr, theta); }
+// The limited slope of a component: FP64 as the reference has it; FP32
+// doubled (vplm2).
+template<typename R> __device__ inline R cell_slope(R yl, R y0, R yr, const Args& A);
+template<> __device__ inline double cell_slope<double>(double yl, double y0, double yr, const Args& A)
+{
+    return plm(yl, y0, yr, A.theta);
+}
+template<> __device__ inline float cell_slope<float>(float yl, float y0, float yr, const Args& A)
+{
+    return vplm2(yl, y0, yr, A.f.two_theta);
+}
 
 // ------------------------------------------------------------- face flux
 // HLLE flux (physics_iso2d.hpp:156-173) plus viscous stress
@@ -221,6 +244,7 @@ __device__ inline void face_flux(const double pa[3], const double pb[3], const d
     }
 }
 
+// FP32 form; the slopes ga, gb, ta, tb are doubled (vplm2).
 template<int AXIS, typename T>
 __device__ inline void face_flux_f(const T pa[3], const T pb[3], const T ga[3], const T gb[3], const T ta[3],
                                    const T tb[3], T x, T y, const FloatConsts& F, T out[3])
@@ -228,8 +252,8 @@ __device__ inline void face_flux_f(const T pa[3], const T pb[3], const T ga[3], 
     T L[3], Rr[3];
     for (int k = 0; k < 3; ++k)
     {
-        L[k] = vfma(bc<T>(0.5f), ga[k], pa[k]);
-        Rr[k] = vfma(bc<T>(-0.5f), gb[k], pb[k]);
+        L[k] = vfma(bc<T>(0.25f), ga[k], pa[k]);
+        Rr[k] = vfma(bc<T>(-0.25f), gb[k], pb[k]);
     }
     // sound_speed_squared at the face: -phi/M^2 with phi = -1/sqrt(r^2 + rs^2)
     const T rinv = vrsqrt(vfma(x, x, vfma(y, y, bc<T>(F.rs2))));
@@ -239,24 +263,22 @@ __device__ inline void face_flux_f(const T pa[3], const T pb[3], const T ga[3], 
     const T vr = AXIS == 0 ? Rr[1] : Rr[2];
     const T ul[3] = {L[0], vmul(L[0], L[1]), vmul(L[0], L[2])};
     const T ur[3] = {Rr[0], vmul(Rr[0], Rr[1]), vmul(Rr[0], Rr[2])};
-    const T pgl = vmul(L[0], cs2), pgr = vmul(Rr[0], cs2);
-    T fl[3], fr[3];
-    fl[0] = vmul(vl, ul[0]);
-    fr[0] = vmul(vr, ur[0]);
-    fl[1] = AXIS == 0 ? vfma(vl, ul[1], pgl) : vmul(vl, ul[1]);
-    fr[1] = AXIS == 0 ? vfma(vr, ur[1], pgr) : vmul(vr, ur[1]);
-    fl[2] = AXIS == 0 ? vmul(vl, ul[2]) : vfma(vl, ul[2], pgl);
-    fr[2] = AXIS == 0 ? vmul(vr, ur[2]) : vfma(vr, ur[2], pgr);
     const T ap = vmax(bc<T>(0.0f), vadd(vmax(vl, vr), cs));
     const T am = vmin(bc<T>(0.0f), vsub(vmin(vl, vr), cs));
-    // (ap fl - am fr - (ul - ur) ap am) / (ap - am) = a fl + b fr + c (ur - ul)
+    // HLLE: (ap fl - am fr - (ul - ur) ap am) / (ap - am) = a fl + b fr + c (ur - ul)
+    // with fl = vl ul + cs2 Sigma_l n, fr = vr ur + cs2 Sigma_r n, regrouped as
+    // (a vl - c) ul + (b vr + c) ur + (a Sigma_l + b Sigma_r) cs2 n
     const T inv = vrcp(vsub(ap, am));
     const T ca = vmul(ap, inv), cb = vmul(vneg(am), inv), cc = vmul(vmul(ap, am), inv);
-    for (int k = 0; k < 3; ++k) out[k] = vfma(cc, vsub(ur[k], ul[k]), vfma(cb, fr[k], vmul(ca, fl[k])));
+    const T wl = vfma(ca, vl, vneg(cc)), wr = vfma(cb, vr, cc);
+    const T pn = vmul(vfma(ca, L[0], vmul(cb, Rr[0])), cs2);
+    out[0] = vfma(wl, ul[0], vmul(wr, ur[0]));
+    out[1] = AXIS == 0 ? vfma(wl, ul[1], vfma(wr, ur[1], pn)) : vfma(wl, ul[1], vmul(wr, ur[1]));
+    out[2] = AXIS == 0 ? vfma(wl, ul[2], vmul(wr, ur[2])) : vfma(wl, ul[2], vfma(wr, ur[2], pn));
     if (F.half_nu != 0.0f)
     {
-        // mu = nu (Sigma_l + Sigma_r) / 2 carries the 1/(2 dl) of the averaged slopes
-        const T mu = vmul(vmul(bc<T>(F.half_nu), vadd(Rr[0], L[0])), bc<T>(F.half_inv_dl));
+        // mu = nu (Sigma_l + Sigma_r) / 2 carries the 1/(4 dl) of the averaged doubled slopes
+        const T mu = vmul(vadd(Rr[0], L[0]), bc<T>(F.visc_mu));
         const T nmu = vneg(mu);
         const T vx_long = vadd(ga[1], gb[1]);
         const T vy_long = vadd(ga[2], gb[2]);
@@ -305,27 +327,30 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
     const T i1 = vrsqrt(vadd(q1, bc<T>(F.rs2))), i2 = vrsqrt(vadd(q2, bc<T>(F.rs2)));
     const T g1 = vmul(vmul(vmul(bc<T>(-bf[0]), i1), i1), i1);
     const T g2 = vmul(vmul(vmul(bc<T>(-bf[3]), i2), i2), i2);
-    const T sr1 = vmul(bc<T>(F.sink_rate), vexp(vmul(vmul(vmul(q1, q1), q1), bc<T>(-F.inv_s6))));
-    const T sr2 = vmul(bc<T>(F.sink_rate), vexp(vmul(vmul(vmul(q2, q2), q2), bc<T>(-F.inv_s6))));
+    // sinks: sink_rate exp(-r^6 / s^6) as sink_rate 2^(q^3 sink_ex2), q = r^2
+    const T e1 = vex2(vmul(vmul(q1, q1), vmul(q1, bc<T>(F.sink_ex2))));
+    const T e2 = vex2(vmul(vmul(q2, q2), vmul(q2, bc<T>(F.sink_ex2))));
+    const T srs = vmul(bc<T>(F.sink_rate), vadd(e1, e2));
     const T r2 = vfma(x, x, vmul(y, y));
     const T rinv = vrsqrt(r2);
     const T rr = vmul(r2, rinv);
     // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
     const T br = vmul(bc<T>(F.buffer_rate),
-                      vrcp(vadd(bc<T>(1.0f), vexp(vmul(vsub(rr, bc<T>(F.R)), bc<T>(F.neg2_inv_buffer_scale))))));
+                      vrcp(vadd(bc<T>(1.0f), vex2(vmul(vsub(rr, bc<T>(F.R)), bc<T>(F.buffer_ex2))))));
     pot = vrsqrt(vadd(r2, bc<T>(F.rs2)));
-    const T vp = vsub(vsqrt(pot), vmul(bc<T>(F.omega), rr));
-    const T ui[3] = {bc<T>(1.0f), vmul(vmul(vneg(vp), y), rinv), vmul(vmul(vp, x), rinv)};
+    // Keplerian velocity of the buffer target, over r: (sqrt(pot) - omega r) / r
+    const T vpr = vmul(vfma(bc<T>(-F.omega), rr, vsqrt(pot)), rinv);
+    const T ui1 = vmul(vneg(vpr), y), ui2 = vmul(vpr, x);
     T ax = vfma(g2, dx2, vmul(g1, dx1));
     ax = vfma(bc<T>(F.omega2), x, ax);
     ax = vfma(bc<T>(F.two_omega), pc[2], ax);
     T ay = vfma(g2, dy2, vmul(g1, dy1));
     ay = vfma(bc<T>(F.omega2), y, ay);
     ay = vfma(bc<T>(-F.two_omega), pc[1], ay);
-    const T srs = vadd(sr1, sr2);
     if constexpr (DIAG)
     {
         // the rate-vector sums of this cell (times the cell area on the flush)
+        const T sr1 = vmul(bc<T>(F.sink_rate), e1), sr2 = vmul(bc<T>(F.sink_rate), e2);
         const T sg1 = vmul(pc[0], g1), sg2 = vmul(pc[0], g2);
         diag_add(acc[0], vmul(pc[0], sr1));
         diag_add(acc[1], vmul(pc[0], sr2));
@@ -341,10 +366,12 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
         diag_add(acc[11], pc[0]);
         diag_add(acc[12], vsub(vmul(x, uc[2]), vmul(y, uc[1])));
     }
+    // buffer toward ui = (1, ui1, ui2) and sinks: (ui - uc) br - uc srs = ui br - uc (br + srs)
+    const T sb = vadd(br, srs);
     T src[3];
-    for (int k = 0; k < 3; ++k) src[k] = vfma(vsub(ui[k], uc[k]), br, vneg(vmul(uc[k], srs)));
-    src[1] = vfma(pc[0], ax, src[1]);
-    src[2] = vfma(pc[0], ay, src[2]);
+    src[0] = vfma(vneg(uc[0]), sb, br);
+    src[1] = vfma(pc[0], ax, vfma(ui1, br, vneg(vmul(uc[1], sb))));
+    src[2] = vfma(pc[0], ay, vfma(ui2, br, vneg(vmul(uc[2], sb))));
     for (int k = 0; k < 3; ++k)
         du[k] = vmul(bc<T>(dtf), vfma(vadd(dfx[k], dfy[k]), bc<T>(-F.inv_dl), src[k]));
 }
@@ -522,13 +549,13 @@ __device__ inline void sweep_prim(const RawRow& r, float p[3])
     p[2] = vmul(m2, inv);
 }
 
-__device__ inline void slope_y(const float p[3], float theta, float g[3])
+__device__ inline void slope_y(const float p[3], float two_theta, float g[3])
 {
     for (int k = 0; k < 3; ++k)
     {
         float l = __shfl_up_sync(0xffffffffu, p[k], 1);
         float r = __shfl_down_sync(0xffffffffu, p[k], 1);
-        g[k] = plm(l, p[k], r, theta);
+        g[k] = vplm2(l, p[k], r, two_theta);
     }
 }
 
@@ -544,7 +571,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
     const bool interior = lane >= 2 && lane < 2 + SW_COLS && jcol < N;
     const size_t NN = size_t(N) * N;
     const FloatConsts& F = A.f;
-    const float theta = F.theta;
+    const float theta = F.two_theta;   // doubled slopes (vplm2)
 
     float bf[6];
     double dt;
@@ -577,8 +604,8 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
     float gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
     for (int k = 0; k < 3; ++k)
     {
-        gxm1[k] = plm(pm2[k], pm1[k], p0[k], theta);
-        gx0[k] = plm(pm1[k], p0[k], p1[k], theta);
+        gxm1[k] = vplm2(pm2[k], pm1[k], p0[k], theta);
+        gx0[k] = vplm2(pm1[k], p0[k], p1[k], theta);
     }
     slope_y(pm1, theta, gym1);
     slope_y(p0, theta, gy0);
@@ -593,7 +620,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
         sweep_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
         CellIn<float> cin;
         if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
-        for (int k = 0; k < 3; ++k) gx1[k] = plm(p0[k], p1[k], p2[k], theta);
+        for (int k = 0; k < 3; ++k) gx1[k] = vplm2(p0[k], p1[k], p2[k], theta);
         slope_y(p1, theta, gy1);
         face_flux<0>(p0, p1, gx0, gx1, gy0, gy1, fmaf(float(i + 1), F.dl, -F.R), yc, A, fxp);
 
@@ -728,13 +755,13 @@ __device__ inline void ring2_row(const Ring2& R, int row, int lane, RawRow2& r)
 
 // y slopes of both columns: the left neighbour of the first column is lane
 // l-1's second column, the right neighbour of the second is lane l+1's first.
-__device__ inline void slope_y2(const float2 p[3], float theta, float2 g[3])
+__device__ inline void slope_y2(const float2 p[3], float two_theta, float2 g[3])
 {
     for (int k = 0; k < 3; ++k)
     {
         const float l = __shfl_up_sync(0xffffffffu, p[k].y, 1);
         const float r = __shfl_down_sync(0xffffffffu, p[k].x, 1);
-        g[k] = vplm(make_float2(l, p[k].x), p[k], make_float2(p[k].y, r), theta);
+        g[k] = vplm2(make_float2(l, p[k].x), p[k], make_float2(p[k].y, r), two_theta);
     }
 }
 
@@ -748,7 +775,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     const bool interior = lane >= 1 && lane < 1 + SW2_COLS / 2 && jcol < N;
     const size_t NN = size_t(N) * N;
     const FloatConsts& F = A.f;
-    const float theta = F.theta;
+    const float theta = F.two_theta;   // doubled slopes (vplm2)
 
     float bf[6];
     double dt;
@@ -799,8 +826,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     float2 gxm1[3], gx0[3], gym1[3], gy0[3], fxm[3];
     for (int k = 0; k < 3; ++k)
     {
-        gxm1[k] = vplm(pm2[k], pm1[k], p0[k], theta);
-        gx0[k] = vplm(pm1[k], p0[k], p1[k], theta);
+        gxm1[k] = vplm2(pm2[k], pm1[k], p0[k], theta);
+        gx0[k] = vplm2(pm1[k], p0[k], p1[k], theta);
     }
     slope_y2(pm1, theta, gym1);
     slope_y2(p0, theta, gy0);
@@ -825,7 +852,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
             if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
         }
-        for (int k = 0; k < 3; ++k) gx1[k] = vplm(p0[k], p1[k], p2[k], theta);
+        for (int k = 0; k < 3; ++k) gx1[k] = vplm2(p0[k], p1[k], p2[k], theta);
         slope_y2(p1, theta, gy1);
         face_flux_f<0, float2>(p0, p1, gx0, gx1, gy0, gy1, bc<float2>(fmaf(float(i + 1), F.dl, -F.R)), yc, F, fxp);
 

@@ -224,6 +224,33 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
     assert lib.mara_minidisk_sweep_columns(3) == -1
 
 
+@pytest.mark.parametrize("block_size,depth", [(64, 2), (100, 1), (80, 3)])
+def test_sweep_launch_shapes_bit_identical(md, block_size, depth):
+    """Every launch shape of the single-mesh sweep (warps per block, waves of
+    strip segments, down to 16-row segments and ragged last segments) gives
+    the same bits: the segments only change which warp computes a cell."""
+    from mara3p_gb300._capi import lib
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    u0 = md.initial_conserved(sd, seed=9, amplitude=0.01)
+    out = []
+    try:
+        for shape in ((0, 0), (4, 1), (1, 1), (2, 3), (1, 7), (4, 16)):
+            assert lib.mara_minidisk_sweep_shape(*shape) == 0
+            run = md.Run(sd, u0.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL)
+            run.advance(4)
+            torch.cuda.synchronize()
+            out.append((shape, run.u.clone(), run.clock_state()))
+    finally:
+        lib.mara_minidisk_sweep_shape(0, 0)
+    (s0, u0r, k0) = out[0]
+    assert torch.isfinite(u0r).all()
+    for shape, u, k in out[1:]:
+        assert torch.equal(u, u0r), shape
+        assert (k.time, k.dt, k.iteration) == (k0.time, k0.dt, k0.iteration), shape
+    for bad in ((3, 1), (8, 1), (-1, 0), (4, 17), (1, -2)):
+        assert lib.mara_minidisk_sweep_shape(*bad) == -1
+
+
 @pytest.mark.parametrize("block_size,depth", [(20, 2), (50, 1), (40, 3), (130, 0)])
 def test_ragged_meshes_fp64_rk2_and_mixed(md, oracle, block_size, depth):
     """Meshes whose size is not a multiple of the 16 x 32 tiles or the 28/60
