@@ -588,8 +588,8 @@ __global__ void wavespeed_key_kernel(int N, FloatConsts F, const double* u, unsi
     {
         const int i = int(c / N), j = int(c % N);
         const float x = fmaf(float(i) + 0.5f, F.dl, -F.R), y = fmaf(float(j) + 0.5f, F.dl, -F.R);
-        const float pot = rsqrt_fast(fmaf(x, x, y * y) + F.rs2);
-        key = key_max(key, speed_key(wavespeed_f(F, d2f(u[c]), d2f(u[NN + c]), d2f(u[2 * NN + c]), pot), c));
+        const float spot = sqrt_fast(rsqrt_fast(fmaf(x, x, y * y) + F.rs2));
+        key = key_max(key, speed_key(wavespeed_f(F, d2f(u[c]), d2f(u[NN + c]), d2f(u[2 * NN + c]), spot), c));
     }
     for (int o = 16; o > 0; o >>= 1) key = key_max(key, __shfl_xor_sync(0xffffffffu, key, o));
     if ((threadIdx.x & 31) == 0) wk[threadIdx.x >> 5] = key;
@@ -694,6 +694,7 @@ Args base_args(const mara_minidisk_params* sd)
     FloatConsts& f = A.f;
     f.rs2 = float(A.rs2);
     f.inv_mach2 = float(1.0 / (A.mach * A.mach));
+    f.inv_mach = float(1.0 / A.mach);
     f.half_nu = float(A.nu * 0.5);
     f.half_inv_dl = float(0.5 / A.dl);
     f.quarter_inv_dl = f.half_inv_dl * 0.5f;

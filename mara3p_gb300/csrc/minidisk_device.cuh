@@ -31,6 +31,7 @@ struct FloatConsts
 {
     float rs2, inv_mach2, half_nu, half_inv_dl, quarter_inv_dl, inv_dl, theta, two_theta, R, dl;
     float sink_rate, inv_s6, buffer_rate, neg2_inv_buffer_scale, omega, omega2, two_omega;
+    float inv_mach;         // 1 / M: the sound speed is sqrt(pot) / M, pot = 1/sqrt(r^2 + rs^2)
     float visc_mu;          // nu / 2 / (4 dl): the viscous coefficient per (Sigma_l + Sigma_r) of doubled slopes
     float sink_ex2;         // -log2(e) / s^6: sink rate = sink_rate 2^(q^3 sink_ex2), q = |x - x_body|^2
     float buffer_ex2;       // -2 log2(e) / buffer_scale
@@ -309,14 +310,14 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
 // Stage increment du = dt * L(u) of one cell (or a pair) in FP32: flux
 // divergence, gravity of both point masses, sinks, rotating-frame terms and
 // the outer buffer (problems/minidisk_scheme.cpp:337-352). uc returns the
-// FP32 conserved state the increment was computed from, pot returns
-// 1/sqrt(r^2 + rs^2), from which the cell-centre sound speed follows.
+// FP32 conserved state the increment was computed from, spot returns
+// sqrt(1/sqrt(r^2 + rs^2)), the cell-centre sound speed times M.
 __device__ __forceinline__ void diag_add(float& a, float v) { a += v; }
 __device__ __forceinline__ void diag_add(float& a, float2 v) { a += v.x + v.y; }
 
 template<typename T, bool DIAG = false>
 __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc[3], const T dfx[3], const T dfy[3],
-                                      const float bf[6], float dtf, T du[3], T uc[3], T& pot, float* acc = nullptr)
+                                      const float bf[6], float dtf, T du[3], T uc[3], T& spot, float* acc = nullptr)
 {
     uc[0] = pc[0];
     uc[1] = vmul(pc[0], pc[1]);
@@ -337,9 +338,9 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
     // 0.5*rate*(1 + tanh(z)) written as rate / (1 + exp(-2z))
     const T br = vmul(bc<T>(F.buffer_rate),
                       vrcp(vadd(bc<T>(1.0f), vex2(vmul(vsub(rr, bc<T>(F.R)), bc<T>(F.buffer_ex2))))));
-    pot = vrsqrt(vadd(r2, bc<T>(F.rs2)));
+    spot = vsqrt(vrsqrt(vadd(r2, bc<T>(F.rs2))));
     // Keplerian velocity of the buffer target, over r: (sqrt(pot) - omega r) / r
-    const T vpr = vmul(vfma(bc<T>(-F.omega), rr, vsqrt(pot)), rinv);
+    const T vpr = vmul(vfma(bc<T>(-F.omega), rr, spot), rinv);
     const T ui1 = vmul(vneg(vpr), y), ui2 = vmul(vpr, x);
     T ax = vfma(g2, dx2, vmul(g1, dx1));
     ax = vfma(bc<T>(F.omega2), x, ax);
@@ -432,13 +433,11 @@ __device__ inline void flush_speed_key(const Args& A, unsigned long long key)
 
 // Fastest wavespeed max(|vx|, |vy|) + cs (iso2d::fastest_wavespeed,
 // physics_iso2d.hpp:108-116) of an FP32 conserved state at a cell whose
-// 1/sqrt(r^2 + rs^2) is pot.
-__device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, float m2, float pot)
+// sqrt(1/sqrt(r^2 + rs^2)) is spot. max(|m1|, |m2|) / s equals the larger of
+// the two velocities exactly (rounding is monotonic).
+__device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, float m2, float spot)
 {
-    const float inv = rcp_fast(s);
-    const float vx = vmul(m1, inv), vy = vmul(m2, inv);
-    const float cs = sqrt_fast(vmul(pot, F.inv_mach2));
-    return vadd(fmaxf(fabsf(vx), fabsf(vy)), cs);
+    return vfma(fmaxf(fabsf(m1), fabsf(m2)), rcp_fast(s), vmul(spot, F.inv_mach));
 }
 
 // One cell's stage result: the FP32 increment (stage 1 of mixed RK2), or the
@@ -450,8 +449,8 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
                                   const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
                                   const CellIn<float>& in, unsigned long long& local_key, float* acc = nullptr)
 {
-    float du[3], uc[3], pot;
-    cell_increment<float, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
+    float du[3], uc[3], spot;
+    cell_increment<float, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, spot, acc);
     if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) A.d_out[k * NN + idx] = du[k];
@@ -464,7 +463,7 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
         A.u_out[k * NN + idx] = in.u[k] + f2d(inc);
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), 0.5f, uc[k]) : vadd(uc[k], du[k]);
     }
-    if (A.amax) local_key = key_max(local_key, speed_key(wavespeed_f(A.f, of[0], of[1], of[2], pot), idx));
+    if (A.amax) local_key = key_max(local_key, speed_key(wavespeed_f(A.f, of[0], of[1], of[2], spot), idx));
 }
 
 // The pair form: columns idx and idx + 1 of one row (idx even).
@@ -473,8 +472,8 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
                                    const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
                                    const CellIn<float2>& in, unsigned long long& local_key, float* acc = nullptr)
 {
-    float2 du[3], uc[3], pot;
-    cell_increment<float2, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, pot, acc);
+    float2 du[3], uc[3], spot;
+    cell_increment<float2, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, spot, acc);
     if (!writes_state<KIND>(A))
     {
         for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(A.d_out + k * NN + idx) = du[k];
@@ -489,8 +488,8 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), bc<float2>(0.5f), uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax)
-        local_key = key_max(local_key, key_max(speed_key(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, pot.x), idx),
-                                               speed_key(wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, pot.y), idx + 1)));
+        local_key = key_max(local_key, key_max(speed_key(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, spot.x), idx),
+                                               speed_key(wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, spot.y), idx + 1)));
 }
 
 // A warp's diagnostic sums into the stage's rate row: FP32 per lane, a
@@ -734,9 +733,10 @@ struct Ring2
 };
 
 template<int KIND>
-__device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int jg, size_t NN, int lane)
+__device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int jg, size_t NN, int lane,
+                                   int slot = -1)
 {
-    const int slot = ring_slot(row);
+    if (slot < 0) slot = ring_slot(row);
     const size_t idx = size_t(wrap1(row, A.N)) * A.N + jg;
     for (int k = 0; k < 3; ++k) cp_async16(&R.u[(slot * 3 + k) * 32 + lane], A.u_in + k * NN + idx);
     if (KIND == K_MIX2)
@@ -745,23 +745,24 @@ __device__ inline void ring2_fetch(const Args& A, const Ring2& R, int row, int j
 }
 
 template<int KIND>
-__device__ inline void ring2_row(const Ring2& R, int row, int lane, RawRow2& r)
+__device__ inline void ring2_row(const Ring2& R, int row, int lane, RawRow2& r, int slot = -1)
 {
-    const int slot = ring_slot(row);
+    if (slot < 0) slot = ring_slot(row);
     for (int k = 0; k < 3; ++k) r.u[k] = R.u[(slot * 3 + k) * 32 + lane];
     if (KIND == K_MIX2)
         for (int k = 0; k < 3; ++k) r.d[k] = R.d[(slot * 3 + k) * 32 + lane];
 }
 
 // y slopes of both columns: the left neighbour of the first column is lane
-// l-1's second column, the right neighbour of the second is lane l+1's first.
-__device__ inline void slope_y2(const float2 p[3], float two_theta, float2 g[3])
+// l-1's second column (returned in left, which the row's y faces reuse), the
+// right neighbour of the second is lane l+1's first.
+__device__ inline void slope_y2(const float2 p[3], float two_theta, float2 g[3], float left[3])
 {
     for (int k = 0; k < 3; ++k)
     {
-        const float l = __shfl_up_sync(0xffffffffu, p[k].y, 1);
+        left[k] = __shfl_up_sync(0xffffffffu, p[k].y, 1);
         const float r = __shfl_down_sync(0xffffffffu, p[k].x, 1);
-        g[k] = vplm2(make_float2(l, p[k].x), p[k], make_float2(p[k].y, r), two_theta);
+        g[k] = vplm2(make_float2(left[k], p[k].x), p[k], make_float2(p[k].y, r), two_theta);
     }
 }
 
@@ -829,22 +830,26 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         gxm1[k] = vplm2(pm2[k], pm1[k], p0[k], theta);
         gx0[k] = vplm2(pm1[k], p0[k], p1[k], theta);
     }
-    slope_y2(pm1, theta, gym1);
-    slope_y2(p0, theta, gy0);
+    float lm1[3], l0[3];
+    slope_y2(pm1, theta, gym1, lm1);
+    slope_y2(p0, theta, gy0, l0);
     face_flux_f<0, float2>(pm1, p0, gxm1, gx0, gym1, gy0, bc<float2>(fmaf(float(i0), F.dl, -F.R)), yc, F, fxm);
 
     unsigned long long local_key = 0ull;
     float acc[DIAG ? DIAG_SUMS : 1] = {};
+    int slot0 = ring_slot(i0);                                // ring slot of row i, kept by increments
     for (int i = i0; i < i1; ++i)
     {
         float2 p2[3], gx1[3], gy1[3], fxp[3];
         CellIn<float2> cin;
         if constexpr (RING)
         {
+            const int slot2 = slot0 >= RING_ROWS - 2 ? slot0 + 2 - RING_ROWS : slot0 + 2;
+            const int slot4 = slot0 == 0 ? RING_ROWS - 1 : slot0 - 1;
             cp_async_wait_one();                              // row i+2 (row i+3 may stay in flight)
-            ring2_row<KIND>(ring, i + 2, lane, raw);
+            ring2_row<KIND>(ring, i + 2, lane, raw, slot2);
             sweep2_prim<KIND>(raw, p2);
-            ring2_fetch<KIND>(A, ring, i + 4, jg, NN, lane);  // into the slot of row i-1
+            ring2_fetch<KIND>(A, ring, i + 4, jg, NN, lane, slot4);  // into the slot of row i-1
         }
         else
         {
@@ -852,17 +857,20 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             sweep2_fetch<KIND>(A, i + 3, jg, NN, raw);        // in flight during this row
             if (interior) load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
         }
+        float l1[3];
         for (int k = 0; k < 3; ++k) gx1[k] = vplm2(p0[k], p1[k], p2[k], theta);
-        slope_y2(p1, theta, gy1);
+        slope_y2(p1, theta, gy1, l1);
         face_flux_f<0, float2>(p0, p1, gx0, gx1, gy0, gy1, bc<float2>(fmaf(float(i + 1), F.dl, -F.R)), yc, F, fxp);
 
-        // y faces on the left of both columns (row i): the first from lane l-1's second column
+        // y faces on the left of both columns (row i): the first from lane l-1's
+        // second column (its primitives shuffled with the row's y slopes; the
+        // density's transverse slope is not used)
         float2 pa[3], ga[3], ta[3], fy[3];
         for (int k = 0; k < 3; ++k)
         {
-            pa[k] = make_float2(__shfl_up_sync(0xffffffffu, p0[k].y, 1), p0[k].x);
+            pa[k] = make_float2(l0[k], p0[k].x);
             ga[k] = make_float2(__shfl_up_sync(0xffffffffu, gy0[k].y, 1), gy0[k].x);
-            ta[k] = make_float2(__shfl_up_sync(0xffffffffu, gx0[k].y, 1), gx0[k].x);
+            ta[k] = k == 0 ? gx0[0] : make_float2(__shfl_up_sync(0xffffffffu, gx0[k].y, 1), gx0[k].x);
         }
         const float xc = fmaf(float(i) + 0.5f, F.dl, -F.R);
         face_flux_f<1, float2>(pa, p0, ga, gy0, ta, gx0, bc<float2>(xc), yv, F, fy);
@@ -878,7 +886,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             if (interior && writes_state<KIND>(A))
             {
                 RawRow2 own;
-                ring2_row<KIND>(ring, i, lane, own);
+                ring2_row<KIND>(ring, i, lane, own, slot0);
                 for (int k = 0; k < 3; ++k)
                 {
                     cin.u[k] = own.u[k];
@@ -897,7 +905,9 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             gx0[k] = gx1[k];
             gy0[k] = gy1[k];
             fxm[k] = fxp[k];
+            l0[k] = l1[k];
         }
+        slot0 = slot0 == RING_ROWS - 1 ? 0 : slot0 + 1;
     }
     // the rows fetched beyond the strip are never read, but no copy may land
     // in shared memory after the warp is gone
