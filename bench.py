@@ -734,7 +734,7 @@ def run_sedov(args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels, then remesh; bound by FP64 recovery and "
                                        "HLLC arithmetic, not by HBM)", "peak_source": f"{kind} hbm_gbs"}
-    extra = {"gpu_launches": (5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
+    extra = {"gpu_launches": (1 + 5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
     if not args.no_e2e:
         # through the public calls with host buffers: the tracks' state to the
         # GPU, one driver step, the (remeshed) state back, every step

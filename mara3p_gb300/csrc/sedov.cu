@@ -14,7 +14,8 @@
 // (mesh::transverse_faces, src/mesh_sliding.hpp:122-172); interface j's
 // faces start at po(j) = co[j] + co[j+1] - co[1] + j.
 //
-// One stage = five kernels, one thread per item:
+// Each call first tabulates the tracks' sines, cosines and centre cotangents
+// (trig_kernel); then one stage = five kernels, one thread per item:
 //   prim_kernel    cell: volume, u / dV, SRHD Newton recovery
 //   grad_kernel    cell: PLM slope on the cell-centre radii (zero at both ends)
 //   radial_kernel  face: faces states from both neighbours' slopes, HLLC flux
@@ -75,6 +76,7 @@ struct Stage
     int32_t* pil;           // [NPmax] merge counters
     int32_t* pir;
     int64_t np_max;
+    const double* tg;       // [T][5] track geometry (trig_kernel)
     int* failures;
 };
 
@@ -94,26 +96,50 @@ __device__ inline int64_t face_offset(const Tracks& t, int j) { return t.co[j] +
 __device__ inline int64_t polar_offset(const Tracks& t, int j) { return t.co[j] + t.co[j + 1] - t.co[1] + j; }
 
 // sedov::cell_volume / face_area (scheme_sedov2d.cpp:40-62)
-__device__ inline double cell_volume(double r0, double r1, double t0, double t1)
+__device__ inline double cell_volume_cos(double r0, double r1, double c0, double c1)
 {
-    const double dcost = -(cos(t1) - cos(t0));
+    const double dcost = -(c1 - c0);
     return 2.0 * M_PI * (r1 * r1 * r1 - r0 * r0 * r0) / 3.0 * dcost;
 }
 
-__device__ inline double face_area(double r0, double r1, double t0, double t1)
+// face_area (scheme_sedov2d.cpp) from the sines and cosines of the two polar
+// angles; the reference's pow(x, 0.5) is the correctly rounded square root.
+__device__ inline double face_area(double r0, double r1, double s0, double c0, double s1, double c1)
 {
-    const double R0 = r0 * sin(t0), R1 = r1 * sin(t1);
-    const double z0 = r0 * cos(t0), z1 = r1 * cos(t1);
+    const double R0 = r0 * s0, R1 = r1 * s1;
+    const double z0 = r0 * c0, z1 = r1 * c1;
     const double dR = R1 - R0, dz = z1 - z0;
-    return M_PI * (R0 + R1) * pow(dR * dR + dz * dz, 0.5);
+    return M_PI * (R0 + R1) * sqrt(dR * dR + dz * dz);
 }
 
-// plm_gradient_scalar_t on coordinates (scheme_plm_gradient.hpp:44-67)
-__device__ inline double plm_x(double xl, double x0, double xr, double yl, double y0, double yr, double theta)
+// Track geometry, the same for every cell of a track and every stage:
+// sin and cos of both polar bounds and the cotangent of the track centre,
+// [T][5] = {sin t0, cos t0, sin t1, cos t1, tan(pi/2 - (t0 + t1)/2)}.
+enum { TG_S0 = 0, TG_C0 = 1, TG_S1 = 2, TG_C1 = 3, TG_COT = 4 };
+
+__global__ void trig_kernel(const int T, const double* theta, double* tg)
 {
-    const double a = (y0 - yl) / (x0 - xl) * theta;
-    const double b = (yr - yl) / (xr - xl);
-    const double c = (yr - y0) / (xr - x0) * theta;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < T; j += gridDim.x * blockDim.x)
+    {
+        const double t0 = theta[2 * j], t1 = theta[2 * j + 1];
+        tg[5 * j + TG_S0] = sin(t0);
+        tg[5 * j + TG_C0] = cos(t0);
+        tg[5 * j + TG_S1] = sin(t1);
+        tg[5 * j + TG_C1] = cos(t1);
+        tg[5 * j + TG_COT] = tan(M_PI_2 - 0.5 * (t0 + t1));
+    }
+}
+
+// plm_gradient_scalar_t on coordinates (scheme_plm_gradient.hpp:44-67), with
+// the reciprocal coordinate spacings il = 1/(x0 - xl), ib = 1/(xr - xl),
+// ir = 1/(xr - x0) taken once for all five components (FP64 division is the
+// slowest FP64 operation here; the products differ from the quotients by an
+// ulp).
+__device__ inline double plm_r(double il, double ib, double ir, double yl, double y0, double yr, double theta)
+{
+    const double a = (y0 - yl) * il * theta;
+    const double b = (yr - yl) * ib;
+    const double c = (yr - y0) * ir * theta;
     const double sa = copysign(1.0, a), sb = copysign(1.0, b), sc = copysign(1.0, c);
     return 0.25 * fabs(sa + sb) * (sa + sc) * fmin(fmin(fabs(a), fabs(b)), fabs(c));
 }
@@ -151,94 +177,124 @@ __device__ inline void radial_slope(const Stage& S, int j, int64_t i, int64_t n,
     const int64_t c = S.t.co[j] + i, f = face_offset(S.t, j) + i;
     const double* r = S.r + f;
     const double xl = 0.5 * (r[-1] + r[0]), x0 = 0.5 * (r[0] + r[1]), xr = 0.5 * (r[1] + r[2]);
+    const double il = 1.0 / (x0 - xl), ib = 1.0 / (xr - xl), ir = 1.0 / (xr - x0);
     const double th = S.use_plm ? 1.0 : 0.0;
     const int64_t C = S.t.C;
     for (int k = 0; k < 5; ++k)
-        g[k] = plm_x(xl, x0, xr, S.P[k * C + c - 1], S.P[k * C + c], S.P[k * C + c + 1], th);
+        g[k] = plm_r(il, ib, ir, S.P[k * C + c - 1], S.P[k * C + c], S.P[k * C + c + 1], th);
+}
+
+// One side of a face: conserved state, flux and outer wavespeeds along axis
+// (conserved_density, flux, outer_wavespeeds: physics_srhd.hpp:182-195,
+// 291-324) from one Lorentz factor, one reciprocal of it and one of the
+// wavespeed denominator: four FP64 divisions and two square roots where the
+// term-by-term form takes nine and four.
+struct Side
+{
+    double u[5], f[5];
+    double vn, am, ap;
+};
+
+__device__ inline void side_of(const SPrim<double>& p, int axis, Side& s)
+{
+    const double gm = kGamma;
+    const double ch = 1.0 + 1.0 / (gm - 1.0);            // enthalpy_density's 1 + 1/(gamma - 1)
+    const double uu = p.u[0] * p.u[0] + p.u[1] * p.u[1] + p.u[2] * p.u[2];
+    const double W = sqrt(1.0 + uu);
+    const double iW = 1.0 / W;
+    const double vn = p.u[axis] * iW;
+    const double e = p.rho + p.p * ch;                   // rho c^2 + p gamma / (gamma - 1)
+    const double h = e / p.rho;
+    const double D = p.rho * W;
+    s.u[0] = D;
+    for (int k = 0; k < 3; ++k) s.u[1 + k] = D * h * p.u[k];
+    s.u[4] = D * (h * W - 1.0) - p.p;
+    for (int k = 0; k < 5; ++k) s.f[k] = vn * s.u[k];
+    s.f[1 + axis] += p.p;
+    s.f[4] += p.p * vn;
+    const double a2 = gm * p.p / e;
+    const double bb = uu * iW * iW;                      // uu / (1 + uu)
+    const double disc = a2 * (1.0 - bb) * (1.0 - bb * a2 - vn * vn * (1.0 - a2));
+    const double k0 = sqrt(disc);
+    const double iden = 1.0 / (1.0 - bb * a2);
+    const double vna = vn * (1.0 - a2);
+    s.vn = vn;
+    s.am = (vna - k0) * iden;
+    s.ap = (vna + k0) * iden;
 }
 
 // The HLLC modes of riemann_solver (physics_srhd.hpp:351-487) along axis:
 // FIXED (face speed 0), MOVING (face speed w), ACROSS (the left star flux
 // with the contact speed, which is returned in *contact). Returns 1 where the
-// reference throws (NaN contact speed or beyond 1e3).
+// reference throws (NaN contact speed or beyond 1e3). Divisions by the same
+// denominator (the HLL fan width, each star state's s - s*) are one
+// reciprocal and products.
 enum { FIXED = 0, MOVING = 1, ACROSS = 2 };
 
 __device__ inline int hllc_mode(const SPrim<double>& pl, const SPrim<double>& pr, int axis, int mode, double w,
                                 double F[5], double* contact)
 {
-    using namespace srhd;
-    const double gm = kGamma;
-    double ul[5], ur[5], fl[5], fr[5];
-    cons_of(pl, gm, ul);
-    cons_of(pr, gm, ur);
-    flux_of(pl, ul, axis, fl);
-    flux_of(pr, ur, axis, fr);
-    double alm, alp, arm, arp;
-    outer_speeds(pl, axis, gm, alm, alp);
-    outer_speeds(pr, axis, gm, arm, arp);
-    const double ar = fmax(alp, arp);
-    const double al = fmin(alm, arm);
+    Side L, R;
+    side_of(pl, axis, L);
+    side_of(pr, axis, R);
+    const double ar = fmax(L.ap, R.ap);
+    const double al = fmin(L.am, R.am);
+    const double ifan = 1.0 / (ar - al);
     double u_hll[5], f_hll[5];
     for (int k = 0; k < 5; ++k)
     {
-        u_hll[k] = rdiv(radd(rsub(rmul(ar, ur[k]), rmul(al, ul[k])), rsub(fl[k], fr[k])), rsub(ar, al));
-        f_hll[k] = hll_average(fl[k], fr[k], ul[k], ur[k], al, ar);
+        u_hll[k] = (ar * R.u[k] - al * L.u[k] + (L.f[k] - R.f[k])) * ifan;
+        f_hll[k] = (ar * L.f[k] - al * R.f[k] - (L.u[k] - R.u[k]) * ar * al) * ifan;
     }
-    const double n[3] = {double(axis == 0), double(axis == 1), double(axis == 2)};
-    const double ue_hll = radd(u_hll[4], u_hll[0]);
-    const double fe_hll = radd(f_hll[4], f_hll[0]);
-    const double um_hll = radd(radd(radd(0.0, rmul(u_hll[1], n[0])), rmul(u_hll[2], n[1])), rmul(u_hll[3], n[2]));
-    const double fm_hll = radd(radd(radd(0.0, rmul(f_hll[1], n[0])), rmul(f_hll[2], n[1])), rmul(f_hll[3], n[2]));
+    const double ue_hll = u_hll[4] + u_hll[0];
+    const double fe_hll = f_hll[4] + f_hll[0];
+    const double um_hll = u_hll[1 + axis];
+    const double fm_hll = f_hll[1 + axis];
     const double a = fe_hll;
-    const double b = rsub(-fm_hll, ue_hll);
+    const double b = -fm_hll - ue_hll;
     const double c = um_hll;
-    const double d = rsub(rmul(b, b), rmul(rmul(4.0, a), c));
-    const double as = d < 0.0 ? 0.0
-                    : (fabs(a) > 1e-8 ? rdiv(rsub(-b, rsqrt_rn(d)), rmul(2.0, a)) : rdiv(-c, b));
+    const double d = b * b - 4.0 * a * c;
+    const double as = d < 0.0 ? 0.0 : (fabs(a) > 1e-8 ? (-b - sqrt(d)) / (2.0 * a) : -c / b);
     if (isnan(as) || as < -1e3 || as > 1e3)
     {
         for (int k = 0; k < 5; ++k) F[k] = 0.0;
         if (contact) *contact = 0.0;
         return 1;
     }
-    const double ps = radd(rmul(-fe_hll, as), fm_hll);
-    auto star = [&](const double u[5], const double f[5], const SPrim<double>& p, double s, double face) {
-        const double v = normal_velocity(p, axis);
-        const double e = radd(u[4], u[0]);
-        const double m = radd(radd(radd(0.0, rmul(u[1], n[0])), rmul(u[2], n[1])), rmul(u[3], n[2]));
-        const double sv = rsub(s, v), sa = rsub(s, as);
-        const double es = rdiv(rsub(radd(rmul(e, sv), rmul(ps, as)), rmul(p.p, v)), sa);
-        const double ms = rdiv(rsub(radd(rmul(m, sv), ps), p.p), sa);
-        const double Ds = rdiv(rmul(u[0], sv), sa);
+    const double ps = -fe_hll * as + fm_hll;
+    auto star = [&](const Side& q, const SPrim<double>& p, double s, double face) {
+        const double v = q.vn;
+        const double e = q.u[4] + q.u[0];
+        const double m = q.u[1 + axis];
+        const double sv = s - v;
+        const double isa = 1.0 / (s - as);
+        const double es = (e * sv + ps * as - p.p * v) * isa;
+        const double ms = (m * sv + ps - p.p) * isa;
+        const double Ds = q.u[0] * sv * isa;
         double us[5];
         us[0] = Ds;
-        for (int k = 0; k < 3; ++k)
-        {
-            const double nk = rsub(u[1 + k], rmul(m, n[k]));
-            const double ns = rdiv(rmul(nk, sv), sa);
-            us[1 + k] = radd(rmul(ms, n[k]), ns);
-        }
-        us[4] = rsub(es, Ds);
-        for (int k = 0; k < 5; ++k) F[k] = rsub(radd(f[k], rmul(s, rsub(us[k], u[k]))), rmul(face, us[k]));
+        for (int k = 0; k < 3; ++k) us[1 + k] = k == axis ? ms : q.u[1 + k] * sv * isa;
+        us[4] = es - Ds;
+        for (int k = 0; k < 5; ++k) F[k] = q.f[k] + s * (us[k] - q.u[k]) - face * us[k];
     };
     if (mode == ACROSS)
     {
-        star(ul, fl, pl, al, as);
+        star(L, pl, al, as);
         if (contact) *contact = as;
         return 0;
     }
     if (mode == MOVING)
     {
-        if (w <= al) { for (int k = 0; k < 5; ++k) F[k] = rsub(fl[k], rmul(w, ul[k])); return 0; }
-        if (w >= ar) { for (int k = 0; k < 5; ++k) F[k] = rsub(fr[k], rmul(w, ur[k])); return 0; }
-        if (w <= as) star(ul, fl, pl, al, w);
-        else star(ur, fr, pr, ar, w);
+        if (w <= al) { for (int k = 0; k < 5; ++k) F[k] = L.f[k] - w * L.u[k]; return 0; }
+        if (w >= ar) { for (int k = 0; k < 5; ++k) F[k] = R.f[k] - w * R.u[k]; return 0; }
+        if (w <= as) star(L, pl, al, w);
+        else star(R, pr, ar, w);
         return 0;
     }
-    if (0.0 <= al) { for (int k = 0; k < 5; ++k) F[k] = fl[k]; return 0; }
-    if (0.0 >= ar) { for (int k = 0; k < 5; ++k) F[k] = fr[k]; return 0; }
-    if (0.0 <= as) star(ul, fl, pl, al, 0.0);
-    else star(ur, fr, pr, ar, 0.0);
+    if (0.0 <= al) { for (int k = 0; k < 5; ++k) F[k] = L.f[k]; return 0; }
+    if (0.0 >= ar) { for (int k = 0; k < 5; ++k) F[k] = R.f[k]; return 0; }
+    if (0.0 <= as) star(L, pl, al, 0.0);
+    else star(R, pr, ar, 0.0);
     return 0;
 }
 
@@ -256,7 +312,7 @@ __global__ void __launch_bounds__(256) prim_kernel(const Stage S)
         const int j = int(track_of(S.t.co, S.t.T, c));
         const int64_t i = c - S.t.co[j];
         const double* r = S.r + face_offset(S.t, j) + i;
-        const double dv = cell_volume(r[0], r[1], S.t.theta[2 * j], S.t.theta[2 * j + 1]);
+        const double dv = cell_volume_cos(r[0], r[1], S.tg[5 * j + TG_C0], S.tg[5 * j + TG_C1]);
         srhd::Zone z{S.u[c] / dv, S.u[C + c] / dv, S.u[2 * C + c] / dv, S.u[3 * C + c] / dv, S.u[4 * C + c] / dv};
         double prim[5] = {0, 0, 0, 0, 0};
         int it = 0;
@@ -410,16 +466,19 @@ __global__ void __launch_bounds__(256) polar_kernel(const Stage S)
                 const SPrim<double> p2 = sample(S, j + 1, rf, ir, none);
                 const SPrim<double> p0 = sample(S, j - 1, rf, il, p1);
                 const SPrim<double> p3 = sample(S, j + 2, rf, ir, p2);
+                const double i10 = 1.0 / (q1 - q0), i20 = 1.0 / (q2 - q0), i21 = 1.0 / (q2 - q1);
+                const double i31 = 1.0 / (q3 - q1), i32 = 1.0 / (q3 - q2);
                 for (int k = 0; k < 5; ++k)
                 {
-                    const double cl = plm_x(q0, q1, q2, comp(p0, k), comp(p1, k), comp(p2, k), 1.0);
-                    const double cr = plm_x(q1, q2, q3, comp(p1, k), comp(p2, k), comp(p3, k), 1.0);
+                    const double cl = plm_r(i10, i20, i21, comp(p0, k), comp(p1, k), comp(p2, k), 1.0);
+                    const double cr = plm_r(i21, i31, i32, comp(p1, k), comp(p2, k), comp(p3, k), 1.0);
                     set_comp(pl, k, comp(p1, k) + (ql - q1) * cl);
                     set_comp(pr, k, comp(p2, k) + (qr - q2) * cr);
                 }
             }
             count_failure(S, hllc_mode(pl, pr, 1, FIXED, 0.0, flux, nullptr));
-            da = face_area(trailing, leading, ql, qr);
+            da = face_area(trailing, leading, S.tg[5 * j + TG_S1], S.tg[5 * j + TG_C1], S.tg[5 * (j + 1) + TG_S0],
+                           S.tg[5 * (j + 1) + TG_C0]);
         }
         for (int k = 0; k < 5; ++k) S.pf[k * S.np_max + p] = flux[k];
         S.pf[5 * S.np_max + p] = da;
@@ -447,10 +506,11 @@ __global__ void __launch_bounds__(256) update_kernel(const Stage S)
         const int64_t n = S.t.co[j + 1] - S.t.co[j];
         const int64_t i = c - S.t.co[j];
         const int64_t f = face_offset(S.t, j) + i;
-        const double t0 = S.t.theta[2 * j], t1 = S.t.theta[2 * j + 1];
+        const double* g = S.tg + 5 * j;
         const double r0 = S.r[f], r1 = S.r[f + 1];
-        const double da0 = face_area(r0, r0, t0, t1), da1 = face_area(r1, r1, t0, t1);
-        const double dv = cell_volume(r0, r1, t0, t1);
+        const double da0 = face_area(r0, r0, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
+        const double da1 = face_area(r1, r1, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
+        const double dv = cell_volume_cos(r0, r1, g[TG_C0], g[TG_C1]);
         // polar fluxes binned on this cell, in face order (mesh::bin_values)
         double gl[5] = {0, 0, 0, 0, 0}, gr[5] = {0, 0, 0, 0, 0};
         if (j > 0)
@@ -482,13 +542,13 @@ __global__ void __launch_bounds__(256) update_kernel(const Stage S)
         // spherical_geometry_source_terms (physics_srhd.hpp:330-345)
         const SPrim<double> p = load_prim(S.P, C, c);
         const double rc = 0.5 * (r0 + r1);
-        const double qc = 0.5 * (t0 + t1);
-        const double cotq = tan(M_PI_2 - qc);
+        const double cotq = g[TG_COT];
         const double ur = p.u[0], uq = p.u[1], up = p.u[2], pg = p.p;
         const double H0 = srhd::enthalpy_density(p, kGamma);
-        const double src[5] = {0.0 / 1.0, (2.0 * pg + H0 * (uq * uq + up * up)) / rc,
-                               (cotq * pg + H0 * (up * up * cotq - ur * uq)) / rc, -up * H0 * (ur + uq * cotq) / rc,
-                               0.0 / 1.0};
+        const double irc = 1.0 / rc;
+        const double src[5] = {0.0, (2.0 * pg + H0 * (uq * uq + up * up)) * irc,
+                               (cotq * pg + H0 * (up * up * cotq - ur * uq)) * irc, -up * H0 * (ur + uq * cotq) * irc,
+                               0.0};
         for (int k = 0; k < 5; ++k)
         {
             const double df = S.rf[k * F + f + 1] * da1 - S.rf[k * F + f] * da0;
@@ -709,6 +769,7 @@ struct Workspace
     int32_t* pir;
     double* r_stage[2];
     double* u_stage[2];
+    double* tg;
     int* failures;
     int64_t np_max;
 };
@@ -719,7 +780,8 @@ int64_t workspace_bytes(int T, int64_t C)
 {
     const int64_t F = C + T, NP = np_bound(T, C);
     auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
-    return 2 * al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) + 256 + 256;
+    return 2 * al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) +
+           al(5 * int64_t(T) * 8) + 256 + 256;
 }
 
 Workspace carve(void* base, int T, int64_t C)
@@ -736,12 +798,19 @@ Workspace carve(void* base, int T, int64_t C)
     w.pir = reinterpret_cast<int32_t*>(take(NP * 4));
     for (int s = 0; s < 2; ++s) w.r_stage[s] = reinterpret_cast<double*>(take(F * 8));
     for (int s = 0; s < 2; ++s) w.u_stage[s] = reinterpret_cast<double*>(take(5 * C * 8));
+    w.tg = reinterpret_cast<double*>(take(5 * int64_t(T) * 8));
     w.failures = reinterpret_cast<int*>(take(256));
     w.np_max = NP;
     return w;
 }
 
 inline int blocks_for(int64_t n) { return int(std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16))); }
+
+int launch_trig(const Tracks& t, double* tg, cudaStream_t s)
+{
+    trig_kernel<<<blocks_for(t.T), 256, 0, s>>>(t.T, t.theta, tg);
+    return launch_status("sedov trig_kernel");
+}
 
 int run_stage(Stage S, cudaStream_t s)
 {
@@ -808,7 +877,9 @@ int mara_sedov_stage(int32_t track_count, int64_t cells, const int64_t* cell_off
     S.pil = polar_index ? polar_index : w.pil;
     S.pir = polar_index ? polar_index + w.np_max : w.pir;
     S.np_max = w.np_max;
+    S.tg = w.tg;
     S.failures = failures;
+    if (int r = launch_trig(S.t, w.tg, s)) return r;
     return run_stage(S, s);
 }
 
@@ -833,7 +904,9 @@ int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_o
     base.pil = w.pil;
     base.pir = w.pir;
     base.np_max = w.np_max;
+    base.tg = w.tg;
     base.failures = failures;
+    if (int r = launch_trig(base.t, w.tg, s)) return r;
     auto stage = [&](int k, const double* rin, const double* uin, double* rout, double* uout, const double* rb,
                      const double* ub, double b, double b1) {
         Stage S = base;
