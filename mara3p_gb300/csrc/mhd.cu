@@ -48,9 +48,34 @@ struct Clock
     unsigned long long failures;  // zones with negative density or pressure
 };
 
+// Division by a divisor d fixed per launch, for numerators below 2^31
+// (Granlund and Montgomery's round-up multiplier): q = (u m) >> s with
+// s = 31 + ceil(log2 d) and m = ceil(2^s / d), exact because
+// m d - 2^s < d <= 2^(s - 31). A 32-bit division by a runtime divisor takes
+// some twenty integer instructions; this takes two.
+struct FastDiv
+{
+    uint64_t m;
+    uint32_t d;
+    int s;
+    __device__ uint32_t div(uint32_t u) const { return uint32_t((uint64_t(u) * m) >> s); }
+};
+
+inline FastDiv fast_div(uint32_t d)
+{
+    int l = 0;
+    while ((uint64_t(1) << l) < d) ++l;
+    FastDiv f;
+    f.d = d;
+    f.s = 31 + l;
+    f.m = ((uint64_t(1) << f.s) + d - 1) / d;
+    return f;
+}
+
 struct Args
 {
     int N;
+    FastDiv div_n, div_n1, div_nn, div_nn1;      // N, N + 1, N^2, N (N + 1)
     double gamma, dl, cfl, theta;
     const double* uc; int64_t ucs, uzs;          // input conserved, (component, cell) strides
     const double* bf[3];
@@ -85,6 +110,30 @@ __device__ inline int64_t fidx(int N, int axis, int i, int j, int k)
 }
 
 __device__ inline int64_t cidx(int N, int i, int j, int k) { return (int64_t(i) * N + j) * N + k; }
+
+// 32-bit forms for the stage kernels: N <= 1024 is checked on the host, so
+// every face array has fewer than 2^31 elements (component offsets stay 64-bit)
+__device__ inline uint32_t nb32(int N, int axis)
+{
+    return uint32_t(N + (axis == 0)) * uint32_t(N + (axis == 1)) * uint32_t(N + (axis == 2));
+}
+__device__ inline uint32_t fidx32(int N, int axis, int i, int j, int k)
+{
+    const uint32_t n1 = N + (axis == 1), n2 = N + (axis == 2);
+    return (uint32_t(i) * n1 + uint32_t(j)) * n2 + uint32_t(k);
+}
+__device__ inline uint32_t cidx32(int N, int i, int j, int k) { return (uint32_t(i) * N + uint32_t(j)) * N + uint32_t(k); }
+
+// (i, j, k) of element u of the cell array (axis -1) or the face array of axis
+__device__ inline void unflatten_fast(const Args& A, int axis, uint32_t u, int& i, int& j, int& k)
+{
+    const FastDiv& plane = axis < 1 ? A.div_nn : A.div_nn1;     // n1 n2: N^2 for cells and axis 0
+    const FastDiv& row = axis == 2 ? A.div_n1 : A.div_n;        // n2
+    const uint32_t a = plane.div(u), r = u - a * plane.d, b = row.div(r);
+    i = int(a);
+    j = int(b);
+    k = int(r - b * row.d);
+}
 
 // (i, j, k) of linear index t of an n0 x n1 x n2 array, in 32-bit arithmetic
 // (every array here has fewer than 2^31 elements: N <= 1024 is checked on the host)
@@ -224,16 +273,16 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
     for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < NN; c += int64_t(gridDim.x) * blockDim.x)
     {
         int i, j, k;
-        unflatten(c, N, N, i, j, k);
+        unflatten_fast(A, -1, uint32_t(c), i, j, k);
+        const uint32_t x0 = fidx32(N, 0, i, j, k), y0 = fidx32(N, 1, i, j, k), z0 = fidx32(N, 2, i, j, k);
+        const uint32_t x1 = x0 + uint32_t(N) * N, y1 = y0 + N, z1 = z0 + 1;
         if constexpr (sizeof(R) == sizeof(float))
         {
             // Mixed: the recovery in FP32 from the FP64 state (integer conversions,
             // one reciprocal); only the energy difference E - kinetic - magnetic
             // is taken in FP64.
-            const float b[3] = {
-                0.5f * (d2f(A.bf[0][fidx(N, 0, i, j, k)]) + d2f(A.bf[0][fidx(N, 0, i + 1, j, k)])),
-                0.5f * (d2f(A.bf[1][fidx(N, 1, i, j, k)]) + d2f(A.bf[1][fidx(N, 1, i, j + 1, k)])),
-                0.5f * (d2f(A.bf[2][fidx(N, 2, i, j, k)]) + d2f(A.bf[2][fidx(N, 2, i, j, k + 1)]))};
+            const float b[3] = {0.5f * (d2f(A.bf[0][x0]) + d2f(A.bf[0][x1])), 0.5f * (d2f(A.bf[1][y0]) + d2f(A.bf[1][y1])),
+                                0.5f * (d2f(A.bf[2][z0]) + d2f(A.bf[2][z1]))};
             const double energy = A.uc[4 * A.ucs + c * A.uzs];
             Prim<float> p;
             p.d = d2f(A.uc[c * A.uzs]);
@@ -266,9 +315,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
             mf = fmaxf(mf, fastest_speed(p, gm));
             continue;
         }
-        const double b1 = 0.5 * (A.bf[0][fidx(N, 0, i, j, k)] + A.bf[0][fidx(N, 0, i + 1, j, k)]);
-        const double b2 = 0.5 * (A.bf[1][fidx(N, 1, i, j, k)] + A.bf[1][fidx(N, 1, i, j + 1, k)]);
-        const double b3 = 0.5 * (A.bf[2][fidx(N, 2, i, j, k)] + A.bf[2][fidx(N, 2, i, j, k + 1)]);
+        const double b1 = 0.5 * (A.bf[0][x0] + A.bf[0][x1]);
+        const double b2 = 0.5 * (A.bf[1][y0] + A.bf[1][y1]);
+        const double b3 = 0.5 * (A.bf[2][z0] + A.bf[2][z1]);
         double u[5];
         for (int q = 0; q < 5; ++q) u[q] = A.uc[q * A.ucs + c * A.uzs];
         // recover_primitive (physics_mhd.hpp:290-303)
@@ -327,26 +376,28 @@ template<typename R, int AXIS>
 __global__ void face_kernel(const Args A)
 {
     const int N = A.N;
-    const int64_t NN = int64_t(N) * N * N;
-    const int64_t NF = nb(N, AXIS);
-    const int n1 = N + (AXIS == 1), n2 = N + (AXIS == 2);
+    const size_t NN = size_t(N) * N * N;
+    const uint32_t NF = nb32(N, AXIS);
     const R* P = static_cast<const R*>(A.P);
     R* F = static_cast<R*>(A.F[AXIS]);
     R* E = static_cast<R*>(A.E[AXIS]);
     const R gm = R(A.gamma), theta = R(A.theta);
-    const int di = AXIS == 0, dj = AXIS == 1, dk = AXIS == 2;
-    for (int64_t f = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; f < NF; f += int64_t(gridDim.x) * blockDim.x)
+    // the stencil's cells l-2 .. l+1 lie on the line along AXIS through the
+    // face: a base index (AXIS coordinate zero) plus the wrapped layer x stride
+    const uint32_t stride = AXIS == 0 ? uint32_t(N) * N : (AXIS == 1 ? uint32_t(N) : 1u);
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < NF; f += gridDim.x * blockDim.x)
     {
         int i, j, k;
-        unflatten(f, n1, n2, i, j, k);
-        const int64_t cm2 = cidx(N, wrap(i - 2 * di, N), wrap(j - 2 * dj, N), wrap(k - 2 * dk, N));
-        const int64_t cm1 = cidx(N, wrap(i - di, N), wrap(j - dj, N), wrap(k - dk, N));
-        const int64_t c0 = cidx(N, wrap(i, N), wrap(j, N), wrap(k, N));
-        const int64_t cp1 = cidx(N, wrap(i + di, N), wrap(j + dj, N), wrap(k + dk, N));
+        unflatten_fast(A, AXIS, f, i, j, k);
+        const int l = AXIS == 0 ? i : (AXIS == 1 ? j : k);
+        const uint32_t base = cidx32(N, AXIS == 0 ? 0 : i, AXIS == 1 ? 0 : j, AXIS == 2 ? 0 : k);
+        const uint32_t cm2 = base + uint32_t(wrap(l - 2, N)) * stride, cm1 = base + uint32_t(wrap(l - 1, N)) * stride;
+        const uint32_t c0 = base + uint32_t(wrap(l, N)) * stride, cp1 = base + uint32_t(wrap(l + 1, N)) * stride;
         R L[8], Rr[8];
         for (int q = 0; q < 8; ++q)
         {
-            const R a = P[q * NN + cm2], b = P[q * NN + cm1], cc = P[q * NN + c0], d = P[q * NN + cp1];
+            const R* Pq = P + q * NN;
+            const R a = Pq[cm2], b = Pq[cm1], cc = Pq[c0], d = Pq[cp1];
             L[q] = b + R(0.5) * plm(a, b, cc, theta);
             Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
         }
@@ -355,48 +406,55 @@ __global__ void face_kernel(const Args A)
         const R bl = R(A.bf[AXIS][f]);
         R fl[5], e[2];
         riemann_hlle<R, AXIS>(pl, pr, bl, gm, fl, e);
-        for (int q = 0; q < 5; ++q) F[q * NF + f] = fl[q];
-        E[0 * NF + f] = e[0];
-        E[1 * NF + f] = e[1];
+        for (int q = 0; q < 5; ++q) F[q * size_t(NF) + f] = fl[q];
+        E[f] = e[0];
+        E[size_t(NF) + f] = e[1];
     }
 }
 
 // E component `comp` on the faces of `axis`: layer index along `axis` taken
-// as is (0..N), transverse cell indices periodic; as a double. Face E arrays
-// hold the two transverse components in increasing axis order.
-template<typename R>
-__device__ inline double ef(const Args& A, int axis, int comp, int i, int j, int k)
+// as is (0..N), transverse cell indices periodic. Face E arrays hold the two
+// transverse components in increasing axis order; nbv[a] is the size of the
+// face array of axis a.
+template<typename T>
+__device__ inline T ef_raw(const Args& A, const uint32_t nbv[3], int axis, int comp, int i, int j, int k)
 {
     const int N = A.N;
     if (axis != 0) i = wrap(i, N);
     if (axis != 1) j = wrap(j, N);
     if (axis != 2) k = wrap(k, N);
-    const int slot = comp < axis ? comp : comp - 1;
-    return double(static_cast<const R*>(A.E[axis])[slot * nb(N, axis) + fidx(N, axis, i, j, k)]);
+    const size_t slot = comp < axis ? comp : comp - 1;
+    return static_cast<const T*>(A.E[axis])[slot * nbv[axis] + fidx32(N, axis, i, j, k)];
+}
+
+template<typename R>
+__device__ inline double ef(const Args& A, const uint32_t nbv[3], int axis, int comp, int i, int j, int k)
+{
+    return double(ef_raw<R>(A, nbv, axis, comp, i, j, k));
 }
 
 // edge_emf_from_face (scheme_mhd_v1.cpp:76-98); edge of axis a at (i, j, k)
 // starts at corner (i, j, k). Averages in the reference's order.
 template<typename R>
-__device__ inline double ee(const Args& A, int axis, int i, int j, int k)
+__device__ inline double ee(const Args& A, const uint32_t nbv[3], int axis, int i, int j, int k)
 {
     // explicit rounding: every face sharing the edge must see the same double
     auto avg = [](double x, double y) { return __dmul_rn(0.5, __dadd_rn(x, y)); };
     double a, b;
     if (axis == 0)
     {
-        a = avg(ef<R>(A, 1, 0, i, j, k - 1), ef<R>(A, 1, 0, i, j, k));
-        b = avg(ef<R>(A, 2, 0, i, j - 1, k), ef<R>(A, 2, 0, i, j, k));
+        a = avg(ef<R>(A, nbv, 1, 0, i, j, k - 1), ef<R>(A, nbv, 1, 0, i, j, k));
+        b = avg(ef<R>(A, nbv, 2, 0, i, j - 1, k), ef<R>(A, nbv, 2, 0, i, j, k));
     }
     else if (axis == 1)
     {
-        a = avg(ef<R>(A, 2, 1, i - 1, j, k), ef<R>(A, 2, 1, i, j, k));
-        b = avg(ef<R>(A, 0, 1, i, j, k - 1), ef<R>(A, 0, 1, i, j, k));
+        a = avg(ef<R>(A, nbv, 2, 1, i - 1, j, k), ef<R>(A, nbv, 2, 1, i, j, k));
+        b = avg(ef<R>(A, nbv, 0, 1, i, j, k - 1), ef<R>(A, nbv, 0, 1, i, j, k));
     }
     else
     {
-        a = avg(ef<R>(A, 0, 2, i, j - 1, k), ef<R>(A, 0, 2, i, j, k));
-        b = avg(ef<R>(A, 1, 2, i - 1, j, k), ef<R>(A, 1, 2, i, j, k));
+        a = avg(ef<R>(A, nbv, 0, 2, i, j - 1, k), ef<R>(A, nbv, 0, 2, i, j, k));
+        b = avg(ef<R>(A, nbv, 1, 2, i - 1, j, k), ef<R>(A, nbv, 1, 2, i, j, k));
     }
     return avg(a, b);
 }
@@ -405,16 +463,9 @@ __device__ inline double ee(const Args& A, int axis, int i, int j, int k)
 // explicitly (no contraction), so each edge EMF is one fixed function of the
 // four face values around it and every face that shares the edge sees the
 // same float; differences of floats are exact in FP64.
-__device__ inline float ee_f(const Args& A, int axis, int i, int j, int k)
+__device__ inline float ee_f(const Args& A, const uint32_t nbv[3], int axis, int i, int j, int k)
 {
-    auto e = [&](int ax, int comp, int a, int b, int c) {
-        const int N = A.N;
-        if (ax != 0) a = wrap(a, N);
-        if (ax != 1) b = wrap(b, N);
-        if (ax != 2) c = wrap(c, N);
-        const int slot = comp < ax ? comp : comp - 1;
-        return static_cast<const float*>(A.E[ax])[slot * nb(N, ax) + fidx(N, ax, a, b, c)];
-    };
+    auto e = [&](int ax, int comp, int a, int b, int c) { return ef_raw<float>(A, nbv, ax, comp, a, b, c); };
     auto avg = [](float x, float y) { return __fmul_rn(0.5f, __fadd_rn(x, y)); };
     float a, b;
     if (axis == 0)
@@ -488,7 +539,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) updat
     __syncthreads();
     const double dt_over_dl_d = s_dtdl;
     const float dt_over_dl = s_dtdl_f;
-    const int64_t nf0 = nb(N, 0), nf1 = nb(N, 1), nf2 = nb(N, 2);
+    const uint32_t nbv[3] = {nb32(N, 0), nb32(N, 1), nb32(N, 2)};
+    const int64_t nf0 = nbv[0], nf1 = nbv[1], nf2 = nbv[2];
     const int64_t total = NN + nf0 + nf1 + nf2;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x)
     {
@@ -496,29 +548,27 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) updat
         {
             const int64_t c = t;
             int i, j, k;
-        unflatten(c, N, N, i, j, k);
-            const R* F0 = static_cast<const R*>(A.F[0]);
-            const R* F1 = static_cast<const R*>(A.F[1]);
-            const R* F2 = static_cast<const R*>(A.F[2]);
-            const int64_t x0 = fidx(N, 0, i, j, k), x1 = fidx(N, 0, i + 1, j, k);
-            const int64_t y0 = fidx(N, 1, i, j, k), y1 = fidx(N, 1, i, j + 1, k);
-            const int64_t z0 = fidx(N, 2, i, j, k), z1 = fidx(N, 2, i, j, k + 1);
+            unflatten_fast(A, -1, uint32_t(c), i, j, k);
+            const uint32_t x0 = fidx32(N, 0, i, j, k), x1 = x0 + uint32_t(N) * N;
+            const uint32_t y0 = fidx32(N, 1, i, j, k), y1 = y0 + N;
+            const uint32_t z0 = fidx32(N, 2, i, j, k), z1 = z0 + 1;
             for (int q = 0; q < 5; ++q)
             {
+                const R* F0 = static_cast<const R*>(A.F[0]) + q * nf0;
+                const R* F1 = static_cast<const R*>(A.F[1]) + q * nf1;
+                const R* F2 = static_cast<const R*>(A.F[2]) + q * nf2;
                 double out;
                 if (sizeof(R) == sizeof(double))
                 {
                     const double u = A.uc[q * A.ucs + c * A.uzs];
-                    const double dc = (double(F0[q * nf0 + x1]) - double(F0[q * nf0 + x0]))
-                                    + (double(F1[q * nf1 + y1]) - double(F1[q * nf1 + y0]))
-                                    + (double(F2[q * nf2 + z1]) - double(F2[q * nf2 + z0]));
+                    const double dc = (double(F0[x1]) - double(F0[x0])) + (double(F1[y1]) - double(F1[y0]))
+                                    + (double(F2[z1]) - double(F2[z0]));
                     out = u - dc * dt / dl;
                 }
                 else
                 {
-                    const float dc = (float(F0[q * nf0 + x1]) - float(F0[q * nf0 + x0]))
-                                   + (float(F1[q * nf1 + y1]) - float(F1[q * nf1 + y0]))
-                                   + (float(F2[q * nf2 + z1]) - float(F2[q * nf2 + z0]));
+                    const float dc = (float(F0[x1]) - float(F0[x0])) + (float(F1[y1]) - float(F1[y0]))
+                                   + (float(F2[z1]) - float(F2[z0]));
                     const float du = __fmul_rn(dc, dt_over_dl);
                     if (MODE == MIX_INCREMENT)
                     {
@@ -541,19 +591,18 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) updat
         int64_t f = t - NN;
         int axis = 0;
         if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
-        const int n1 = N + (axis == 1), n2 = N + (axis == 2);
         int i, j, k;
-        unflatten(f, n1, n2, i, j, k);
+        unflatten_fast(A, axis, uint32_t(f), i, j, k);
         // solenoidal_difference (mesh_cartesian_3d.hpp:265-274)
         if constexpr (sizeof(R) == sizeof(float))
         {
             double cf;
             if (axis == 0)
-                cf = curl_f(ee_f(A, 2, i, j + 1, k), ee_f(A, 2, i, j, k), ee_f(A, 1, i, j, k + 1), ee_f(A, 1, i, j, k));
+                cf = curl_f(ee_f(A, nbv, 2, i, j + 1, k), ee_f(A, nbv, 2, i, j, k), ee_f(A, nbv, 1, i, j, k + 1), ee_f(A, nbv, 1, i, j, k));
             else if (axis == 1)
-                cf = curl_f(ee_f(A, 0, i, j, k + 1), ee_f(A, 0, i, j, k), ee_f(A, 2, i + 1, j, k), ee_f(A, 2, i, j, k));
+                cf = curl_f(ee_f(A, nbv, 0, i, j, k + 1), ee_f(A, nbv, 0, i, j, k), ee_f(A, nbv, 2, i + 1, j, k), ee_f(A, nbv, 2, i, j, k));
             else
-                cf = curl_f(ee_f(A, 1, i + 1, j, k), ee_f(A, 1, i, j, k), ee_f(A, 0, i, j + 1, k), ee_f(A, 0, i, j, k));
+                cf = curl_f(ee_f(A, nbv, 1, i + 1, j, k), ee_f(A, nbv, 1, i, j, k), ee_f(A, nbv, 0, i, j + 1, k), ee_f(A, nbv, 0, i, j, k));
             double out = fma(-cf, dt_over_dl_d, A.bf[axis][f]);
             if (A.bavg[axis]) out = half_exact(A.bavg[axis][f] + out);
             A.bf_out[axis][f] = out;
@@ -561,11 +610,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) updat
         }
         double cf;
         if (axis == 0)
-            cf = (ee<R>(A, 2, i, j + 1, k) - ee<R>(A, 2, i, j, k)) - (ee<R>(A, 1, i, j, k + 1) - ee<R>(A, 1, i, j, k));
+            cf = (ee<R>(A, nbv, 2, i, j + 1, k) - ee<R>(A, nbv, 2, i, j, k)) - (ee<R>(A, nbv, 1, i, j, k + 1) - ee<R>(A, nbv, 1, i, j, k));
         else if (axis == 1)
-            cf = (ee<R>(A, 0, i, j, k + 1) - ee<R>(A, 0, i, j, k)) - (ee<R>(A, 2, i + 1, j, k) - ee<R>(A, 2, i, j, k));
+            cf = (ee<R>(A, nbv, 0, i, j, k + 1) - ee<R>(A, nbv, 0, i, j, k)) - (ee<R>(A, nbv, 2, i + 1, j, k) - ee<R>(A, nbv, 2, i, j, k));
         else
-            cf = (ee<R>(A, 1, i + 1, j, k) - ee<R>(A, 1, i, j, k)) - (ee<R>(A, 0, i, j + 1, k) - ee<R>(A, 0, i, j, k));
+            cf = (ee<R>(A, nbv, 1, i + 1, j, k) - ee<R>(A, nbv, 1, i, j, k)) - (ee<R>(A, nbv, 0, i, j + 1, k) - ee<R>(A, nbv, 0, i, j, k));
         double out = A.bf[axis][f] - cf * dt / dl;
         if (A.bavg[axis]) out = A.bavg[axis][f] * 0.5 + out * (1 - 0.5);
         A.bf_out[axis][f] = out;
@@ -645,8 +694,8 @@ __global__ void init_faces_kernel(int N, const Mode* modes, int count, double a_
         int64_t f = t;
         int axis = 0;
         if (f >= nf0) { f -= nf0; axis = 1; if (f >= nf1) { f -= nf1; axis = 2; } }
-        const int n1 = N + (axis == 1), n2 = N + (axis == 2);
         int i, j, k;
+        const int n1 = N + (axis == 1), n2 = N + (axis == 2);
         unflatten(f, n1, n2, i, j, k);
         auto ae = [&] (int ax, int a, int b, int c) { return edge_a(modes, count, a_amp, N, ax, a, b, c); };
         if (axis == 0)
@@ -743,6 +792,10 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     Args A;
     std::memset(&A, 0, sizeof A);
     A.N = N;
+    A.div_n = fast_div(uint32_t(N));
+    A.div_n1 = fast_div(uint32_t(N + 1));
+    A.div_nn = fast_div(uint32_t(N) * uint32_t(N));
+    A.div_nn1 = fast_div(uint32_t(N) * uint32_t(N + 1));
     A.gamma = mp->gamma_law_index;
     A.dl = 1.0 / double(N);
     A.cfl = mp->cfl;
