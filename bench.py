@@ -319,7 +319,7 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         host_in = torch.empty((3, N, N), dtype=torch.float64, pin_memory=True)
-        host_out = torch.empty_like(host_in)
+        host_out = torch.empty((3, N, N), dtype=torch.float64, pin_memory=True)
         host_in.copy_(run.u.cpu())
         hws = torch.empty(lib.mara_minidisk_host_workspace_bytes(ctypes.byref(c), 2, prec), dtype=torch.uint8,
                           device="cuda")
@@ -397,6 +397,38 @@ def _line(args, world, value, unit, ms_per_step, dtype, config, roofline, extra=
     return line
 
 
+def host_loop(pairs_in, step, pairs_out, steps):
+    """End-to-end time per step through a public call: each step copies the
+    inputs from pinned host buffers to the device (pairs_in: (host, device)),
+    runs `step`, and copies the results back (pairs_out: (device, host)).
+    Returns (seconds per step, H2D bytes, D2H bytes per step)."""
+    import torch
+    for h, d in pairs_in:
+        d.copy_(h, non_blocking=True)
+    step()
+    for d, h in pairs_out:
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for h, d in pairs_in:
+            d.copy_(h, non_blocking=True)
+        step()
+        for d, h in pairs_out:
+            h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    el = (time.perf_counter() - t0) / steps
+    return (el, sum(h.numel() * h.element_size() for h, _ in pairs_in),
+            sum(h.numel() * h.element_size() for _, h in pairs_out))
+
+
+def pinned_like(t):
+    import torch
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h
+
+
 def run_mhd(args):
     """128^3 constrained-transport MHD (examples/mhd3d.cpp RK2), seeded
     velocity and vector-potential modes (k <= 4, rms v 0.5, beta 10)."""
@@ -443,12 +475,22 @@ def run_mhd(args):
                                   ("bx_faces", sm.bf[0], sf.bf[0]))}
         accuracy = {"steps": k, "rel_l1_vs_fp64": rel, "time_mixed": tm, "time_fp64": tf,
                     "dt": "CFL in each path (times differ by the FP32 wavespeed)", "max_div_b_mixed": dbm}
+    e2e = None
+    if not args.no_e2e:
+        st = run.state
+        dev = [st.uc] + list(st.bf)
+        hosts = [pinned_like(t) for t in dev]
+        el, bi, bo = host_loop(list(zip(hosts, dev)), lambda: run.advance(1), list(zip(dev, hosts)),
+                               max(2, min(args.steps, 10)))
+        e2e = {"value": cells * world / el, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bo, "call": "mhd.Run.advance (mara_mhd_advance), state and face fields "
+                                                 "copied in and out through pinned host buffers every step"}
     line = _line(args, world, value, "cell-updates/s", ms / args.steps,
                  "f32 compute, f64 state" if prec == mh.MIXED else "f64",
                  {"workload": "mhd-128", "cells": cells, "scheme": "PLM(1.5)+HLLE+CT, RK2, CFL 0.3",
                   "precision": args.precision, "l2": "state 126 MB + intermediates > L2, no flush"}, roof,
                  {"max_div_b": run.max_div_b(), "failures": c["failures"], "time": c["time"],
-                  "clocks": sampler.summary(), "gpu_launches": 13 * args.steps, "accuracy": accuracy})
+                  "clocks": sampler.summary(), "gpu_launches": 13 * args.steps, "accuracy": accuracy, "e2e": e2e})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -497,8 +539,34 @@ def run_srhd(args):
     achieved = 80.0 * n / (best["ms"] * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
             "kernel": "c2p_mlp_kernel (FP64-Newton bound; 80 B/zone algorithmic)", "peak_source": f"{kind} hbm_gbs"}
+    e2e = None
+    if not args.no_e2e:
+        hc = pinned_like(cons)
+        dc = torch.empty_like(cons)
+        out = {}
+
+        def step():
+            out["r"] = sr.recover_primitive(dc, mlp=net, refine32=2)
+
+        dc.copy_(hc)
+        step()
+        hp = torch.empty(out["r"].prim.shape, dtype=torch.float64, pin_memory=True)
+        bi = hc.numel() * 8
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        k = max(2, min(args.steps, 10))
+        for _ in range(k):
+            dc.copy_(hc, non_blocking=True)
+            step()
+            hp.copy_(out["r"].prim, non_blocking=True)
+        torch.cuda.synchronize()
+        el = (time.perf_counter() - t0) / k
+        e2e = {"value": n * world / el, "unit": "zones/s", "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": hp.numel() * 8,
+               "call": "srhd.recover_primitive with the learned guess, conserved in and primitives out through "
+                       "pinned host buffers"}
     line = _line(args, world, best["zones_per_s"] * world, "zones/s", best["ms"], "f64 (bf16 guess)",
-                 {"workload": "srhd-c2p-2^24", "zones": n, "gamma": 4.0 / 3.0}, roof, {"variants": results})
+                 {"workload": "srhd-c2p-2^24", "zones": n, "gamma": 4.0 / 3.0}, roof, {"variants": results, "e2e": e2e})
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -674,10 +742,20 @@ def run_tube(args):
     achieved = 160.0 * N * N / (best["ms_per_step"] * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "whole RK2 step (FP64 Newton recovery bound)", "peak_source": f"{kind} hbm_gbs"}
+    e2e = None
+    if not args.no_e2e:
+        tube = sr.ShockTube(N=N)
+        kw = dict(guess=sr.GUESS_MLP, mlp=net, refine32=2)
+        hu = pinned_like(tube.u)
+        el, bi, bo = host_loop([(hu, tube.u)], lambda: tube.advance(1, precision=prec, **kw), [(tube.u, hu)],
+                               max(2, min(args.steps, 10)))
+        e2e = {"value": N * N * world / el, "unit": "cell-updates/s", "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bo, "call": "srhd.ShockTube.advance with the learned guess, state copied in "
+                                                 "and out through pinned host buffers every step"}
     line = _line(args, world, best["cell_updates_per_s"] * world, "cell-updates/s", best["ms_per_step"],
                  "f32 compute, f64 state" if prec else "f64",
                  {"workload": "srhd-tube-1024", "cells": N * N, "scheme": "PLM(1.5)+HLLE, RK2, CFL 0.3",
-                  "precision": args.precision}, roof, {"variants": results})
+                  "precision": args.precision}, roof, {"variants": results, "e2e": e2e})
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -146,7 +146,9 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
  * (host) and writes the final time to *time_out. Device buffers come from
  * the caller's `workspace` of mara_minidisk_host_workspace_bytes. Synchronous
  * on `stream`. This is the reference-facing call: state in host memory, as
- * the reference's nd::shared_array holds it. */
+ * the reference's nd::shared_array holds it. With page-locked u_in and u_out
+ * and mixed RK2, the kernels read u_in and write u_out over the host link
+ * themselves (the same bits as the copies); u_out may alias u_in. */
 int64_t mara_minidisk_host_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision);
 int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_in, double* u_out, double time,
                                int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,

@@ -579,7 +579,10 @@ __global__ void initial_kernel(int N, int n, int level, double R, double rs2, do
 // to the speed key of the fastest cell (as the stage kernels do), then that
 // cell's FP64 wavespeed (key_to_wavespeed_kernel). An FP64 reduction over
 // every cell costs FP64 divisions per cell, which GB300 runs slowly.
-__global__ void wavespeed_key_kernel(int N, FloatConsts F, const double* u, unsigned long long* key_out)
+// With u_copy set, the kernel also copies u into it: the host-buffer call
+// reads the caller's pinned state over the host link once, here.
+__global__ void wavespeed_key_kernel(int N, FloatConsts F, const double* u, unsigned long long* key_out,
+                                     double* u_copy)
 {
     __shared__ unsigned long long wk[NT / 32];
     const size_t NN = size_t(N) * N;
@@ -589,7 +592,14 @@ __global__ void wavespeed_key_kernel(int N, FloatConsts F, const double* u, unsi
         const int i = int(c / N), j = int(c % N);
         const float x = fmaf(float(i) + 0.5f, F.dl, -F.R), y = fmaf(float(j) + 0.5f, F.dl, -F.R);
         const float spot = sqrt_fast(rsqrt_fast(fmaf(x, x, y * y) + F.rs2));
-        key = key_max(key, speed_key(wavespeed_f(F, d2f(u[c]), d2f(u[NN + c]), d2f(u[2 * NN + c]), spot), c));
+        const double s = u[c], m1 = u[NN + c], m2 = u[2 * NN + c];
+        if (u_copy)
+        {
+            u_copy[c] = s;
+            u_copy[NN + c] = m1;
+            u_copy[2 * NN + c] = m2;
+        }
+        key = key_max(key, speed_key(wavespeed_f(F, d2f(s), d2f(m1), d2f(m2), spot), c));
     }
     for (int o = 16; o > 0; o >>= 1) key = key_max(key, __shfl_xor_sync(0xffffffffu, key, o));
     if ((threadIdx.x & 31) == 0) wk[threadIdx.x >> 5] = key;
@@ -952,8 +962,10 @@ int64_t mara_minidisk_workspace_bytes(const mara_minidisk_params* sd, int32_t rk
 namespace mara {
 namespace md {
 
+// u_copy (mixed precision only): also copy u there, and take the fastest
+// cell's FP64 wavespeed from the copy.
 int clock_init(const mara_minidisk_params* sd, const double* u, double time, mara_minidisk_clock* clock,
-               int precision, cudaStream_t s)
+               int precision, cudaStream_t s, double* u_copy)
 {
     mara_minidisk_clock c;
     std::memset(&c, 0, sizeof c);
@@ -968,9 +980,9 @@ int clock_init(const mara_minidisk_params* sd, const double* u, double time, mar
     if (precision == MARA_MIXED)
     {
         // the CFL dt stays an FP64 quantity: the fastest cell's FP64 wavespeed
-        wavespeed_key_kernel<<<blocks, NT, 0, s>>>(N, base_args(sd).f, u, amax);
+        wavespeed_key_kernel<<<blocks, NT, 0, s>>>(N, base_args(sd).f, u, amax, u_copy);
         if (int r = launch_status("wavespeed_key_kernel")) return r;
-        key_to_wavespeed_kernel<<<1, 32, 0, s>>>(clock, clock_args(sd, MARA_DT_CFL, 2, 0, 0), u);
+        key_to_wavespeed_kernel<<<1, 32, 0, s>>>(clock, clock_args(sd, MARA_DT_CFL, 2, 0, 0), u_copy ? u_copy : u);
         return launch_status("key_to_wavespeed_kernel");
     }
     wavespeed_kernel<<<blocks, NT, 0, s>>>(N, sd->block_size, sd->depth, sd->domain_radius,
@@ -1001,6 +1013,21 @@ int mara_minidisk_advance(const mara_minidisk_params* sd, double* u, mara_minidi
 int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock,
                                int32_t steps, int32_t rk_order, int32_t precision, int32_t dt_mode,
                                void* workspace, mara_minidisk_diagnostics* diag, void* stream)
+{
+    return advance_impl(sd, u, clock, steps, rk_order, precision, dt_mode, workspace, diag, stream, nullptr);
+}
+
+} // extern "C"
+
+namespace mara {
+namespace md {
+
+// The advance loop. final_out (mixed RK2 only): the last step's second stage
+// writes the new state there instead of u, which is then left at the state
+// before that step; the host-buffer call passes the caller's pinned output.
+int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock, int32_t steps,
+                 int32_t rk_order, int32_t precision, int32_t dt_mode, void* workspace,
+                 mara_minidisk_diagnostics* diag, void* stream, double* final_out)
 {
     if (int r = check_params(sd)) return r;
     MARA_REQUIRE(u && clock && workspace, "mara_minidisk_advance: null buffer");
@@ -1048,11 +1075,14 @@ int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_m
         {
             Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1; a1.diag = rate0;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
-            Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = alt; a2.amax = amax;
+            const bool last_out = final_out && step + 1 == steps;
+            Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = last_out ? final_out : alt;
+            a2.amax = amax;
             a2.amax_key = 1;
             a2.diag = rate1;
             if (int r = grid_stage(a2, K_MIX2, s)) return r;
-            std::swap(cur, alt);
+            if (last_out) cur = final_out;
+            else std::swap(cur, alt);
         }
         else
         {
@@ -1065,10 +1095,28 @@ int mara_minidisk_advance_diag(const mara_minidisk_params* sd, double* u, mara_m
         const double* key_state = precision == MARA_MIXED && amax ? cur : nullptr;
         if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag, key_state)) return r;
     }
-    if (cur != u)
+    if (cur != u && cur != final_out)
         MARA_CUDA(cudaMemcpyAsync(u, cur, 3 * NN * sizeof(double), cudaMemcpyDeviceToDevice, s));
     return MARA_OK;
 }
+
+// The device address of a pinned (page-locked or registered) host buffer, or
+// null for any other memory.
+const void* pinned_device_address(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+} // namespace md
+} // namespace mara
+
+extern "C" {
 
 int64_t mara_minidisk_host_workspace_bytes(const mara_minidisk_params* sd, int32_t rk_order, int32_t precision)
 {
@@ -1091,10 +1139,26 @@ int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_i
     double* u = reinterpret_cast<double*>(base);
     auto* clock = reinterpret_cast<mara_minidisk_clock*>(base + bytes);
     void* ws = base + bytes + 256;
-    MARA_CUDA(cudaMemcpyAsync(u, u_in, bytes, cudaMemcpyHostToDevice, s));
-    if (int r = clock_init(sd, u, time, clock, precision, s)) return r;
-    if (int r = mara_minidisk_advance(sd, u, clock, steps, rk_order, precision, dt_mode, ws, stream)) return r;
-    MARA_CUDA(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToHost, s));
+    // Mixed RK2 with pinned host buffers: the clock init reads the caller's
+    // state over the host link while copying it to the device, and the last
+    // stage writes the result straight into the caller's output, so each
+    // transfer overlaps a kernel instead of following it.
+    const double* in_dev = precision == MARA_MIXED && rk_order == 2 && steps > 0
+                         ? static_cast<const double*>(pinned_device_address(u_in)) : nullptr;
+    double* out_dev = in_dev ? static_cast<double*>(const_cast<void*>(pinned_device_address(u_out))) : nullptr;
+    if (in_dev && out_dev)
+    {
+        if (int r = clock_init(sd, in_dev, time, clock, precision, s, u)) return r;
+        if (int r = advance_impl(sd, u, clock, steps, rk_order, precision, dt_mode, ws, nullptr, stream, out_dev))
+            return r;
+    }
+    else
+    {
+        MARA_CUDA(cudaMemcpyAsync(u, u_in, bytes, cudaMemcpyHostToDevice, s));
+        if (int r = clock_init(sd, u, time, clock, precision, s)) return r;
+        if (int r = mara_minidisk_advance(sd, u, clock, steps, rk_order, precision, dt_mode, ws, stream)) return r;
+        MARA_CUDA(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToHost, s));
+    }
     mara_minidisk_clock c;
     MARA_CUDA(cudaMemcpyAsync(&c, clock, sizeof c, cudaMemcpyDeviceToHost, s));
     MARA_CUDA(cudaStreamSynchronize(s));

@@ -1055,7 +1055,10 @@ Args base_args(const mara_minidisk_params* sd);
 ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, int end_step, int begin_step);
 int grid_stage(Args A, int kind, cudaStream_t s);
 int clock_init(const mara_minidisk_params* sd, const double* u, double time, mara_minidisk_clock* clock,
-               int precision, cudaStream_t s);
+               int precision, cudaStream_t s, double* u_copy = nullptr);
+int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock* clock, int32_t steps,
+                 int32_t rk_order, int32_t precision, int32_t dt_mode, void* workspace,
+                 mara_minidisk_diagnostics* diag, void* stream, double* final_out);
 
 } // namespace md
 } // namespace mara

@@ -224,6 +224,42 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
     assert lib.mara_minidisk_sweep_columns(3) == -1
 
 
+@pytest.mark.parametrize("dt_mode_name", ["DT_CFL", "DT_FORMULA"])
+@pytest.mark.parametrize("steps", [1, 3])
+def test_host_call_pinned_matches_pageable(md, dt_mode_name, steps):
+    """mara_minidisk_advance_host with pinned host buffers (mixed RK2: the
+    clock init reads the caller's state over the host link while copying it,
+    and the last stage writes into the caller's output) gives the same bits
+    and time as with pageable buffers (plain copies); the input is left
+    alone, and an output that aliases the input works. FP64 takes the copy
+    path in both cases."""
+    from mara3p_gb300._capi import check, lib
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=64, depth=2, plm_theta=1.5))
+    c = sd.to_c()
+    N = sd.cells_per_side
+    u0 = md.initial_conserved(sd, seed=3, amplitude=0.01).cpu()
+    dt_mode = getattr(md, dt_mode_name)
+    stream = torch.cuda.current_stream().cuda_stream
+    for prec in (md.MIXED, md.FP64):
+        ws = torch.empty(lib.mara_minidisk_host_workspace_bytes(ctypes.byref(c), 2, prec), dtype=torch.uint8,
+                         device="cuda")
+        outs = []
+        for pinned, alias in ((False, False), (True, False), (True, True)):
+            hin = torch.empty((3, N, N), dtype=torch.float64, pin_memory=pinned)
+            hin.copy_(u0)
+            hout = hin if alias else torch.full((3, N, N), float("nan"), dtype=torch.float64, pin_memory=pinned)
+            t = ctypes.c_double()
+            check(lib.mara_minidisk_advance_host(ctypes.byref(c), hin.data_ptr(), hout.data_ptr(), 0.5, steps, 2,
+                                                 prec, dt_mode, ctypes.byref(t), ws.data_ptr(), stream))
+            if not alias:
+                assert torch.equal(hin, u0)
+            outs.append((hout.clone(), t.value))
+        assert torch.isfinite(outs[0][0]).all() and outs[0][1] > 0.5
+        for u, t in outs[1:]:
+            assert torch.equal(u, outs[0][0]), (prec, steps, dt_mode_name)
+            assert t == outs[0][1]
+
+
 @pytest.mark.parametrize("block_size,depth", [(64, 2), (100, 1), (80, 3)])
 def test_sweep_launch_shapes_bit_identical(md, block_size, depth):
     """Every launch shape of the single-mesh sweep (warps per block, waves of
