@@ -490,7 +490,7 @@ def run_mhd(args):
                  {"workload": "mhd-128", "cells": cells, "scheme": "PLM(1.5)+HLLE+CT, RK2, CFL 0.3",
                   "precision": args.precision, "l2": "state 126 MB + intermediates > L2, no flush"}, roof,
                  {"max_div_b": run.max_div_b(), "failures": c["failures"], "time": c["time"],
-                  "clocks": sampler.summary(), "gpu_launches": 13 * args.steps, "accuracy": accuracy, "e2e": e2e})
+                  "clocks": sampler.summary(), "gpu_launches": 15 * args.steps, "accuracy": accuracy, "e2e": e2e})
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -12,7 +12,8 @@
 //                   two transverse E-field components on all N+1 layers of the
 //                   face array (layer N uses its own normal field bf[N], as the
 //                   reference's flux_arrays does; cells are periodic)
-//   update_kernel   u -= div(F) dt/dl; B.dA -= curl(E_edge) dt/dl, edge EMFs by
+//   update_kernel   (two launches: cells, then faces)
+//                   u -= div(F) dt/dl; B.dA -= curl(E_edge) dt/dl, edge EMFs by
 //                   the reference's face averaging (edge_emf_from_face);
 //                   optionally averaged with the RK partner state.
 // Layout: uc SoA [5][N][N][N] (any (component, cell) stride pair on input to
@@ -520,8 +521,14 @@ __device__ inline double half_exact(double x)
     return e >= 2u && e <= 0x7FEu ? __longlong_as_double(b - (1LL << 52)) : x;
 }
 
-template<typename R, int MODE>
-__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) update_kernel(const Args A)
+// PART 0: the cells (MODE applies); PART 1: the three face arrays (FP64 in
+// every mode). Two launches, so that each part gets its own register budget:
+// both wait on scattered reads, and the face part at 32 registers runs eight
+// blocks per SM (the single kernel ran five; measured 0.704 -> 0.661 ms per
+// 128^3 step).
+template<typename R, int MODE, int PART>
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? (PART == 0 ? 5 : 8) : 4)
+update_kernel(const Args A)
 {
     const int N = A.N;
     const int64_t NN = int64_t(N) * N * N;
@@ -541,10 +548,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 4) updat
     const float dt_over_dl = s_dtdl_f;
     const uint32_t nbv[3] = {nb32(N, 0), nb32(N, 1), nb32(N, 2)};
     const int64_t nf0 = nbv[0], nf1 = nbv[1], nf2 = nbv[2];
-    const int64_t total = NN + nf0 + nf1 + nf2;
-    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total; t += int64_t(gridDim.x) * blockDim.x)
+    const int64_t begin = PART == 0 ? 0 : NN, end = PART == 0 ? NN : NN + nf0 + nf1 + nf2;
+    for (int64_t t = begin + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < end; t += int64_t(gridDim.x) * blockDim.x)
     {
-        if (t < NN)
+        if (PART == 0)
         {
             const int64_t c = t;
             int i, j, k;
@@ -831,15 +838,17 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     face_kernel<R, 1><<<blocks_for(nb(N, 1)), 256, 0, s>>>(A);
     face_kernel<R, 2><<<blocks_for(nb(N, 2)), 256, 0, s>>>(A);
     if (int r = launch_status("mhd face_kernel")) return r;
-    const int ub = blocks_for(NN + nb(N, 0) + nb(N, 1) + nb(N, 2));
+    const int ub = blocks_for(NN), fb = blocks_for(nb(N, 0) + nb(N, 1) + nb(N, 2));
     if constexpr (sizeof(R) == sizeof(float))
     {
-        if (mixed_mode == MIX_INCREMENT) update_kernel<R, MIX_INCREMENT><<<ub, 256, 0, s>>>(A);
-        else if (mixed_mode == MIX_FROM_INCREMENT) update_kernel<R, MIX_FROM_INCREMENT><<<ub, 256, 0, s>>>(A);
-        else update_kernel<R, MIX_PLAIN><<<ub, 256, 0, s>>>(A);
+        if (mixed_mode == MIX_INCREMENT) update_kernel<R, MIX_INCREMENT, 0><<<ub, 256, 0, s>>>(A);
+        else if (mixed_mode == MIX_FROM_INCREMENT) update_kernel<R, MIX_FROM_INCREMENT, 0><<<ub, 256, 0, s>>>(A);
+        else update_kernel<R, MIX_PLAIN, 0><<<ub, 256, 0, s>>>(A);
     }
-    else update_kernel<R, MIX_PLAIN><<<ub, 256, 0, s>>>(A);
-    return launch_status("mhd update_kernel");
+    else update_kernel<R, MIX_PLAIN, 0><<<ub, 256, 0, s>>>(A);
+    if (int r = launch_status("mhd update_kernel (cells)")) return r;
+    update_kernel<R, MIX_PLAIN, 1><<<fb, 256, 0, s>>>(A);
+    return launch_status("mhd update_kernel (faces)");
 }
 
 int run_stage(int precision, const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
