@@ -135,13 +135,19 @@ __global__ void trig_kernel(const int T, const double* theta, double* tg)
 // ir = 1/(xr - x0) taken once for all five components (FP64 division is the
 // slowest FP64 operation here; the products differ from the quotients by an
 // ulp).
+// The limiter itself runs on the integer pipes: the magnitudes of doubles
+// order as their bit patterns, and the result is the smallest magnitude with
+// the common sign, or zero where the signs differ (the reference's
+// 0.25 |sa + sb| (sa + sc) min(...) form, without six FP64 operations).
 __device__ inline double plm_r(double il, double ib, double ir, double yl, double y0, double yr, double theta)
 {
     const double a = (y0 - yl) * il * theta;
     const double b = (yr - yl) * ib;
     const double c = (yr - y0) * ir * theta;
-    const double sa = copysign(1.0, a), sb = copysign(1.0, b), sc = copysign(1.0, c);
-    return 0.25 * fabs(sa + sb) * (sa + sc) * fmin(fmin(fabs(a), fabs(b)), fabs(c));
+    const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b), bc = __double_as_longlong(c);
+    const long long mask = 0x7FFFFFFFFFFFFFFFLL;
+    const long long m = min(min(ba & mask, bb & mask), bc & mask);
+    return ((ba ^ bb) | (ba ^ bc)) < 0 ? 0.0 : __longlong_as_double(m | (ba & ~mask));
 }
 
 __device__ inline double comp(const SPrim<double>& p, int k) { return k == 0 ? p.rho : (k == 4 ? p.p : p.u[k - 1]); }
@@ -186,9 +192,10 @@ __device__ inline void radial_slope(const Stage& S, int j, int64_t i, int64_t n,
 
 // One side of a face: conserved state, flux and outer wavespeeds along axis
 // (conserved_density, flux, outer_wavespeeds: physics_srhd.hpp:182-195,
-// 291-324) from one Lorentz factor, one reciprocal of it and one of the
-// wavespeed denominator: four FP64 divisions and two square roots where the
-// term-by-term form takes nine and four.
+// 291-324) from one reciprocal square root for the Lorentz factor and its
+// inverse, and one reciprocal of the wavespeed denominator: three FP64
+// divisions and two square roots where the term-by-term form takes nine and
+// four.
 struct Side
 {
     double u[5], f[5];
@@ -200,8 +207,8 @@ __device__ inline void side_of(const SPrim<double>& p, int axis, Side& s)
     const double gm = kGamma;
     const double ch = 1.0 + 1.0 / (gm - 1.0);            // enthalpy_density's 1 + 1/(gamma - 1)
     const double uu = p.u[0] * p.u[0] + p.u[1] * p.u[1] + p.u[2] * p.u[2];
-    const double W = sqrt(1.0 + uu);
-    const double iW = 1.0 / W;
+    const double iW = rsqrt(1.0 + uu);                  // 1/W, and W = (1 + uu)/W
+    const double W = (1.0 + uu) * iW;
     const double vn = p.u[axis] * iW;
     const double e = p.rho + p.p * ch;                   // rho c^2 + p gamma / (gamma - 1)
     const double h = e / p.rho;
