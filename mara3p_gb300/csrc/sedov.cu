@@ -320,10 +320,16 @@ __global__ void __launch_bounds__(256) prim_kernel(const Stage S)
         const int64_t i = c - S.t.co[j];
         const double* r = S.r + face_offset(S.t, j) + i;
         const double dv = cell_volume_cos(r[0], r[1], S.tg[5 * j + TG_C0], S.tg[5 * j + TG_C1]);
-        srhd::Zone z{S.u[c] / dv, S.u[C + c] / dv, S.u[2 * C + c] / dv, S.u[3 * C + c] / dv, S.u[4 * C + c] / dv};
+        const double idv = 1.0 / dv;
+        srhd::Zone z{S.u[c] * idv, S.u[C + c] * idv, S.u[2 * C + c] * idv, S.u[3 * C + c] * idv,
+                     S.u[4 * C + c] * idv};
         double prim[5] = {0, 0, 0, 0, 0};
         int it = 0;
-        const int st = srhd::newton(z, kGamma, kFloor, 0.0, 50, prim, it);
+        // the reference's iteration from p = 0 with its stopping rule, its
+        // update as three reciprocals and an inverse square root; a zone it
+        // does not bring home takes the term-by-term iteration
+        int st = srhd::newton_fast(z, kGamma, kFloor, 0.0, 50, prim, it);
+        if (st != 0) st = srhd::newton(z, kGamma, kFloor, 0.0, 50, prim, it);
         if (st != 0)
             for (int k = 0; k < 5; ++k) prim[k] = 0.0;
         count_failure(S, st != 0);
@@ -400,17 +406,23 @@ __global__ void __launch_bounds__(256) radial_kernel(const Stage S)
     }
 }
 
+// Face radii are positive, so they order as their bit patterns: the merge
+// path and the samples compare them on the integer pipes, which leaves the
+// FP64 pipe (the bound of these kernels) to the arithmetic.
+__device__ inline long long rbits(double r) { return __double_as_longlong(r); }
+
 // sedov::sample (scheme_sedov2d.cpp:235-253) on track j (or the fallback)
 __device__ inline SPrim<double> sample(const Stage& S, int j, double r, int64_t index, const SPrim<double>& fallback)
 {
     const int64_t n = S.t.co[j + 1] - S.t.co[j];
     const double* rf = S.r + face_offset(S.t, j);
-    if (r <= rf[0] || r >= rf[n]) return fallback;
+    const long long rb = rbits(r);
+    if (rb <= rbits(rf[0]) || rb >= rbits(rf[n])) return fallback;
     index = min(index, n);
     // the walk of the reference from the hint; r lies strictly inside the
     // track, so it ends within [0, n - 1]; the bound only guards bad input
-    for (int64_t guard = 0; guard <= n && r < rf[index]; ++guard) --index;
-    for (int64_t guard = 0; guard <= n && r > rf[index + 1]; ++guard) ++index;
+    for (int64_t guard = 0; guard <= n && rb < rbits(rf[index]); ++guard) --index;
+    for (int64_t guard = 0; guard <= n && rb > rbits(rf[index + 1]); ++guard) ++index;
     index = max(int64_t(0), min(index, n - 1));
     const double rc = 0.5 * (rf[index] + rf[index + 1]);
     const int64_t c = S.t.co[j] + index;
@@ -445,11 +457,15 @@ __global__ void __launch_bounds__(256) polar_kernel(const Stage S)
         while (a < b)
         {
             const int64_t mid = (a + b) >> 1;
-            if (L[mid] <= R[d - mid - 1]) a = mid + 1; else b = mid;
+            if (rbits(L[mid]) <= rbits(R[d - mid - 1])) a = mid + 1; else b = mid;
         }
         const int64_t il = a - 1, ir = m - a;
-        const double trailing = fmax(il >= 0 ? L[il] : -INFINITY, ir >= 0 ? R[ir] : -INFINITY);
-        const double leading = fmin(a < nl ? L[a] : INFINITY, m + 1 - a < nr ? R[m + 1 - a] : INFINITY);
+        // the larger radius of the two trailing faces and the smaller of the
+        // two leading ones (a missing face is -inf / +inf), compared as bits
+        const double tl = il >= 0 ? L[il] : -INFINITY, tr = ir >= 0 ? R[ir] : -INFINITY;
+        const double ll = a < nl ? L[a] : INFINITY, lr = m + 1 - a < nr ? R[m + 1 - a] : INFINITY;
+        const double trailing = rbits(tl) >= rbits(tr) ? tl : tr;
+        const double leading = rbits(ll) <= rbits(lr) ? ll : lr;
         S.pil[p] = int32_t(il);
         S.pir[p] = int32_t(ir);
         const bool valid = il >= 0 && il + 1 < nl && ir >= 0 && ir + 1 < nr;
