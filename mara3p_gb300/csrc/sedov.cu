@@ -193,9 +193,9 @@ __device__ inline void radial_slope(const Stage& S, int j, int64_t i, int64_t n,
 // One side of a face: conserved state, flux and outer wavespeeds along axis
 // (conserved_density, flux, outer_wavespeeds: physics_srhd.hpp:182-195,
 // 291-324) from one reciprocal square root for the Lorentz factor and its
-// inverse, and one reciprocal of the wavespeed denominator: three FP64
-// divisions and two square roots where the term-by-term form takes nine and
-// four.
+// inverse, one reciprocal for the specific enthalpy and the sound speed, and
+// one of the wavespeed denominator: two FP64 divisions and two square roots
+// where the term-by-term form takes nine and four.
 struct Side
 {
     double u[5], f[5];
@@ -211,7 +211,8 @@ __device__ inline void side_of(const SPrim<double>& p, int axis, Side& s)
     const double W = (1.0 + uu) * iW;
     const double vn = p.u[axis] * iW;
     const double e = p.rho + p.p * ch;                   // rho c^2 + p gamma / (gamma - 1)
-    const double h = e / p.rho;
+    const double ire = 1.0 / (p.rho * e);                // h = e / rho and a2 = gamma p / e from one reciprocal
+    const double h = e * e * ire;
     const double D = p.rho * W;
     s.u[0] = D;
     for (int k = 0; k < 3; ++k) s.u[1 + k] = D * h * p.u[k];
@@ -219,7 +220,7 @@ __device__ inline void side_of(const SPrim<double>& p, int axis, Side& s)
     for (int k = 0; k < 5; ++k) s.f[k] = vn * s.u[k];
     s.f[1 + axis] += p.p;
     s.f[4] += p.p * vn;
-    const double a2 = gm * p.p / e;
+    const double a2 = gm * p.p * p.rho * ire;
     const double bb = uu * iW * iW;                      // uu / (1 + uu)
     const double disc = a2 * (1.0 - bb) * (1.0 - bb * a2 - vn * vn * (1.0 - a2));
     const double k0 = sqrt(disc);
