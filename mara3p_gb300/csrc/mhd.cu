@@ -5,7 +5,7 @@
 // examples/mhd3d.cpp:78-88,186-215.
 //
 // One stage = four kernels:
-//   prim_kernel     face_to_cell + recover_primitive of every cell into P[8][N^3];
+//   prim_kernel     face_to_cell + recover_primitive of every cell into P[N^3][8];
 //                   fastest wavespeed reduced into the clock (CFL dt)
 //   dt_kernel       dt = cfl * dl / max speed (scheme_mhd_v1.cpp:287)
 //   face_kernel<a>  PLM slopes along axis a, face states, HLLE flux F[5] and the
@@ -84,7 +84,7 @@ struct Args
     const double* bavg[3];
     double* uc_out;                              // SoA
     double* bf_out[3];
-    void* P;                                     // [8][N^3] (double or float)
+    void* P;                                     // [N^3][8] cell records (double or float)
     void* F[3];                                  // [5][face count of axis a]
     void* E[3];                                  // [2][face count]: the two transverse components
     Clock* clock;
@@ -149,6 +149,42 @@ __device__ inline void unflatten(int64_t t, int n1, int n2, int& i, int& j, int&
 
 template<typename R>
 struct Prim { R d, v[3], p, b[3]; };
+
+// The primitives of the stage kernels are one 8-value record per cell,
+// [N^3][8] (rho, v, p, B), written and read as 16-byte vectors: a face reads
+// its four stencil cells in 8 (FP32) or 16 (FP64) vector loads instead of 32
+// scalar ones.
+__device__ inline void store_cell(float* P, size_t c, const Prim<float>& p)
+{
+    float4* q = reinterpret_cast<float4*>(P + 8 * c);
+    q[0] = make_float4(p.d, p.v[0], p.v[1], p.v[2]);
+    q[1] = make_float4(p.p, p.b[0], p.b[1], p.b[2]);
+}
+__device__ inline void store_cell(double* P, size_t c, const Prim<double>& p)
+{
+    double2* q = reinterpret_cast<double2*>(P + 8 * c);
+    q[0] = make_double2(p.d, p.v[0]);
+    q[1] = make_double2(p.v[1], p.v[2]);
+    q[2] = make_double2(p.p, p.b[0]);
+    q[3] = make_double2(p.b[1], p.b[2]);
+}
+__device__ inline void load_cell(const float* P, size_t c, float out[8])
+{
+    const float4* q = reinterpret_cast<const float4*>(P + 8 * c);
+    const float4 a = q[0], b = q[1];
+    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+__device__ inline void load_cell(const double* P, size_t c, double out[8])
+{
+    const double2* q = reinterpret_cast<const double2*>(P + 8 * c);
+    for (int h = 0; h < 4; ++h)
+    {
+        const double2 v = q[h];
+        out[2 * h] = v.x;
+        out[2 * h + 1] = v.y;
+    }
+}
 
 // Division and square root: IEEE in FP64 (the reference's arithmetic), single
 // MUFU approximations in the mixed path's FP32 (relative error ~1e-7).
@@ -305,14 +341,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
             const float kin_mag = 0.5f * sum3(S, p.v) + 0.5f * sum3(b, b);
             p.p = d2f(energy - f2d(__fsub_rn(kin_mag, de))) * (gm - 1.0f);
             if (p.d < 0.0f || p.p < 0.0f) ++bad;
-            P[0 * NN + c] = p.d;
-            P[1 * NN + c] = p.v[0];
-            P[2 * NN + c] = p.v[1];
-            P[3 * NN + c] = p.v[2];
-            P[4 * NN + c] = p.p;
-            P[5 * NN + c] = p.b[0];
-            P[6 * NN + c] = p.b[1];
-            P[7 * NN + c] = p.b[2];
+            store_cell(P, c, p);
             mf = fmaxf(mf, fastest_speed(p, gm));
             continue;
         }
@@ -336,14 +365,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
         }
         p.p = R(pg);
         if (d < 0.0 || pg < 0.0) ++bad;
-        P[0 * NN + c] = p.d;
-        P[1 * NN + c] = p.v[0];
-        P[2 * NN + c] = p.v[1];
-        P[3 * NN + c] = p.v[2];
-        P[4 * NN + c] = p.p;
-        P[5 * NN + c] = p.b[0];
-        P[6 * NN + c] = p.b[1];
-        P[7 * NN + c] = p.b[2];
+        store_cell(P, c, p);
         m = fmax(m, double(fastest_speed(p, gm)));
     }
     if (sizeof(R) == sizeof(float)) m = double(mf);
@@ -394,11 +416,15 @@ __global__ void face_kernel(const Args A)
         const uint32_t base = cidx32(N, AXIS == 0 ? 0 : i, AXIS == 1 ? 0 : j, AXIS == 2 ? 0 : k);
         const uint32_t cm2 = base + uint32_t(wrap(l - 2, N)) * stride, cm1 = base + uint32_t(wrap(l - 1, N)) * stride;
         const uint32_t c0 = base + uint32_t(wrap(l, N)) * stride, cp1 = base + uint32_t(wrap(l + 1, N)) * stride;
+        R xa[8], xb[8], xc[8], xd[8];
+        load_cell(P, cm2, xa);
+        load_cell(P, cm1, xb);
+        load_cell(P, c0, xc);
+        load_cell(P, cp1, xd);
         R L[8], Rr[8];
         for (int q = 0; q < 8; ++q)
         {
-            const R* Pq = P + q * NN;
-            const R a = Pq[cm2], b = Pq[cm1], cc = Pq[c0], d = Pq[cp1];
+            const R a = xa[q], b = xb[q], cc = xc[q], d = xd[q];
             L[q] = b + R(0.5) * plm(a, b, cc, theta);
             Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
         }
@@ -765,7 +791,7 @@ Workspace carve(void* base, int N, int precision, bool rk2)
     const int64_t NF = nb(N, 0);   // every face array has (N+1) N^2 entries
     auto up = [] (char* q) { return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255)); };
     Workspace w{};
-    w.P = p; p = up(p + 8 * NN * r);
+    w.P = up(p); p = up(static_cast<char*>(w.P) + 8 * NN * r);     // 16-byte vector records need alignment
     for (int a = 0; a < 3; ++a) { w.F[a] = p; p = up(p + 5 * NF * r); }
     for (int a = 0; a < 3; ++a) { w.E[a] = p; p = up(p + 2 * NF * r); }
     if (rk2)
