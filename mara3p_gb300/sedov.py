@@ -95,7 +95,7 @@ class Tracks:
         if np.any(ncells < 2):
             raise ValueError("every track needs at least 2 cells")
         co = np.concatenate([[0], np.cumsum(ncells)]).astype(np.int64)
-        self.ncells = ncells
+        self._ncells = ncells
         self.co = torch.from_numpy(co).to(device)
         self.theta = torch.from_numpy(np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))).to(device)
         radii = np.asarray(radii, dtype=np.float64)
@@ -110,6 +110,15 @@ class Tracks:
             check(1, "mara_sedov_workspace_bytes")
         self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=device)
         self.failures = torch.zeros(1, dtype=torch.int32, device=device)
+
+    @property
+    def ncells(self) -> np.ndarray:
+        """Cells per track (host copy, read from the device offsets after a
+        remesh the first time it is asked for)."""
+        if self._ncells is None:
+            co = self.co.cpu().numpy()
+            self._ncells = co[1:] - co[:-1]
+        return self._ncells
 
     @property
     def polar_capacity(self) -> int:
@@ -177,7 +186,7 @@ class Tracks:
         self.co = co
         self.radii = radii[: self.cells + self.T]
         self.u = u[: 5 * self.cells].view(5, self.cells)
-        self.ncells = (co[1:] - co[:-1]).cpu().numpy()
+        self._ncells = None                      # read back from co on demand
         nbytes = lib.mara_sedov_workspace_bytes(self.T, self.cells)
         if self.workspace.numel() < nbytes:
             self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
