@@ -76,7 +76,7 @@ struct Stage
     int32_t* pil;           // [NPmax] merge counters
     int32_t* pir;
     int64_t np_max;
-    const double* tg;       // [T][5] track geometry (trig_kernel)
+    const double* tg;       // [T][TG_N] track geometry (trig_kernel)
     int* failures;
 };
 
@@ -112,21 +112,29 @@ __device__ inline double face_area(double r0, double r1, double s0, double c0, d
     return M_PI * (R0 + R1) * sqrt(dR * dR + dz * dz);
 }
 
-// Track geometry, the same for every cell of a track and every stage:
-// sin and cos of both polar bounds and the cotangent of the track centre,
-// [T][5] = {sin t0, cos t0, sin t1, cos t1, tan(pi/2 - (t0 + t1)/2)}.
-enum { TG_S0 = 0, TG_C0 = 1, TG_S1 = 2, TG_C1 = 3, TG_COT = 4 };
+// Track geometry, the same for every cell of a track and every stage,
+// [T][TG_N]: sin and cos of both polar bounds, the cotangent of the track
+// centre q_j = (t0 + t1)/2, q_j itself, and the reciprocal centre spacings
+// 1/(q_j - q_{j-1}) and 1/(q_{j+1} - q_{j-1}) of the theta PLM (zero where a
+// neighbour is missing).
+enum { TG_S0 = 0, TG_C0 = 1, TG_S1 = 2, TG_C1 = 3, TG_COT = 4, TG_QC = 5, TG_IPREV = 6, TG_ISPAN = 7, TG_N = 8 };
 
 __global__ void trig_kernel(const int T, const double* theta, double* tg)
 {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < T; j += gridDim.x * blockDim.x)
     {
         const double t0 = theta[2 * j], t1 = theta[2 * j + 1];
-        tg[5 * j + TG_S0] = sin(t0);
-        tg[5 * j + TG_C0] = cos(t0);
-        tg[5 * j + TG_S1] = sin(t1);
-        tg[5 * j + TG_C1] = cos(t1);
-        tg[5 * j + TG_COT] = tan(M_PI_2 - 0.5 * (t0 + t1));
+        double* g = tg + TG_N * j;
+        g[TG_S0] = sin(t0);
+        g[TG_C0] = cos(t0);
+        g[TG_S1] = sin(t1);
+        g[TG_C1] = cos(t1);
+        g[TG_COT] = tan(M_PI_2 - 0.5 * (t0 + t1));
+        auto qc = [&](int k) { return 0.5 * (theta[2 * k] + theta[2 * k + 1]); };
+        const double q = qc(j);
+        g[TG_QC] = q;
+        g[TG_IPREV] = j >= 1 ? 1.0 / (q - qc(j - 1)) : 0.0;
+        g[TG_ISPAN] = j >= 1 && j + 1 < T ? 1.0 / (qc(j + 1) - qc(j - 1)) : 0.0;
     }
 }
 
@@ -320,7 +328,7 @@ __global__ void __launch_bounds__(256) prim_kernel(const Stage S)
         const int j = int(track_of(S.t.co, S.t.T, c));
         const int64_t i = c - S.t.co[j];
         const double* r = S.r + face_offset(S.t, j) + i;
-        const double dv = cell_volume_cos(r[0], r[1], S.tg[5 * j + TG_C0], S.tg[5 * j + TG_C1]);
+        const double dv = cell_volume_cos(r[0], r[1], S.tg[TG_N * j + TG_C0], S.tg[TG_N * j + TG_C1]);
         const double idv = 1.0 / dv;
         srhd::Zone z{S.u[c] * idv, S.u[C + c] * idv, S.u[2 * C + c] * idv, S.u[3 * C + c] * idv,
                      S.u[4 * C + c] * idv};
@@ -484,14 +492,16 @@ __global__ void __launch_bounds__(256) polar_kernel(const Stage S)
             }
             else
             {
-                auto qc = [&](int k) { return 0.5 * (S.t.theta[2 * k] + S.t.theta[2 * k + 1]); };
-                const double q0 = qc(j - 1), q1 = qc(j), q2 = qc(j + 1), q3 = qc(j + 2);
+                // track centres and reciprocal spacings from the geometry table
+                const double* g1 = S.tg + TG_N * j;
+                const double* g2 = g1 + TG_N;
+                const double q1 = g1[TG_QC], q2 = g2[TG_QC];
                 const SPrim<double> p1 = sample(S, j, rf, il, none);
                 const SPrim<double> p2 = sample(S, j + 1, rf, ir, none);
                 const SPrim<double> p0 = sample(S, j - 1, rf, il, p1);
                 const SPrim<double> p3 = sample(S, j + 2, rf, ir, p2);
-                const double i10 = 1.0 / (q1 - q0), i20 = 1.0 / (q2 - q0), i21 = 1.0 / (q2 - q1);
-                const double i31 = 1.0 / (q3 - q1), i32 = 1.0 / (q3 - q2);
+                const double i10 = g1[TG_IPREV], i20 = g1[TG_ISPAN], i21 = g2[TG_IPREV];
+                const double i31 = g2[TG_ISPAN], i32 = g2[TG_N + TG_IPREV];
                 for (int k = 0; k < 5; ++k)
                 {
                     const double cl = plm_r(i10, i20, i21, comp(p0, k), comp(p1, k), comp(p2, k), 1.0);
@@ -501,8 +511,8 @@ __global__ void __launch_bounds__(256) polar_kernel(const Stage S)
                 }
             }
             count_failure(S, hllc_mode(pl, pr, 1, FIXED, 0.0, flux, nullptr));
-            da = face_area(trailing, leading, S.tg[5 * j + TG_S1], S.tg[5 * j + TG_C1], S.tg[5 * (j + 1) + TG_S0],
-                           S.tg[5 * (j + 1) + TG_C0]);
+            da = face_area(trailing, leading, S.tg[TG_N * j + TG_S1], S.tg[TG_N * j + TG_C1],
+                           S.tg[TG_N * (j + 1) + TG_S0], S.tg[TG_N * (j + 1) + TG_C0]);
         }
         for (int k = 0; k < 5; ++k) S.pf[k * S.np_max + p] = flux[k];
         S.pf[5 * S.np_max + p] = da;
@@ -530,7 +540,7 @@ __global__ void __launch_bounds__(256) update_kernel(const Stage S)
         const int64_t n = S.t.co[j + 1] - S.t.co[j];
         const int64_t i = c - S.t.co[j];
         const int64_t f = face_offset(S.t, j) + i;
-        const double* g = S.tg + 5 * j;
+        const double* g = S.tg + TG_N * j;
         const double r0 = S.r[f], r1 = S.r[f + 1];
         const double da0 = face_area(r0, r0, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
         const double da1 = face_area(r1, r1, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
@@ -805,7 +815,7 @@ int64_t workspace_bytes(int T, int64_t C)
     const int64_t F = C + T, NP = np_bound(T, C);
     auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
     return 2 * al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) +
-           al(5 * int64_t(T) * 8) + 256 + 256;
+           al(TG_N * int64_t(T) * 8) + 256 + 256;
 }
 
 Workspace carve(void* base, int T, int64_t C)
@@ -822,7 +832,7 @@ Workspace carve(void* base, int T, int64_t C)
     w.pir = reinterpret_cast<int32_t*>(take(NP * 4));
     for (int s = 0; s < 2; ++s) w.r_stage[s] = reinterpret_cast<double*>(take(F * 8));
     for (int s = 0; s < 2; ++s) w.u_stage[s] = reinterpret_cast<double*>(take(5 * C * 8));
-    w.tg = reinterpret_cast<double*>(take(5 * int64_t(T) * 8));
+    w.tg = reinterpret_cast<double*>(take(TG_N * int64_t(T) * 8));
     w.failures = reinterpret_cast<int*>(take(256));
     w.np_max = NP;
     return w;
