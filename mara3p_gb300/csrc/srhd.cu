@@ -49,17 +49,78 @@ __device__ inline void store(const C2PArgs& a, int64_t i, const double prim[5], 
     if (st != 0 && a.failures) atomicAdd(a.failures, 1ull);
 }
 
-__global__ void c2p_default_kernel(const C2PArgs a)
+__device__ inline Zone load_zone(const C2PArgs& a, int64_t i)
 {
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < a.n; i += int64_t(gridDim.x) * blockDim.x)
-    {
-        const double* c = a.cons + i * a.zs;
-        Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
+    const double* c = a.cons + i * a.zs;
+    return Zone{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
+}
+
+// The reference's recovery from p = 0 of every zone, bit for bit. Each
+// thread runs its zone's first kFirstDefault iterations (all but about one
+// zone in a hundred converge within them); a zone still iterating waits in a
+// per-CTA queue (zone, pressure, iteration count) and resumes later with
+// blockDim.x queued zones at a time, so the slow zones (up to the 51
+// iterations of the budget) finish in full warps instead of holding up warps
+// of converged zones. Resuming gives the same iterates.
+constexpr int kFirstDefault = 6;
+constexpr int kDefaultThreads = 256;
+
+__global__ void __launch_bounds__(kDefaultThreads) c2p_default_kernel(const C2PArgs a)
+{
+    __shared__ int64_t q_zone[2 * kDefaultThreads];
+    __shared__ double q_p[2 * kDefaultThreads];
+    __shared__ int q_it[2 * kDefaultThreads];
+    __shared__ int q_n;
+    if (threadIdx.x == 0) q_n = 0;
+    auto finish = [&](int64_t i, const Zone& z, double p, double W0, bool found, int it) {
         double prim[5] = {0, 0, 0, 0, 0};
-        int it = 0;
-        int st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it);
-        store(a, i, prim, it, st);
+        int iters = 0;
+        const int st = newton_finish(z, a.floor, p, W0, found, it, prim, iters);
+        store(a, i, prim, iters, st);
+    };
+    auto drain = [&](int from, int count) {
+        for (int t = threadIdx.x; t < count; t += blockDim.x)
+        {
+            const int e = from + t;
+            const int64_t i = q_zone[e];
+            const Zone z = load_zone(a, i);
+            double p = q_p[e], W0 = 1.0;
+            int it = q_it[e];
+            const bool found = newton_steps(z, a.gamma, p, it, 50, 51, W0);
+            finish(i, z, p, W0, found, it);
+        }
+    };
+    for (int64_t base = int64_t(blockIdx.x) * blockDim.x; base < a.n; base += int64_t(gridDim.x) * blockDim.x)
+    {
+        __syncthreads();
+        const int64_t i = base + threadIdx.x;
+        if (i < a.n)
+        {
+            const Zone z = load_zone(a, i);
+            double p = 0.0, W0 = 1.0;
+            int it = 0;
+            const bool found = newton_steps(z, a.gamma, p, it, 50, kFirstDefault, W0);
+            if (found || it > 50)
+                finish(i, z, p, W0, found, it);
+            else
+            {
+                const int e = atomicAdd(&q_n, 1);
+                q_zone[e] = i;
+                q_p[e] = p;
+                q_it[e] = it;
+            }
+        }
+        __syncthreads();
+        const int queued = q_n;
+        if (queued >= int(blockDim.x))
+        {
+            drain(queued - int(blockDim.x), int(blockDim.x));
+            __syncthreads();
+            if (threadIdx.x == 0) q_n = queued - int(blockDim.x);
+        }
     }
+    __syncthreads();
+    drain(0, q_n);
 }
 
 __device__ inline void polish(const C2PArgs& a, int64_t i, const Zone& z, double guess)
@@ -88,12 +149,53 @@ __global__ void c2p_refined_kernel(const C2PArgs a)
     }
 }
 
+// The end of a seeded polish: primitives from the converged iteration, or the
+// fall-back to the reference's start, budget and arithmetic.
+__device__ inline void finish_seeded(const C2PArgs& a, int64_t i, const Zone& z, double p, double W0, bool found,
+                                     int it)
+{
+    double prim[5] = {0, 0, 0, 0, 0};
+    int iters = 0, it2 = 0;
+    int st = newton_fast_finish(z, a.floor, p, W0, found, it, prim, iters);
+    if (st != 0)
+    {
+        st = newton(z, a.gamma, a.floor, 0.0, 50, prim, it2);
+        iters += it2;
+    }
+    store(a, i, prim, iters, st);
+}
+
 // Learned guess: the MLP predicts p for kZones zones per CTA (srhd_mlp.cuh),
-// then each thread polishes its zone.
+// then each thread polishes its zone for up to kFirstPolish iterations. A
+// zone still short of the stopping rule waits in a per-CTA queue (its zone,
+// pressure and iteration count) and resumes later with kThreads queued
+// zones at a time, so the few slow zones finish in full warps instead of
+// holding a warp of converged zones for the rest of their budget. Resuming
+// gives the same iterates, so the result does not depend on the queue.
+constexpr int kFirstPolish = 3;
+
 __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
 {
     __shared__ mlp::Shared sm;
+    __shared__ int64_t q_zone[2 * mlp::kZones];
+    __shared__ double q_p[2 * mlp::kZones];
+    __shared__ int q_it[2 * mlp::kZones];
+    __shared__ int q_n;
+    if (threadIdx.x == 0) q_n = 0;
     mlp::begin(*a.mlp, sm);
+    // resume queue entries [from, from + count) with one thread each
+    auto drain = [&](int from, int count) {
+        for (int t = threadIdx.x; t < count; t += blockDim.x)
+        {
+            const int e = from + t;
+            const int64_t i = q_zone[e];
+            const Zone z = load_zone(a, i);
+            double p = q_p[e], W0 = 1.0;
+            int it = q_it[e];
+            const bool found = newton_fast_steps(z, a.gamma, p, it, a.seeded_budget, a.seeded_budget + 1, W0);
+            finish_seeded(a, i, z, p, W0, found, it);
+        }
+    };
     uint32_t phase = 0;
     for (int64_t base = int64_t(blockIdx.x) * mlp::kZones; base < a.n; base += int64_t(gridDim.x) * mlp::kZones)
     {
@@ -116,11 +218,33 @@ __global__ void __launch_bounds__(mlp::kThreads) c2p_mlp_kernel(const C2PArgs a)
         {
             int64_t i = base + t;
             if (i >= a.n) continue;
-            const double* c = a.cons + i * a.zs;
-            Zone z{c[0], c[a.cs], c[2 * a.cs], c[3 * a.cs], c[4 * a.cs]};
-            polish(a, i, z, mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau));
+            const Zone z = load_zone(a, i);
+            double guess = mlp::pressure_from_output(sm.out[t], z.D, z.S1, z.S2, z.S3, z.tau);
+            if (a.refine32 > 0) guess = refine_fp32(z, a.gamma, guess, a.refine32);
+            double p = guess, W0 = 1.0;
+            int it = 0;
+            const bool found = newton_fast_steps(z, a.gamma, p, it, a.seeded_budget, kFirstPolish, W0);
+            if (found || it > a.seeded_budget)
+                finish_seeded(a, i, z, p, W0, found, it);
+            else
+            {
+                const int e = atomicAdd(&q_n, 1);
+                q_zone[e] = i;
+                q_p[e] = p;
+                q_it[e] = it;
+            }
+        }
+        __syncthreads();
+        const int queued = q_n;
+        if (queued >= int(blockDim.x))
+        {
+            drain(queued - int(blockDim.x), int(blockDim.x));
+            __syncthreads();
+            if (threadIdx.x == 0) q_n = queued - int(blockDim.x);
         }
     }
+    __syncthreads();
+    drain(0, q_n);
     mlp::end(sm);
 }
 
@@ -226,7 +350,7 @@ int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component
     {
         int blocks = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
         if (refine32 == 0)
-            srhd::c2p_default_kernel<<<blocks, 256, 0, s>>>(a);
+            srhd::c2p_default_kernel<<<blocks, srhd::kDefaultThreads, 0, s>>>(a);
         else
             srhd::c2p_refined_kernel<<<blocks, 256, 0, s>>>(a);
         return launch_status("c2p kernel");

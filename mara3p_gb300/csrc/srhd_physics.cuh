@@ -12,11 +12,17 @@ namespace srhd {
 
 struct Zone { double D, S1, S2, S3, tau; };
 
-// Newton on p from p_start (physics_srhd.hpp:231-285). Returns status
-// 0 ok / 1 not converged / 2 non-positive pressure; writes the primitive
-// (rho, u1, u2, u3, p) and the number of iterations run.
-__device__ inline int newton(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
-                             double prim[5], int& iterations)
+// Newton on p from p_start (physics_srhd.hpp:231-285), in resumable pieces:
+// newton_steps runs the reference's iterations from (p, iteration) while
+// iteration <= iter_max and iteration < stop, returning true (with W0) once
+// the stopping rule holds (|f| < 1e-12, or 1e-8 on the last allowed
+// iteration); resuming from the same (p, iteration) gives the same iterates
+// as one uninterrupted run. newton_finish applies the floor and forms the
+// primitives. newton is the whole recovery: status 0 ok / 1 not converged /
+// 2 non-positive pressure; it writes the primitive (rho, u1, u2, u3, p) and
+// the number of iterations run.
+__device__ inline bool newton_steps(const Zone& z, double gm, double& p, int& iteration, int iter_max, int stop,
+                                    double& W0)
 {
     const double c2 = 1.0;
     const double tol = 1e-12;
@@ -26,12 +32,7 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     const double Dc2 = D;   // D * c^2
     const double gm1 = __dadd_rn(gm, -1.0);
     const double b2max = 1.0 - 1e-10;
-    bool found = false;
-    int iteration = 0;
-    double W0 = 1.0;
-    double p = p_start;
-
-    while (iteration <= iter_max)
+    while (iteration <= iter_max && iteration < stop)
     {
         double Et = __dadd_rn(__dadd_rn(tau, p), Dc2);
         double b2 = fmin(__ddiv_rn(__ddiv_rn(SS, Et), Et), b2max);
@@ -50,11 +51,18 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
         if (fabs(f) < tol || (fabs(f) < tol * 1e4 && iteration == iter_max))
         {
             W0 = W;
-            found = true;
-            break;
+            return true;
         }
         ++iteration;
     }
+    return false;
+}
+
+__device__ inline int newton_finish(const Zone& z, double temperature_floor, double p, double W0, bool found,
+                                    int iteration, double prim[5], int& iterations)
+{
+    const double D = z.D, tau = z.tau;
+    const double Dc2 = D;
     iterations = found ? iteration + 1 : iteration;
     if (temperature_floor > 0.0)
         p = fmax(p, __dmul_rn(temperature_floor, D));
@@ -67,6 +75,15 @@ __device__ inline int newton(const Zone& z, double gm, double temperature_floor,
     prim[3] = __ddiv_rn(__dmul_rn(W0, z.S3), Et);
     prim[4] = p;
     return 0;
+}
+
+__device__ inline int newton(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
+                             double prim[5], int& iterations)
+{
+    int iteration = 0;
+    double W0 = 1.0, p = p_start;
+    const bool found = newton_steps(z, gm, p, iteration, iter_max, iter_max + 1, W0);
+    return newton_finish(z, temperature_floor, p, W0, found, iteration, prim, iterations);
 }
 
 // FP64 reciprocal and inverse square root for the seeded polish: an FP32
@@ -98,8 +115,14 @@ __device__ inline double rsqrt_nr(double x)
 // inverse square root per iteration instead of eight divisions and a square
 // root. The seeded paths use it; the reference's own start (newton) keeps the
 // reference's arithmetic bit for bit.
-__device__ inline int newton_fast(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
-                                  double prim[5], int& iterations)
+// newton_fast in resumable pieces. newton_fast_steps runs the iterations
+// from (p, iteration) while iteration <= iter_max and iteration < stop,
+// returning true (with W0) once the stopping rule holds; a caller may stop
+// early and resume later from the same (p, iteration), which gives the same
+// iterates as one uninterrupted run. newton_fast_finish applies the floor and
+// forms the primitives.
+__device__ inline bool newton_fast_steps(const Zone& z, double gm, double& p, int& iteration, int iter_max, int stop,
+                                         double& W0)
 {
     const double tol = 1e-12;
     const double D = z.D, tau = z.tau;
@@ -107,11 +130,7 @@ __device__ inline int newton_fast(const Zone& z, double gm, double temperature_f
     const double iD = rcp_nr(D);
     const double gm1 = gm - 1.0;
     const double b2max = 1.0 - 1e-10;
-    bool found = false;
-    int iteration = 0;
-    double W0 = 1.0;
-    double p = p_start;
-    while (iteration <= iter_max)
+    while (iteration <= iter_max && iteration < stop)
     {
         const double Et = (tau + p) + D;
         const double iE = rcp_nr(Et);
@@ -131,11 +150,17 @@ __device__ inline int newton_fast(const Zone& z, double gm, double temperature_f
         if (fabs(f) < tol || (fabs(f) < tol * 1e4 && iteration == iter_max))
         {
             W0 = W;
-            found = true;
-            break;
+            return true;
         }
         ++iteration;
     }
+    return false;
+}
+
+__device__ inline int newton_fast_finish(const Zone& z, double temperature_floor, double p, double W0, bool found,
+                                         int iteration, double prim[5], int& iterations)
+{
+    const double D = z.D, tau = z.tau;
     iterations = found ? iteration + 1 : iteration;
     if (temperature_floor > 0.0) p = fmax(p, temperature_floor * D);
     if (!found) return 1;
@@ -147,6 +172,15 @@ __device__ inline int newton_fast(const Zone& z, double gm, double temperature_f
     prim[3] = __ddiv_rn(__dmul_rn(W0, z.S3), Et);
     prim[4] = p;
     return 0;
+}
+
+__device__ inline int newton_fast(const Zone& z, double gm, double temperature_floor, double p_start, int iter_max,
+                                  double prim[5], int& iterations)
+{
+    int iteration = 0;
+    double W0 = 1.0, p = p_start;
+    const bool found = newton_fast_steps(z, gm, p, iteration, iter_max, iter_max + 1, W0);
+    return newton_fast_finish(z, temperature_floor, p, W0, found, iteration, prim, iterations);
 }
 
 // The same Newton update in FP32, used to sharpen a pressure guess cheaply
