@@ -104,6 +104,47 @@ def dist_info():
     return rank, world, local
 
 
+# Replicas only: under torchrun every rank advances its own seeded mesh (seed
+# base + rank) with no data exchange; the process group serves the barriers
+# around the timed region and the maximum of the ranks' times, and rank 0
+# prints the one line, whose value counts the units of all ranks.
+def init_replicas(world: int) -> None:
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def emit(line: dict, rank: int) -> bool:
+    """Print the JSON line on rank 0 only; returns whether it printed."""
+    if rank != 0:
+        return False
+    print(json.dumps(line), flush=True)
+    return True
+
+
+def finish_replicas(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -226,15 +267,13 @@ def run_reference(args):
 
 def run_ours(args):
     import torch
-    import torch.distributed as dist
 
     import mara3p_gb300.minidisk as md
     from mara3p_gb300._capi import check, lib
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
+    init_replicas(world)
     sd = md.SolverData(**WORKLOADS[args.workload])
     N = sd.cells_per_side
     cells = N * N
@@ -245,8 +284,7 @@ def run_ours(args):
 
     run.advance(args.warmup)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as sampler:
         torch.cuda.synchronize()
@@ -254,13 +292,8 @@ def run_ours(args):
         run.advance(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    barrier(world)
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     value = cells * args.steps * world / (ms * 1e-3)
     gpu_launches = 1 + 3 * args.steps     # clock begin + per step (stage 1, stage 2, clock)
 
@@ -332,16 +365,11 @@ def run_ours(args):
                                                  stream.cuda_stream))
         host_step()
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        barrier(world)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             host_step()
-        el = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([el], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(time.perf_counter() - t0, world)
         e2e = {"value": cells * e2e_steps * world / el, "unit": "cell-updates/s",
                "h2d_bytes_per_step": 3 * cells * 8, "d2h_bytes_per_step": 3 * cells * 8,
                "call": "mara_minidisk_advance_host (pinned host state in/out, 1 RK2 step per call)"}
@@ -384,9 +412,8 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
             "clocks": sampler.summary(), "accuracy": accuracy,
         }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+        emit(line, rank)
+    finish_replicas(world)
 
 
 def _line(args, world, value, unit, ms_per_step, dtype, config, roofline, extra=None):
@@ -581,15 +608,13 @@ def run_ensemble(args):
     import dataclasses
 
     import torch
-    import torch.distributed as dist
 
     import mara3p_gb300.ensemble as en
     import mara3p_gb300.minidisk as md
 
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
+    init_replicas(world)
     members = en.seeded_members(5 + rank, ENSEMBLE_MEMBERS, md.SolverData(**WORKLOADS[args.workload]))
     cells = sum(sd.cells_per_side ** 2 for sd in members)
     u0 = [md.initial_conserved(sd, seed=100 + m, amplitude=0.01) for m, sd in enumerate(members)]
@@ -605,19 +630,13 @@ def run_ensemble(args):
     def timed(fn, steps):
         fn(args.warmup)
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        barrier(world)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         fn(steps)
         b.record(stream)
         torch.cuda.synchronize()
-        ms = a.elapsed_time(b)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(a.elapsed_time(b), world)
 
     with ClockSampler(local) as sampler:
         ms = timed(e.advance, args.steps)
@@ -695,10 +714,8 @@ def run_ensemble(args):
                         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
                         "clocks": sampler.summary()})
     e.close()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    emit(line, rank)
+    finish_replicas(world)
 
 
 def run_tube(args):
