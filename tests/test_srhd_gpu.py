@@ -191,6 +191,39 @@ def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
     assert mean_seeded * 2.0 <= mean_base, (mean_base, mean_seeded)
 
 
+@pytest.mark.parametrize("n", [1, 127, 129, 1000, 40000])
+def test_slow_zone_queue_sizes_and_failures(sr, oracle, trained, n):
+    """The recovery kernels queue zones still iterating after their first
+    iterations and resume them in full warps. Batches that end inside a tile,
+    zones that fail (queued or not) and the AoS layout: the reference-start
+    recovery stays bit for bit the oracle's (primitives, iteration counts,
+    statuses), and the learned guess gives the same statuses and, for
+    converged zones, the same iterations as a batch of the same zones run
+    alone in a large batch (resuming gives the same iterates)."""
+    net, _, _, _ = trained
+    _, cons = seeded_zones(oracle, n, seed=500 + n)
+    cons = cons.reshape(-1, 5)
+    if n >= 3:
+        cons[n // 3] = [1.0, 0.0, 0.0, 0.0, -0.5]        # negative pressure: status 2
+        cons[-1] = [1e-3, 5.0, 0.0, 0.0, 1e-9]           # |S| far above tau + D
+    flat = np.ascontiguousarray(cons).ravel()
+    prim_o, it_o, st_o = oracle_recover(oracle, flat)
+    t = torch.from_numpy(cons.copy()).cuda()
+    r = sr.recover_primitive(t, GAMMA, layout="aos")
+    assert np.array_equal(r.status.cpu().numpy(), st_o)
+    assert np.array_equal(r.iterations.cpu().numpy(), it_o)
+    assert np.array_equal(r.prim.cpu().numpy().ravel(), prim_o)
+    # the learned guess: each zone's result does not depend on the batch it runs in
+    s1 = sr.recover_primitive(t, GAMMA, layout="aos", mlp=net, refine32=2)
+    big = torch.cat([t, torch.from_numpy(seeded_zones(oracle, 3000, seed=7)[1].reshape(-1, 5)).cuda()])
+    s2 = sr.recover_primitive(big, GAMMA, layout="aos", mlp=net, refine32=2)
+    assert np.array_equal(s1.status.cpu().numpy(), s2.status.cpu().numpy()[:n])
+    if n >= 3:
+        assert s1.status[n // 3].item() == 2 and st_o[n // 3] == 2
+    assert torch.equal(s1.iterations, s2.iterations[:n])
+    assert torch.equal(s1.prim, s2.prim[:n])
+
+
 def test_mlp_gain_over_no_network(sr, oracle, trained):
     """What the trained network adds: at the same FP32 refinement budget,
     starting from its guess needs fewer FP64 Newton iterations than starting
