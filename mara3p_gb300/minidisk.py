@@ -216,10 +216,37 @@ class Run:
         if diagnostics:
             self.diag = torch.zeros(ctypes.sizeof(MinidiskDiagnostics), dtype=torch.uint8, device=u.device)
 
-    def advance(self, steps: int) -> None:
+    def _advance_call(self, steps: int) -> None:
         check(lib.mara_minidisk_advance_diag(ctypes.byref(self.c), _ptr(self.u), self.clock.data_ptr(), steps,
                                              self.rk_order, self.precision, self.dt_mode,
                                              self.workspace.data_ptr(), _any_ptr(self.diag), _stream()), "advance")
+
+    def use_graph(self, steps_per_replay: int = 10) -> None:
+        """Replay `steps_per_replay` steps from one captured CUDA graph
+        (the reference driver's `fold` batch): small meshes, whose kernels
+        take less time than their launches, stop waiting on the host. The
+        same kernels run on the same buffers, so results do not change; a
+        held formula dt is re-chosen at the start of each replay, as at the
+        start of each advance call. Preparing the graph advances the run by
+        steps_per_replay steps: one direct call (which also loads the
+        kernels) before the capture, which itself runs nothing."""
+        if steps_per_replay < 1:
+            raise ValueError("steps_per_replay must be at least 1")
+        self._advance_call(steps_per_replay)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            self._advance_call(steps_per_replay)
+        self._graph, self._graph_steps = graph, steps_per_replay
+
+    def advance(self, steps: int) -> None:
+        graph = getattr(self, "_graph", None)
+        if graph is not None:
+            while steps >= self._graph_steps:
+                graph.replay()
+                steps -= self._graph_steps
+        if steps > 0:
+            self._advance_call(steps)
 
     def diagnostics(self) -> dict:
         """rate (per stage of the last step), integral and steps of the

@@ -224,6 +224,28 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
     assert lib.mara_minidisk_sweep_columns(3) == -1
 
 
+@pytest.mark.parametrize("precision", ["MIXED", "FP64"])
+@pytest.mark.parametrize("dt_mode_name", ["DT_CFL", "DT_FORMULA"])
+def test_graph_replay_matches_direct_advance(md, precision, dt_mode_name):
+    """Run.use_graph replays captured steps: the same bits, clock and time as
+    advancing directly (including a remainder shorter than one replay)."""
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=64, depth=1, plm_theta=1.5))
+    u0 = md.initial_conserved(sd, seed=21, amplitude=0.01)
+    kw = dict(rk_order=2, precision=getattr(md, precision), dt_mode=getattr(md, dt_mode_name))
+    direct = md.Run(sd, u0.clone(), **kw)
+    direct.advance(4 + 13)
+    replay = md.Run(sd, u0.clone(), **kw)
+    replay.use_graph(4)                 # advances 4 steps while preparing
+    replay.advance(13)                  # 3 replays + 1 direct step
+    torch.cuda.synchronize()
+    assert torch.isfinite(direct.u).all()
+    assert torch.equal(direct.u, replay.u)
+    a, b = direct.clock_state(), replay.clock_state()
+    assert (a.time, a.dt, a.iteration) == (b.time, b.dt, b.iteration)
+    with pytest.raises(ValueError):
+        replay.use_graph(0)
+
+
 @pytest.mark.parametrize("dt_mode_name", ["DT_CFL", "DT_FORMULA"])
 @pytest.mark.parametrize("steps", [1, 3])
 def test_host_call_pinned_matches_pageable(md, dt_mode_name, steps):
