@@ -26,16 +26,18 @@ __device__ inline float d2f(double x)
     return __uint_as_float(f | sign);
 }
 
+// f2d: the magnitude bits shifted into place with the exponent rebiased by
+// (1023 - 127) << 20, or by (2047 - 255) << 20 for infinities and NaN (whose
+// payload moves with them); zero and subnormals become signed zero. Equal,
+// for every one of the 2^32 inputs, to the field-by-field form it replaces.
 __device__ inline double f2d(float x)
 {
     const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xFFu;
-    const unsigned m = b & 0x7FFFFFu;
-    const unsigned ee = e == 255u ? 2047u : e + 896u;
-    unsigned hi = (b & 0x80000000u) | (ee << 20) | (m >> 3);
-    unsigned lo = m << 29;
-    hi = e == 0u ? (b & 0x80000000u) : hi;
-    lo = e == 0u ? 0u : lo;
+    const unsigned mag = b & 0x7FFFFFFFu, sign = b & 0x80000000u;
+    const unsigned bias = mag >= 0x7F800000u ? 0x70000000u : 0x38000000u;
+    const bool tiny = mag < 0x00800000u;
+    const unsigned hi = tiny ? sign : (((mag >> 3) + bias) | sign);
+    const unsigned lo = tiny ? 0u : (b << 29);
     return __hiloint2double(int(hi), int(lo));
 }
 
