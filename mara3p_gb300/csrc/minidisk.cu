@@ -400,8 +400,11 @@ __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A)
 int g_sweep_block_warps = 0, g_sweep_waves = 0;
 
 // Rows per warp: enough segments along x that all strips fill `waves` waves
-// of resident warps, but never fewer than 32 rows (16 when oversubscribed)
-// so the two halo rows stay a small overhead.
+// of resident warps, down to 2 rows (32 with a single wave). Only small and
+// medium meshes reach short segments; there filling the GPU with warps
+// matters more than the halo rows each segment recomputes (256^2: 1.34 G
+// cell-updates/s with 16-row segments, 1.75 G with 8, 2.11 G with 4, 2.23 G
+// with 2).
 template<int KIND, int COLS, bool DIAG>
 int launch_sweep(Args A, cudaStream_t s)
 {
@@ -424,7 +427,7 @@ int launch_sweep(Args A, cudaStream_t s)
     A.tiles_y = (A.N + cols - 1) / cols;
     const int capacity = blocks_per_sm[dev & 63][wpb] * wpb * sm_count[dev & 63];
     const int segments = std::max(1, waves * capacity / A.tiles_y);
-    A.sweep_rows = std::max(waves > 1 ? 16 : 32, (A.N + segments - 1) / segments);
+    A.sweep_rows = std::max(waves > 1 ? 2 : 32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
     const int warps = strips_x * A.tiles_y;
     sweep_kernel<KIND, COLS, DIAG><<<(warps + wpb - 1) / wpb, wpb * 32, smem, s>>>(A);
