@@ -84,6 +84,8 @@ def parse():
                     help="ensemble launch shape blocks_per_sm,chunks_per_warp,cols_per_lane,register_variant "
                          "(default: tuned)")
     ap.add_argument("--no-looped", action="store_true", help="ensemble: skip the looped single-mesh comparison")
+    ap.add_argument("--no-diagnostics-timing", action="store_true",
+                    help="minidisk: skip timing the step with the fused time-series sums")
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip); the "
                          "4096^2 configuration's own 2000 by default")
@@ -391,6 +393,24 @@ def run_ours(args):
     # relative L1 per component after S steps. (The reference's fixed-formula
     # dt lets this configuration develop negative densities after ~600 steps
     # in both precisions, so the CFL dt is used.)
+    # the time series (forces, torques, work, accretion and buffer rates)
+    # fused into the stage kernels: the same step with the sums on
+    diag_line = None
+    if prec == md.MIXED and not args.no_diagnostics_timing:
+        drun = md.Run(sd, u0.clone(), rk_order=2, precision=prec, dt_mode=md.DT_CFL, diagnostics=True)
+        drun.use_graph(GRAPH_STEPS)
+        torch.cuda.synchronize()
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        drun.advance(args.steps)
+        d1.record(stream)
+        torch.cuda.synchronize()
+        dms = d0.elapsed_time(d1) / args.steps
+        diag_line = {"ms_per_step": dms, "cell_updates_per_s": cells / (dms * 1e-3),
+                     "overhead": dms / (ms / args.steps) - 1.0,
+                     "what": "Run(diagnostics=True): 13 rate sums fused into both stage kernels, integrated by "
+                             "the clock kernel"}
+        del drun
     accuracy = None
     if prec == md.MIXED and args.accuracy_steps > 0:
         runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_CFL) for p in (md.FP64, md.MIXED)}
@@ -417,7 +437,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "l2": f"no flush: FP64 state {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
-            "clocks": sampler.summary(), "accuracy": accuracy,
+            "clocks": sampler.summary(), "accuracy": accuracy, "diagnostics": diag_line,
         }
         emit(line, rank)
     finish_replicas(world)
