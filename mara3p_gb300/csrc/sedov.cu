@@ -73,6 +73,7 @@ struct Stage
     double* G;              // [5][C] radial slopes
     double* rf;             // [6][F] radial flux and contact speed
     double* pf;             // [6][NPmax] polar flux and area
+    double* fa;             // [F] radial face areas (radial_kernel), shared by the two cells of each face
     int32_t* pil;           // [NPmax] merge counters
     int32_t* pir;
     int64_t np_max;
@@ -409,6 +410,10 @@ __global__ void __launch_bounds__(256) radial_kernel(const Stage S)
         count_failure(S, bad);
         for (int k = 0; k < 5; ++k) S.rf[k * F + f] = flux[k];
         S.rf[5 * F + f] = speed;
+        {
+            const double* g = S.tg + TG_N * j;
+            S.fa[f] = face_area(S.r[f], S.r[f], g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
+        }
         // delta_face_positions + the RK combination
         const double moved = S.r[f] + speed * S.dt;
         S.r_out[f] = S.r_base ? S.r_base[f] * S.b + moved * S.b1 : moved;
@@ -542,8 +547,7 @@ __global__ void __launch_bounds__(256) update_kernel(const Stage S)
         const int64_t f = face_offset(S.t, j) + i;
         const double* g = S.tg + TG_N * j;
         const double r0 = S.r[f], r1 = S.r[f + 1];
-        const double da0 = face_area(r0, r0, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
-        const double da1 = face_area(r1, r1, g[TG_S0], g[TG_C0], g[TG_S1], g[TG_C1]);
+        const double da0 = S.fa[f], da1 = S.fa[f + 1];    // face_area of both radial faces (radial_kernel)
         const double dv = cell_volume_cos(r0, r1, g[TG_C0], g[TG_C1]);
         // polar fluxes binned on this cell, in face order (mesh::bin_values)
         double gl[5] = {0, 0, 0, 0, 0}, gr[5] = {0, 0, 0, 0, 0};
@@ -804,6 +808,7 @@ struct Workspace
     double* r_stage[2];
     double* u_stage[2];
     double* tg;
+    double* fa;
     int* failures;
     int64_t np_max;
 };
@@ -815,7 +820,7 @@ int64_t workspace_bytes(int T, int64_t C)
     const int64_t F = C + T, NP = np_bound(T, C);
     auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
     return 2 * al(5 * C * 8) + al(6 * F * 8) + al(6 * NP * 8) + 2 * al(NP * 4) + 2 * al(F * 8) + 2 * al(5 * C * 8) +
-           al(TG_N * int64_t(T) * 8) + 256 + 256;
+           al(TG_N * int64_t(T) * 8) + al(F * 8) + 256 + 256;
 }
 
 Workspace carve(void* base, int T, int64_t C)
@@ -833,6 +838,7 @@ Workspace carve(void* base, int T, int64_t C)
     for (int s = 0; s < 2; ++s) w.r_stage[s] = reinterpret_cast<double*>(take(F * 8));
     for (int s = 0; s < 2; ++s) w.u_stage[s] = reinterpret_cast<double*>(take(5 * C * 8));
     w.tg = reinterpret_cast<double*>(take(TG_N * int64_t(T) * 8));
+    w.fa = reinterpret_cast<double*>(take(F * 8));
     w.failures = reinterpret_cast<int*>(take(256));
     w.np_max = NP;
     return w;
@@ -912,6 +918,7 @@ int mara_sedov_stage(int32_t track_count, int64_t cells, const int64_t* cell_off
     S.pir = polar_index ? polar_index + w.np_max : w.pir;
     S.np_max = w.np_max;
     S.tg = w.tg;
+    S.fa = w.fa;
     S.failures = failures;
     if (int r = launch_trig(S.t, w.tg, s)) return r;
     return run_stage(S, s);
@@ -939,6 +946,7 @@ int mara_sedov_advance(int32_t track_count, int64_t cells, const int64_t* cell_o
     base.pir = w.pir;
     base.np_max = w.np_max;
     base.tg = w.tg;
+    base.fa = w.fa;
     base.failures = failures;
     if (int r = launch_trig(base.t, w.tg, s)) return r;
     auto stage = [&](int k, const double* rin, const double* uin, double* rout, double* uout, const double* rb,
