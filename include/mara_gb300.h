@@ -188,7 +188,9 @@ int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clo
  *     that loads the library until the process exits;
  *   - the first call on a device looks up the array's device address with
  *     that device current (cudaGetSymbolAddress); make that first call before
- *     any stream capture;
+ *     any stream capture. The address is kept for the life of the process, so
+ *     do not call this entry point again after cudaDeviceReset (or any other
+ *     teardown of the device's primary context) in the same process;
  *   - all calls share the one array: calls whose GPU work overlaps (other
  *     streams, other threads) race and corrupt each other's results.
  *     Nothing in it needs to start at zero: every step writes its scratch

@@ -87,10 +87,13 @@ def build_driver(verbose: bool = False) -> Path:
 
 def build_oracle(reference: bool = False) -> None:
     """Compile oracle/ (test infrastructure) with make; reference=True also
-    builds oracle/_ref from the reference checkout when it is present."""
+    builds oracle/_ref from the reference checkout when one is present (the
+    Makefile's REF variable names where; the MARA_REF environment variable
+    overrides it)."""
     _run(["make", "-s", "-C", str(ROOT / "oracle")])
-    if reference and Path("/root/reference").is_dir():
-        _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"])
+    if reference:
+        ref = os.environ.get("MARA_REF")
+        _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref-if-present", *([f"REF={ref}"] if ref else [])])
 
 
 if __name__ == "__main__":

@@ -2,8 +2,10 @@
 // the FP64 binary orbit (used on the host and on the device).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include "mara_gb300.h"
 
@@ -31,6 +33,28 @@ inline int launch_status(const char* what)
 }
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+// One-time set-up per device (a kernel attribute, an occupancy query) that is
+// safe to reach from several host threads. Only a set-up that succeeded is
+// remembered: one that failed returns its status to its caller and runs again
+// on the next call. Devices are indexed modulo 64.
+struct PerDeviceOnce
+{
+    std::atomic<bool> done[64] = {};
+    std::mutex m;
+
+    template<typename F>
+    int run(int dev, F&& setup)
+    {
+        std::atomic<bool>& d = done[dev & 63];
+        if (d.load(std::memory_order_acquire)) return MARA_OK;
+        std::lock_guard<std::mutex> lock(m);
+        if (d.load(std::memory_order_relaxed)) return MARA_OK;
+        const int r = setup();
+        if (r == MARA_OK) d.store(true, std::memory_order_release);
+        return r;
+    }
+};
 
 // Binary state in the rotating frame at time t: the Kepler orbit of
 // src/physics_two_body.hpp:54-157 (a = 1, M = 1, G = 1) rotated by -omega_frame*t

@@ -408,24 +408,29 @@ int g_sweep_block_warps = 0, g_sweep_waves = 0;
 template<int KIND, int COLS, bool DIAG>
 int launch_sweep(Args A, cudaStream_t s)
 {
-    static int blocks_per_sm[64][9] = {};
-    static int sm_count[64] = {};
+    // resident blocks per SM and the SM count, per device and block size
+    // (block_warps is 1, 2 or 4), queried once
+    static PerDeviceOnce once[5];
+    static int blocks_per_sm[64][5] = {};
+    static int sm_count[64][5] = {};
     const int wpb = g_sweep_block_warps > 0 ? g_sweep_block_warps : SW_WARPS;
     const int waves = g_sweep_waves > 0 ? g_sweep_waves : 2;
     const size_t smem = COLS == 2 ? size_t(wpb) * RING_WARP_BYTES : 0;
     int dev = 0;
     MARA_CUDA(cudaGetDevice(&dev));
-    if (blocks_per_sm[dev & 63][wpb] == 0)
-    {
-        int b = 0, n = 0;
-        MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS, DIAG>, wpb * 32, smem));
-        MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-        sm_count[dev & 63] = n;
-        blocks_per_sm[dev & 63][wpb] = b > 0 ? b : 1;
-    }
+    if (int r = once[wpb].run(dev, [&]() -> int {
+            int b = 0, n = 0;
+            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sweep_kernel<KIND, COLS, DIAG>, wpb * 32,
+                                                                    smem));
+            MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+            sm_count[dev & 63][wpb] = n;
+            blocks_per_sm[dev & 63][wpb] = b > 0 ? b : 1;
+            return MARA_OK;
+        }))
+        return r;
     const int cols = COLS == 2 ? SW2_COLS : SW_COLS;
     A.tiles_y = (A.N + cols - 1) / cols;
-    const int capacity = blocks_per_sm[dev & 63][wpb] * wpb * sm_count[dev & 63];
+    const int capacity = blocks_per_sm[dev & 63][wpb] * wpb * sm_count[dev & 63][wpb];
     const int segments = std::max(1, waves * capacity / A.tiles_y);
     A.sweep_rows = std::max(waves > 1 ? 2 : 32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
@@ -770,12 +775,15 @@ bool state_tensor_map(const double* u, int N, CUtensorMap* map)
 template<typename R, int KIND>
 int launch_stage(const Args& A, int tiles, cudaStream_t s)
 {
-    static std::once_flag flags[64];
+    static PerDeviceOnce once;
     int dev = 0;
-    cudaGetDevice(&dev);
-    std::call_once(flags[dev & 63], [] {
-        cudaFuncSetAttribute(stage_kernel<R, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(Smem<R>)));
-    });
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (int r = once.run(dev, []() -> int {
+            MARA_CUDA(cudaFuncSetAttribute(stage_kernel<R, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(sizeof(Smem<R>))));
+            return MARA_OK;
+        }))
+        return r;
     Args a = A;
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);

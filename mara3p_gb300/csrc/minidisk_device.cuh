@@ -809,8 +809,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         sweep2_prim<KIND>(raw, p0);
         ring2_row<KIND>(ring, i0 + 1, lane, raw);
         sweep2_prim<KIND>(raw, p1);
-        ring2_fetch<KIND>(A, ring, i0 + 2, jg, NN, lane);     // into the slots of rows i0 - 2, i0 - 1
-        ring2_fetch<KIND>(A, ring, i0 + 3, jg, NN, lane);
+        ring2_fetch<KIND>(A, ring, i0 + 2, jg, NN, lane);     // into the fifth, free slot
+        ring2_fetch<KIND>(A, ring, i0 + 3, jg, NN, lane);     // into the slot of row i0 - 2
     }
     else
     {

@@ -302,14 +302,15 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(const Weights* w, const
 int grad_launch(const Weights* w, const float* feat, const float* target, const int64_t* idx, int64_t begin,
                 int64_t count, float* grad, float* loss, cudaStream_t s)
 {
-    static bool configured[64] = {};
+    static PerDeviceOnce once;
     int dev = 0;
-    cudaGetDevice(&dev);
-    if (!configured[dev & 63])
-    {
-        MARA_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(TrainSmem))));
-        configured[dev & 63] = true;
-    }
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (int r = once.run(dev, []() -> int {
+            MARA_CUDA(cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(sizeof(TrainSmem))));
+            return MARA_OK;
+        }))
+        return r;
     int blocks = int(std::min<int64_t>((count + kTile - 1) / kTile, 152 * 2));
     grad_kernel<<<blocks, kTile, sizeof(TrainSmem), s>>>(w, feat, target, idx, begin, count, grad, loss);
     return launch_status("grad_kernel");

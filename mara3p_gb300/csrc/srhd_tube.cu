@@ -314,13 +314,15 @@ __global__ void __launch_bounds__(NT) tube_flux_kernel(const Flux A)
 template<typename R, int SOLVER>
 int launch_flux(const Flux& F, cudaStream_t s)
 {
-    static std::once_flag flags[64];
+    static PerDeviceOnce once;
     int dev = 0;
-    cudaGetDevice(&dev);
-    std::call_once(flags[dev & 63], [] {
-        cudaFuncSetAttribute(tube_flux_kernel<R, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(sizeof(TileSmem<R>)));
-    });
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (int r = once.run(dev, []() -> int {
+            MARA_CUDA(cudaFuncSetAttribute(tube_flux_kernel<R, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(sizeof(TileSmem<R>))));
+            return MARA_OK;
+        }))
+        return r;
     Flux A = F;
     A.tiles_y = (A.N + TY - 1) / TY;
     const int tiles = ((A.N + TX - 1) / TX) * A.tiles_y;

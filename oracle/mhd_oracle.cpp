@@ -175,17 +175,22 @@ struct Mesh
 
 // One advance_mhd_ct (scheme_mhd_v1.cpp:265-299). Returns dt; status != 0 if
 // a primitive recovery failed.
+// Every loop runs its outer index on `threads` workers; each cell's
+// arithmetic is the same as in a serial loop and the wavespeed maximum does
+// not depend on the order, so the result does not depend on `threads`.
 double advance_ct(int N, const double* uc, const double* bf1, const double* bf2, const double* bf3,
                   double dl, double cfl, double theta, double gm,
-                  double* uc_out, double* bf1_out, double* bf2_out, double* bf3_out, int& status)
+                  double* uc_out, double* bf1_out, double* bf2_out, double* bf3_out, int& status, int threads = 1)
 {
     Mesh M{N};
     const size_t NN = size_t(N) * N * N;
     std::vector<double> P(NN * 8);
-    status = 0;
-    double amax = 0.0;
+    std::vector<double> amax_row(N, 0.0);
+    std::vector<int> status_row(N, 0);
     // primitive_array: face_to_cell then recover_primitive
-    for (int i = 0; i < N; ++i)
+    oracle::parallel_for(N, threads, [&] (int i) {
+        double& amax = amax_row[i];
+        int& status = status_row[i];
         for (int j = 0; j < N; ++j)
             for (int k = 0; k < N; ++k)
             {
@@ -200,6 +205,14 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                 prim_to_array(p, &P[c * 8]);
                 amax = std::max(amax, fastest_speed(p, gm));
             }
+    });
+    status = 0;
+    double amax = 0.0;
+    for (int i = 0; i < N; ++i)
+    {
+        status |= status_row[i];
+        amax = std::max(amax, amax_row[i]);
+    }
     // face fluxes and E-fields on the N+1 layers of each face array (the
     // reference's flux_arrays shapes): face (i,j,k) of axis a lies between
     // cell (i,j,k) - e_a and cell (i,j,k) (cells periodic); its normal field
@@ -214,7 +227,7 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
         F[a].resize(fsize(a) * 5);
         E[a].resize(fsize(a) * 3);
         const double* bfa = a == 0 ? bf1 : (a == 1 ? bf2 : bf3);
-        for (int i = 0; i < N + (a == 0); ++i)
+        oracle::parallel_for(N + (a == 0), threads, [&] (int i) {
             for (int j = 0; j < N + (a == 1); ++j)
                 for (int k = 0; k < N + (a == 2); ++k)
                 {
@@ -239,6 +252,7 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                     for (int q = 0; q < 5; ++q) F[a][id * 5 + q] = f.c[q];
                     for (int q = 0; q < 3; ++q) E[a][id * 3 + q] = e.x[q];
                 }
+        });
     }
     // E of face array a at layer index n (no wrap) and transverse cells (wrapped)
     auto ef = [&] (int a, int comp, int i, int j, int k) {
@@ -265,7 +279,7 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
         return 0.5 * (a + b);
     };
     const double dt = cfl * dl / amax;
-    for (int i = 0; i < N; ++i)
+    oracle::parallel_for(N, threads, [&] (int i) {
         for (int j = 0; j < N; ++j)
             for (int k = 0; k < N; ++k)
             {
@@ -279,8 +293,9 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                     uc_out[c * 5 + q] = uc[c * 5 + q] - dc * dt / dl;
                 }
             }
+    });
     // solenoidal_difference: cf1 = d2(ee3) - d3(ee2), cf2 = d3(ee1) - d1(ee3), cf3 = d1(ee2) - d2(ee1)
-    for (int i = 0; i <= N; ++i)
+    oracle::parallel_for(N + 1, threads, [&] (int i) {
         for (int j = 0; j < N; ++j)
             for (int k = 0; k < N; ++k)
             {
@@ -288,7 +303,8 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                 size_t f = (size_t(i) * N + j) * N + k;
                 bf1_out[f] = bf1[f] - cf * dt / dl;
             }
-    for (int i = 0; i < N; ++i)
+    });
+    oracle::parallel_for(N, threads, [&] (int i) {
         for (int j = 0; j <= N; ++j)
             for (int k = 0; k < N; ++k)
             {
@@ -296,7 +312,8 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                 size_t f = (size_t(i) * (N + 1) + j) * N + k;
                 bf2_out[f] = bf2[f] - cf * dt / dl;
             }
-    for (int i = 0; i < N; ++i)
+    });
+    oracle::parallel_for(N, threads, [&] (int i) {
         for (int j = 0; j < N; ++j)
             for (int k = 0; k <= N; ++k)
             {
@@ -304,6 +321,7 @@ double advance_ct(int N, const double* uc, const double* bf1, const double* bf2,
                 size_t f = (size_t(i) * N + j) * (N + 1) + k;
                 bf3_out[f] = bf3[f] - cf * dt / dl;
             }
+    });
     return dt;
 }
 
@@ -355,19 +373,33 @@ double oracle_mhd_advance_ct(int32_t N, const double* uc, const double* bf1, con
 
 // `steps` RK2 steps of examples/mhd3d.cpp (advance_runge_kutta order 2 over
 // advance_mhd_ct); arrays updated in place; returns the final time.
+double oracle_mhd_rk2_threads(int32_t N, double* uc, double* bf1, double* bf2, double* bf3, double time,
+                              int32_t steps, double dl, double cfl, double plm_theta, double gamma_law_index,
+                              int32_t threads);
+
 double oracle_mhd_rk2(int32_t N, double* uc, double* bf1, double* bf2, double* bf3, double time, int32_t steps,
                       double dl, double cfl, double plm_theta, double gamma_law_index)
+{
+    return oracle_mhd_rk2_threads(N, uc, bf1, bf2, bf3, time, steps, dl, cfl, plm_theta, gamma_law_index, 1);
+}
+
+// The same on `threads` workers (same result for any thread count).
+double oracle_mhd_rk2_threads(int32_t N, double* uc, double* bf1, double* bf2, double* bf3, double time,
+                              int32_t steps, double dl, double cfl, double plm_theta, double gamma_law_index,
+                              int32_t threads)
 {
     const size_t nc = size_t(N) * N * N * 5, nf = size_t(N + 1) * N * N;
     std::vector<double> u1(nc), b11(nf), b21(nf), b31(nf), u2(nc), b12(nf), b22(nf), b32(nf);
     int status = 0;
     for (int s = 0; s < steps; ++s)
     {
+        int s0 = 0, s1 = 0;
         double dt0 = advance_ct(N, uc, bf1, bf2, bf3, dl, cfl, plm_theta, gamma_law_index,
-                                u1.data(), b11.data(), b21.data(), b31.data(), status);
+                                u1.data(), b11.data(), b21.data(), b31.data(), s0, threads);
         double t1 = time + dt0;
         double dt1 = advance_ct(N, u1.data(), b11.data(), b21.data(), b31.data(), dl, cfl, plm_theta, gamma_law_index,
-                                u2.data(), b12.data(), b22.data(), b32.data(), status);
+                                u2.data(), b12.data(), b22.data(), b32.data(), s1, threads);
+        status |= s0 | s1;
         double t2 = t1 + dt1;
         for (size_t q = 0; q < nc; ++q) uc[q] = uc[q] * 0.5 + u2[q] * (1 - 0.5);
         for (size_t q = 0; q < nf; ++q)

@@ -190,6 +190,23 @@ def test_mhd_rk2_bitexact(oracle, mhd_golden):
         assert np.array_equal(bf[k], mhd_golden[f"mhd/rk2_bf{k + 1}"])
 
 
+def test_mhd_rk2_threads_bitexact(oracle, mhd_golden):
+    """The threaded oracle loop gives the reference's RK2 result bit for bit."""
+    o = _mhd_oracle(oracle)
+    o.oracle_mhd_rk2_threads.restype = ctypes.c_double
+    N, g, cfl, theta = mhd_golden["mhd/params"]
+    N = int(N)
+    uc = mhd_golden["mhd/uc"].copy()
+    bf = [mhd_golden[f"mhd/bf{k}"].copy() for k in (1, 2, 3)]
+    t = o.oracle_mhd_rk2_threads(N, dptr(uc), *[dptr(b) for b in bf], ctypes.c_double(0.0), 2,
+                                 ctypes.c_double(1.0 / N), ctypes.c_double(cfl), ctypes.c_double(theta),
+                                 ctypes.c_double(g), 4)
+    assert t == mhd_golden["mhd/rk2_time"][0]
+    assert np.array_equal(uc, mhd_golden["mhd/rk2_uc"])
+    for k in range(3):
+        assert np.array_equal(bf[k], mhd_golden[f"mhd/rk2_bf{k + 1}"])
+
+
 def test_mhd_reference_known_answers(oracle, mhd_golden):
     """test_mhd's round trips (src/physics_mhd.hpp:405-415): within 1e-10."""
     o = _mhd_oracle(oracle)
