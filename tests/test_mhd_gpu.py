@@ -8,6 +8,7 @@ div B still at FP64 rounding."""
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -102,6 +103,31 @@ def test_rk2_fp64_matches_oracle_longer(mh, oracle):
     run.advance(10)
     t = oracle.oracle_mhd_rk2(N, dptr(uc), *[dptr(b) for b in bf], ctypes.c_double(0.0), 10, ctypes.c_double(1.0 / N),
                               ctypes.c_double(cfg.cfl), ctypes.c_double(cfg.plm_theta), ctypes.c_double(cfg.gamma_law_index))
+    assert abs(run.clock.read()["time"] - t) <= 1e-13 * t
+    assert rel_l1_components(s.uc.cpu().numpy().reshape(5, -1), soa(uc, N), 5) < 1e-11
+    for k in range(3):
+        assert np.abs(s.bf[k].cpu().numpy().ravel() - bf[k]).sum() / np.abs(bf[k]).sum() < 1e-11
+    b_scale = max(float(b.abs().max()) for b in s.bf)
+    assert run.max_div_b() < 1e-13 * b_scale
+
+
+def test_config3_full_size_fp64_matches_oracle(mh, oracle):
+    """The MHD configuration at its own size (128^3, seeded modes, CFL dt):
+    three FP64 RK2 steps against the oracle on all host threads at 1e-11,
+    with div B at FP64 rounding."""
+    oracle.oracle_mhd_rk2_threads.restype = ctypes.c_double
+    cfg = mh.MhdConfig(N=128)
+    s = mh.initial_state(cfg, seed=1, modes=24)
+    N = cfg.N
+    uc = np.ascontiguousarray(s.uc.cpu().numpy().reshape(5, -1).T).ravel()
+    bf = [b.cpu().numpy().ravel().copy() for b in s.bf]
+    run = mh.Run(s)
+    run.advance(3)
+    t = oracle.oracle_mhd_rk2_threads(N, dptr(uc), *[dptr(b) for b in bf], ctypes.c_double(0.0), 3,
+                                      ctypes.c_double(1.0 / N), ctypes.c_double(cfg.cfl),
+                                      ctypes.c_double(cfg.plm_theta), ctypes.c_double(cfg.gamma_law_index),
+                                      os.cpu_count() or 1)
+    assert t > 0.0
     assert abs(run.clock.read()["time"] - t) <= 1e-13 * t
     assert rel_l1_components(s.uc.cpu().numpy().reshape(5, -1), soa(uc, N), 5) < 1e-11
     for k in range(3):

@@ -10,13 +10,14 @@ Tolerances (relative L1 per component, sum|gpu - ref| / sum|ref|):
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 import pytest
 
 from oracle.oracle import dptr, params
 from tests.golden.make_golden import MINIDISK_CASES
-from tests.helpers import CONFIG1_PARAMS, SMALL_PARAMS, params_from_vector, rel_l1_components
+from tests.helpers import CONFIG1_PARAMS, CONFIG2_PARAMS, SMALL_PARAMS, params_from_vector, rel_l1_components
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -133,6 +134,44 @@ def test_config1_full_size_one_step(md, oracle):
     run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)
     run.advance(2)
     oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 2, 2, 0, 8)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
+
+
+THREADS = os.cpu_count() or 1
+
+
+def test_config1_full_size_1000_steps_fp64(md, oracle):
+    """Configuration 1 at its own size and physics (256^2, 4x4 blocks of
+    64^2, theta 1.5, CFL dt): one RK2 step at 1e-12 and 1000 RK2 steps at
+    1e-9 against the oracle, with the clocks' times alike."""
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, plm_theta=1.5))
+    u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
+    run.advance(1)
+    t = oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 1, 2, 1, THREADS)
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
+    run.advance(999)
+    t = oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(t), 999, 2, 1, THREADS)
+    assert np.isfinite(ref).all()
+    assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_1000_STEPS
+    assert abs(run.time - t) <= 1e-12 * t
+
+
+def test_config2_full_size_one_step_fp64(md, oracle):
+    """Configuration 2 itself (4096^2, theta 1.5, q 0.5, e 0.1, Mach 20, CFL
+    dt): one FP64 RK2 step at 1e-12 against the oracle on all host threads,
+    and the CFL dt (an FP64 reduction over all 16.8 M cells) at 1e-14."""
+    sd = md.SolverData(**CONFIG2_PARAMS)
+    u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
+    ref = u0.cpu().numpy().ravel().copy()
+    run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
+    run.advance(1)
+    dt_ref = oracle.oracle_minidisk_dt_cfl(ctypes.byref(params(sd)), dptr(ref))
+    t = oracle.oracle_minidisk_advance(ctypes.byref(params(sd)), dptr(ref), ctypes.c_double(0.0), 1, 2, 1, THREADS)
+    c = run.clock_state()
+    assert abs(c.dt - dt_ref) <= 1e-14 * dt_ref
+    assert abs(c.time - t) <= 1e-14 * t
     assert rel_l1_components(run.u.cpu().numpy(), ref) < FP64_ONE_STEP
 
 

@@ -5,21 +5,22 @@ all of the GPU's memory, a plugin that only receives the caller's buffers)
 use this entry point: its scratch is a static device array inside the
 library. The test calls it through the C ABI and checks, on two calls in a
 row, that it produces what mara_minidisk_advance produces with a
-caller-owned workspace. This file sorts last so that a run stopping at the
-first failure has already run every other test; it also passes alone.
+caller-owned workspace: the same kernels on the same inputs, so the states
+and clocks must be bit-identical. One case fills the whole static array (a
+mesh of exactly the limit, mixed RK2). This file sorts last so that a run
+stopping at the first failure has already run every other test; it also
+passes alone.
 """
 from __future__ import annotations
 
 import ctypes
 
-import numpy as np
 import pytest
 
 from tests.helpers import CONFIG1_PARAMS, rel_l1_components
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
-TOLERANCE = 1e-12      # the FP64 one-step tolerance of the minidisk GPU tests
 
 
 @pytest.fixture(scope="module")
@@ -30,6 +31,10 @@ def md():
     return m
 
 
+def lib_max_cells() -> int:
+    return 512 * 512     # MARA_MINIDISK_NOALLOC_MAX_CELLS in include/mara_gb300.h
+
+
 def clock_buffer(md, sd, u):
     from mara3p_gb300._capi import MinidiskClock, check, lib
     clock = torch.zeros(ctypes.sizeof(MinidiskClock), dtype=torch.uint8, device="cuda")
@@ -38,10 +43,15 @@ def clock_buffer(md, sd, u):
     return clock
 
 
-@pytest.mark.parametrize("precision,dt_mode", [(0, 0), (1, 1)])
-def test_noalloc_matches_workspace_advance_on_two_calls(md, precision, dt_mode):
+@pytest.mark.parametrize("precision,dt_mode,mesh", [(0, 0, (64, 2)), (1, 1, (64, 2)), (1, 1, (128, 2))])
+def test_noalloc_matches_workspace_advance_on_two_calls(md, precision, dt_mode, mesh):
     from mara3p_gb300._capi import check, lib
-    sd = md.SolverData(**CONFIG1_PARAMS)
+    block_size, depth = mesh
+    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth))
+    N = sd.cells_per_side
+    need = lib.mara_minidisk_workspace_bytes(ctypes.byref(sd.to_c()), 2, precision)
+    if N * N == lib_max_cells():
+        assert need == 36 * N * N, "the limit case must fill the whole static array"
     c = sd.to_c()
     stream = torch.cuda.current_stream().cuda_stream
     u0 = md.initial_conserved(sd, seed=21, amplitude=0.01)
@@ -55,8 +65,7 @@ def test_noalloc_matches_workspace_advance_on_two_calls(md, precision, dt_mode):
         check(lib.mara_minidisk_advance_noalloc(ctypes.byref(c), ub.data_ptr(), cb.data_ptr(), steps, 2, precision,
                                                 dt_mode, stream), "advance_noalloc")
         torch.cuda.synchronize()
-        err = rel_l1_components(ub.cpu().numpy(), ua.cpu().numpy())
-        assert err <= TOLERANCE, (call, err)
+        assert torch.equal(ua, ub), (call, rel_l1_components(ub.cpu().numpy(), ua.cpu().numpy()))
         assert torch.equal(ca, cb), f"clocks differ after call {call}"
 
 
