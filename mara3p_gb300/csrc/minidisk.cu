@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
                     fs += __ldg(A.d1 + idx); f1 += __ldg(A.d1 + NN + idx); f2 += __ldg(A.d1 + 2 * NN + idx);
                 }
                 float inv = rcp_fast(fs);
-                p0 = R(fs); p1 = R(f1 * inv); p2 = R(f2 * inv);
+                p0 = R(fs); p1 = R(div_corrected(f1, fs, inv)); p2 = R(div_corrected(f2, fs, inv));
             }
         }
         S.p[0][ei][ej] = p0; S.p[1][ei][ej] = p1; S.p[2][ei][ej] = p2;

@@ -544,8 +544,8 @@ __device__ inline void sweep_prim(const RawRow& r, float p[3])
     }
     const float inv = vrcp(s);
     p[0] = s;
-    p[1] = vmul(m1, inv);
-    p[2] = vmul(m2, inv);
+    p[1] = div_corrected(m1, s, inv);
+    p[2] = div_corrected(m2, s, inv);
 }
 
 __device__ inline void slope_y(const float p[3], float two_theta, float g[3])
@@ -694,8 +694,8 @@ __device__ inline void sweep2_prim(const RawRow2& r, float2 p[3])
     }
     const float2 inv = vrcp(s);
     p[0] = s;
-    p[1] = vmul(m1, inv);
-    p[2] = vmul(m2, inv);
+    p[1] = make_float2(div_corrected(m1.x, s.x, inv.x), div_corrected(m1.y, s.y, inv.y));
+    p[2] = make_float2(div_corrected(m2.x, s.x, inv.x), div_corrected(m2.y, s.y, inv.y));
 }
 
 // Per-warp ring of five rows in shared memory, filled by per-lane
