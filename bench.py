@@ -86,6 +86,11 @@ def parse():
     ap.add_argument("--no-looped", action="store_true", help="ensemble: skip the looped single-mesh comparison")
     ap.add_argument("--no-diagnostics-timing", action="store_true",
                     help="minidisk: skip timing the step with the fused time-series sums")
+    ap.add_argument("--no-fp64-variant", action="store_true",
+                    help="minidisk: skip timing the plain FP64 GPU path on the same mesh")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="default run: skip the compact lines of the other workloads (MHD, SRHD, tube, ensemble, "
+                         "sedov) in the headline line")
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip); the "
                          "4096^2 configuration's own 2000 by default")
@@ -98,6 +103,53 @@ def measured_peaks():
         d = json.loads(path.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+_FP64_RATE = None
+
+
+def fp64_peak() -> float:
+    """Thread-level DFMA/s of this GPU, measured live (mara_measure_fp64_rate)."""
+    global _FP64_RATE
+    if _FP64_RATE is None:
+        import torch
+
+        from mara3p_gb300._capi import check, lib
+        r = ctypes.c_double()
+        check(lib.mara_measure_fp64_rate(ctypes.byref(r), torch.cuda.current_stream().cuda_stream), "fp64 rate")
+        _FP64_RATE = r.value
+    return _FP64_RATE
+
+
+def fp64_pipe_fraction(key: str, units: float, ms: float):
+    """The FP64-pipe roofline of an FP64-bound kernel: its FP64 thread
+    instructions per unit (an ncu count in profiles/fp64_ops.json) x units
+    per CUDA-event millisecond, against the live-measured DFMA rate."""
+    f = ROOT / "profiles" / "fp64_ops.json"
+    if not f.exists():
+        return None
+    rec = json.loads(f.read_text()).get(key)
+    if rec is None:
+        return None
+    peak = fp64_peak()
+    achieved = rec["fp64_inst_per_unit"] * units / (ms * 1e-3)
+    return {"bound": "fp64", "achieved": achieved / 1e9, "peak": peak / 1e9,
+            "unit": "G FP64 thread-instructions/s", "frac": achieved / peak,
+            "fp64_inst_per_unit": rec["fp64_inst_per_unit"], "kernels": rec.get("kernels"),
+            "peak_source": "measured live: mara_measure_fp64_rate (DFMA chains on every SM)",
+            "counts_source": "profiles/fp64_ops.json (ncu sm__inst_executed_pipe_fp64 x 32 per unit)"}
+
+
+def fp64_roofline(key: str, units: float, ms: float, hbm: dict) -> dict:
+    """The roofline of an FP64-bound workload: the FP64 pipe where its counts
+    are known (the HBM figures kept beside it), else the HBM line."""
+    fp = fp64_pipe_fraction(key, units, ms)
+    if fp is None:
+        return hbm
+    fp["hbm"] = {k: hbm[k] for k in ("achieved", "peak", "unit", "frac")}
+    fp["kernel"] = hbm.get("kernel")
+    fp["traffic"] = hbm.get("traffic")
+    return fp
 
 
 def dist_info():
@@ -242,6 +294,22 @@ def cpu_baseline(sd_kw: dict, seconds: float) -> dict:
     return CpuBaseline(sd_kw, seconds).measure()
 
 
+def minidisk_config(workload: str, world: int) -> dict:
+    """The `config` of a minidisk workload's line, the same in both arms."""
+    kw = WORKLOADS[workload]
+    N = kw["block_size"] << kw["depth"]
+    nb = 1 << kw["depth"]
+    return {"workload": workload, "cells": N * N,
+            "mesh": f"{N}^2 ({nb}x{nb} blocks of {kw['block_size']}^2)",
+            "scheme": f"PLM(theta={kw['plm_theta']})+HLLE+viscosity+gravity/sink/buffer sources, RK2, "
+                      f"CFL {kw['cfl']} wavespeed reduction",
+            "physics": {k: kw[k] for k in ("domain_radius", "mass_ratio", "eccentricity", "mach_number", "nu",
+                                           "softening_length", "sink_radius", "sink_rate", "buffer_rate",
+                                           "buffer_scale")},
+            "parallelism": f"replicas x{world}",
+            "l2": f"no flush: FP64 state {3 * N * N * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -259,13 +327,48 @@ def run_reference(args):
         "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N * N / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "cells": N * N, "scheme": "PLM+HLLE+viscosity+sources, RK2",
-                   "precision": "fp64 (reference CPU scheme)"},
+        "config": minidisk_config(args.workload, args.gpus),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": r["cores"], "kind": r["kind"],
                          "sample": r["sample"]},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def mixed_accuracy(md, sd, u0, steps: int) -> dict:
+    """Mixed vs FP64 relative L1 after `steps` RK2 steps from one state, each
+    path with its own CFL dt (an FP64 evaluation in both), also at half the
+    horizon; globally and over the interior, the mesh less a frame of 0.5
+    along the box edges. The frame holds the periodic seams where the buffer
+    ring r ~ domain_radius meets the box edge: the tangential velocity jumps
+    by about 2 Omega R across them, and that shear layer amplifies any
+    difference between two runs (FP64 runs from states 1e-12 apart included)."""
+    import torch
+    N = sd.cells_per_side
+    x = (torch.arange(N, device="cuda", dtype=torch.float64) + 0.5) * (2 * sd.domain_radius / N) - sd.domain_radius
+    inner = x.abs() < sd.domain_radius - 0.5
+    mask = (inner[:, None] & inner[None, :]).to(torch.float64)
+    runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_CFL) for p in (md.FP64, md.MIXED)}
+    out = {"dt": "CFL 0.3, FP64 in each path",
+           "interior": "|x|, |y| < domain_radius - 0.5 (the periodic seams excluded)"}
+    done = 0
+    for target in sorted({steps // 2, steps}):
+        for r in runs.values():
+            r.advance(target - done)
+        done = target
+        torch.cuda.synchronize()
+        a, b = runs[md.MIXED].u, runs[md.FP64].u
+        rel = [float((a[k] - b[k]).abs().sum() / b[k].abs().sum()) for k in range(3)]
+        reli = [float(((a[k] - b[k]).abs() * mask).sum() / (b[k].abs() * mask).sum()) for k in range(3)]
+        out[str(target)] = {"rel_l1_vs_fp64": {"density": rel[0], "momentum_x": rel[1], "momentum_y": rel[2]},
+                            "interior_rel_l1_vs_fp64": {"density": reli[0], "momentum_x": reli[1],
+                                                        "momentum_y": reli[2]},
+                            "time": runs[md.MIXED].time, "time_fp64": runs[md.FP64].time}
+    out["steps"] = steps
+    out["rel_l1_vs_fp64"] = out[str(steps)]["rel_l1_vs_fp64"]
+    out["finite"] = bool(torch.isfinite(runs[md.MIXED].u).all().item() and torch.isfinite(runs[md.FP64].u).all().item())
+    del runs
+    return out
 
 
 def run_ours(args):
@@ -411,19 +514,32 @@ def run_ours(args):
                      "what": "Run(diagnostics=True): 13 rate sums fused into both stage kernels, integrated by "
                              "the clock kernel"}
         del drun
+    # the plain FP64 GPU path on the same mesh and state: the metric's comparator
+    variants = None
+    if prec == md.MIXED and not args.no_fp64_variant:
+        frun = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
+        frun.advance(1)
+        torch.cuda.synchronize()
+        k = max(2, min(args.steps, 5))
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        frun.advance(k)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1) / k
+        fval = cells * world / (fms * 1e-3)
+        fbytes = (STAGE_BYTES[("fp64", 1)] + STAGE_BYTES[("fp64", 2)]) * cells
+        variants = {"fp64": {"value": fval, "unit": "cell-updates/s", "ms_per_step": fms, "steps": k,
+                             "mixed_over_fp64": value / fval,
+                             "hbm_frac": fbytes / (fms * 1e-3) / 1e9 / measured_peaks()[0],
+                             "kernel": "stage_kernel<double, 0> (16x32 tiles, TMA halo copy), same RK2 + CFL step"}}
+        fp64_pipe = fp64_pipe_fraction("minidisk-4096/fp64", cells, fms)
+        if fp64_pipe is not None:
+            variants["fp64"]["fp64_pipe"] = fp64_pipe
+        del frun
     accuracy = None
     if prec == md.MIXED and args.accuracy_steps > 0:
-        runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_CFL) for p in (md.FP64, md.MIXED)}
-        for r in runs.values():
-            r.advance(args.accuracy_steps)
-        torch.cuda.synchronize()
-        a, b = runs[md.MIXED].u, runs[md.FP64].u
-        rel = [float((a[k] - b[k]).abs().sum() / b[k].abs().sum()) for k in range(3)]
-        accuracy = {"steps": args.accuracy_steps, "dt": "CFL 0.3, FP64 in each path",
-                    "rel_l1_vs_fp64": {"density": rel[0], "momentum_x": rel[1], "momentum_y": rel[2]},
-                    "time": runs[md.MIXED].time, "time_fp64": runs[md.FP64].time,
-                    "finite": bool(torch.isfinite(a).all().item() and torch.isfinite(b).all().item())}
-        del runs, a, b
+        accuracy = mixed_accuracy(md, sd, u0, args.accuracy_steps)
 
     if rank == 0:
         line = {
@@ -431,16 +547,12 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 compute, f64 state" if prec == md.MIXED else "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "cells": cells, "mesh": f"{N}^2 ({1 << sd.depth}x{1 << sd.depth} "
-                       f"blocks of {sd.block_size}^2)", "scheme": "PLM(theta=1.5)+HLLE+viscosity+gravity/sink/buffer "
-                       "sources, RK2, CFL 0.3 wavespeed reduction", "precision": args.precision,
-                       "parallelism": f"replicas x{world}",
-                       "l2": f"no flush: FP64 state {3 * cells * 8 / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB"},
+            "config": minidisk_config(args.workload, world),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
-            "clocks": sampler.summary(), "accuracy": accuracy, "diagnostics": diag_line,
+            "clocks": sampler.summary(), "accuracy": accuracy, "diagnostics": diag_line, "variants": variants,
         }
-        emit(line, rank)
-    finish_replicas(world)
+        return line
+    return None
 
 
 def _line(args, world, value, unit, ms_per_step, dtype, config, roofline, extra=None):
@@ -545,8 +657,7 @@ def run_mhd(args):
                   "precision": args.precision, "l2": "state 126 MB + intermediates > L2, no flush"}, roof,
                  {"max_div_b": run.max_div_b(), "failures": c["failures"], "time": c["time"],
                   "clocks": sampler.summary(), "gpu_launches": 15 * args.steps, "accuracy": accuracy, "e2e": e2e})
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 def run_srhd(args):
@@ -593,6 +704,10 @@ def run_srhd(args):
     achieved = 80.0 * n / (best["ms"] * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
             "kernel": "c2p_mlp_kernel (FP64-Newton bound; 80 B/zone algorithmic)", "peak_source": f"{kind} hbm_gbs"}
+    roof = fp64_roofline("srhd-c2p/mlp", n, best["ms"], roof)
+    fd = fp64_pipe_fraction("srhd-c2p/default", n, results["default"]["ms"])
+    if fd is not None:
+        results["default"]["fp64_pipe_frac"] = fd["frac"]
     e2e = None
     if not args.no_e2e:
         hc = pinned_like(cons)
@@ -621,8 +736,7 @@ def run_srhd(args):
                        "pinned host buffers"}
     line = _line(args, world, best["zones_per_s"] * world, "zones/s", best["ms"], "f64 (bf16 guess)",
                  {"workload": "srhd-c2p-2^24", "zones": n, "gamma": 4.0 / 3.0}, roof, {"variants": results, "e2e": e2e})
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 def run_ensemble(args):
@@ -741,8 +855,7 @@ def run_ensemble(args):
                         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
                         "clocks": sampler.summary()})
     e.close()
-    emit(line, rank)
-    finish_replicas(world)
+    return line if rank == 0 else None
 
 
 def run_tube(args):
@@ -786,6 +899,7 @@ def run_tube(args):
     achieved = 160.0 * N * N / (best["ms_per_step"] * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "whole RK2 step (FP64 Newton recovery bound)", "peak_source": f"{kind} hbm_gbs"}
+    roof = fp64_roofline(f"srhd-tube/{args.precision}/mlp", N * N, best["ms_per_step"], roof)
     e2e = None
     if not args.no_e2e:
         tube = sr.ShockTube(N=N)
@@ -800,8 +914,7 @@ def run_tube(args):
                  "f32 compute, f64 state" if prec else "f64",
                  {"workload": "srhd-tube-1024", "cells": N * N, "scheme": "PLM(1.5)+HLLE, RK2, CFL 0.3",
                   "precision": args.precision}, roof, {"variants": results, "e2e": e2e})
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
 
 
 def run_sedov(args):
@@ -856,6 +969,7 @@ def run_sedov(args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels, then remesh; bound by FP64 recovery and "
                                        "HLLC arithmetic, not by HBM)", "peak_source": f"{kind} hbm_gbs"}
+    roof = fp64_roofline("sedov-tracks", Cm, ms, roof)
     extra = {"gpu_launches": (1 + 5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
     if not args.no_e2e:
         # through the public calls with host buffers: the tracks' state to the
@@ -920,26 +1034,74 @@ def run_sedov(args):
                   "inputs": f"state resident, {(96.0 * C) / 2**20:.0f} MiB read and written per step (below L2, "
                             "no flush: the step is arithmetic-bound)"},
                  roof, extra)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line if rank == 0 else None
+
+
+RUNNERS = {"mhd-128": "run_mhd", "srhd-c2p": "run_srhd", "srhd-tube": "run_tube",
+           "minidisk-ensemble-64": "run_ensemble", "sedov-tracks": "run_sedov"}
+
+
+def compact(line: dict) -> dict:
+    """The figures of a workload's line that the headline line carries."""
+    keep = ("metric", "value", "unit", "ms_per_step", "dtype", "config", "variants", "accuracy", "max_div_b",
+            "failures", "looped_single_mesh", "gpu_launches", "cpu_baseline")
+    out = {k: line[k] for k in keep if line.get(k) is not None}
+    if line.get("e2e"):
+        out["e2e"] = {k: line["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}
+    roof = line.get("roofline") or {}
+    out["roofline"] = {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac", "kernel") if k in roof}
+    return out
+
+
+def other_workloads(args) -> dict:
+    """Short runs of the other workloads (mixed precision, their own default
+    sizes), each timed as its own --workload run times it, for the headline
+    line: MHD 128^3, the 2^24-zone SRHD recovery, the 1024^2 shock tube, the
+    64-member ensemble and the 1024-track sedov step."""
+    import argparse as ap_
+    import gc
+
+    import torch
+    out = {}
+    for name, fn in RUNNERS.items():
+        sub = ap_.Namespace(**vars(args))
+        sub.workload = name
+        sub.precision = "mixed"
+        sub.steps = min(args.steps, 10)
+        sub.warmup = max(args.warmup, 3)
+        sub.no_cpu_baseline = name != "sedov-tracks"
+        sub.no_looped = False
+        sub.launch = None
+        sub.accuracy_steps = 50
+        t0 = time.perf_counter()
+        line = globals()[fn](sub)
+        torch.cuda.synchronize()
+        gc.collect()
+        torch.cuda.empty_cache()
+        if line is not None:
+            out[name] = compact(line)
+            out[name]["wall_s"] = time.perf_counter() - t0
+    return out
 
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "mhd-128":
-        run_mhd(args)
-    elif args.workload == "srhd-c2p":
-        run_srhd(args)
-    elif args.workload == "srhd-tube":
-        run_tube(args)
-    elif args.workload == "minidisk-ensemble-64":
-        run_ensemble(args)
-    elif args.workload == "sedov-tracks":
-        run_sedov(args)
+        return
+    rank, world, _ = dist_info()
+    if args.workload in RUNNERS:
+        line = globals()[RUNNERS[args.workload]](args)
+        if args.workload == "minidisk-ensemble-64":
+            finish_replicas(world)
     else:
-        run_ours(args)
+        line = run_ours(args)
+        if (line is not None and args.workload == "minidisk-4096" and world == 1 and not args.no_workloads
+                and args.precision == "mixed"):
+            line["workloads"] = other_workloads(args)
+        finish_replicas(world)
+    if line is not None:
+        emit(line, rank)
 
 
 if __name__ == "__main__":

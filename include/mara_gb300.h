@@ -534,6 +534,103 @@ int mara_sedov_remesh(int32_t track_count, int64_t cells, const int64_t* cell_of
 int mara_sedov_min_spacing(int32_t track_count, int64_t cells, const int64_t* cell_offset, const double* radii,
                            double* out, void* stream);
 
+/* ---------------------------------------------------------------- mhd: the split block API */
+/* The reference's per-block CT scheme, mhd_scheme_v2 (src/scheme_mhd_v2.hpp:71-210,
+ * src/scheme_mhd_v2.cpp:75-278), FP64, one call per reference function.
+ * Device buffers in the reference's row-major AoS layouts: conserved
+ * 5-tuples (D, S1, S2, S3, E), primitive 8-tuples (rho, v1, v2, v3, p, B1,
+ * B2, B3), godunov data 8-tuples (the 5 HLLE fluxes, then E1, E2, E3), face
+ * fields and edge EMFs as scalars. For a cell array of shape (n0, n1, n2) the
+ * face array of axis a is one longer along a, and the edge array of axis a
+ * one longer along the two other axes. The reference fixes gamma at 5/3. */
+
+/* primitive_array (:75-81): uc (n0, n1, n2) conserved, bf1..3 the block's
+ * faces; pc (n0, n1, n2) primitives. failures (device, nullable) counts cells
+ * where mhd::recover_primitive throws (negative density or pressure). */
+int mara_mhd_v2_primitive_array(int32_t n0, int32_t n1, int32_t n2, const double* uc, const double* bf1,
+                                const double* bf2, const double* bf3, double gamma_law_index, double* pc,
+                                unsigned long long* failures, void* stream);
+
+/* godunov_fluxes (:143-163), first order: pc (m0, m1, m2) primitives (a block
+ * extended by one cell on every side); bf1..3 the faces between those cells,
+ * shapes (m0-1, m1, m2), (m0, m1-1, m2), (m0, m1, m2-1); gf1..3 the godunov
+ * data on those faces (normal E component zero). */
+int mara_mhd_v2_godunov_fluxes(int32_t m0, int32_t m1, int32_t m2, const double* pc, const double* bf1,
+                               const double* bf2, const double* bf3, double gamma_law_index, double* gf1,
+                               double* gf2, double* gf3, void* stream);
+
+/* electromotive_forces (:168-192): gf1..3 of a (m0, m1, m2) cell array as
+ * godunov_fluxes writes them; ee1 (m0, m1-1, m2-1), ee2 (m0-1, m1, m2-1),
+ * ee3 (m0-1, m1-1, m2): each edge EMF the mean of the adjacent means of the
+ * two transverse faces' E along it. */
+int mara_mhd_v2_electromotive_forces(int32_t m0, int32_t m1, int32_t m2, const double* gf1, const double* gf2,
+                                     const double* gf3, double* ee1, double* ee2, double* ee3, void* stream);
+
+/* updated_conserved_density (:197-219): uc (n0, n1, n2); gf1..3 extended by
+ * one zone on their transverse axes, (n0+1, n1+2, n2+2) etc.;
+ * uc_out = uc - div(F) dt / dl. */
+int mara_mhd_v2_updated_conserved_density(int32_t n0, int32_t n1, int32_t n2, const double* uc, const double* gf1,
+                                          const double* gf2, const double* gf3, double dt, double dl,
+                                          double* uc_out, void* stream);
+
+/* curl (:224-237): the staggered curl of the block's edge values ee1
+ * (n0, n1+1, n2+1), ee2 (n0+1, n1, n2+1), ee3 (n0+1, n1+1, n2), divided by
+ * dl, on the block's faces cf1 (n0+1, n1, n2), cf2, cf3. */
+int mara_mhd_v2_curl(int32_t n0, int32_t n1, int32_t n2, const double* ee1, const double* ee2, const double* ee3,
+                     double dl, double* cf1, double* cf2, double* cf3, void* stream);
+
+/* updated_magnetic_flux_density (:242-257): bf1..3 the block's faces; ee1..3
+ * the edge EMFs of the block extended by one cell on every side (as
+ * electromotive_forces gives them: (n0+2, n1+1, n2+1) etc.), of which the
+ * block's own edges are used; bf_out = bf - curl(E) dt / dl. */
+int mara_mhd_v2_updated_magnetic_flux_density(int32_t n0, int32_t n1, int32_t n2, const double* bf1,
+                                              const double* bf2, const double* bf3, const double* ee1,
+                                              const double* ee2, const double* ee3, double dt, double dl,
+                                              double* bf1_out, double* bf2_out, double* bf3_out, void* stream);
+
+/* ---------------------------------------------------------------- pointwise physics */
+/* Batches of n points, device buffers, FP64, the reference's formulas and
+ * order. axis is the face normal: 1..3 (unit_vector_on(axis)). */
+
+/* mhd::recover_primitive (src/physics_mhd.hpp:290-303): u [n][5], cell
+ * fields b [n][3] -> p [n][8]; status[i] (nullable) 1 where the reference
+ * throws; failures (nullable, device) counts them. */
+int mara_mhd_recover_primitive(const double* u, const double* b, int64_t n, double gamma_law_index, double* p,
+                               int32_t* status, unsigned long long* failures, void* stream);
+/* mhd::conserved_density (:305-318): p [n][8] -> u [n][5]. */
+int mara_mhd_conserved_density(const double* p, int64_t n, double gamma_law_index, double* u, void* stream);
+/* mhd::flux (:324-349): p [n][8] -> f [n][5]. */
+int mara_mhd_flux(const double* p, int64_t n, int32_t axis, double gamma_law_index, double* f, void* stream);
+/* mhd::fast_speed_squared (:216-222) along the axis: out [n]. */
+int mara_mhd_fast_speed_squared(const double* p, int64_t n, int32_t axis, double gamma_law_index, double* out,
+                                void* stream);
+/* mhd::fastest_speed (:239-249): out [n]. */
+int mara_mhd_fastest_speed(const double* p, int64_t n, double gamma_law_index, double* out, void* stream);
+/* mhd::riemann_hlle (:358-390): pl, pr [n][8], the face's normal field
+ * b_longitudinal [n] -> out [n][8] (HLLE flux 5, then the E-field 3). */
+int mara_mhd_riemann_hlle(const double* pl, const double* pr, const double* b_longitudinal, int64_t n, int32_t axis,
+                          double gamma_law_index, double* out, void* stream);
+
+/* iso2d (src/physics_iso2d.hpp:99-173) with the local cs^2 of every point
+ * (cs2 [n]); p = (Sigma, v1, v2) [n][3], axis 1 or 2. */
+int mara_iso2d_flux(const double* p, const double* cs2, int64_t n, int32_t axis, double* f, void* stream);
+/* out [n][2] = (vn - cs, vn + cs) */
+int mara_iso2d_outer_wavespeeds(const double* p, const double* cs2, int64_t n, int32_t axis, double* out,
+                                void* stream);
+/* out [n] = max |outer wavespeed| over both axes */
+int mara_iso2d_fastest_wavespeed(const double* p, const double* cs2, int64_t n, double* out, void* stream);
+/* HLLE flux between pl and pr [n][3] -> f [n][3] */
+int mara_iso2d_riemann_hlle(const double* pl, const double* pr, const double* cs2, int64_t n, int32_t axis,
+                            double* f, void* stream);
+
+/* ---------------------------------------------------------------- measurement */
+/* FP64 fused multiply-add throughput of the current GPU in thread-level DFMA
+ * per second (*dfma_per_second, host): a timed kernel of independent FMA
+ * chains on every SM, best of three launches after a warm-up; synchronizes
+ * the stream. The roofline denominator of the kernels that the FP64 pipe
+ * bounds. A measurement helper with no counterpart in the reference. */
+int mara_measure_fp64_rate(double* dfma_per_second, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -182,6 +182,27 @@ SIGNATURES.update({
                                [ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp]),
     "mara_srhd_riemann": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
                                          _vp, _vp, _vp]),
+    "mara_measure_fp64_rate": (ctypes.c_int, [c_double_p, _vp]),
+    # mhd_scheme_v2 block API and pointwise physics
+    "mara_mhd_v2_primitive_array": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 4 + [ctypes.c_double, _vp, _vp, _vp]),
+    "mara_mhd_v2_godunov_fluxes": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 4 + [ctypes.c_double] + [_vp] * 4),
+    "mara_mhd_v2_electromotive_forces": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 7),
+    "mara_mhd_v2_updated_conserved_density": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 4 +
+                                              [ctypes.c_double] * 2 + [_vp, _vp]),
+    "mara_mhd_v2_curl": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 3 + [ctypes.c_double] + [_vp] * 4),
+    "mara_mhd_v2_updated_magnetic_flux_density": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 6 +
+                                                  [ctypes.c_double] * 2 + [_vp] * 4),
+    "mara_mhd_recover_primitive": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_double, _vp, _vp, _vp, _vp]),
+    "mara_mhd_conserved_density": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_double, _vp, _vp]),
+    "mara_mhd_flux": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _vp, _vp]),
+    "mara_mhd_fast_speed_squared": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _vp, _vp]),
+    "mara_mhd_fastest_speed": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_double, _vp, _vp]),
+    "mara_mhd_riemann_hlle": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, _vp,
+                                             _vp]),
+    "mara_iso2d_flux": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),
+    "mara_iso2d_outer_wavespeeds": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),
+    "mara_iso2d_fastest_wavespeed": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, _vp]),
+    "mara_iso2d_riemann_hlle": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),
 })
 
 

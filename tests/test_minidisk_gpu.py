@@ -219,6 +219,25 @@ def test_mixed_precision_close_to_fp64(md, rk_order, steps, block_size):
     assert a.time == b.time
 
 
+def test_mixed_long_horizon_config2_physics(md):
+    """The mixed path against the plain FP64 path over 2000 CFL steps of the
+    large-minidisk physics (q 0.5, e 0.1, Mach 20, theta 1.5) on a 1024^2
+    mesh of the same domain: density and momentum relative L1 at most 1e-6.
+    (The primitive velocity is an FMA-corrected quotient: with the biased
+    single-MUFU reciprocal the 4096^2 configuration was 4.8e-6 from FP64
+    after 1000 steps, with the corrected quotient 7.4e-7.)"""
+    sd = md.SolverData(**dict(CONFIG2_PARAMS, depth=4))
+    u0 = md.initial_conserved(sd, seed=1234, amplitude=0.01)
+    a = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
+    b = md.Run(sd, u0.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL)
+    a.advance(2000)
+    b.advance(2000)
+    assert torch.isfinite(a.u).all() and torch.isfinite(b.u).all()
+    err = rel_l1_components(b.u.cpu().numpy(), a.u.cpu().numpy())
+    assert err <= 1e-6, err
+    assert abs(a.time - b.time) <= 1e-6 * a.time
+
+
 def test_mass_conservation_full_size(md):
     """Size-independent property at the config-2 size (4096^2): with sinks,
     buffer and viscosity off, the flux divergence telescopes and total mass
