@@ -52,6 +52,12 @@ def load_reference() -> ctypes.CDLL | None:
     return lib
 
 
+def load_reference_v2() -> ctypes.CDLL | None:
+    """oracle/_ref/libref_v2.so: the reference's mhd_scheme_v2 block API."""
+    path = HERE / "_ref" / "libref_v2.so"
+    return ctypes.CDLL(str(path)) if path.exists() else None
+
+
 def params(sd) -> MinidiskParams:
     """Oracle params from any object with the solver_data_t field names."""
     return MinidiskParams(**{name: getattr(sd, name) for name, _ in MinidiskParams._fields_})

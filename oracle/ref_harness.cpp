@@ -20,58 +20,9 @@
 #include "scheme_mhd_v1.hpp"
 #include "scheme_plm_gradient.hpp"
 #include "scheme_sedov2d.hpp"
+#include "ref_marshal.hpp"
 
 namespace {
-
-template<typename Tuple, std::size_t... I>
-void load_tuple(Tuple& t, const double* src, std::index_sequence<I...>)
-{
-    ((std::get<I>(t.impl).value = src[I]), ...);
-}
-
-template<typename Tuple, std::size_t... I>
-void store_tuple(const Tuple& t, double* dst, std::index_sequence<I...>)
-{
-    ((dst[I] = std::get<I>(t.impl).value), ...);
-}
-
-template<typename Tuple>
-constexpr std::size_t tuple_size_v = std::tuple_size_v<decltype(Tuple().impl)>;
-
-template<typename Tuple>
-Tuple to_tuple(const double* src)
-{
-    Tuple t;
-    load_tuple(t, src, std::make_index_sequence<tuple_size_v<Tuple>>());
-    return t;
-}
-
-template<typename Tuple>
-void from_tuple(const Tuple& t, double* dst)
-{
-    store_tuple(t, dst, std::make_index_sequence<tuple_size_v<Tuple>>());
-}
-
-template<typename Tuple>
-nd::shared_array<Tuple, 2> make_array2(const double* data, std::size_t n0, std::size_t n1)
-{
-    constexpr auto K = tuple_size_v<Tuple>;
-    auto a = nd::make_unique_array<Tuple, 2>(nd::uivec(n0, n1));
-    for (std::size_t i = 0; i < n0; ++i)
-        for (std::size_t j = 0; j < n1; ++j)
-            a(i, j) = to_tuple<Tuple>(data + (i * n1 + j) * K);
-    return nd::make_shared_array(std::move(a));
-}
-
-template<typename Tuple>
-void read_array2(const nd::shared_array<Tuple, 2>& a, double* out)
-{
-    constexpr auto K = tuple_size_v<Tuple>;
-    auto n0 = shape(a, 0), n1 = shape(a, 1);
-    for (std::size_t i = 0; i < n0; ++i)
-        for (std::size_t j = 0; j < n1; ++j)
-            from_tuple(a(i, j), out + (i * n1 + j) * K);
-}
 
 minidisk::solver_data_t solver_data(const double* v)
 {
@@ -263,6 +214,65 @@ void ref_mhd_riemann_hlle(const double* pl, const double* pr, const double* bl, 
         out[8 * i + 5] = e.component_1().value;
         out[8 * i + 6] = e.component_2().value;
         out[8 * i + 7] = e.component_3().value;
+    }
+}
+
+// iso2d pointwise physics (src/physics_iso2d.hpp:99-173) on n points with
+// their local cs^2; axis in {1, 2}. Per point: flux(pl) [3], outer_wavespeeds(pl)
+// [2], fastest_wavespeed(pl), riemann_hlle(pl, pr) [3].
+void ref_iso2d_pointwise(const double* pl, const double* pr, const double* cs2, int64_t n, uint32_t axis,
+                         double* flux, double* outer, double* fastest, double* hlle)
+{
+    const auto nhat = geometric::unit_vector_on(axis);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const auto a = to_tuple<iso2d::primitive_t>(pl + 3 * i);
+        const auto b = to_tuple<iso2d::primitive_t>(pr + 3 * i);
+        const auto c2 = dimensional::unit_specific_energy(cs2[i]);
+        from_tuple(iso2d::flux(a, nhat, c2), flux + 3 * i);
+        const auto [wm, wp] = iso2d::outer_wavespeeds(a, nhat, c2);
+        outer[2 * i] = wm.value;
+        outer[2 * i + 1] = wp.value;
+        fastest[i] = iso2d::fastest_wavespeed(a, c2).value;
+        from_tuple(iso2d::riemann_hlle(a, b, c2, nhat), hlle + 3 * i);
+    }
+}
+
+// mhd pointwise physics (src/physics_mhd.hpp:216-356) on n primitive
+// 8-tuples; axis in {1, 2, 3}. Per point: flux [5], fast_speed_squared along
+// the axis, fastest_speed.
+void ref_mhd_pointwise(const double* p, int64_t n, uint32_t axis, double gamma_law_index, double* flux, double* cf2,
+                       double* fastest)
+{
+    const auto nhat = geometric::unit_vector_on(axis);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const auto a = to_tuple<mhd::primitive_t>(p + 8 * i);
+        from_tuple(mhd::flux(a, nhat, gamma_law_index), flux + 5 * i);
+        cf2[i] = mhd::fast_speed_squared(a, nhat, gamma_law_index).value;
+        fastest[i] = mhd::fastest_speed(a, gamma_law_index).value;
+    }
+}
+
+// mhd::recover_primitive (src/physics_mhd.hpp:290-303) of n conserved
+// 5-tuples with cell fields b [n][3]; status 0, or 1 where it throws
+// (negative density or pressure; the primitives are then left zero).
+void ref_mhd_recover_primitive(const double* u, const double* b, int64_t n, double gamma_law_index, double* p,
+                               int32_t* status)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const auto c = to_tuple<mhd::conserved_density_t>(u + 5 * i);
+        const auto bv = geometric::euclidean_vector(mhd::unit_magnetic_field(b[3 * i]),
+                                                    mhd::unit_magnetic_field(b[3 * i + 1]),
+                                                    mhd::unit_magnetic_field(b[3 * i + 2]));
+        try {
+            from_tuple(mhd::recover_primitive(c, bv, gamma_law_index), p + 8 * i);
+            status[i] = 0;
+        } catch (...) {
+            for (int k = 0; k < 8; ++k) p[8 * i + k] = 0.0;
+            status[i] = 1;
+        }
     }
 }
 

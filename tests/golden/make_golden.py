@@ -2,7 +2,7 @@
 
 Run where the reference checkout is present (it is not on the GPU hosts):
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [--physics-only]
 
 oracle/_ref/libref.so is the reference's own scheme and physics code
 (problems/minidisk_scheme.cpp, src/physics_*.hpp, src/scheme_*) compiled in
@@ -21,7 +21,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parents[1]))
 
-from oracle.oracle import MinidiskParams, dptr, iptr, load_oracle, load_reference, solver_vector  # noqa: E402
+from oracle.oracle import (MinidiskParams, dptr, iptr, load_oracle, load_reference,  # noqa: E402
+                           load_reference_v2, solver_vector)
 
 MINIDISK_CASES = {
     # name: solver_data (block_size 16, depth 2 -> 64^2 mesh), seed, perturbation, time, dt scale
@@ -412,7 +413,147 @@ def mhd_fixtures(o, r) -> dict[str, np.ndarray]:
     return out
 
 
+# Block shapes of the mhd_scheme_v2 fixtures: a non-cubic block and the same
+# block extended by one cell on every side (the shapes its calls take).
+V2_BLOCK = (3, 4, 5)
+V2_GAMMA = 5.0 / 3.0   # the reference's scheme_mhd_v2 fixes gamma_law_index
+
+
+def staggered(shape, axis, grow, side):
+    return tuple(n + (grow if a == axis else side) for a, n in enumerate(shape))
+
+
+def mhd_prims(rng, n, b=None):
+    """n valid MHD primitive 8-tuples (rho, v, p, B); B drawn unless given."""
+    p = np.zeros((n, 8))
+    p[:, 0] = rng.uniform(0.5, 2.0, n)
+    p[:, 1:4] = rng.uniform(-1.0, 1.0, (n, 3))
+    p[:, 4] = rng.uniform(0.1, 2.0, n)
+    p[:, 5:8] = rng.uniform(-1.0, 1.0, (n, 3)) if b is None else b
+    return p
+
+
+def mhd_conserved(p, g):
+    d, v, pg, b = p[:, 0], p[:, 1:4], p[:, 4], p[:, 5:8]
+    u = np.zeros((p.shape[0], 5))
+    u[:, 0] = d
+    u[:, 1:4] = d[:, None] * v
+    u[:, 4] = 0.5 * d * (v * v).sum(1) + pg / (g - 1.0) + 0.5 * (b * b).sum(1)
+    return u
+
+
+def physics_fixtures(r) -> dict[str, np.ndarray]:
+    """Pointwise iso2d and mhd physics (src/physics_iso2d.hpp:99-173,
+    src/physics_mhd.hpp:216-390) on seeded points, by the reference's own
+    functions."""
+    out = {}
+    rng = np.random.default_rng(2024)
+    n = 96
+    pl = np.stack([rng.uniform(0.5, 2.0, n), rng.uniform(-3, 3, n), rng.uniform(-3, 3, n)], 1).ravel()
+    pr = np.stack([rng.uniform(0.5, 2.0, n), rng.uniform(-3, 3, n), rng.uniform(-3, 3, n)], 1).ravel()
+    cs2 = np.exp(rng.uniform(np.log(1e-4), np.log(4.0), n))
+    out["iso2d/pl"], out["iso2d/pr"], out["iso2d/cs2"] = pl, pr, cs2
+    for axis in (1, 2):
+        flux, outer, fastest, hlle = np.zeros(3 * n), np.zeros(2 * n), np.zeros(n), np.zeros(3 * n)
+        r.ref_iso2d_pointwise(dptr(pl), dptr(pr), dptr(cs2), ctypes.c_int64(n), ctypes.c_uint32(axis), dptr(flux),
+                              dptr(outer), dptr(fastest), dptr(hlle))
+        out[f"iso2d/axis{axis}/flux"], out[f"iso2d/axis{axis}/outer"] = flux, outer
+        out[f"iso2d/fastest"], out[f"iso2d/axis{axis}/hlle"] = fastest, hlle
+    for g in (5.0 / 3.0, 1.4):
+        tag = f"mhd_g{g:.4f}"
+        a = mhd_prims(rng, n).ravel()
+        b = mhd_prims(rng, n).ravel()
+        bl = rng.uniform(-1.0, 1.0, n)
+        out[f"{tag}/pl"], out[f"{tag}/pr"], out[f"{tag}/bl"] = a, b, bl
+        for axis in (1, 2, 3):
+            flux, cf2, fastest, hlle = np.zeros(5 * n), np.zeros(n), np.zeros(n), np.zeros(8 * n)
+            r.ref_mhd_pointwise(dptr(a), ctypes.c_int64(n), ctypes.c_uint32(axis), ctypes.c_double(g), dptr(flux),
+                                dptr(cf2), dptr(fastest))
+            r.ref_mhd_riemann_hlle(dptr(a), dptr(b), dptr(bl), ctypes.c_int64(n), ctypes.c_uint32(axis),
+                                   ctypes.c_double(g), dptr(hlle))
+            out[f"{tag}/axis{axis}/flux"], out[f"{tag}/axis{axis}/cf2"] = flux, cf2
+            out[f"{tag}/fastest"], out[f"{tag}/axis{axis}/hlle"] = fastest, hlle
+        # recovery from conserved densities, with a few states the reference
+        # rejects: negative pressure (energy below kinetic + magnetic) and
+        # negative density
+        prim = mhd_prims(rng, n)
+        u = mhd_conserved(prim, g)
+        u[5, 4] = 0.4 * (0.5 * u[5, 0] * (prim[5, 1:4] ** 2).sum() + 0.5 * (prim[5, 5:8] ** 2).sum())
+        u[17, 4] = 0.0
+        u[40, 0] = -u[40, 0]
+        bc = np.ascontiguousarray(prim[:, 5:8]).ravel()
+        u = u.ravel()
+        back, status = np.zeros(8 * n), np.zeros(n, dtype=np.int32)
+        r.ref_mhd_recover_primitive(dptr(u), dptr(bc), ctypes.c_int64(n), ctypes.c_double(g), dptr(back), iptr(status))
+        assert status.sum() == 3, status
+        out[f"{tag}/recover_u"], out[f"{tag}/recover_b"] = u, bc
+        out[f"{tag}/recover_p"], out[f"{tag}/recover_status"] = back, status
+    return out
+
+
+def mhd_v2_fixtures(rv) -> dict[str, np.ndarray]:
+    """mhd_scheme_v2's block calls (src/scheme_mhd_v2.cpp:75-278) on seeded
+    blocks, by the reference's own code (oracle/_ref/libref_v2.so)."""
+    out = {}
+    rng = np.random.default_rng(77)
+    c = V2_BLOCK
+    m = tuple(x + 2 for x in c)
+    size = lambda s: int(np.prod(s))  # noqa: E731
+    i32 = [ctypes.c_int32(x) for x in c]
+    m32 = [ctypes.c_int32(x) for x in m]
+    out["v2/block"], out["v2/extended"] = np.array(c), np.array(m)
+    # primitive_array: faces drawn, conserved from primitives holding the cells' mean fields
+    bf = [rng.uniform(-1, 1, size(staggered(c, a, 1, 0))) for a in range(3)]
+    b3 = [x.reshape(staggered(c, a, 1, 0)) for a, x in enumerate(bf)]
+    bc = np.stack([0.5 * (b3[0][:-1] + b3[0][1:]), 0.5 * (b3[1][:, :-1] + b3[1][:, 1:]),
+                   0.5 * (b3[2][:, :, :-1] + b3[2][:, :, 1:])], -1).reshape(-1, 3)
+    uc = mhd_conserved(mhd_prims(rng, size(c), bc), V2_GAMMA).ravel()
+    pc = np.zeros(8 * size(c))
+    assert rv.ref_mhd_v2_primitive_array(*i32, dptr(uc), *[dptr(x) for x in bf], dptr(pc)) == 0
+    out.update({"v2/prim/uc": uc, "v2/prim/bf1": bf[0], "v2/prim/bf2": bf[1], "v2/prim/bf3": bf[2], "v2/prim/pc": pc})
+    # godunov_fluxes on the extended block
+    pe = mhd_prims(rng, size(m)).ravel()
+    bfe = [rng.uniform(-1, 1, size(staggered(m, a, -1, 0))) for a in range(3)]
+    gf = [np.zeros(8 * size(staggered(m, a, -1, 0))) for a in range(3)]
+    assert rv.ref_mhd_v2_godunov_fluxes(*m32, dptr(pe), *[dptr(x) for x in bfe], *[dptr(x) for x in gf]) == 0
+    out.update({"v2/god/pc": pe, **{f"v2/god/bf{a + 1}": bfe[a] for a in range(3)},
+                **{f"v2/god/gf{a + 1}": gf[a] for a in range(3)}})
+    # electromotive_forces of those godunov data
+    ee = [np.zeros(size(staggered(m, a, 0, -1))) for a in range(3)]
+    assert rv.ref_mhd_v2_electromotive_forces(*m32, *[dptr(x) for x in gf], *[dptr(x) for x in ee]) == 0
+    out.update({f"v2/emf/ee{a + 1}": ee[a] for a in range(3)})
+    # updated_conserved_density with drawn godunov data (extended transversely)
+    uc2 = mhd_conserved(mhd_prims(rng, size(c)), V2_GAMMA).ravel()
+    gx = [rng.uniform(-1, 1, 8 * size(staggered(c, a, 1, 2))) for a in range(3)]
+    uo = np.zeros_like(uc2)
+    assert rv.ref_mhd_v2_updated_conserved_density(*i32, dptr(uc2), *[dptr(x) for x in gx], ctypes.c_double(0.013),
+                                                   ctypes.c_double(0.1), dptr(uo)) == 0
+    out.update({"v2/ucd/uc": uc2, **{f"v2/ucd/gf{a + 1}": gx[a] for a in range(3)}, "v2/ucd/out": uo,
+                "v2/ucd/dt_dl": np.array([0.013, 0.1])})
+    # curl of the block's own edges
+    ek = [rng.uniform(-1, 1, size(staggered(c, a, 0, 1))) for a in range(3)]
+    cf = [np.zeros(size(staggered(c, a, 1, 0))) for a in range(3)]
+    assert rv.ref_mhd_v2_curl(*i32, *[dptr(x) for x in ek], ctypes.c_double(0.1), *[dptr(x) for x in cf]) == 0
+    out.update({**{f"v2/curl/ee{a + 1}": ek[a] for a in range(3)}, **{f"v2/curl/cf{a + 1}": cf[a] for a in range(3)}})
+    # updated_magnetic_flux_density with the extended block's edge EMFs
+    bb = [rng.uniform(-1, 1, size(staggered(c, a, 1, 0))) for a in range(3)]
+    ex = [rng.uniform(-1, 1, size(staggered(c, a, 2, 1))) for a in range(3)]
+    bo = [np.zeros_like(x) for x in bb]
+    assert rv.ref_mhd_v2_updated_magnetic_flux_density(*i32, *[dptr(x) for x in bb], *[dptr(x) for x in ex],
+                                                       ctypes.c_double(0.013), ctypes.c_double(0.1),
+                                                       *[dptr(x) for x in bo]) == 0
+    out.update({**{f"v2/umfd/bf{a + 1}": bb[a] for a in range(3)}, **{f"v2/umfd/ee{a + 1}": ex[a] for a in range(3)},
+                **{f"v2/umfd/out{a + 1}": bo[a] for a in range(3)}})
+    return out
+
+
 def main() -> None:
+    if "--physics-only" in sys.argv:
+        r, rv = load_reference(), load_reference_v2()
+        if r is None or rv is None:
+            raise SystemExit("oracle/_ref is missing: run `make -C oracle ref` where the reference is present")
+        np.savez_compressed(HERE / "physics_golden.npz", **physics_fixtures(r), **mhd_v2_fixtures(rv))
+        return
     o = load_oracle()
     r = load_reference()
     if r is None:
@@ -427,6 +568,10 @@ def main() -> None:
     np.savez_compressed(HERE / "mhd_golden.npz", **mhd_fixtures(o, r))
     np.savez_compressed(HERE / "two_body_golden.npz", **two_body_fixture(r))
     np.savez_compressed(HERE / "sedov_golden.npz", **sedov_fixtures(o, r), **sedov_remesh_fixture(r))
+    rv = load_reference_v2()
+    if rv is None:
+        raise SystemExit("oracle/_ref/libref_v2.so is missing: run `make -C oracle ref`")
+    np.savez_compressed(HERE / "physics_golden.npz", **physics_fixtures(r), **mhd_v2_fixtures(rv))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size, "bytes")
 

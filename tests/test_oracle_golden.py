@@ -217,3 +217,72 @@ def test_mhd_reference_known_answers(oracle, mhd_golden):
     assert np.array_equal(cons, mhd_golden["mhd_kat/cons"])
     assert np.array_equal(back, mhd_golden["mhd_kat/back"])
     assert np.all(np.abs(back - kat) < 1e-10)
+
+
+# ---- mhd_scheme_v2 block operations: the numpy restatement against the
+# reference's own outputs (tests/golden/physics_golden.npz)
+
+@pytest.fixture(scope="module")
+def physics_golden():
+    from pathlib import Path
+    return dict(np.load(Path(__file__).resolve().parent / "golden" / "physics_golden.npz"))
+
+
+def _v2_shapes(g):
+    c = tuple(int(x) for x in g["v2/block"])
+    m = tuple(int(x) for x in g["v2/extended"])
+    stag = lambda s, a, grow, side: tuple(n + (grow if k == a else side) for k, n in enumerate(s))  # noqa: E731
+    return c, m, stag
+
+
+def test_mhd_v2_face_to_cell_matches_reference(physics_golden):
+    """primitive_array's cell fields are face_to_cell of the faces."""
+    from oracle import mhd_v2_oracle as v2
+    g = physics_golden
+    c, _, stag = _v2_shapes(g)
+    b = [g[f"v2/prim/bf{a + 1}"].reshape(stag(c, a, 1, 0)) for a in range(3)]
+    pc = g["v2/prim/pc"].reshape(*c, 8)
+    assert np.array_equal(v2.face_to_cell(*b), pc[..., 5:8])
+
+
+def test_mhd_v2_electromotive_forces_bitexact(physics_golden):
+    from oracle import mhd_v2_oracle as v2
+    g = physics_golden
+    _, m, stag = _v2_shapes(g)
+    gf = [g[f"v2/god/gf{a + 1}"].reshape(*stag(m, a, -1, 0), 8) for a in range(3)]
+    for a, e in enumerate(v2.electromotive_forces(*gf)):
+        assert e.shape == stag(m, a, 0, -1)
+        assert np.array_equal(e.ravel(), g[f"v2/emf/ee{a + 1}"])
+
+
+def test_mhd_v2_updated_conserved_density_bitexact(physics_golden):
+    from oracle import mhd_v2_oracle as v2
+    g = physics_golden
+    c, _, stag = _v2_shapes(g)
+    dt, dl = g["v2/ucd/dt_dl"]
+    gf = [g[f"v2/ucd/gf{a + 1}"].reshape(*stag(c, a, 1, 2), 8) for a in range(3)]
+    out = v2.updated_conserved_density(g["v2/ucd/uc"].reshape(*c, 5), *gf, dt, dl)
+    assert np.array_equal(out.ravel(), g["v2/ucd/out"])
+
+
+def test_mhd_v2_curl_and_flux_update_bitexact(physics_golden):
+    from oracle import mhd_v2_oracle as v2
+    g = physics_golden
+    c, _, stag = _v2_shapes(g)
+    dt, dl = g["v2/ucd/dt_dl"]
+    ee = [g[f"v2/curl/ee{a + 1}"].reshape(stag(c, a, 0, 1)) for a in range(3)]
+    for a, cf in enumerate(v2.curl(*ee, dl)):
+        assert np.array_equal(cf.ravel(), g[f"v2/curl/cf{a + 1}"])
+    bf = [g[f"v2/umfd/bf{a + 1}"].reshape(stag(c, a, 1, 0)) for a in range(3)]
+    ex = [g[f"v2/umfd/ee{a + 1}"].reshape(stag(c, a, 2, 1)) for a in range(3)]
+    for a, b in enumerate(v2.updated_magnetic_flux_density(*bf, *ex, dt, dl)):
+        assert np.array_equal(b.ravel(), g[f"v2/umfd/out{a + 1}"])
+
+
+def test_mhd_v2_curl_of_reference_is_divergence_free(physics_golden):
+    """A property of the reference's own curl output: div(curl E) = 0 to rounding."""
+    g = physics_golden
+    c, _, stag = _v2_shapes(g)
+    cf = [g[f"v2/curl/cf{a + 1}"].reshape(stag(c, a, 1, 0)) for a in range(3)]
+    div = np.diff(cf[0], axis=0) + np.diff(cf[1], axis=1) + np.diff(cf[2], axis=2)
+    assert np.abs(div).max() < 1e-13 * max(np.abs(x).max() for x in cf)
