@@ -14,7 +14,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from ._capi import MhdParams, check, lib
+from ._capi import MaraError, MhdParams, check, lib
 
 FP64, MIXED = 0, 1
 
@@ -129,6 +129,25 @@ class Run:
         check(lib.mara_mhd_advance(ctypes.byref(s.cfg.to_c()), _p(s.uc), _p(s.bf[0]), _p(s.bf[1]), _p(s.bf[2]),
                                    self.clock.buf.data_ptr(), steps, 2, self.precision, self.ws.data_ptr(), _stream()),
               "mhd advance")
+
+    def advance_checked(self, steps: int) -> None:
+        """advance(steps), failing where the reference throws: its
+        mhd::recover_primitive throws on a negative density or pressure
+        (src/physics_mhd.hpp:290-303), which ends examples/mhd3d. If any zone
+        failed during the call, the state and clock from before it are put
+        back and MaraError is raised."""
+        s = self.state
+        before = self.clock.read()["failures"]
+        snap = (s.uc.clone(), [b.clone() for b in s.bf], self.clock.buf.clone())
+        self.advance(steps)
+        failed = self.clock.read()["failures"] - before
+        if failed:
+            s.uc.copy_(snap[0])
+            for b, b0 in zip(s.bf, snap[1]):
+                b.copy_(b0)
+            self.clock.buf.copy_(snap[2])
+            raise MaraError(f"mhd advance: {failed} zone recoveries failed (negative density or pressure); "
+                            "the state before the call is restored")
 
     def max_div_b(self) -> float:
         out = torch.zeros(1, dtype=torch.float64, device="cuda")

@@ -18,7 +18,7 @@ import math
 import numpy as np
 import torch
 
-from ._capi import check, lib
+from ._capi import MaraError, check, lib
 
 GAMMA = 4.0 / 3.0
 
@@ -202,6 +202,89 @@ class Tracks:
     def failure_count(self) -> int:
         return int(self.failures.item())
 
+    def reset_failures(self) -> None:
+        self.failures.zero_()
+
+    def snapshot(self) -> dict:
+        """A device copy of the tracks' state (offsets, radii, conserved)."""
+        return {"co": self.co.clone(), "radii": self.radii.clone(), "u": self.u.clone(), "cells": self.cells,
+                "ncells": None if self._ncells is None else self._ncells.copy()}
+
+    def restore(self, snap: dict) -> None:
+        """Put back a snapshot's state (copied, so the snapshot stays usable)."""
+        self.co, self.radii, self.u = snap["co"].clone(), snap["radii"].clone(), snap["u"].clone()
+        self.cells = snap["cells"]
+        self._ncells = None if snap["ncells"] is None else snap["ncells"].copy()
+        nbytes = lib.mara_sedov_workspace_bytes(self.T, self.cells)
+        if self.workspace.numel() < nbytes:
+            self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=self.u.device)
+
     def host_state(self) -> tuple[np.ndarray, np.ndarray]:
         """(radii, u as (cells, 5) tuples) on the host."""
         return self.radii.cpu().numpy(), self.u.cpu().numpy().T.copy()
+
+
+class Driver:
+    """The time loop of problems/sedov2d.cpp:697-741 around `Tracks`, with its
+    safety mode: each step is the RK advance with dt = cfl * min spacing / c
+    (c = 1) followed by the remesh of every track. Where the reference
+    catches an exception (a failed primitive recovery, an HLLC contact speed
+    it rejects), the GPU counts failures; a step whose count is not zero is
+    handled as the reference handles the exception:
+      - at the iteration that failed last, the failure is final: the state
+        before the step is put back and MaraError is raised;
+      - otherwise the state before the last successful step is restored
+        (the reference's backup) and the next step runs in safety mode,
+        dt x 1e-3 and PLM off; a successful step leaves safety mode.
+    As in the reference, a failure at iteration 0 is final (its backup is
+    empty and the iteration of the last failure starts at 0). The failure
+    count is read after the advance and again after the remesh (one host
+    synchronisation each); a failed advance skips the remesh, as the
+    reference's exception does.
+
+    tracks: a Tracks (or anything with its advance / remesh / min_spacing /
+    snapshot / restore / reset_failures / failure_count methods);
+    ghosts(time) -> (ghost_in, ghost_out), each (rk_order, T, 5) boundary
+    primitives for the step starting at `time`."""
+
+    def __init__(self, tracks, ghosts, cfl: float = 0.5, rk_order: int = 1, max_aspect: float = 2.0,
+                 min_aspect: float = 0.5, inner_radius: float = 1.0, time: float = 0.0, iteration: int = 0):
+        self.tracks = tracks
+        self.ghosts = ghosts
+        self.cfl, self.rk_order = cfl, rk_order
+        self.max_aspect, self.min_aspect, self.inner_radius = max_aspect, min_aspect, inner_radius
+        self.time, self.iteration = time, iteration
+        self.backup = None           # (snapshot, time, iteration) before the last successful step
+        self.safety = False
+        self.failed_iter = 0
+
+    def step(self) -> dict:
+        """One step of the loop; returns what it did (dt, whether it was a
+        safety-mode step, whether it rolled back)."""
+        t = self.tracks
+        safety = self.safety
+        dt = self.cfl * (1e-3 if safety else 1.0) * t.min_spacing()
+        ghost_in, ghost_out = self.ghosts(self.time)
+        pre = (t.snapshot(), self.time, self.iteration)
+        t.reset_failures()
+        t.advance(dt, ghost_in, ghost_out, rk_order=self.rk_order, use_plm=not safety)
+        failures = t.failure_count()
+        if failures == 0:
+            # the reference's exception would skip the remesh: so does a failed advance
+            t.remesh(self.max_aspect, self.min_aspect, self.inner_radius)
+            failures = t.failure_count()
+        if failures == 0:
+            self.time += dt
+            self.iteration += 1
+            self.backup = pre
+            self.safety = False
+            return {"dt": dt, "safety": safety, "rolled_back": False, "iteration": self.iteration}
+        if self.iteration == self.failed_iter:
+            t.restore(pre[0])
+            raise MaraError(f"sedov step {self.iteration} failed ({failures} failed zones, faces or tracks) and "
+                            "cannot be retried: it is the first step, or the step that failed last")
+        self.failed_iter = self.iteration
+        snap, self.time, self.iteration = self.backup
+        t.restore(snap)
+        self.safety = True
+        return {"dt": dt, "safety": safety, "rolled_back": True, "iteration": self.iteration, "failures": failures}

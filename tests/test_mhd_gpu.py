@@ -147,3 +147,22 @@ def test_mixed_close_to_fp64_and_divergence_free(mh):
     b_scale = max(float(x.abs().max()) for x in b.bf)
     assert rb.max_div_b() < 1e-13 * b_scale
     assert rb.clock.read()["failures"] == 0
+
+
+def test_advance_checked_restores_and_raises_on_failed_zones(mh):
+    """A zone whose energy is set negative on the host fails its recovery
+    (the reference throws there): advance_checked puts the state back and
+    raises; an unpoisoned run advances normally."""
+    from mara3p_gb300._capi import MaraError
+    cfg = mh.MhdConfig(N=16)
+    s = mh.initial_state(cfg, seed=4, modes=8)
+    run = mh.Run(s)
+    run.advance_checked(2)
+    assert run.clock.read()["iteration"] == 2
+    s.uc[4, 3, 4, 5] = -10.0
+    before = [s.uc.clone()] + [b.clone() for b in s.bf]
+    t0 = run.clock.read()["time"]
+    with pytest.raises(MaraError, match="restored"):
+        run.advance_checked(1)
+    assert torch.equal(s.uc, before[0]) and all(torch.equal(b, b0) for b, b0 in zip(s.bf, before[1:]))
+    assert run.clock.read()["time"] == t0
