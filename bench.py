@@ -1056,14 +1056,15 @@ def compact(line: dict) -> dict:
 def other_workloads(args) -> dict:
     """Short runs of the other workloads (mixed precision, their own default
     sizes), each timed as its own --workload run times it, for the headline
-    line: MHD 128^3, the 2^24-zone SRHD recovery, the 1024^2 shock tube, the
-    64-member ensemble and the 1024-track sedov step."""
+    line: the 256^2 minidisk, MHD 128^3, the 2^24-zone SRHD recovery, the
+    1024^2 shock tube, the 64-member ensemble and the 1024-track sedov step."""
     import argparse as ap_
     import gc
 
     import torch
     out = {}
-    for name, fn in RUNNERS.items():
+    runners = {"minidisk-256": "run_ours", **RUNNERS}
+    for name, fn in runners.items():
         sub = ap_.Namespace(**vars(args))
         sub.workload = name
         sub.precision = "mixed"
@@ -1072,7 +1073,8 @@ def other_workloads(args) -> dict:
         sub.no_cpu_baseline = name != "sedov-tracks"
         sub.no_looped = False
         sub.launch = None
-        sub.accuracy_steps = 50
+        sub.accuracy_steps = 100 if name == "minidisk-256" else 50   # configuration 1 runs 100 steps
+        sub.no_diagnostics_timing = True
         t0 = time.perf_counter()
         line = globals()[fn](sub)
         torch.cuda.synchronize()
