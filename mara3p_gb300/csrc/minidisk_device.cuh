@@ -4,6 +4,7 @@
 // slopes, the HLLE + viscous face flux, the mixed cell update and the
 // warp-strip sweep of one strip segment.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "common.cuh"
@@ -766,8 +767,144 @@ __device__ inline void slope_y2(const float2 p[3], float two_theta, float2 g[3],
     }
 }
 
-template<int KIND, bool DIAG = false, bool RING = false>
-__device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy, Ring2 ring = Ring2{})
+// The same five-row ring filled by the tensor memory accelerator: for each
+// row one elected lane issues one bulk tensor copy of the strip's 64 columns
+// of the three FP64 components (box 64 x 1 x 3 of the [3][N][N] state), and
+// in stage 2 one of the FP32 increment (box 68 x 1 x 3 from column j0 - 4, so
+// that the box starts on a 16-byte boundary), completing on the slot's
+// mbarrier. The lanes wait on the barrier (a bounded wait) and read their
+// two columns as from the per-lane ring. Strips whose 64 columns wrap across
+// the periodic seam (the first and the last) keep the per-lane ring: a box
+// cannot wrap.
+constexpr int TRING_U_SLOT = 3 * 64 * 8;                     // 1536 B per slot: 3 components x 64 doubles
+constexpr int TRING_D_COLS = 68;                             // floats per component row of the increment box
+constexpr int TRING_D_SLOT = 896;                            // 3 x 68 floats (816 B), padded to 128-byte slots
+constexpr int TRING_BAR_OFFSET = RING_ROWS * (TRING_U_SLOT + TRING_D_SLOT);
+constexpr int TRING_WARP_BYTES = TRING_BAR_OFFSET + 128;     // + five mbarriers: 12288 B per warp
+static_assert(TRING_WARP_BYTES >= RING_WARP_BYTES, "the per-lane ring must fit in a TMA ring's region");
+static_assert(TRING_U_SLOT % 128 == 0 && TRING_D_SLOT % 128 == 0 && TRING_WARP_BYTES % 128 == 0,
+              "bulk tensor copies land on 128-byte boundaries");
+
+struct RingT
+{
+    unsigned char* base;       // 128-byte aligned: u slots, then d slots, then the barriers
+    const CUtensorMap* umap;   // [3][N][N] FP64 state, box 64 x 1 x 3
+    const CUtensorMap* dmap;   // [3][N][N] FP32 increment, box 68 x 1 x 3 (stage 2)
+    int xu, xd;                // first column of the boxes: j0 - 2, j0 - 4 (both 16-byte aligned)
+    int row0;                  // first row fetched (i0 - 2); fetches follow in row order
+    int last_fetch, last_wait; // highest row fetched / waited for
+    bool broken;               // a copy did not complete in time: rows come from global memory from then on
+};
+
+// a strip whose 64 columns j0 - 2 .. j0 + 61 (and the increment box's 68
+// from j0 - 4) lie inside the mesh
+__host__ __device__ inline bool tma_strip(int sy, int N) { return sy >= 1 && sy * SW2_COLS + 64 <= N; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ uint32_t tring_bar(const RingT& R, int slot)
+{
+    return smem_u32(R.base + TRING_BAR_OFFSET + 8 * slot);
+}
+
+__device__ inline void tring_init(RingT& R, int lane)
+{
+    if (lane == 0)
+    {
+        for (int s = 0; s < RING_ROWS; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(tring_bar(R, s)), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+}
+
+// Row `row` into its slot. Every lane has finished reading the row the slot
+// held before (its last read was an iteration ago); the proxy fence orders
+// those reads before the copy's writes.
+template<int KIND>
+__device__ inline void tring_fetch(const Args& A, RingT& R, int row, int lane)
+{
+    if (R.broken) return;
+    const int slot = ring_slot(row);
+    __syncwarp();
+    if (lane == 0)
+    {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const uint32_t bar = tring_bar(R, slot);
+        const uint32_t bytes = TRING_U_SLOT + (KIND == K_MIX2 ? 3 * TRING_D_COLS * 4 : 0);
+        const int r = wrap1(row, A.N);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                     " [%0], [%1, {%2, %3, %4}], [%5];"
+                     :: "r"(smem_u32(R.base + slot * TRING_U_SLOT)), "l"(reinterpret_cast<uint64_t>(R.umap)),
+                        "r"(R.xu), "r"(r), "r"(0), "r"(bar)
+                     : "memory");
+        if (KIND == K_MIX2)
+            asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2, %3, %4}], [%5];"
+                         :: "r"(smem_u32(R.base + RING_ROWS * TRING_U_SLOT + slot * TRING_D_SLOT)),
+                            "l"(reinterpret_cast<uint64_t>(R.dmap)), "r"(R.xd), "r"(r), "r"(0), "r"(bar)
+                         : "memory");
+    }
+    R.last_fetch = row;
+}
+
+// Bounded wait for row `row` (the phase of its slot's barrier that its fetch
+// completes: the k-th fetch into a slot completes phase k, and with fetches
+// in row order k = (row - row0) / 5). True where every lane saw it complete.
+__device__ inline bool tring_wait(const RingT& R, int row)
+{
+    const uint32_t bar = tring_bar(R, ring_slot(row));
+    const uint32_t parity = uint32_t((row - R.row0) / RING_ROWS) & 1u;
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 20) && !done; ++it)
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    return __all_sync(0xffffffffu, done != 0);
+}
+
+// This lane's two columns of row `row` from its slot (the row has arrived)
+template<int KIND>
+__device__ inline void tring_row(const RingT& R, int row, int lane, RawRow2& r)
+{
+    const int slot = ring_slot(row);
+    const double2* u = reinterpret_cast<const double2*>(R.base + slot * TRING_U_SLOT);
+    for (int k = 0; k < 3; ++k) r.u[k] = u[k * 32 + lane];
+    if (KIND == K_MIX2)
+    {
+        // float index k * 68 + (2 lane + 2): the box starts two columns left of the strip
+        const float2* d = reinterpret_cast<const float2*>(R.base + RING_ROWS * TRING_U_SLOT + slot * TRING_D_SLOT);
+        for (int k = 0; k < 3; ++k) r.d[k] = d[k * (TRING_D_COLS / 2) + lane + 1];
+    }
+}
+
+// Row `row` for the recovery: from the ring once it has arrived, else (a
+// timed-out copy) from global memory, for this row and every later one.
+template<int KIND>
+__device__ inline void tring_get(const Args& A, RingT& R, int row, int jg, size_t NN, int lane, RawRow2& r)
+{
+    if (!R.broken)
+    {
+        if (tring_wait(R, row))
+        {
+            R.last_wait = row;
+            tring_row<KIND>(R, row, lane, r);
+            return;
+        }
+        R.broken = true;
+    }
+    sweep2_fetch<KIND>(A, row, jg, NN, r);
+}
+
+// Before the warp leaves: wait (bounded) for the rows fetched but not
+// waited for, so that no copy lands in shared memory after the warp is gone.
+__device__ inline void tring_drain(const RingT& R)
+{
+    for (int row = R.last_wait + 1; row <= R.last_fetch; ++row) tring_wait(R, row);
+}
+
+template<int KIND, bool DIAG = false, int RING = 0>
+__device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int sy, Ring2 ring = Ring2{},
+                                             RingT* tma = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int N = A.N;
@@ -797,7 +934,26 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
 
     float2 pm2[3], pm1[3], p0[3], p1[3];
     RawRow2 raw;
-    if constexpr (RING)
+    if constexpr (RING == 2)
+    {
+        RingT& T = *tma;
+        T.row0 = i0 - 2;
+        T.last_fetch = T.last_wait = i0 - 3;
+        T.broken = false;
+        tring_init(T, lane);
+        for (int r = i0 - 2; r <= i0 + 1; ++r) tring_fetch<KIND>(A, T, r, lane);
+        tring_get<KIND>(A, T, i0 - 2, jg, NN, lane, raw);
+        sweep2_prim<KIND>(raw, pm2);
+        tring_get<KIND>(A, T, i0 - 1, jg, NN, lane, raw);
+        sweep2_prim<KIND>(raw, pm1);
+        tring_get<KIND>(A, T, i0, jg, NN, lane, raw);
+        sweep2_prim<KIND>(raw, p0);
+        tring_get<KIND>(A, T, i0 + 1, jg, NN, lane, raw);
+        sweep2_prim<KIND>(raw, p1);
+        tring_fetch<KIND>(A, T, i0 + 2, lane);     // into the fifth, free slot
+        tring_fetch<KIND>(A, T, i0 + 3, lane);     // into the slot of row i0 - 2
+    }
+    else if constexpr (RING == 1)
     {
         for (int r = i0 - 2; r <= i0 + 1; ++r) ring2_fetch<KIND>(A, ring, r, jg, NN, lane);
         cp_async_wait_all();
@@ -842,7 +998,13 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     {
         float2 p2[3], gx1[3], gy1[3], fxp[3];
         CellIn<float2> cin;
-        if constexpr (RING)
+        if constexpr (RING == 2)
+        {
+            tring_get<KIND>(A, *tma, i + 2, jg, NN, lane, raw);
+            sweep2_prim<KIND>(raw, p2);
+            tring_fetch<KIND>(A, *tma, i + 4, lane);              // into the slot of row i-1
+        }
+        else if constexpr (RING == 1)
         {
             const int slot2 = slot0 >= RING_ROWS - 2 ? slot0 + 2 - RING_ROWS : slot0 + 2;
             const int slot4 = slot0 == 0 ? RING_ROWS - 1 : slot0 - 1;
@@ -881,7 +1043,24 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
             dfy[k] = vsub(make_float2(fy[k].y, right), fy[k]);
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
-        if constexpr (RING)
+        if constexpr (RING == 2)
+        {
+            if (interior && writes_state<KIND>(A))
+            {
+                if (!tma->broken)
+                {
+                    RawRow2 own;
+                    tring_row<KIND>(*tma, i, lane, own);
+                    for (int k = 0; k < 3; ++k)
+                    {
+                        cin.u[k] = own.u[k];
+                        cin.d[k] = own.d[k];
+                    }
+                }
+                else load_cell_in<KIND>(A, size_t(i) * N + jg, NN, cin);
+            }
+        }
+        else if constexpr (RING == 1)
         {
             if (interior && writes_state<KIND>(A))
             {
@@ -911,7 +1090,8 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     }
     // the rows fetched beyond the strip are never read, but no copy may land
     // in shared memory after the warp is gone
-    if constexpr (RING) cp_async_wait_all();
+    if constexpr (RING == 1) cp_async_wait_all();
+    if constexpr (RING == 2) tring_drain(*tma);
     if constexpr (DIAG) diag_flush(A, acc);
     if (A.amax) flush_speed_key(A, local_key);
 }

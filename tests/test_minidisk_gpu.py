@@ -238,6 +238,29 @@ def test_mixed_long_horizon_config2_physics(md):
     assert abs(a.time - b.time) <= 1e-6 * a.time
 
 
+@pytest.mark.parametrize("block_size,depth", [(64, 3), (100, 2), (128, 5)])
+def test_sweep_tma_ring_bit_identical(md, block_size, depth):
+    """Rows staged by bulk tensor copies and by per-lane asynchronous copies
+    (the default) give bit-identical states and clocks: meshes of 512^2,
+    400^2 (strips of both kinds) and 4096^2."""
+    from mara3p_gb300._capi import lib
+    sd = md.SolverData(**dict(CONFIG2_PARAMS, block_size=block_size, depth=depth))
+    u0 = md.initial_conserved(sd, seed=31, amplitude=0.01)
+    out = []
+    try:
+        for tma in (1, 0):
+            assert lib.mara_minidisk_sweep_tma(tma) in (0, 1)
+            run = md.Run(sd, u0.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL)
+            run.advance(6)
+            torch.cuda.synchronize()
+            out.append((run.u.clone(), run.clock.clone()))
+    finally:
+        lib.mara_minidisk_sweep_tma(0)
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
+    assert lib.mara_minidisk_sweep_tma(2) == -1
+
+
 def test_mass_conservation_full_size(md):
     """Size-independent property at the config-2 size (4096^2): with sinks,
     buffer and viscosity off, the flux divergence telescopes and total mass
