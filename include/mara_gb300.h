@@ -392,6 +392,14 @@ int mara_mhd_mode_table(uint64_t seed, int32_t modes, double* table);
 int mara_mhd_initial_state(const mara_mhd_params* mp, const double* table, int32_t modes, double v_amp, double a_amp,
                            double* uc, double* bf1, double* bf2, double* bf3, void* workspace, void* stream);
 
+/* The mixed stage as two fused launches (enable 1, the default; meshes with
+ * N a multiple of 32: face solves and cell updates, then edge EMFs, face
+ * updates and the next stage's primitives) or as the primitive, face and
+ * update kernels (enable 0). Both give identical results. chunks > 0 fixes
+ * the fused kernels' number of i-chunks (0 chooses it from the SM count).
+ * Process-wide; no counterpart in the reference. */
+int mara_mhd_fused_stage(int32_t enable, int32_t chunks);
+
 /* max over cells of |div B| * dl (sum of the face differences), into *out (device double). */
 int mara_mhd_max_div_b(const mara_mhd_params* mp, const double* bf1, const double* bf2, const double* bf3,
                        double* out, void* stream);

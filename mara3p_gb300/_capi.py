@@ -136,6 +136,7 @@ class MhdParams(ctypes.Structure):
 _HP = ctypes.POINTER(MhdParams)
 SIGNATURES.update({
     "mara_mhd_clock_bytes": (ctypes.c_int64, []),
+    "mara_mhd_fused_stage": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
     "mara_mhd_clock_init": (ctypes.c_int, [_vp, ctypes.c_double, _vp]),
     "mara_mhd_workspace_bytes": (ctypes.c_int64, [_HP, ctypes.c_int32, ctypes.c_int32]),
     "mara_mhd_advance_ct": (ctypes.c_int, [_HP, _vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,

@@ -4,7 +4,7 @@
 // src/mesh_cartesian_3d.hpp:236-305) and the RK2 driver of
 // examples/mhd3d.cpp:78-88,186-215.
 //
-// One stage = four kernels:
+// One stage = four kernels (FP64, or the mixed path with the fused stage off):
 //   prim_kernel     face_to_cell + recover_primitive of every cell into P[N^3][8];
 //                   fastest wavespeed reduced into the clock (CFL dt)
 //   dt_kernel       dt = cfl * dl / max speed (scheme_mhd_v1.cpp:287)
@@ -16,6 +16,9 @@
 //                   u -= div(F) dt/dl; B.dA -= curl(E_edge) dt/dl, edge EMFs by
 //                   the reference's face averaging (edge_emf_from_face);
 //                   optionally averaged with the RK partner state.
+// The mixed path on meshes with N a multiple of 32 replaces the face and
+// update kernels by two fused launches (flux_kernel, emf_kernel, below) that
+// also recover the next stage's primitives, with identical results.
 // Layout: uc SoA [5][N][N][N] (any (component, cell) stride pair on input to
 // the drop-in call); bf1 [N+1][N][N], bf2 [N][N+1][N], bf3 [N][N][N+1] as the
 // reference holds them (the two periodic boundary layers stay identical).
@@ -91,6 +94,7 @@ struct Args
     Clock* clock;
     int stage;
     float* dinc;                                 // [5][N^3] mixed RK2 stage-1 increments
+    const double* next_uc;                       // fused mixed path: SoA state the next stage recovers from
 };
 
 // Cell updates of the mixed path (a template argument of the prim and update
@@ -184,6 +188,44 @@ __device__ inline void load_cell(const double* P, size_t c, double out[8])
     }
 }
 
+// The mixed recovery of cell c: face_to_cell in FP32 from the FP64 face
+// fields, then recover_primitive (physics_mhd.hpp:290-303) in FP32 from the
+// FP64 state (integer conversions, one reciprocal); only the energy
+// difference E - kinetic - magnetic is taken in FP64. MIX_FROM_INCREMENT
+// recovers u0 + the FP32 stage-1 increment. True where the reference throws
+// (negative density or pressure). One function for the primitive kernel and
+// the EMF kernel's next-stage recovery, so that both compile the same arithmetic.
+struct Field3 { float b[3]; };
+__device__ __forceinline__ Field3 cell_field(double x0, double x1, double y0, double y1, double z0, double z1)
+{
+    return Field3{{0.5f * (d2f(x0) + d2f(x1)), 0.5f * (d2f(y0) + d2f(y1)), 0.5f * (d2f(z0) + d2f(z1))}};
+}
+
+template<int MODE>
+__device__ __forceinline__ bool recover_mixed(const double* uc, int64_t ucs, int64_t uzs, const float* dinc, int64_t NN,
+                                              int64_t c, const Field3 f, float gm, Prim<float>& p)
+{
+    const double energy = uc[4 * ucs + c * uzs];
+    p.d = d2f(uc[c * uzs]);
+    float S[3] = {d2f(uc[ucs + c * uzs]), d2f(uc[2 * ucs + c * uzs]), d2f(uc[3 * ucs + c * uzs])};
+    float de = 0.0f;   // energy increment, folded into the FP64 difference below
+    if (MODE == MIX_FROM_INCREMENT)
+    {
+        p.d = __fadd_rn(p.d, dinc[c]);
+        for (int q = 0; q < 3; ++q) S[q] = __fadd_rn(S[q], dinc[(q + 1) * NN + c]);
+        de = dinc[4 * NN + c];
+    }
+    const float inv = rcp_fast(p.d);
+    for (int q = 0; q < 3; ++q)
+    {
+        p.v[q] = div_corrected(S[q], p.d, inv);
+        p.b[q] = f.b[q];
+    }
+    const float kin_mag = 0.5f * sum3(S, p.v) + 0.5f * sum3(f.b, f.b);
+    p.p = d2f(energy - f2d(__fsub_rn(kin_mag, de))) * (gm - 1.0f);
+    return p.d < 0.0f || p.p < 0.0f;
+}
+
 // ---------------------------------------------------------------- kernels
 template<typename R, int MODE>
 __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_kernel(const Args A)
@@ -204,32 +246,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
         const uint32_t x1 = x0 + uint32_t(N) * N, y1 = y0 + N, z1 = z0 + 1;
         if constexpr (sizeof(R) == sizeof(float))
         {
-            // Mixed: the recovery in FP32 from the FP64 state (integer conversions,
-            // one reciprocal); only the energy difference E - kinetic - magnetic
-            // is taken in FP64.
-            const float b[3] = {0.5f * (d2f(A.bf[0][x0]) + d2f(A.bf[0][x1])), 0.5f * (d2f(A.bf[1][y0]) + d2f(A.bf[1][y1])),
-                                0.5f * (d2f(A.bf[2][z0]) + d2f(A.bf[2][z1]))};
-            const double energy = A.uc[4 * A.ucs + c * A.uzs];
             Prim<float> p;
-            p.d = d2f(A.uc[c * A.uzs]);
-            float S[3] = {d2f(A.uc[A.ucs + c * A.uzs]), d2f(A.uc[2 * A.ucs + c * A.uzs]),
-                          d2f(A.uc[3 * A.ucs + c * A.uzs])};
-            float de = 0.0f;   // energy increment, folded into the FP64 difference below
-            if (MODE == MIX_FROM_INCREMENT)
-            {
-                p.d = __fadd_rn(p.d, A.dinc[c]);
-                for (int q = 0; q < 3; ++q) S[q] = __fadd_rn(S[q], A.dinc[(q + 1) * NN + c]);
-                de = A.dinc[4 * NN + c];
-            }
-            const float inv = rcp_fast(p.d);
-            for (int q = 0; q < 3; ++q)
-            {
-                p.v[q] = div_corrected(S[q], p.d, inv);
-                p.b[q] = b[q];
-            }
-            const float kin_mag = 0.5f * sum3(S, p.v) + 0.5f * sum3(b, b);
-            p.p = d2f(energy - f2d(__fsub_rn(kin_mag, de))) * (gm - 1.0f);
-            if (p.d < 0.0f || p.p < 0.0f) ++bad;
+            if (recover_mixed<MODE>(A.uc, A.ucs, A.uzs, A.dinc, NN, c,
+                                    cell_field(A.bf[0][x0], A.bf[0][x1], A.bf[1][y0], A.bf[1][y1], A.bf[2][z0], A.bf[2][z1]),
+                                    gm, p))
+                ++bad;
             store_cell(P, c, p);
             mf = fmaxf(mf, fastest_speed(p, gm));
             continue;
@@ -277,18 +298,44 @@ __global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 5 : 3) prim_
     }
 }
 
+// begin: both stages' wavespeed maxima to zero. Otherwise dt of `stage`, and
+// the other stage's maximum to zero (it was consumed by that stage's dt; the
+// fused mixed path accumulates the next stage's maximum during this stage).
 __global__ void dt_kernel(Clock* clock, int stage, double cfl, double dl, int begin)
 {
     if (threadIdx.x != 0) return;
     if (begin) { clock->amax[0] = 0ull; clock->amax[1] = 0ull; }
-    else clock->dt[stage] = cfl * dl / __longlong_as_double((long long)clock->amax[stage]);
+    else
+    {
+        clock->dt[stage] = cfl * dl / __longlong_as_double((long long)clock->amax[stage]);
+        clock->amax[stage ^ 1] = 0ull;
+    }
+}
+
+// PLM face states from the four cells l-2 .. l+1 along AXIS (a, b | c, d)
+// and the HLLE flux and transverse E-field of the face (godunov_fluxes_plm,
+// scheme_mhd_v1.cpp:152-178). One function for the face kernels and the
+// fused stage kernel, so that both compile the same arithmetic.
+template<typename R, int AXIS>
+__device__ __forceinline__ void face_solve(const R xa[8], const R xb[8], const R xc[8], const R xd[8], R bl, R gm,
+                                           R theta, R F[5], R E[2])
+{
+    R L[8], Rr[8];
+    for (int q = 0; q < 8; ++q)
+    {
+        const R a = xa[q], b = xb[q], cc = xc[q], d = xd[q];
+        L[q] = b + R(0.5) * plm(a, b, cc, theta);
+        Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
+    }
+    Prim<R> pl{L[0], {L[1], L[2], L[3]}, L[4], {L[5], L[6], L[7]}};
+    Prim<R> pr{Rr[0], {Rr[1], Rr[2], Rr[3]}, Rr[4], {Rr[5], Rr[6], Rr[7]}};
+    riemann_hlle<R, AXIS>(pl, pr, bl, gm, F, E);
 }
 
 template<typename R, int AXIS>
 __global__ void face_kernel(const Args A)
 {
     const int N = A.N;
-    const size_t NN = size_t(N) * N * N;
     const uint32_t NF = nb32(N, AXIS);
     const R* P = static_cast<const R*>(A.P);
     R* F = static_cast<R*>(A.F[AXIS]);
@@ -310,18 +357,8 @@ __global__ void face_kernel(const Args A)
         load_cell(P, cm1, xb);
         load_cell(P, c0, xc);
         load_cell(P, cp1, xd);
-        R L[8], Rr[8];
-        for (int q = 0; q < 8; ++q)
-        {
-            const R a = xa[q], b = xb[q], cc = xc[q], d = xd[q];
-            L[q] = b + R(0.5) * plm(a, b, cc, theta);
-            Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
-        }
-        Prim<R> pl{L[0], {L[1], L[2], L[3]}, L[4], {L[5], L[6], L[7]}};
-        Prim<R> pr{Rr[0], {Rr[1], Rr[2], Rr[3]}, Rr[4], {Rr[5], Rr[6], Rr[7]}};
-        const R bl = R(A.bf[AXIS][f]);
         R fl[5], e[2];
-        riemann_hlle<R, AXIS>(pl, pr, bl, gm, fl, e);
+        face_solve<R, AXIS>(xa, xb, xc, xd, R(A.bf[AXIS][f]), gm, theta, fl, e);
         for (int q = 0; q < 5; ++q) F[q * size_t(NF) + f] = fl[q];
         E[f] = e[0];
         E[size_t(NF) + f] = e[1];
@@ -543,6 +580,415 @@ update_kernel(const Args A)
     }
 }
 
+// ---------------------------------------------------------------- fused mixed stage
+// The mixed stage as two launches in place of the three face kernels and the
+// two update launches, with the same arithmetic (the results are identical).
+// Both own a TJ x TK column of cells (j, k) per block and march along i over
+// a chunk [i0, i1) of cell planes.
+//
+// flux_kernel: per plane c, the x faces of layer c+1 and the y and z faces of
+// plane c (each tile solves its own faces and those of the high neighbour
+// row / column that its cells need: no face is solved by more than two
+// tiles), then the cells of plane c from the fluxes held in shared memory.
+// The face E-fields go to global memory (F never does).
+//
+// emf_kernel: per plane c, the face E-fields of layer c and planes c-1, c
+// (with a one-face halo) into shared memory, the edge EMFs at i = c, then the
+// x faces of layer c and the y and z faces of plane c-1 (they need the EMFs of
+// the plane above, so they trail by one plane), and then, optionally, the
+// primitives of the next RK stage for the cells of plane c-1 from the
+// updated state and faces, with the next stage's fastest wavespeed: the
+// primitive kernel runs only for the first stage of a call.
+namespace fused {
+constexpr int TJ = 8, TK = 32, THREADS = 256;
+// Face E-fields in the EMF kernel, rows of XK (YK, ZK) floats with element
+// kk at row offset kk + 4 (kk + 1 for z), so that the x and y rows' interior
+// kk in [0, TK) is 16-byte aligned for vector copies
+constexpr int XK = TK + 8, XN = (TJ + 2) * XK;      // x-face E: jj in [-1, TJ], kk in [-1, TK]
+constexpr int YK = TK + 8, YN = (TJ + 1) * YK;      // y-face E: jj in [0, TJ], kk in [-1, TK]
+constexpr int ZK = TK + 1, ZN = (TJ + 2) * ZK;      // z-face E: jj in [-1, TJ], kk in [0, TK]
+constexpr int XO = 4, YO = 4;                       // row offset of kk = 0
+constexpr int FXN = TJ * TK;                        // x faces of the tile
+constexpr int FYN = (TJ + 1) * TK;                  // y faces: jj in [0, TJ], kk in [0, TK)
+constexpr int FZK = TK + 1, FZN = TJ * FZK;         // z faces: jj in [0, TJ), kk in [0, TK]
+constexpr int E0K = TK + 1, E0N = (TJ + 1) * E0K;   // EMFs along i: jj in [0, TJ], kk in [0, TK]
+constexpr int E1K = TK + 1, E1N = TJ * E1K;         // along j: jj in [0, TJ), kk in [0, TK]
+constexpr int E2K = TK, E2N = (TJ + 1) * E2K;       // along k: jj in [0, TJ], kk in [0, TK)
+constexpr int pad32(int n) { return (n + 31) & ~31; }
+// work items per phase, each kind padded to whole warps so that no warp mixes kinds
+constexpr int SOLVE_Y = pad32(FYN), SOLVE_Z = pad32(FZN);
+constexpr int EDGE_0 = pad32(E0N), EDGE_1 = pad32(E1N), EDGE_2 = pad32(E2N);
+// copies per plane: x and y rows as TK/4 16-byte pieces plus the two halo
+// elements; z rows (N + 1 floats, unaligned) element by element
+constexpr int ROW_PIECES = TK / 4 + 2;
+constexpr int LOAD_X = 2 * (TJ + 2) * ROW_PIECES, LOAD_Y = 2 * (TJ + 1) * ROW_PIECES, LOAD_Z = 2 * ZN;
+
+struct FluxSmem
+{
+    float fx[2][5][FXN];       // x-face fluxes; layer l in slot l & 1
+    float fy[5][FYN];          // y-face fluxes of plane c
+    float fz[5][FZN];
+};
+
+struct __align__(16) EmfSmem
+{
+    float ex[2][2][XN];        // x-face E components 1, 2; layer l in slot l & 1
+    float ey[4][2][YN];        // y-face E components 0, 2; plane p in slot p & 3
+    float ez[4][2][ZN];        // z-face E components 0, 1
+    float e0[2][E0N], e1[2][E1N], e2[2][E2N];
+    double bx[2][FXN];         // updated x faces; layer l in slot l & 1
+    double by[FYN];            // updated y faces of plane c-1 (row TJ: the neighbour's, for the cells)
+    double bz[FZN];
+    double wmax[THREADS / 32];
+    unsigned long long wbad[THREADS / 32];
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ float avg(float x, float y) { return __fmul_rn(0.5f, __fadd_rn(x, y)); }
+
+struct Tile
+{
+    int j0, k0, i0, i1;
+    bool last_j, last_k;
+};
+
+__device__ __forceinline__ Tile tile_of(int N, int chunks)
+{
+    const int tiles_k = N / TK, tiles = (N / TJ) * tiles_k;
+    const int chunk = int(blockIdx.x) / tiles, tile = int(blockIdx.x) - chunk * tiles;
+    Tile t;
+    t.j0 = (tile / tiles_k) * TJ;
+    t.k0 = (tile % tiles_k) * TK;
+    t.i0 = int(int64_t(chunk) * N / chunks);
+    t.i1 = int(int64_t(chunk + 1) * N / chunks);
+    t.last_j = t.j0 + TJ == N;
+    t.last_k = t.k0 + TK == N;
+    return t;
+}
+} // namespace fused
+
+// The four primitive records of a face stencil, read from global memory (the
+// primitive array is small enough to stay in L2).
+__device__ __forceinline__ void stencil(const float* P, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, float xa[8],
+                                        float xb[8], float xc[8], float xd[8])
+{
+    load_cell(P, c0, xa);
+    load_cell(P, c1, xb);
+    load_cell(P, c2, xc);
+    load_cell(P, c3, xd);
+}
+
+template<int MODE>
+__global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, int chunks)
+{
+    using namespace fused;
+    __shared__ FluxSmem S;
+    __shared__ float s_dtdl;
+    const int N = A.N;
+    const Tile T = tile_of(N, chunks);
+    const float* P = static_cast<const float*>(A.P);
+    const float gm = float(A.gamma), theta = float(A.theta);
+    const int64_t NN = int64_t(N) * N * N;
+    const uint32_t nbv[3] = {nb32(N, 0), nb32(N, 1), nb32(N, 2)};
+    float* E0 = static_cast<float*>(A.E[0]);
+    float* E1 = static_cast<float*>(A.E[1]);
+    float* E2 = static_cast<float*>(A.E[2]);
+    if (threadIdx.x == 0) s_dtdl = float(A.clock->dt[A.stage] / A.dl);
+
+    // x faces of layer lx over the tile: fluxes into slot lx & 1, E-fields
+    // out when this chunk owns the layer
+    auto solve_x = [&](int t, int lx, bool write_e) {
+        const int jj = t / TK, kk = t - jj * TK;
+        const int j = T.j0 + jj, k = T.k0 + kk;
+        float xa[8], xb[8], xc[8], xd[8], F[5], Ef[2];
+        stencil(P, cidx32(N, wrap(lx - 2, N), j, k), cidx32(N, wrap(lx - 1, N), j, k), cidx32(N, wrap(lx, N), j, k),
+                cidx32(N, wrap(lx + 1, N), j, k), xa, xb, xc, xd);
+        const uint32_t f = fidx32(N, 0, lx, j, k);
+        face_solve<float, 0>(xa, xb, xc, xd, float(A.bf[0][f]), gm, theta, F, Ef);
+        for (int n = 0; n < 5; ++n) S.fx[lx & 1][n][t] = F[n];
+        if (write_e)
+        {
+            E0[f] = Ef[0];
+            E0[size_t(nbv[0]) + f] = Ef[1];
+        }
+    };
+
+    for (int t = threadIdx.x; t < FXN; t += THREADS) solve_x(t, T.i0, true);
+    for (int c = T.i0; c < T.i1; ++c)
+    {
+        __syncthreads();                   // the previous plane's cell updates are done
+        const bool x_owned = c + 1 < T.i1 || c + 1 == N;
+        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += THREADS)
+        {
+            if (t < FXN)
+            {
+                solve_x(t, c + 1, x_owned);
+            }
+            else if (t < FXN + SOLVE_Y)
+            {
+                const int u = t - FXN;
+                if (u >= FYN) continue;
+                const int jj = u / TK, kk = u - jj * TK;            // jj = TJ: the high neighbour's face
+                const int j = T.j0 + jj, k = T.k0 + kk;
+                float xa[8], xb[8], xc[8], xd[8], F[5], Ef[2];
+                stencil(P, cidx32(N, c, wrap(j - 2, N), k), cidx32(N, c, wrap(j - 1, N), k), cidx32(N, c, wrap(j, N), k),
+                        cidx32(N, c, wrap(j + 1, N), k), xa, xb, xc, xd);
+                const uint32_t f = fidx32(N, 1, c, j, k);
+                face_solve<float, 1>(xa, xb, xc, xd, float(A.bf[1][f]), gm, theta, F, Ef);
+                for (int n = 0; n < 5; ++n) S.fy[n][u] = F[n];
+                if (jj < TJ || T.last_j)
+                {
+                    E1[f] = Ef[0];
+                    E1[size_t(nbv[1]) + f] = Ef[1];
+                }
+            }
+            else
+            {
+                const int u = t - FXN - SOLVE_Y;
+                if (u >= FZN) continue;
+                const int jj = u / FZK, kk = u - jj * FZK;           // kk = TK: the high neighbour's face
+                const int j = T.j0 + jj, k = T.k0 + kk;
+                float xa[8], xb[8], xc[8], xd[8], F[5], Ef[2];
+                stencil(P, cidx32(N, c, j, wrap(k - 2, N)), cidx32(N, c, j, wrap(k - 1, N)), cidx32(N, c, j, wrap(k, N)),
+                        cidx32(N, c, j, wrap(k + 1, N)), xa, xb, xc, xd);
+                const uint32_t f = fidx32(N, 2, c, j, k);
+                face_solve<float, 2>(xa, xb, xc, xd, float(A.bf[2][f]), gm, theta, F, Ef);
+                for (int n = 0; n < 5; ++n) S.fz[n][u] = F[n];
+                if (kk < TK || T.last_k)
+                {
+                    E2[f] = Ef[0];
+                    E2[size_t(nbv[2]) + f] = Ef[1];
+                }
+            }
+        }
+        __syncthreads();
+        const float dtdl = s_dtdl;
+        for (int t = threadIdx.x; t < FXN; t += THREADS)
+        {
+            const int jj = t / TK, kk = t - jj * TK;
+            const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0 + kk);
+            for (int q = 0; q < 5; ++q)
+            {
+                const float* fy = S.fy[q];
+                const float* fz = S.fz[q];
+                const float dc = (S.fx[(c + 1) & 1][q][t] - S.fx[c & 1][q][t]) + (fy[(jj + 1) * TK + kk] - fy[jj * TK + kk])
+                               + (fz[jj * FZK + kk + 1] - fz[jj * FZK + kk]);
+                const float du = __fmul_rn(dc, dtdl);
+                if (MODE == MIX_INCREMENT)
+                {
+                    A.dinc[q * NN + cell] = -du;
+                    continue;
+                }
+                const double u = A.uc[q * A.ucs + cell * A.uzs];
+                double out = MODE == MIX_FROM_INCREMENT ? u + f2d(__fmul_rn(0.5f, __fsub_rn(A.dinc[q * NN + cell], du)))
+                                                        : u - f2d(du);
+                if (A.uavg) out = half_exact(A.uavg[q * NN + cell] + out);
+                A.uc_out[q * NN + cell] = out;
+            }
+        }
+    }
+}
+
+// NEXT: the primitives the EMF kernel recovers for the next RK stage:
+// 0 none, MIX_INCREMENT (the next step's first stage: from A.next_uc) or
+// MIX_FROM_INCREMENT (the second stage: A.next_uc plus the FP32 increment).
+template<int NEXT>
+__global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, int chunks)
+{
+    using namespace fused;
+    __shared__ EmfSmem S;
+    __shared__ double s_dtdl;
+    const int N = A.N;
+    const Tile T = tile_of(N, chunks);
+    const uint32_t nbv[3] = {nb32(N, 0), nb32(N, 1), nb32(N, 2)};
+    const float* E0 = static_cast<const float*>(A.E[0]);
+    const float* E1 = static_cast<const float*>(A.E[1]);
+    const float* E2 = static_cast<const float*>(A.E[2]);
+    const int64_t NN = int64_t(N) * N * N;
+    const float gm = float(A.gamma);
+    if (threadIdx.x == 0) s_dtdl = A.clock->dt[A.stage] / A.dl;
+
+    // face E-fields of layer lx (when load_x) and of plane py, as one cp.async group
+    auto load = [&](bool load_x, int lx, int py) {
+        const uint32_t pw = uint32_t(wrap(py, N));
+        for (int t = threadIdx.x; t < LOAD_X + LOAD_Y + LOAD_Z; t += THREADS)
+        {
+            if (t < LOAD_X + LOAD_Y)
+            {
+                // row piece: 0 .. TK/4-1 the interior, TK/4 kk = -1, TK/4+1 kk = TK
+                const bool x = t < LOAD_X;
+                if (x && !load_x) continue;
+                const int v = x ? t : t - LOAD_X;
+                const int row = v / ROW_PIECES, piece = v - row * ROW_PIECES;
+                const int rows = x ? TJ + 2 : TJ + 1, h = row / rows, r = row - h * rows;
+                const int kk = piece < TK / 4 ? 4 * piece : (piece == TK / 4 ? -1 : TK);
+                const uint32_t f = x ? fidx32(N, 0, lx, wrap(T.j0 + r - 1, N), wrap(T.k0 + kk, N))
+                                     : fidx32(N, 1, pw, T.j0 + r, wrap(T.k0 + kk, N));
+                const float* src = x ? E0 + size_t(h) * nbv[0] + f : E1 + size_t(h) * nbv[1] + f;
+                float* dst = x ? &S.ex[lx & 1][h][r * XK + XO + kk] : &S.ey[py & 3][h][r * YK + YO + kk];
+                if (piece < TK / 4) cp_async16(dst, src);
+                else cp_async4(dst, src);
+            }
+            else
+            {
+                const int v = t - LOAD_X - LOAD_Y, h = v / ZN, u = v - h * ZN;
+                const int r = u / ZK, q = u - r * ZK;               // jj = r - 1, kk = q
+                const uint32_t f = fidx32(N, 2, pw, wrap(T.j0 + r - 1, N), T.k0 + q);
+                cp_async4(&S.ez[py & 3][h][u], E2 + size_t(h) * nbv[2] + f);
+            }
+        }
+        cp_async_commit();
+    };
+
+    double m = 0.0;
+    float mf = 0.0f;
+    unsigned long long bad = 0;
+    load(false, 0, T.i0 - 1);
+    load(true, T.i0, T.i0);
+    for (int c = T.i0; c <= T.i1; ++c)
+    {
+        const bool first = c == T.i0, last = c == T.i1;
+        cp_async_wait_all();
+        __syncthreads();                   // this plane's fields landed; the previous plane's work is done
+        if (!last) load(true, c + 1, c + 1);
+        const int s = c & 1, sp = (c - 1) & 1, ys = c & 3, yp = (c - 1) & 3;
+        // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order)
+        for (int t = threadIdx.x; t < EDGE_0 + EDGE_1 + EDGE_2; t += THREADS)
+        {
+            if (t < EDGE_0)
+            {
+                if (t >= E0N) continue;
+                const int jj = t / E0K, kk = t - jj * E0K;
+                const float* y0 = S.ey[ys][0] + YO - 1;
+                const float* z0 = S.ez[ys][0];
+                S.e0[s][t] = avg(avg(y0[jj * YK + kk], y0[jj * YK + kk + 1]), avg(z0[jj * ZK + kk], z0[(jj + 1) * ZK + kk]));
+            }
+            else if (t < EDGE_0 + EDGE_1)
+            {
+                const int u = t - EDGE_0;
+                if (u >= E1N) continue;
+                const int jj = u / E1K, kk = u - jj * E1K;
+                const float* x1 = S.ex[s][0] + XO - 1;
+                const float a = avg(S.ez[yp][1][(jj + 1) * ZK + kk], S.ez[ys][1][(jj + 1) * ZK + kk]);
+                const float b = avg(x1[(jj + 1) * XK + kk], x1[(jj + 1) * XK + kk + 1]);
+                S.e1[s][u] = avg(a, b);
+            }
+            else
+            {
+                const int u = t - EDGE_0 - EDGE_1;
+                if (u >= E2N) continue;
+                const int jj = u / E2K, kk = u - jj * E2K;
+                const float a = avg(S.ex[s][1][jj * XK + XO + kk], S.ex[s][1][(jj + 1) * XK + XO + kk]);
+                const float b = avg(S.ey[yp][1][jj * YK + YO + kk], S.ey[ys][1][jj * YK + YO + kk]);
+                S.e2[s][u] = avg(a, b);
+            }
+        }
+        __syncthreads();
+        // faces: x of layer c (the tile); y and z of plane c-1, with the high
+        // neighbour's row and column, which the next-stage cells need
+        const double dtdl_d = s_dtdl;
+        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += THREADS)
+        {
+            if (t < FXN)
+            {
+                const int jj = t / TK, kk = t - jj * TK;
+                const double cf = curl_f(S.e2[s][(jj + 1) * E2K + kk], S.e2[s][jj * E2K + kk], S.e1[s][jj * E1K + kk + 1],
+                                         S.e1[s][jj * E1K + kk]);
+                const uint32_t f = fidx32(N, 0, c, T.j0 + jj, T.k0 + kk);
+                double out = fma(-cf, dtdl_d, A.bf[0][f]);
+                if (A.bavg[0]) out = half_exact(A.bavg[0][f] + out);
+                S.bx[s][t] = out;
+                if (!last || c == N) A.bf_out[0][f] = out;
+            }
+            else if (t < FXN + SOLVE_Y)
+            {
+                const int u = t - FXN;
+                if (first || u >= FYN || (!NEXT && u >= FXN && !T.last_j)) continue;
+                const int jj = u / TK, kk = u - jj * TK;
+                const double cf = curl_f(S.e0[sp][jj * E0K + kk + 1], S.e0[sp][jj * E0K + kk], S.e2[s][jj * E2K + kk],
+                                         S.e2[sp][jj * E2K + kk]);
+                const uint32_t f = fidx32(N, 1, c - 1, T.j0 + jj, T.k0 + kk);
+                double out = fma(-cf, dtdl_d, A.bf[1][f]);
+                if (A.bavg[1]) out = half_exact(A.bavg[1][f] + out);
+                S.by[u] = out;
+                if (jj < TJ || T.last_j) A.bf_out[1][f] = out;
+            }
+            else
+            {
+                const int u = t - FXN - SOLVE_Y;
+                if (first || u >= FZN) continue;
+                const int jj = u / FZK, kk = u - jj * FZK;
+                if (!NEXT && kk == TK && !T.last_k) continue;
+                const double cf = curl_f(S.e1[s][jj * E1K + kk], S.e1[sp][jj * E1K + kk], S.e0[sp][(jj + 1) * E0K + kk],
+                                         S.e0[sp][jj * E0K + kk]);
+                const uint32_t f = fidx32(N, 2, c - 1, T.j0 + jj, T.k0 + kk);
+                double out = fma(-cf, dtdl_d, A.bf[2][f]);
+                if (A.bavg[2]) out = half_exact(A.bavg[2][f] + out);
+                S.bz[u] = out;
+                if (kk < TK || T.last_k) A.bf_out[2][f] = out;
+            }
+        }
+        if (NEXT && !first)
+        {
+            __syncthreads();
+            // the next stage's primitives of plane c-1 (the primitive kernel's arithmetic)
+            float* P = static_cast<float*>(A.P);
+            for (int t = threadIdx.x; t < FXN; t += THREADS)
+            {
+                const int jj = t / TK, kk = t - jj * TK;
+                const int64_t cell = cidx32(N, c - 1, T.j0 + jj, T.k0 + kk);
+                Prim<float> p;
+                if (recover_mixed<NEXT>(A.next_uc, NN, 1, A.dinc, NN, cell,
+                                        cell_field(S.bx[sp][t], S.bx[s][t], S.by[t], S.by[t + TK], S.bz[jj * FZK + kk],
+                                                   S.bz[jj * FZK + kk + 1]),
+                                        gm, p))
+                    ++bad;
+                store_cell(P, cell, p);
+                mf = fmaxf(mf, fastest_speed(p, gm));
+            }
+        }
+    }
+    if (NEXT)
+    {
+        m = double(mf);
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+            bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        }
+        if ((threadIdx.x & 31) == 0)
+        {
+            S.wmax[threadIdx.x >> 5] = m;
+            S.wbad[threadIdx.x >> 5] = bad;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            double r = 0.0;
+            unsigned long long nbad = 0;
+            for (int w = 0; w < THREADS / 32; ++w)
+            {
+                r = fmax(r, S.wmax[w]);
+                nbad += S.wbad[w];
+            }
+            atomicMax(&A.clock->amax[A.stage ^ 1], (unsigned long long)__double_as_longlong(r));
+            if (nbad) atomicAdd(&A.clock->failures, nbad);
+        }
+    }
+}
+
 __global__ void clock_end_kernel(Clock* clock, int rk_order)
 {
     if (threadIdx.x != 0) return;
@@ -702,15 +1148,19 @@ int check(const mara_mhd_params* mp)
 
 inline int blocks_for(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
-// One stage: u_out/b_out = advance_mhd_ct(u_in/b_in) [averaged with avg].
-template<typename R>
-int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
-          const double* u_in, int64_t ucs, int64_t uzs, const double* const b_in[3],
-          const double* uavg, const double* const bavg[3], double* u_out, double* const b_out[3],
-          int mixed_mode, cudaStream_t s)
+// The fused mixed stage (flux_kernel + emf_kernel): 1 = on wherever the
+// mesh allows it (N a multiple of 32), 0 = the face and update kernels.
+// g_ct_chunks > 0 fixes the number of i chunks; 0 chooses it from the SM count.
+int g_ct_fused = 1;
+int g_ct_chunks = 0;
+
+inline bool fused_path(int precision, int N) { return precision == MARA_MIXED && g_ct_fused && N % fused::TK == 0; }
+
+Args stage_args(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st, const double* u_in, int64_t ucs,
+                int64_t uzs, const double* const b_in[3], const double* uavg, const double* const bavg[3],
+                double* u_out, double* const b_out[3])
 {
     const int N = mp->N;
-    const int64_t NN = int64_t(N) * N * N;
     Args A;
     std::memset(&A, 0, sizeof A);
     A.N = N;
@@ -739,6 +1189,13 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     A.clock = clock;
     A.stage = st;
     A.dinc = reinterpret_cast<float*>(w.u1);   // the FP32 increments reuse the stage-1 state region
+    return A;
+}
+
+template<typename R>
+int launch_prim(const Args& A, int mixed_mode, cudaStream_t s)
+{
+    const int64_t NN = int64_t(A.N) * A.N * A.N;
     if constexpr (sizeof(R) == sizeof(float))
     {
         if (mixed_mode == MIX_INCREMENT) prim_kernel<R, MIX_INCREMENT><<<blocks_for(NN), 256, 0, s>>>(A);
@@ -746,7 +1203,20 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
         else prim_kernel<R, MIX_PLAIN><<<blocks_for(NN), 256, 0, s>>>(A);
     }
     else prim_kernel<R, MIX_PLAIN><<<blocks_for(NN), 256, 0, s>>>(A);
-    if (int r = launch_status("mhd prim_kernel")) return r;
+    return launch_status("mhd prim_kernel");
+}
+
+// One stage: u_out/b_out = advance_mhd_ct(u_in/b_in) [averaged with avg].
+template<typename R>
+int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
+          const double* u_in, int64_t ucs, int64_t uzs, const double* const b_in[3],
+          const double* uavg, const double* const bavg[3], double* u_out, double* const b_out[3],
+          int mixed_mode, cudaStream_t s)
+{
+    const int N = mp->N;
+    const int64_t NN = int64_t(N) * N * N;
+    const Args A = stage_args(mp, w, clock, st, u_in, ucs, uzs, b_in, uavg, bavg, u_out, b_out);
+    if (int r = launch_prim<R>(A, mixed_mode, s)) return r;
     dt_kernel<<<1, 32, 0, s>>>(clock, st, mp->cfl, A.dl, 0);
     if (int r = launch_status("mhd dt_kernel")) return r;
     face_kernel<R, 0><<<blocks_for(nb(N, 0)), 256, 0, s>>>(A);
@@ -764,6 +1234,64 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     if (int r = launch_status("mhd update_kernel (cells)")) return r;
     update_kernel<R, MIX_PLAIN, 1><<<fb, 256, 0, s>>>(A);
     return launch_status("mhd update_kernel (faces)");
+}
+
+// i chunks of a fused kernel: at least two waves of resident blocks and at
+// most 16 planes per chunk (blocks of equal work finish in waves, and a short
+// last wave of long blocks leaves most SMs idle; measured at 128^3 and 256^3),
+// at least four planes per chunk (each chunk solves one extra layer of faces)
+template<typename K>
+int fused_chunks(K kernel, int N, int* chunks)
+{
+    static PerDeviceOnce once;
+    static int slots[64] = {};
+    int dev = 0;
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (int r = once.run(dev, [&]() -> int {
+            int b = 0, n = 0;
+            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, fused::THREADS, 0));
+            MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+            slots[dev & 63] = n * (b > 0 ? b : 1);
+            return MARA_OK;
+        }))
+        return r;
+    const int tiles = (N / fused::TJ) * (N / fused::TK);
+    int c = g_ct_chunks;
+    if (c <= 0) c = std::max(1, std::min(N / 4, std::max(N / 16, (2 * slots[dev & 63] + tiles - 1) / tiles)));
+    *chunks = std::min(c, N);
+    return MARA_OK;
+}
+
+// The fused mixed stage: [primitives,] dt, flux_kernel, emf_kernel. `next`
+// (0, MIX_INCREMENT or MIX_FROM_INCREMENT) makes the EMF kernel recover the
+// next stage's primitives from next_uc (and its maximum wavespeed), so that
+// the next stage runs with need_prim = false. b_out must not alias b_in or
+// bavg: the EMF kernel re-solves the faces its tile's cells share with the
+// neighbouring tiles and reads their inputs while the owners write.
+int stage_fused(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st, const double* u_in, int64_t ucs,
+                int64_t uzs, const double* const b_in[3], const double* const bavg[3], double* u_out,
+                double* const b_out[3], int mixed_mode, bool need_prim, int next, const double* next_uc,
+                cudaStream_t s)
+{
+    const int N = mp->N;
+    Args A = stage_args(mp, w, clock, st, u_in, ucs, uzs, b_in, nullptr, bavg, u_out, b_out);
+    A.next_uc = next_uc;
+    if (need_prim)
+        if (int r = launch_prim<float>(A, mixed_mode, s)) return r;
+    dt_kernel<<<1, 32, 0, s>>>(clock, st, mp->cfl, A.dl, 0);
+    if (int r = launch_status("mhd dt_kernel")) return r;
+    const int tiles = (N / fused::TJ) * (N / fused::TK);
+    int cf = 0, ce = 0;
+    if (int r = fused_chunks(flux_kernel<MIX_FROM_INCREMENT>, N, &cf)) return r;
+    if (int r = fused_chunks(emf_kernel<MIX_INCREMENT>, N, &ce)) return r;
+    if (mixed_mode == MIX_INCREMENT) flux_kernel<MIX_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
+    else if (mixed_mode == MIX_FROM_INCREMENT) flux_kernel<MIX_FROM_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
+    else flux_kernel<MIX_PLAIN><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
+    if (int r = launch_status("mhd flux_kernel")) return r;
+    if (next == MIX_INCREMENT) emf_kernel<MIX_INCREMENT><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
+    else if (next == MIX_FROM_INCREMENT) emf_kernel<MIX_FROM_INCREMENT><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
+    else emf_kernel<0><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
+    return launch_status("mhd emf_kernel");
 }
 
 int run_stage(int precision, const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
@@ -784,6 +1312,15 @@ using namespace mara::mhd;
 extern "C" {
 
 int64_t mara_mhd_clock_bytes(void) { return int64_t(sizeof(Clock)); }
+
+int mara_mhd_fused_stage(int32_t enable, int32_t chunks)
+{
+    MARA_REQUIRE(enable == 0 || enable == 1, "mara_mhd_fused_stage: enable must be 0 or 1");
+    MARA_REQUIRE(chunks >= 0 && chunks <= 1024, "mara_mhd_fused_stage: chunks must be in [0, 1024]");
+    g_ct_fused = enable;
+    g_ct_chunks = chunks;
+    return MARA_OK;
+}
 
 int64_t mara_mhd_workspace_bytes(const mara_mhd_params* mp, int32_t rk_order, int32_t precision)
 {
@@ -821,8 +1358,15 @@ int mara_mhd_advance_ct(const mara_mhd_params* mp, const double* uc, int64_t com
     double* b_out[3] = {bf1_out, bf2_out, bf3_out};
     dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);
     if (int r = launch_status("mhd dt_kernel")) return r;
-    if (int r = run_stage(precision, mp, w, c, 0, uc, component_stride, cell_stride, b_in, nullptr, nullptr, uc_out,
-                          b_out, s)) return r;
+    if (fused_path(precision, mp->N))
+    {
+        if (int r = stage_fused(mp, w, c, 0, uc, component_stride, cell_stride, b_in, nullptr, uc_out, b_out, MIX_PLAIN,
+                                true, 0, nullptr, s))
+            return r;
+    }
+    else if (int r = run_stage(precision, mp, w, c, 0, uc, component_stride, cell_stride, b_in, nullptr, nullptr, uc_out,
+                               b_out, s))
+        return r;
     clock_end_kernel<<<1, 32, 0, s>>>(c, 1);
     return launch_status("mhd clock_end_kernel");
 }
@@ -843,6 +1387,36 @@ int mara_mhd_advance(const mara_mhd_params* mp, double* uc, double* bf1, double*
     double* b0[3] = {bf1, bf2, bf3};
     const double* b0c[3] = {bf1, bf2, bf3};
     const double* b1c[3] = {w.b1[0], w.b1[1], w.b1[2]};
+    if (steps > 0 && fused_path(precision, mp->N))
+    {
+        // Fused mixed RK2. Stage 2 may not write B over its averaging partner
+        // (stage_fused), so the face fields alternate between the caller's
+        // arrays and scratch in the (here unused) flux arrays of the
+        // workspace, and come back to the caller's arrays at the end.
+        double* X[3] = {static_cast<double*>(w.F[0]), static_cast<double*>(w.F[1]), static_cast<double*>(w.F[2])};
+        bool in_caller = true;
+        dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);
+        if (int r = launch_status("mhd dt_kernel")) return r;
+        for (int step = 0; step < steps; ++step)
+        {
+            double* const* cur = in_caller ? b0 : X;
+            double* const* nxt = in_caller ? X : b0;
+            const double* curc[3] = {cur[0], cur[1], cur[2]};
+            if (int r = stage_fused(mp, w, c, 0, uc, NN, 1, curc, nullptr, nullptr, w.b1, MIX_INCREMENT, step == 0,
+                                    MIX_FROM_INCREMENT, uc, s))
+                return r;
+            if (int r = stage_fused(mp, w, c, 1, uc, NN, 1, b1c, curc, uc, nxt, MIX_FROM_INCREMENT, false,
+                                    step + 1 < steps ? MIX_INCREMENT : 0, uc, s))
+                return r;
+            clock_end_kernel<<<1, 32, 0, s>>>(c, 2);
+            if (int r = launch_status("mhd clock_end_kernel")) return r;
+            in_caller = !in_caller;
+        }
+        if (!in_caller)
+            for (int a = 0; a < 3; ++a)
+                MARA_CUDA(cudaMemcpyAsync(b0[a], X[a], sizeof(double) * size_t(nb(mp->N, a)), cudaMemcpyDeviceToDevice, s));
+        return MARA_OK;
+    }
     for (int step = 0; step < steps; ++step)
     {
         dt_kernel<<<1, 32, 0, s>>>(c, 0, mp->cfl, 1.0 / mp->N, 1);

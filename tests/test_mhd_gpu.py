@@ -166,3 +166,62 @@ def test_advance_checked_restores_and_raises_on_failed_zones(mh):
         run.advance_checked(1)
     assert torch.equal(s.uc, before[0]) and all(torch.equal(b, b0) for b, b0 in zip(s.bf, before[1:]))
     assert run.clock.read()["time"] == t0
+
+
+def _mixed_runs(mh, N, steps, chunks, seed=7):
+    """(state tensors, clock) of a mixed RK2 run with the fused stage on and off."""
+    from mara3p_gb300._capi import check, lib
+    out = []
+    try:
+        for enable in (1, 0):
+            check(lib.mara_mhd_fused_stage(enable, chunks), "fused stage")
+            s = mh.initial_state(mh.MhdConfig(N=N), seed=seed, modes=24)
+            r = mh.Run(s, precision=mh.MIXED)
+            r.advance(steps)
+            torch.cuda.synchronize()
+            out.append(([s.uc.clone()] + [b.clone() for b in s.bf], r.clock.read()))
+    finally:
+        check(lib.mara_mhd_fused_stage(1, 0), "fused stage")
+    return out
+
+
+@pytest.mark.parametrize("N,steps,chunks", [(32, 6, 0), (32, 3, 32), (64, 4, 5), (96, 2, 7), (128, 3, 0)])
+def test_mixed_fused_stage_bit_identical(mh, N, steps, chunks):
+    """The fused mixed stage (faces, edge EMFs and both updates in one launch)
+    against the face and update kernels over mixed RK2 steps: states, face
+    fields and clocks identical bit for bit, at several splittings of the i
+    axis (one plane per chunk included) and at the 128^3 configuration."""
+    (fa, ca), (fb, cb) = _mixed_runs(mh, N, steps, chunks)
+    for x, y in zip(fa, fb):
+        assert torch.equal(x, y)
+    assert ca["time"] == cb["time"] and ca["dt"] == cb["dt"]
+    assert ca["failures"] == cb["failures"] == 0
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_mixed_fused_single_stage_bit_identical(mh, layout):
+    """advance_ct (one forward-Euler stage, input in either layout) with the
+    fused stage on and off: identical outputs."""
+    from mara3p_gb300._capi import check, lib
+    N = 64
+    s = mh.initial_state(mh.MhdConfig(N=N), seed=9, modes=24)
+    uc_in = s.uc.reshape(5, -1).t().contiguous() if layout == "aos" else None
+    outs = []
+    try:
+        for enable in (1, 0):
+            check(lib.mara_mhd_fused_stage(enable, 0), "fused stage")
+            out, clock = mh.advance_ct(s, uc_in=uc_in, layout=layout, precision=mh.MIXED)
+            torch.cuda.synchronize()
+            outs.append(([out.uc] + list(out.bf), clock.read()["time"]))
+    finally:
+        check(lib.mara_mhd_fused_stage(1, 0), "fused stage")
+    for x, y in zip(outs[0][0], outs[1][0]):
+        assert torch.equal(x, y)
+    assert outs[0][1] == outs[1][1]
+
+
+def test_fused_stage_switch_rejects_bad_arguments(mh):
+    from mara3p_gb300._capi import lib
+    assert lib.mara_mhd_fused_stage(2, 0) != 0
+    assert lib.mara_mhd_fused_stage(1, -1) != 0
+    assert lib.mara_mhd_fused_stage(1, 0) == 0
