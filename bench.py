@@ -121,6 +121,30 @@ def fp64_peak() -> float:
     return _FP64_RATE
 
 
+def host_link(host_buf, h2d_bytes: int, d2h_bytes: int, ms_per_call: float, stage_ms) -> dict:
+    """The host link's rates (mara_measure_host_link, on the call's own pinned
+    output buffer and a device buffer of its size) and the floor they put
+    under one host-buffer call: the input read over the link by a kernel,
+    then stage 1 (which needs the CFL maximum over the whole input), then
+    stage 2 writing the output over the link (its compute hidden under the
+    writes). No schedule with the reference's CFL time step does better."""
+    import torch
+
+    from mara3p_gb300._capi import check, lib
+    dev = torch.empty(host_buf.numel() * host_buf.element_size(), dtype=torch.uint8, device="cuda")
+    g = (ctypes.c_double * 5)()
+    check(lib.mara_measure_host_link(host_buf.data_ptr(), dev.data_ptr(), dev.numel(), g,
+                                     torch.cuda.current_stream().cuda_stream), "host link")
+    del dev
+    names = ["h2d_copy_engine_gbs", "d2h_copy_engine_gbs", "kernel_read_gbs", "kernel_write_gbs",
+             "read_and_write_together_gbs"]
+    out = {k: round(v, 1) for k, v in zip(names, g)}
+    floor = (h2d_bytes / (g[2] * 1e9) + d2h_bytes / (g[3] * 1e9)) * 1e3 + stage_ms[0]
+    out.update({"floor_ms_per_call": floor, "frac_of_floor": floor / ms_per_call,
+                "floor": "input read by a kernel at kernel_read_gbs + stage 1 + output written at kernel_write_gbs"})
+    return out
+
+
 def fp64_pipe_fraction(key: str, units: float, ms: float):
     """The FP64-pipe roofline of an FP64-bound kernel: its FP64 thread
     instructions per unit (an ncu count in profiles/fp64_ops.json) x units
@@ -484,7 +508,10 @@ def run_ours(args):
         el = max_over_ranks(time.perf_counter() - t0, world)
         e2e = {"value": cells * e2e_steps * world / el, "unit": "cell-updates/s",
                "h2d_bytes_per_step": 3 * cells * 8, "d2h_bytes_per_step": 3 * cells * 8,
-               "call": "mara_minidisk_advance_host (pinned host state in/out, 1 RK2 step per call)"}
+               "call": "mara_minidisk_advance_host (pinned host state in/out, 1 RK2 step per call)",
+               "ms_per_call": el / e2e_steps * 1e3}
+        e2e["link"] = host_link(host_out, e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"],
+                                e2e["ms_per_call"], [s1, s2])
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -648,6 +648,17 @@ int mara_iso2d_riemann_hlle(const double* pl, const double* pr, const double* cs
  * bounds. A measurement helper with no counterpart in the reference. */
 int mara_measure_fp64_rate(double* dfma_per_second, void* stream);
 
+/* Host-link rates in GB/s (gbs[5], host): [0] copy-engine host->device,
+ * [1] copy-engine device->host, [2] a kernel reading pinned host memory,
+ * [3] a kernel writing it, [4] both kernels at once on halves of the buffers
+ * (total bytes of both directions / time). host: pinned host memory (page-
+ * locked, with a device address), device: device memory, both `bytes` long
+ * and 16-byte aligned; their contents are overwritten. Best of three after a
+ * warm-up round; synchronizes the stream. The bound of the host-buffer calls
+ * (mara_minidisk_advance_host reads and writes the state this way). A
+ * measurement helper with no counterpart in the reference. */
+int mara_measure_host_link(void* host, void* device, int64_t bytes, double* gbs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

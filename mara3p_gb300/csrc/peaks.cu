@@ -69,3 +69,76 @@ extern "C" int mara_measure_fp64_rate(double* dfma_per_second, void* stream)
     *dfma_per_second = fmas / (double(best) * 1e-3);
     return MARA_OK;
 }
+
+// ---------------------------------------------------------------- host link
+// The rates of the host link in the forms the host-buffer calls use: copy
+// engine both ways, and kernels reading and writing pinned host memory
+// through its device address (16-byte accesses), alone and both at once.
+namespace {
+
+__global__ void link_copy_kernel(const double2* __restrict__ src, double2* __restrict__ dst, size_t n)
+{
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        dst[i] = src[i];
+}
+
+} // namespace
+
+extern "C" int mara_measure_host_link(void* host, void* device, int64_t bytes, double* gbs, void* stream)
+{
+    using namespace mara;
+    MARA_REQUIRE(host && device && gbs, "mara_measure_host_link: null buffer");
+    MARA_REQUIRE(bytes >= (1 << 20) && bytes % 32 == 0, "mara_measure_host_link: bytes must be a multiple of 32, >= 1 MiB");
+    cudaPointerAttributes pa;
+    MARA_CUDA(cudaPointerGetAttributes(&pa, host));
+    MARA_REQUIRE(pa.type == cudaMemoryTypeHost && pa.devicePointer, "mara_measure_host_link: host is not pinned host memory");
+    MARA_REQUIRE((reinterpret_cast<uintptr_t>(pa.devicePointer) & 15) == 0 && (reinterpret_cast<uintptr_t>(device) & 15) == 0,
+                 "mara_measure_host_link: buffers must be 16-byte aligned");
+    cudaStream_t s = as_stream(stream);
+    int dev = 0, sms = 0;
+    MARA_CUDA(cudaGetDevice(&dev));
+    MARA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 16;
+    auto* hdev = static_cast<double2*>(pa.devicePointer);
+    auto* d = static_cast<double2*>(device);
+    const size_t n = size_t(bytes) / 16, half = n / 2;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    MARA_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    int rc = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+             cudaEventCreate(&e2) == cudaSuccess ? MARA_OK : fail(MARA_ERR_CUDA, "mara_measure_host_link: event create");
+    // best of three per form (after one untimed round), milliseconds
+    double best[5] = {1e30, 1e30, 1e30, 1e30, 1e30};
+    for (int rep = 0; rep < 4 && rc == MARA_OK; ++rep)
+    {
+        for (int form = 0; form < 5 && rc == MARA_OK; ++form)
+        {
+            cudaEventRecord(e0, s);
+            if (form == 0) cudaMemcpyAsync(device, host, size_t(bytes), cudaMemcpyHostToDevice, s);
+            else if (form == 1) cudaMemcpyAsync(host, device, size_t(bytes), cudaMemcpyDeviceToHost, s);
+            else if (form == 2) link_copy_kernel<<<blocks, 256, 0, s>>>(hdev, d, n);
+            else if (form == 3) link_copy_kernel<<<blocks, 256, 0, s>>>(d, hdev, n);
+            else
+            {
+                // read one half of the host buffer while writing the other
+                cudaStreamWaitEvent(s2, e0, 0);
+                link_copy_kernel<<<blocks / 2, 256, 0, s>>>(hdev, d, half);
+                link_copy_kernel<<<blocks / 2, 256, 0, s2>>>(d + half, hdev + half, n - half);
+                cudaEventRecord(e2, s2);
+                cudaStreamWaitEvent(s, e2, 0);
+            }
+            cudaEventRecord(e1, s);
+            rc = launch_status("mara_measure_host_link");
+            if (rc == MARA_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(MARA_ERR_CUDA, "mara_measure_host_link: sync");
+            float ms = 0.0f;
+            if (rc == MARA_OK && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < best[form]) best[form] = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    cudaStreamDestroy(s2);
+    if (rc != MARA_OK) return rc;
+    for (int f = 0; f < 5; ++f) gbs[f] = double(bytes) / (best[f] * 1e-3) / 1e9;
+    return MARA_OK;
+}
