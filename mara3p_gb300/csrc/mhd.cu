@@ -623,8 +623,10 @@ constexpr int EDGE_0 = pad32(E0N), EDGE_1 = pad32(E1N), EDGE_2 = pad32(E2N);
 constexpr int ROW_PIECES = TK / 4 + 2;
 constexpr int LOAD_X = 2 * (TJ + 2) * ROW_PIECES, LOAD_Y = 2 * (TJ + 1) * ROW_PIECES, LOAD_Z = 2 * ZN;
 
-struct FluxSmem
+struct __align__(16) FluxSmem
 {
+    double uc[5][FXN];         // the cells' state of plane c (staged during the solves)
+    float dinc[5][FXN];        // their FP32 stage-1 increments (RK2 stage 2)
     float fx[2][5][FXN];       // x-face fluxes; layer l in slot l & 1
     float fy[5][FYN];          // y-face fluxes of plane c
     float fz[5][FZN];
@@ -633,8 +635,10 @@ struct FluxSmem
 struct __align__(16) EmfSmem
 {
     float ex[2][2][XN];        // x-face E components 1, 2; layer l in slot l & 1
-    float ey[4][2][YN];        // y-face E components 0, 2; plane p in slot p & 3
-    float ez[4][2][ZN];        // z-face E components 0, 1
+    float ey[3][2][YN];        // y-face E components 0, 2; plane p in slot p mod 3
+    float ez[3][2][ZN];        // z-face E components 0, 1
+    double bin[FXN + FYN + FZN];   // the faces' input field (staged during the edge phase):
+    double bav[FXN + FYN + FZN];   // x faces of the tile, y rows [0, TJ], z columns [0, TK]; the RK partner
     float e0[2][E0N], e1[2][E1N], e2[2][E2N];
     double bx[2][FXN];         // updated x faces; layer l in slot l & 1
     double by[FYN];            // updated y faces of plane c-1 (row TJ: the neighbour's, for the cells)
@@ -648,6 +652,13 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
     const unsigned s = unsigned(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ int mod3(int p) { return (p % 3 + 3) % 3; }
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
 {
     const unsigned s = unsigned(__cvta_generic_to_shared(smem));
@@ -725,10 +736,36 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
         }
     };
 
+    // the cell update's inputs go through shared memory, copied while the
+    // faces are solved: SoA state (component stride a multiple of two
+    // doubles, 16-byte aligned) and the FP32 increments
+    constexpr bool READS_U = MODE != MIX_INCREMENT, READS_D = MODE == MIX_FROM_INCREMENT;
+    const bool stage_u = READS_U && A.uzs == 1 && A.ucs % 2 == 0 && (reinterpret_cast<uintptr_t>(A.uc) & 15) == 0;
+    auto stage_cells = [&](int c) {
+        // rows of TK cells: TK/2 16-byte pieces of state, TK/4 of increments, per component
+        constexpr int UP = TJ * TK / 2, DP = TJ * TK / 4;
+        for (int t = threadIdx.x; t < 5 * (UP + DP); t += THREADS)
+        {
+            const bool u = t < 5 * UP;
+            const int v = u ? t : t - 5 * UP, per = u ? UP : DP;
+            const int q = v / per, w = v - q * per, width = u ? TK / 2 : TK / 4;
+            const int jj = w / width, piece = w - jj * width;
+            const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0);
+            if (u)
+            {
+                if (stage_u) cp_async16(&S.uc[q][jj * TK + 2 * piece], A.uc + q * A.ucs + cell + 2 * piece);
+            }
+            else if (READS_D)
+                cp_async16(&S.dinc[q][jj * TK + 4 * piece], A.dinc + q * NN + cell + 4 * piece);
+        }
+        cp_async_commit();
+    };
+
     for (int t = threadIdx.x; t < FXN; t += THREADS) solve_x(t, T.i0, true);
     for (int c = T.i0; c < T.i1; ++c)
     {
         __syncthreads();                   // the previous plane's cell updates are done
+        if (READS_U) stage_cells(c);
         const bool x_owned = c + 1 < T.i1 || c + 1 == N;
         for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += THREADS)
         {
@@ -773,6 +810,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
                 }
             }
         }
+        if (READS_U) cp_async_wait_all();
         __syncthreads();
         const float dtdl = s_dtdl;
         for (int t = threadIdx.x; t < FXN; t += THREADS)
@@ -791,8 +829,8 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
                     A.dinc[q * NN + cell] = -du;
                     continue;
                 }
-                const double u = A.uc[q * A.ucs + cell * A.uzs];
-                double out = MODE == MIX_FROM_INCREMENT ? u + f2d(__fmul_rn(0.5f, __fsub_rn(A.dinc[q * NN + cell], du)))
+                const double u = stage_u ? S.uc[q][t] : A.uc[q * A.ucs + cell * A.uzs];
+                double out = MODE == MIX_FROM_INCREMENT ? u + f2d(__fmul_rn(0.5f, __fsub_rn(S.dinc[q][t], du)))
                                                         : u - f2d(du);
                 if (A.uavg) out = half_exact(A.uavg[q * NN + cell] + out);
                 A.uc_out[q * NN + cell] = out;
@@ -808,7 +846,8 @@ template<int NEXT>
 __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, int chunks)
 {
     using namespace fused;
-    __shared__ EmfSmem S;
+    extern __shared__ __align__(16) unsigned char emf_smem[];
+    EmfSmem& S = *reinterpret_cast<EmfSmem*>(emf_smem);
     __shared__ double s_dtdl;
     const int N = A.N;
     const Tile T = tile_of(N, chunks);
@@ -837,7 +876,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 const uint32_t f = x ? fidx32(N, 0, lx, wrap(T.j0 + r - 1, N), wrap(T.k0 + kk, N))
                                      : fidx32(N, 1, pw, T.j0 + r, wrap(T.k0 + kk, N));
                 const float* src = x ? E0 + size_t(h) * nbv[0] + f : E1 + size_t(h) * nbv[1] + f;
-                float* dst = x ? &S.ex[lx & 1][h][r * XK + XO + kk] : &S.ey[py & 3][h][r * YK + YO + kk];
+                float* dst = x ? &S.ex[lx & 1][h][r * XK + XO + kk] : &S.ey[mod3(py)][h][r * YK + YO + kk];
                 if (piece < TK / 4) cp_async16(dst, src);
                 else cp_async4(dst, src);
             }
@@ -846,7 +885,51 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 const int v = t - LOAD_X - LOAD_Y, h = v / ZN, u = v - h * ZN;
                 const int r = u / ZK, q = u - r * ZK;               // jj = r - 1, kk = q
                 const uint32_t f = fidx32(N, 2, pw, wrap(T.j0 + r - 1, N), T.k0 + q);
-                cp_async4(&S.ez[py & 3][h][u], E2 + size_t(h) * nbv[2] + f);
+                cp_async4(&S.ez[mod3(py)][h][u], E2 + size_t(h) * nbv[2] + f);
+            }
+        }
+        cp_async_commit();
+    };
+
+    // the face update's inputs of step c (x faces of layer c; y and z faces
+    // of plane c-1 unless `first`), as one cp.async group: x and y rows in
+    // 16-byte pieces (rows of TK doubles start at multiples of 32 elements),
+    // z rows (N + 1 doubles) element by element
+    const bool with_avg = A.bavg[0] != nullptr;
+    auto aligned16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+    const bool vec = aligned16(A.bf[0]) && aligned16(A.bf[1]) && (!with_avg || (aligned16(A.bavg[0]) && aligned16(A.bavg[1])));
+    auto piece16 = [&](double* dst, const double* src) {
+        if (vec) cp_async16(dst, src);
+        else
+        {
+            cp_async8(dst, src);
+            cp_async8(dst + 1, src + 1);
+        }
+    };
+    auto stage_faces = [&](int c, bool first) {
+        constexpr int XP = TJ * TK / 2, YP = (TJ + 1) * TK / 2;
+        const int arrays = with_avg ? 2 : 1;
+        for (int t = threadIdx.x; t < arrays * (XP + YP + FZN); t += THREADS)
+        {
+            const int a = t / (XP + YP + FZN), v = t - a * (XP + YP + FZN);
+            double* dst = a ? S.bav : S.bin;
+            const double* const* src = a ? A.bavg : A.bf;
+            if (v < XP)
+            {
+                const int jj = v / (TK / 2), piece = v - jj * (TK / 2);
+                piece16(dst + jj * TK + 2 * piece, src[0] + fidx32(N, 0, c, T.j0 + jj, T.k0 + 2 * piece));
+            }
+            else if (v < XP + YP)
+            {
+                if (first) continue;
+                const int w = v - XP, jj = w / (TK / 2), piece = w - jj * (TK / 2);
+                piece16(dst + FXN + jj * TK + 2 * piece, src[1] + fidx32(N, 1, c - 1, T.j0 + jj, T.k0 + 2 * piece));
+            }
+            else
+            {
+                if (first) continue;
+                const int w = v - XP - YP, jj = w / FZK, kk = w - jj * FZK;
+                cp_async8(dst + FXN + FYN + w, src[2] + fidx32(N, 2, c - 1, T.j0 + jj, T.k0 + kk));
             }
         }
         cp_async_commit();
@@ -862,8 +945,9 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
         const bool first = c == T.i0, last = c == T.i1;
         cp_async_wait_all();
         __syncthreads();                   // this plane's fields landed; the previous plane's work is done
+        stage_faces(c, first);
         if (!last) load(true, c + 1, c + 1);
-        const int s = c & 1, sp = (c - 1) & 1, ys = c & 3, yp = (c - 1) & 3;
+        const int s = c & 1, sp = (c - 1) & 1, ys = mod3(c), yp = mod3(c - 1);
         // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order)
         for (int t = threadIdx.x; t < EDGE_0 + EDGE_1 + EDGE_2; t += THREADS)
         {
@@ -895,6 +979,8 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 S.e2[s][u] = avg(a, b);
             }
         }
+        if (last) cp_async_wait_all();
+        else cp_async_wait_prior();        // the staged faces; the next plane's fields may stay in flight
         __syncthreads();
         // faces: x of layer c (the tile); y and z of plane c-1, with the high
         // neighbour's row and column, which the next-stage cells need
@@ -907,8 +993,8 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 const double cf = curl_f(S.e2[s][(jj + 1) * E2K + kk], S.e2[s][jj * E2K + kk], S.e1[s][jj * E1K + kk + 1],
                                          S.e1[s][jj * E1K + kk]);
                 const uint32_t f = fidx32(N, 0, c, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, A.bf[0][f]);
-                if (A.bavg[0]) out = half_exact(A.bavg[0][f] + out);
+                double out = fma(-cf, dtdl_d, S.bin[t]);
+                if (with_avg) out = half_exact(S.bav[t] + out);
                 S.bx[s][t] = out;
                 if (!last || c == N) A.bf_out[0][f] = out;
             }
@@ -920,8 +1006,8 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 const double cf = curl_f(S.e0[sp][jj * E0K + kk + 1], S.e0[sp][jj * E0K + kk], S.e2[s][jj * E2K + kk],
                                          S.e2[sp][jj * E2K + kk]);
                 const uint32_t f = fidx32(N, 1, c - 1, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, A.bf[1][f]);
-                if (A.bavg[1]) out = half_exact(A.bavg[1][f] + out);
+                double out = fma(-cf, dtdl_d, S.bin[FXN + u]);
+                if (with_avg) out = half_exact(S.bav[FXN + u] + out);
                 S.by[u] = out;
                 if (jj < TJ || T.last_j) A.bf_out[1][f] = out;
             }
@@ -934,8 +1020,8 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
                 const double cf = curl_f(S.e1[s][jj * E1K + kk], S.e1[sp][jj * E1K + kk], S.e0[sp][(jj + 1) * E0K + kk],
                                          S.e0[sp][jj * E0K + kk]);
                 const uint32_t f = fidx32(N, 2, c - 1, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, A.bf[2][f]);
-                if (A.bavg[2]) out = half_exact(A.bavg[2][f] + out);
+                double out = fma(-cf, dtdl_d, S.bin[FXN + FYN + u]);
+                if (with_avg) out = half_exact(S.bav[FXN + FYN + u] + out);
                 S.bz[u] = out;
                 if (kk < TK || T.last_k) A.bf_out[2][f] = out;
             }
@@ -1236,12 +1322,25 @@ int stage(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st,
     return launch_status("mhd update_kernel (faces)");
 }
 
+// Dynamic shared memory of the EMF kernel (above the 48 KB of a static
+// allocation), allowed once per device and instantiation
+template<int NEXT>
+int emf_attribute(int dev)
+{
+    static PerDeviceOnce once;
+    return once.run(dev, []() -> int {
+        MARA_CUDA(cudaFuncSetAttribute(emf_kernel<NEXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(sizeof(fused::EmfSmem))));
+        return MARA_OK;
+    });
+}
+
 // i chunks of a fused kernel: at least two waves of resident blocks and at
 // most 16 planes per chunk (blocks of equal work finish in waves, and a short
 // last wave of long blocks leaves most SMs idle; measured at 128^3 and 256^3),
 // at least four planes per chunk (each chunk solves one extra layer of faces)
 template<typename K>
-int fused_chunks(K kernel, int N, int* chunks)
+int fused_chunks(K kernel, size_t smem, int N, int* chunks)
 {
     static PerDeviceOnce once;
     static int slots[64] = {};
@@ -1249,7 +1348,7 @@ int fused_chunks(K kernel, int N, int* chunks)
     MARA_CUDA(cudaGetDevice(&dev));
     if (int r = once.run(dev, [&]() -> int {
             int b = 0, n = 0;
-            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, fused::THREADS, 0));
+            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, fused::THREADS, smem));
             MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
             slots[dev & 63] = n * (b > 0 ? b : 1);
             return MARA_OK;
@@ -1281,16 +1380,21 @@ int stage_fused(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int
     dt_kernel<<<1, 32, 0, s>>>(clock, st, mp->cfl, A.dl, 0);
     if (int r = launch_status("mhd dt_kernel")) return r;
     const int tiles = (N / fused::TJ) * (N / fused::TK);
-    int cf = 0, ce = 0;
-    if (int r = fused_chunks(flux_kernel<MIX_FROM_INCREMENT>, N, &cf)) return r;
-    if (int r = fused_chunks(emf_kernel<MIX_INCREMENT>, N, &ce)) return r;
+    int cf = 0, ce = 0, dev = 0;
+    const size_t esm = sizeof(fused::EmfSmem);
+    MARA_CUDA(cudaGetDevice(&dev));
+    if (int r = emf_attribute<0>(dev)) return r;
+    if (int r = emf_attribute<MIX_INCREMENT>(dev)) return r;
+    if (int r = emf_attribute<MIX_FROM_INCREMENT>(dev)) return r;
+    if (int r = fused_chunks(flux_kernel<MIX_FROM_INCREMENT>, 0, N, &cf)) return r;
+    if (int r = fused_chunks(emf_kernel<MIX_INCREMENT>, esm, N, &ce)) return r;
     if (mixed_mode == MIX_INCREMENT) flux_kernel<MIX_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
     else if (mixed_mode == MIX_FROM_INCREMENT) flux_kernel<MIX_FROM_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
     else flux_kernel<MIX_PLAIN><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
     if (int r = launch_status("mhd flux_kernel")) return r;
-    if (next == MIX_INCREMENT) emf_kernel<MIX_INCREMENT><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
-    else if (next == MIX_FROM_INCREMENT) emf_kernel<MIX_FROM_INCREMENT><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
-    else emf_kernel<0><<<tiles * ce, fused::THREADS, 0, s>>>(A, ce);
+    if (next == MIX_INCREMENT) emf_kernel<MIX_INCREMENT><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
+    else if (next == MIX_FROM_INCREMENT) emf_kernel<MIX_FROM_INCREMENT><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
+    else emf_kernel<0><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
     return launch_status("mhd emf_kernel");
 }
 

@@ -225,3 +225,34 @@ def test_fused_stage_switch_rejects_bad_arguments(mh):
     assert lib.mara_mhd_fused_stage(2, 0) != 0
     assert lib.mara_mhd_fused_stage(1, -1) != 0
     assert lib.mara_mhd_fused_stage(1, 0) == 0
+
+
+def test_mixed_fused_unaligned_face_arrays(mh):
+    """Face arrays that are 8- but not 16-byte aligned (allowed at the C ABI)
+    take the fused path's element copies: the same outputs as aligned copies
+    of the same data."""
+    import ctypes as ct
+
+    from mara3p_gb300._capi import check, lib
+    N = 32
+    s = mh.initial_state(mh.MhdConfig(N=N), seed=13, modes=24)
+    cfg = s.cfg.to_c()
+    ws = torch.empty(lib.mara_mhd_workspace_bytes(ct.byref(cfg), 1, mh.MIXED), dtype=torch.uint8, device="cuda")
+    outs = []
+    for offset in (0, 1):
+        bins, bouts = [], []
+        for b in s.bf:
+            buf = torch.zeros(b.numel() + 2, dtype=torch.float64, device="cuda")
+            buf[offset:offset + b.numel()] = b.reshape(-1)
+            bins.append(buf[offset:offset + b.numel()])
+            bouts.append(torch.zeros(b.numel() + 2, dtype=torch.float64, device="cuda")[offset:offset + b.numel()])
+        uc_out = torch.empty_like(s.uc)
+        clock = mh.Clock()
+        check(lib.mara_mhd_advance_ct(ct.byref(cfg), s.uc.data_ptr(), N ** 3, 1, *[b.data_ptr() for b in bins],
+                                      uc_out.data_ptr(), *[b.data_ptr() for b in bouts], clock.buf.data_ptr(),
+                                      mh.MIXED, ws.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        assert offset == 0 or bins[0].data_ptr() % 16 == 8
+        outs.append([uc_out] + bouts)
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
