@@ -41,6 +41,20 @@ __device__ inline float plm(float yl, float y0, float yr, float theta)
     return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
 }
 
+// Twice plm(float) in one multiply: for a = y0 - yl, b = yr - yl, c = yr - y0,
+// 2 minmod(theta a, b / 2, theta c) = sign x min(2 theta min(|a|, |c|), |b|).
+// Scaling by two and taking minima commute with rounding, so this is exactly
+// twice the three-multiply form (normal values; the signs tested are those of
+// a, b, c, which scaling by theta > 0 keeps), and y +- 0.25 x plm2 rounds to
+// the same float as y +- 0.5 x plm.
+__device__ inline float plm2(float yl, float y0, float yr, float two_theta)
+{
+    const float a = y0 - yl, b = yr - yl, c = yr - y0;
+    const float m = fminf(two_theta * fminf(fabsf(a), fabsf(c)), fabsf(b));
+    const int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
+    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
+}
+
 // Component `axis` of v. The FP32 path takes the normal components this way
 // rather than as a dot product with the unit normal: the products by 0 and 1
 // change nothing but the sign of a zero, and cost six FMAs per call.
