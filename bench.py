@@ -470,17 +470,19 @@ def run_ours(args):
     dom_bytes = STAGE_BYTES[(pname, dominant)] * cells
     peak, peak_kind = measured_peaks()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = None
+    traffic, traffic_source = None, None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         tk = json.loads(tfile.read_text()).get(f"{args.workload}/{pname}/stage{dominant}")
         if tk is not None:
             traffic = float(tk["bytes_per_cell"]) * cells
+            traffic_source = tk["source"] + " x cells, from profiles/traffic.json (not measured in this run)"
     step_bytes = (STAGE_BYTES[(pname, 1)] + STAGE_BYTES[(pname, 2)]) * cells
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic,
                 "kernel": f"sweep_kernel (stage {dominant})" if prec == md.MIXED else f"stage_kernel<double, 0> (stage {dominant})",
                 "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic_source": traffic_source,
                 "stage_ms": [s1, s2],
                 "step_frac": step_bytes / (ms / args.steps * 1e-3) / 1e9 / peak}
 

@@ -256,3 +256,23 @@ def test_mixed_fused_unaligned_face_arrays(mh):
         outs.append([uc_out] + bouts)
     for x, y in zip(*outs):
         assert torch.equal(x, y)
+
+
+def test_advance_checked_on_the_fused_path(mh):
+    """The rollback of advance_checked with the mixed fused stage (N = 32):
+    a poisoned zone is counted by the first stage's recovery, the state and
+    clock are put back, and an unpoisoned three-step call (odd, so the face
+    fields end in the workspace scratch and are copied back) advances."""
+    from mara3p_gb300._capi import MaraError
+    s = mh.initial_state(mh.MhdConfig(N=32), seed=6, modes=8)
+    run = mh.Run(s, precision=mh.MIXED)
+    run.advance_checked(3)
+    c = run.clock.read()
+    assert c["iteration"] == 3 and c["failures"] == 0
+    s.uc[4, 5, 6, 7] = -10.0
+    before = [s.uc.clone()] + [b.clone() for b in s.bf]
+    t0 = c["time"]
+    with pytest.raises(MaraError, match="restored"):
+        run.advance_checked(2)
+    assert torch.equal(s.uc, before[0]) and all(torch.equal(b, b0) for b, b0 in zip(s.bf, before[1:]))
+    assert run.clock.read()["time"] == t0
