@@ -1348,7 +1348,9 @@ int emf_attribute(int dev)
 // most 16 planes per chunk (blocks of equal work finish in waves, and a short
 // last wave of long blocks leaves most SMs idle; measured at 128^3 and 256^3),
 // at least four planes per chunk (each chunk solves one extra layer of faces)
-template<typename K>
+// (WHICH keeps one occupancy cache per kernel: both kernels have the same
+// function type, so the type alone would share one)
+template<int WHICH, typename K>
 int fused_chunks(K kernel, size_t smem, int N, int* chunks)
 {
     static PerDeviceOnce once;
@@ -1395,8 +1397,8 @@ int stage_fused(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int
     if (int r = emf_attribute<0>(dev)) return r;
     if (int r = emf_attribute<MIX_INCREMENT>(dev)) return r;
     if (int r = emf_attribute<MIX_FROM_INCREMENT>(dev)) return r;
-    if (int r = fused_chunks(flux_kernel<MIX_FROM_INCREMENT>, 0, N, &cf)) return r;
-    if (int r = fused_chunks(emf_kernel<MIX_INCREMENT>, esm, N, &ce)) return r;
+    if (int r = fused_chunks<0>(flux_kernel<MIX_FROM_INCREMENT>, 0, N, &cf)) return r;
+    if (int r = fused_chunks<1>(emf_kernel<MIX_INCREMENT>, esm, N, &ce)) return r;
     if (mixed_mode == MIX_INCREMENT) flux_kernel<MIX_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
     else if (mixed_mode == MIX_FROM_INCREMENT) flux_kernel<MIX_FROM_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
     else flux_kernel<MIX_PLAIN><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
