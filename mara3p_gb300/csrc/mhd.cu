@@ -609,7 +609,13 @@ update_kernel(const Args A)
 // updated state and faces, with the next stage's fastest wavespeed: the
 // primitive kernel runs only for the first stage of a call.
 namespace fused {
-constexpr int TJ = 8, TK = 32, THREADS = 256;
+constexpr int TJ = 8, TK = 32;
+// Threads per block. Nine warps let a plane's 832 face updates (EMF) take
+// three rounds per thread instead of a fourth for a quarter of the threads;
+// for the 808 face solves (flux) nine warps held the kernel to 56 registers
+// and were slower. Measured at 128^3 (RK2 step, flux/EMF threads):
+// 256/256 0.502 ms, 288/288 0.505, 288/256 0.509, 256/288 0.497.
+constexpr int FLUX_THREADS = 256, EMF_THREADS = 288;
 // Face E-fields in the EMF kernel, rows of XK (YK, ZK) floats with element
 // kk at row offset kk + 4 (kk + 1 for z), so that the x and y rows' interior
 // kk in [0, TK) is 16-byte aligned for vector copies
@@ -626,7 +632,9 @@ constexpr int E2K = TK, E2N = (TJ + 1) * E2K;       // along k: jj in [0, TJ], k
 constexpr int pad32(int n) { return (n + 31) & ~31; }
 // work items per phase, each kind padded to whole warps so that no warp mixes kinds
 constexpr int SOLVE_Y = pad32(FYN), SOLVE_Z = pad32(FZN);
-constexpr int EDGE_0 = pad32(E0N), EDGE_1 = pad32(E1N), EDGE_2 = pad32(E2N);
+// edge items are not padded: the three kinds cost alike, and padding would
+// add a fourth round
+constexpr int EDGE_0 = E0N, EDGE_1 = E1N, EDGE_2 = E2N;
 // copies per plane: x and y rows as TK/4 16-byte pieces plus the two halo
 // elements; z rows (N + 1 floats, unaligned) element by element
 constexpr int ROW_PIECES = TK / 4 + 2;
@@ -652,8 +660,8 @@ struct __align__(16) EmfSmem
     double bx[2][FXN];         // updated x faces; layer l in slot l & 1
     double by[FYN];            // updated y faces of plane c-1 (row TJ: the neighbour's, for the cells)
     double bz[FZN];
-    double wmax[THREADS / 32];
-    unsigned long long wbad[THREADS / 32];
+    double wmax[EMF_THREADS / 32];
+    unsigned long long wbad[EMF_THREADS / 32];
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
@@ -711,7 +719,7 @@ __device__ __forceinline__ void stencil(const float* P, uint32_t c0, uint32_t c1
 }
 
 template<int MODE>
-__global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, int chunks)
+__global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args A, int chunks)
 {
     using namespace fused;
     __shared__ FluxSmem S;
@@ -753,7 +761,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
     auto stage_cells = [&](int c) {
         // rows of TK cells: TK/2 16-byte pieces of state, TK/4 of increments, per component
         constexpr int UP = TJ * TK / 2, DP = TJ * TK / 4;
-        for (int t = threadIdx.x; t < 5 * (UP + DP); t += THREADS)
+        for (int t = threadIdx.x; t < 5 * (UP + DP); t += FLUX_THREADS)
         {
             const bool u = t < 5 * UP;
             const int v = u ? t : t - 5 * UP, per = u ? UP : DP;
@@ -770,13 +778,13 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
         cp_async_commit();
     };
 
-    for (int t = threadIdx.x; t < FXN; t += THREADS) solve_x(t, T.i0, true);
+    for (int t = threadIdx.x; t < FXN; t += FLUX_THREADS) solve_x(t, T.i0, true);
     for (int c = T.i0; c < T.i1; ++c)
     {
         __syncthreads();                   // the previous plane's cell updates are done
         if (READS_U) stage_cells(c);
         const bool x_owned = c + 1 < T.i1 || c + 1 == N;
-        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += THREADS)
+        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += FLUX_THREADS)
         {
             if (t < FXN)
             {
@@ -822,7 +830,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
         if (READS_U) cp_async_wait_all();
         __syncthreads();
         const float dtdl = s_dtdl;
-        for (int t = threadIdx.x; t < FXN; t += THREADS)
+        for (int t = threadIdx.x; t < FXN; t += FLUX_THREADS)
         {
             const int jj = t / TK, kk = t - jj * TK;
             const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0 + kk);
@@ -852,7 +860,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) flux_kernel(const Args A, i
 // 0 none, MIX_INCREMENT (the next step's first stage: from A.next_uc) or
 // MIX_FROM_INCREMENT (the second stage: A.next_uc plus the FP32 increment).
 template<int NEXT>
-__global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, int chunks)
+__global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A, int chunks)
 {
     using namespace fused;
     extern __shared__ __align__(16) unsigned char emf_smem[];
@@ -871,7 +879,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
     // face E-fields of layer lx (when load_x) and of plane py, as one cp.async group
     auto load = [&](bool load_x, int lx, int py) {
         const uint32_t pw = uint32_t(wrap(py, N));
-        for (int t = threadIdx.x; t < LOAD_X + LOAD_Y + LOAD_Z; t += THREADS)
+        for (int t = threadIdx.x; t < LOAD_X + LOAD_Y + LOAD_Z; t += EMF_THREADS)
         {
             if (t < LOAD_X + LOAD_Y)
             {
@@ -918,7 +926,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
     auto stage_faces = [&](int c, bool first) {
         constexpr int XP = TJ * TK / 2, YP = (TJ + 1) * TK / 2;
         const int arrays = with_avg ? 2 : 1;
-        for (int t = threadIdx.x; t < arrays * (XP + YP + FZN); t += THREADS)
+        for (int t = threadIdx.x; t < arrays * (XP + YP + FZN); t += EMF_THREADS)
         {
             const int a = t / (XP + YP + FZN), v = t - a * (XP + YP + FZN);
             double* dst = a ? S.bav : S.bin;
@@ -958,7 +966,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
         if (!last) load(true, c + 1, c + 1);
         const int s = c & 1, sp = (c - 1) & 1, ys = mod3(c), yp = mod3(c - 1);
         // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order)
-        for (int t = threadIdx.x; t < EDGE_0 + EDGE_1 + EDGE_2; t += THREADS)
+        for (int t = threadIdx.x; t < EDGE_0 + EDGE_1 + EDGE_2; t += EMF_THREADS)
         {
             if (t < EDGE_0)
             {
@@ -994,7 +1002,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
         // faces: x of layer c (the tile); y and z of plane c-1, with the high
         // neighbour's row and column, which the next-stage cells need
         const double dtdl_d = s_dtdl;
-        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += THREADS)
+        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += EMF_THREADS)
         {
             if (t < FXN)
             {
@@ -1040,7 +1048,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
             __syncthreads();
             // the next stage's primitives of plane c-1 (the primitive kernel's arithmetic)
             float* P = static_cast<float*>(A.P);
-            for (int t = threadIdx.x; t < FXN; t += THREADS)
+            for (int t = threadIdx.x; t < FXN; t += EMF_THREADS)
             {
                 const int jj = t / TK, kk = t - jj * TK;
                 const int64_t cell = cidx32(N, c - 1, T.j0 + jj, T.k0 + kk);
@@ -1073,7 +1081,7 @@ __global__ void __launch_bounds__(fused::THREADS, 4) emf_kernel(const Args A, in
         {
             double r = 0.0;
             unsigned long long nbad = 0;
-            for (int w = 0; w < THREADS / 32; ++w)
+            for (int w = 0; w < EMF_THREADS / 32; ++w)
             {
                 r = fmax(r, S.wmax[w]);
                 nbad += S.wbad[w];
@@ -1351,7 +1359,7 @@ int emf_attribute(int dev)
 // (WHICH keeps one occupancy cache per kernel: both kernels have the same
 // function type, so the type alone would share one)
 template<int WHICH, typename K>
-int fused_chunks(K kernel, size_t smem, int N, int* chunks)
+int fused_chunks(K kernel, int threads, size_t smem, int N, int* chunks)
 {
     static PerDeviceOnce once;
     static int slots[64] = {};
@@ -1359,7 +1367,7 @@ int fused_chunks(K kernel, size_t smem, int N, int* chunks)
     MARA_CUDA(cudaGetDevice(&dev));
     if (int r = once.run(dev, [&]() -> int {
             int b = 0, n = 0;
-            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, fused::THREADS, smem));
+            MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem));
             MARA_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
             slots[dev & 63] = n * (b > 0 ? b : 1);
             return MARA_OK;
@@ -1397,15 +1405,15 @@ int stage_fused(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int
     if (int r = emf_attribute<0>(dev)) return r;
     if (int r = emf_attribute<MIX_INCREMENT>(dev)) return r;
     if (int r = emf_attribute<MIX_FROM_INCREMENT>(dev)) return r;
-    if (int r = fused_chunks<0>(flux_kernel<MIX_FROM_INCREMENT>, 0, N, &cf)) return r;
-    if (int r = fused_chunks<1>(emf_kernel<MIX_INCREMENT>, esm, N, &ce)) return r;
-    if (mixed_mode == MIX_INCREMENT) flux_kernel<MIX_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
-    else if (mixed_mode == MIX_FROM_INCREMENT) flux_kernel<MIX_FROM_INCREMENT><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
-    else flux_kernel<MIX_PLAIN><<<tiles * cf, fused::THREADS, 0, s>>>(A, cf);
+    if (int r = fused_chunks<0>(flux_kernel<MIX_FROM_INCREMENT>, fused::FLUX_THREADS, 0, N, &cf)) return r;
+    if (int r = fused_chunks<1>(emf_kernel<MIX_INCREMENT>, fused::EMF_THREADS, esm, N, &ce)) return r;
+    if (mixed_mode == MIX_INCREMENT) flux_kernel<MIX_INCREMENT><<<tiles * cf, fused::FLUX_THREADS, 0, s>>>(A, cf);
+    else if (mixed_mode == MIX_FROM_INCREMENT) flux_kernel<MIX_FROM_INCREMENT><<<tiles * cf, fused::FLUX_THREADS, 0, s>>>(A, cf);
+    else flux_kernel<MIX_PLAIN><<<tiles * cf, fused::FLUX_THREADS, 0, s>>>(A, cf);
     if (int r = launch_status("mhd flux_kernel")) return r;
-    if (next == MIX_INCREMENT) emf_kernel<MIX_INCREMENT><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
-    else if (next == MIX_FROM_INCREMENT) emf_kernel<MIX_FROM_INCREMENT><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
-    else emf_kernel<0><<<tiles * ce, fused::THREADS, esm, s>>>(A, ce);
+    if (next == MIX_INCREMENT) emf_kernel<MIX_INCREMENT><<<tiles * ce, fused::EMF_THREADS, esm, s>>>(A, ce);
+    else if (next == MIX_FROM_INCREMENT) emf_kernel<MIX_FROM_INCREMENT><<<tiles * ce, fused::EMF_THREADS, esm, s>>>(A, ce);
+    else emf_kernel<0><<<tiles * ce, fused::EMF_THREADS, esm, s>>>(A, ce);
     return launch_status("mhd emf_kernel");
 }
 
