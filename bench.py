@@ -94,6 +94,10 @@ def parse():
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="mixed vs FP64 error check: RK2 steps of both paths from one state (0 = skip); the "
                          "4096^2 configuration's own 2000 by default")
+    ap.add_argument("--accuracy-control", action="store_true",
+                    help="minidisk: with the error check, a third run, FP64 from the same state with each value "
+                         "moved by one unit of 2^-24 (one FP32 rounding), compared with the FP64 run the same way "
+                         "(about 90 s more at 4096^2)")
     return ap.parse_args()
 
 
@@ -359,7 +363,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def mixed_accuracy(md, sd, u0, steps: int) -> dict:
+def mixed_accuracy(md, sd, u0, steps: int, control: bool = False) -> dict:
     """Mixed vs FP64 relative L1 after `steps` RK2 steps from one state, each
     path with its own CFL dt (an FP64 evaluation in both), also at half the
     horizon; globally and over the interior, the mesh less a frame of 0.5
@@ -373,6 +377,15 @@ def mixed_accuracy(md, sd, u0, steps: int) -> dict:
     inner = x.abs() < sd.domain_radius - 0.5
     mask = (inner[:, None] & inner[None, :]).to(torch.float64)
     runs = {p: md.Run(sd, u0.clone(), rk_order=2, precision=p, dt_mode=md.DT_CFL) for p in (md.FP64, md.MIXED)}
+    if control:
+        # the control: FP64 from the state with every value moved by a relative
+        # 2^-24 of seeded sign, once, at the start (the mixed path rounds to
+        # FP32 in every flux of every step, a larger perturbation)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(12345)
+        sign = torch.randint(0, 2, u0.shape, generator=g, device="cuda").to(torch.float64) * 2 - 1
+        runs["control"] = md.Run(sd, u0 * (1 + sign * 2.0 ** -24), rk_order=2, precision=md.FP64,
+                                 dt_mode=md.DT_CFL)
     out = {"dt": "CFL 0.3, FP64 in each path",
            "interior": "|x|, |y| < domain_radius - 0.5 (the periodic seams excluded)"}
     done = 0
@@ -388,6 +401,13 @@ def mixed_accuracy(md, sd, u0, steps: int) -> dict:
                             "interior_rel_l1_vs_fp64": {"density": reli[0], "momentum_x": reli[1],
                                                         "momentum_y": reli[2]},
                             "time": runs[md.MIXED].time, "time_fp64": runs[md.FP64].time}
+        if control:
+            c = runs["control"].u
+            out[str(target)]["control_fp64_perturbed_2e-24"] = {
+                "rel_l1_vs_fp64": {"density": float((c[0] - b[0]).abs().sum() / b[0].abs().sum())},
+                "interior_rel_l1_vs_fp64": {"density": float(((c[0] - b[0]).abs() * mask).sum()
+                                                             / (b[0].abs() * mask).sum())},
+                "time": runs["control"].time}
     out["steps"] = steps
     out["rel_l1_vs_fp64"] = out[str(steps)]["rel_l1_vs_fp64"]
     out["finite"] = bool(torch.isfinite(runs[md.MIXED].u).all().item() and torch.isfinite(runs[md.FP64].u).all().item())
@@ -568,7 +588,7 @@ def run_ours(args):
         del frun
     accuracy = None
     if prec == md.MIXED and args.accuracy_steps > 0:
-        accuracy = mixed_accuracy(md, sd, u0, args.accuracy_steps)
+        accuracy = mixed_accuracy(md, sd, u0, args.accuracy_steps, args.accuracy_control)
 
     if rank == 0:
         line = {
