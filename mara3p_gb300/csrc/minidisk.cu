@@ -387,7 +387,18 @@ __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A, cons
                                                               const __grid_constant__ CUtensorMap dmap)
 {
     extern __shared__ __align__(128) unsigned char ring_smem[];  // two-column form: one ring per warp
-    const int warp = blockIdx.x * int(blockDim.x >> 5) + (threadIdx.x >> 5);
+    int block = int(blockIdx.x);
+    if (A.side_binary)
+    {
+        // block 0 is scheduled first: its binary job overlaps the whole stage
+        if (block == 0)
+        {
+            if (threadIdx.x == 0) side_binary_job(A);
+            return;
+        }
+        block -= 1;
+    }
+    const int warp = block * int(blockDim.x >> 5) + (threadIdx.x >> 5);
     const int sx = warp / A.tiles_y, sy = warp - sx * A.tiles_y;
     const int i0 = sx * A.sweep_rows;
     if (i0 >= A.N) return;                    // uniform per warp
@@ -491,7 +502,7 @@ int launch_sweep(Args A, cudaStream_t s)
     A.sweep_rows = std::max(waves > 1 ? 2 : 32, (A.N + segments - 1) / segments);
     const int strips_x = (A.N + A.sweep_rows - 1) / A.sweep_rows;
     const int warps = strips_x * A.tiles_y;
-    const int blocks = (warps + wpb - 1) / wpb;
+    const int blocks = (warps + wpb - 1) / wpb + (A.side_binary ? 1 : 0);
     if (tma) sweep_kernel<KIND, COLS, DIAG, true><<<blocks, wpb * 32, smem, s>>>(A, umap, dmap);
     else sweep_kernel<KIND, COLS, DIAG, false><<<blocks, wpb * 32, smem, s>>>(A, umap, dmap);
     return launch_status("minidisk sweep kernel");
@@ -762,6 +773,9 @@ Args base_args(const mara_minidisk_params* sd)
     A.mach = sd->mach_number;
     A.nu = sd->nu;
     A.omega = sd->omega_frame;
+    A.mass_ratio = sd->mass_ratio;
+    A.eccentricity = sd->eccentricity;
+    A.side_binary = 0;
     A.sink_rate = sd->sink_rate;
     A.s6 = std::pow(sd->sink_radius, 6.0);
     A.buffer_rate = sd->buffer_rate;
@@ -895,15 +909,17 @@ ClockArgs clock_args(const mara_minidisk_params* sd, int dt_mode, int rk_order, 
     a.rk_order = rk_order;
     a.end_step = end_step;
     a.begin_step = begin_step;
+    a.binaries = 1;
     return a;
 }
 
 int clock_step(const mara_minidisk_params* sd, mara_minidisk_clock* clock, int dt_mode, int rk_order,
                int end_step, int begin_step, cudaStream_t s, mara_minidisk_diagnostics* diag = nullptr,
-               const double* key_state = nullptr)
+               const double* key_state = nullptr, int binaries = 1)
 {
     ClockArgs a = clock_args(sd, dt_mode, rk_order, end_step, begin_step);
     a.diag = diag;
+    a.binaries = binaries;
     if (key_state)
     {
         a.wavespeed_key = 1;
@@ -1119,6 +1135,9 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
 
     double* rate0 = diag ? diag->rate[0] : nullptr;
     double* rate1 = diag ? diag->rate[1] : nullptr;
+    // mixed RK2 on the sweep path: the stage binaries are solved inside the
+    // sweeps (Args::side_binary), off the step's critical path
+    const bool side_binaries = precision == MARA_MIXED && rk_order == 2 && N >= 64;
 
     // a held formula dt is chosen by the call's first step
     if (int r = clock_step(sd, clock, dt_mode == MARA_DT_FORMULA_HELD ? MARA_DT_FORMULA : dt_mode, rk_order, 0, 1, s,
@@ -1142,13 +1161,16 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
         }
         else if (rk_order == 2)
         {
+            // the sweeps (N >= 64) solve the stage binaries in their block 0
             Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1; a1.diag = rate0;
+            a1.side_binary = side_binaries ? 1 : 0;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             const bool last_out = final_out && step + 1 == steps;
             Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = last_out ? final_out : alt;
             a2.amax = amax;
             a2.amax_key = 1;
             a2.diag = rate1;
+            a2.side_binary = side_binaries ? 2 : 0;
             if (int r = grid_stage(a2, K_MIX2, s)) return r;
             if (last_out) cur = final_out;
             else std::swap(cur, alt);
@@ -1162,7 +1184,9 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
         }
         // mixed CFL: the reduction named the fastest cell of the new state cur
         const double* key_state = precision == MARA_MIXED && amax ? cur : nullptr;
-        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag, key_state)) return r;
+        if (int r = clock_step(sd, clock, dt_mode, rk_order, 1, step + 1 < steps, s, diag, key_state,
+                               side_binaries ? 0 : 1))
+            return r;
     }
     if (cur != u && cur != final_out)
         MARA_CUDA(cudaMemcpyAsync(u, cur, 3 * NN * sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -64,6 +64,13 @@ struct Args
     int amax_key;          // mixed kinds: 1 = write the speed key of the fastest cell (speed_key) instead
     double* diag;          // optional: rate row of this stage (diagnostic sums 0..12 of the stage input)
     FloatConsts f;
+    // Mixed RK2 sweeps: block 0 of the launch solves a binary off the
+    // critical path (side_binary_job): 1 = the stage-2 binary, at t + dt,
+    // into clock->binary[1] (stage 1 reads binary[0]); 2 = the next step's
+    // stage-1 binary, at the RK2 end time, into clock->binary[0] (stage 2
+    // reads binary[1]). 0 = none.
+    int side_binary;
+    double mass_ratio, eccentricity;
 };
 
 // Diagnostic sums taken per cell (the rate-vector entries 0..12 of
@@ -1111,6 +1118,7 @@ struct ClockArgs
     const double* u_key[2];
     int N, n, level;
     double rs2, mach;
+    int binaries;     // begin_step: 1 = solve both stage binaries here; 0 = the sweeps' binary jobs do
 };
 
 // iso2d::fastest_wavespeed at the cell-centre sound speed, FP64, of cell c of
@@ -1163,6 +1171,31 @@ __device__ inline void store_binary(double* dst, const Binary& b)
 // The parts of one clock update. `lanes` threads of one warp may share the
 // begin-step work: lane 0 does everything else, lane 1 (when present)
 // computes the second stage's binary while lane 0 computes the first.
+// The time after an RK2 step from t with step dt: the weighted_sum of the
+// stage times (one function for the clock and the sweeps' binary job, so
+// that both form the same double)
+__device__ inline double rk2_end_time(double t, double dt)
+{
+    const double t2 = (t + dt) + dt;
+    return t * 0.5 + t2 * (1.0 - 0.5);
+}
+
+__device__ inline void store_binary(double* dst, const Binary& b);
+
+// A sweep launch's binary job (Args::side_binary), by one thread of block 0:
+// the FP64 Kepler solve that the clock kernel would otherwise run between
+// the steps, overlapped with the stage it precedes. The clock memory is
+// written here and read by the next launches only.
+static __device__ __noinline__ void side_binary_job(const Args& A)
+{
+    mara_minidisk_clock* c = const_cast<mara_minidisk_clock*>(A.clock);
+    const double t = c->time, dt = c->dt;
+    if (A.side_binary == 1)
+        store_binary(c->binary[1], binary_state(A.mass_ratio, A.eccentricity, A.omega, t + dt));
+    else
+        store_binary(c->binary[0], binary_state(A.mass_ratio, A.eccentricity, A.omega, rk2_end_time(t, dt)));
+}
+
 __device__ inline void clock_end_step(mara_minidisk_clock* c, const ClockArgs& a)
 {
     if (a.diag) finish_diagnostics(c, a);
@@ -1179,8 +1212,7 @@ __device__ inline void clock_end_step(mara_minidisk_clock* c, const ClockArgs& a
     double t = c->time, dt = c->dt;
     if (a.rk_order == 2)
     {
-        double t2 = (t + dt) + dt;
-        c->time = t * 0.5 + t2 * (1.0 - 0.5);   // weighted_sum of the RK2 solution times
+        c->time = rk2_end_time(t, dt);   // weighted_sum of the RK2 solution times
     }
     else
     {
@@ -1217,8 +1249,9 @@ __device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a,
     if (a.begin_step)
     {
         const double t = c->time, dt = c->dt;
-        for (int s = lane; s < 2; s += lanes)
-            store_binary(c->binary[s], binary_state(a.mass_ratio, a.eccentricity, a.omega, s == 0 ? t : t + dt));
+        if (a.binaries)
+            for (int s = lane; s < 2; s += lanes)
+                store_binary(c->binary[s], binary_state(a.mass_ratio, a.eccentricity, a.omega, s == 0 ? t : t + dt));
         if (lanes > 1) __syncwarp(0x3u);
         if (lane == 0)
         {
