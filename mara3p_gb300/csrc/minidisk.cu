@@ -24,6 +24,7 @@
 #include <cudaTypedefs.h>
 #include <cstdint>
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
         for (int k = 0; k < 6; ++k) b6[k] = A.bin[k];
     }
     double local_max = 0.0;
-    unsigned long long local_key = 0ull;   // mixed kinds
+    KeyMax local_key;                      // mixed kinds
     float bf[6];
     for (int k = 0; k < 6; ++k) bf[k] = d2f(b6[k]);
     const float dtf = d2f(dt);
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const Args A, const __grid_co
 
     if (A.amax && sizeof(R) == sizeof(float))
     {
-        flush_speed_key(A, local_key);
+        flush_speed_key(A, local_key.key());
     }
     else if (A.amax)
     {
@@ -803,6 +804,10 @@ Args base_args(const mara_minidisk_params* sd)
     f.visc_mu = float(A.nu * 0.5 * 0.25 / A.dl);
     f.sink_ex2 = float(-1.4426950408889634 / A.s6);
     f.buffer_ex2 = float(-2.0 * 1.4426950408889634 / A.buffer_scale);
+    // q^3 |sink_ex2| >= 127 (after the three roundings of the device's
+    // product, still above 126.99): 2^(q^3 sink_ex2) < 2^-126 flushes to zero
+    const double c = std::fabs(double(f.sink_ex2));
+    f.sink_far = std::isfinite(c) && c > 0.0 ? float(std::cbrt(127.0 / c) * (1.0 + 1e-6)) : INFINITY;
     return A;
 }
 

@@ -36,6 +36,7 @@ struct FloatConsts
     float visc_mu;          // nu / 2 / (4 dl): the viscous coefficient per (Sigma_l + Sigma_r) of doubled slopes
     float sink_ex2;         // -log2(e) / s^6: sink rate = sink_rate 2^(q^3 sink_ex2), q = |x - x_body|^2
     float buffer_ex2;       // -2 log2(e) / buffer_scale
+    float sink_far;         // q at and beyond which 2^(q^3 sink_ex2) is below the smallest normal float: exactly 0
 };
 
 struct Args
@@ -165,17 +166,33 @@ __device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float2 vmax(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 __device__ __forceinline__ float2 vmin(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
 
+// Three-input minimum and maximum (sm_100 and later).
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // The FP32 slopes are kept DOUBLED: for a = y0 - yl, b = yr - yl, c = yr - y0,
-// 2 minmod(theta a, b / 2, theta c) = sign x min(2 theta min(|a|, |c|), |b|)
-// (plm_gradient_scalar_t, scheme_plm_gradient.hpp:44-67). Scaling by two and
-// taking minima commute with rounding, so this is exactly twice the slope of
-// the three-multiply form, in one multiply; consumers take a quarter of it
-// for the face values.
+// 2 minmod(theta a, b / 2, theta c) = minmod(x, b, z) with x = 2 theta a,
+// z = 2 theta c (plm_gradient_scalar_t, scheme_plm_gradient.hpp:44-67);
+// consumers take a quarter of it for the face values. The three-argument
+// minmod is a median, max(min(x, b, z), min(max(x, b, z), 0)): the smallest
+// when all three are positive, the largest when all are negative, else zero.
+// Scaling by 2 theta and taking minima commute with rounding, so this is
+// exactly twice the three-multiply slope (only the sign of a zero result can
+// differ from a sign-bit test).
 __device__ __forceinline__ float minmod2(float a, float b, float c, float two_theta)
 {
-    const float m = fminf(vmul(two_theta, fminf(fabsf(a), fabsf(c))), fabsf(b));
-    const int sa = __float_as_int(a), sb = __float_as_int(b), sc = __float_as_int(c);
-    return ((sa ^ sb) | (sa ^ sc)) < 0 ? 0.0f : copysignf(m, a);
+    const float x = vmul(two_theta, a), z = vmul(two_theta, c);
+    return fmaxf(min3f(x, b, z), fminf(max3f(x, b, z), 0.0f));
 }
 
 template<typename T>
@@ -323,6 +340,17 @@ __device__ inline void face_flux(const float pa[3], const float pb[3], const flo
 __device__ __forceinline__ void diag_add(float& a, float v) { a += v; }
 __device__ __forceinline__ void diag_add(float& a, float2 v) { a += v.x + v.y; }
 
+// True where the calling lanes' q1 and q2 (each column of a pair) are all
+// at least q_far.
+__device__ __forceinline__ bool all_beyond(float q1, float q2, float q_far)
+{
+    return __all_sync(__activemask(), q1 >= q_far && q2 >= q_far);
+}
+__device__ __forceinline__ bool all_beyond(float2 q1, float2 q2, float q_far)
+{
+    return __all_sync(__activemask(), q1.x >= q_far && q1.y >= q_far && q2.x >= q_far && q2.y >= q_far);
+}
+
 template<typename T, bool DIAG = false>
 __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc[3], const T dfx[3], const T dfy[3],
                                       const float bf[6], float dtf, T du[3], T uc[3], T& spot, float* acc = nullptr)
@@ -336,10 +364,17 @@ __device__ inline void cell_increment(const FloatConsts& F, T x, T y, const T pc
     const T i1 = vrsqrt(vadd(q1, bc<T>(F.rs2))), i2 = vrsqrt(vadd(q2, bc<T>(F.rs2)));
     const T g1 = vmul(vmul(vmul(bc<T>(-bf[0]), i1), i1), i1);
     const T g2 = vmul(vmul(vmul(bc<T>(-bf[3]), i2), i2), i2);
-    // sinks: sink_rate exp(-r^6 / s^6) as sink_rate 2^(q^3 sink_ex2), q = r^2
-    const T e1 = vex2(vmul(vmul(q1, q1), vmul(q1, bc<T>(F.sink_ex2))));
-    const T e2 = vex2(vmul(vmul(q2, q2), vmul(q2, bc<T>(F.sink_ex2))));
-    const T srs = vmul(bc<T>(F.sink_rate), vadd(e1, e2));
+    // sinks: sink_rate exp(-r^6 / s^6) as sink_rate 2^(q^3 sink_ex2), q = r^2.
+    // Where every cell of the warp lies at q >= sink_far from both bodies
+    // (nearly all of the mesh), the flushed 2^(...) is exactly zero for all
+    // of them, and the warp skips it.
+    T e1 = bc<T>(0.0f), e2 = bc<T>(0.0f), srs = bc<T>(0.0f);
+    if (!all_beyond(q1, q2, F.sink_far))
+    {
+        e1 = vex2(vmul(vmul(q1, q1), vmul(q1, bc<T>(F.sink_ex2))));
+        e2 = vex2(vmul(vmul(q2, q2), vmul(q2, bc<T>(F.sink_ex2))));
+        srs = vmul(bc<T>(F.sink_rate), vadd(e1, e2));
+    }
     const T r2 = vfma(x, x, vmul(y, y));
     const T rinv = vrsqrt(r2);
     const T rr = vmul(r2, rinv);
@@ -427,6 +462,37 @@ __device__ __forceinline__ unsigned long long speed_key(float v, size_t idx)
 
 __device__ __forceinline__ unsigned long long key_max(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
+// A thread's running maximum of speed keys, for cells visited in any order.
+struct KeyMax
+{
+    unsigned long long k = 0ull;
+    __device__ __forceinline__ void take(float v, size_t idx) { k = key_max(k, speed_key(v, idx)); }
+    __device__ __forceinline__ unsigned long long key() const { return k; }
+};
+
+// The same maximum for a sweep lane, whose cells arrive in increasing index
+// order: the wavespeed bits and the index of the fastest so far, kept apart
+// (one unsigned comparison per cell instead of a 64-bit key and its
+// comparison). >= moves ties to the later, larger index, so key() equals
+// KeyMax's key over the same cells.
+struct LaneMax
+{
+    unsigned bits = 0u, idx = 0u;
+    __device__ __forceinline__ void take(float v, size_t i)
+    {
+        const unsigned b = __float_as_uint(v);
+        if (b >= bits)
+        {
+            bits = b;
+            idx = unsigned(i);
+        }
+    }
+    __device__ __forceinline__ unsigned long long key() const
+    {
+        return (static_cast<unsigned long long>(bits) << 32) | idx;
+    }
+};
+
 // The end of a warp's CFL reduction: the key, or the FP32 maximum as double
 // bits where the caller asked for the wavespeed itself.
 __device__ inline void flush_speed_key(const Args& A, unsigned long long key)
@@ -452,10 +518,10 @@ __device__ inline float wavespeed_f(const FloatConsts& F, float s, float m1, flo
 // FP64 state u_in + du (with the RK2 average of the two increments in stage
 // 2). The CFL wavespeed of the new state is taken from its FP32 image: the
 // stage input plus du (RK1), or u0 + (d1 + du)/2 = u1 + (du - d1)/2 (RK2).
-template<int KIND, bool DIAG = false>
+template<int KIND, bool DIAG = false, typename Max>
 __device__ inline void mixed_cell(const Args& A, float x, float y, const float pc[3], const float dfx[3],
                                   const float dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                  const CellIn<float>& in, unsigned long long& local_key, float* acc = nullptr)
+                                  const CellIn<float>& in, Max& local_max, float* acc = nullptr)
 {
     float du[3], uc[3], spot;
     cell_increment<float, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, spot, acc);
@@ -467,18 +533,18 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
     float of[3];
     for (int k = 0; k < 3; ++k)
     {
-        const float inc = KIND == K_MIX2 ? vmul(vadd(in.d[k], du[k]), 0.5f) : du[k];
-        A.u_out[k * NN + idx] = in.u[k] + f2d(inc);
+        const float inc = KIND == K_MIX2 ? vadd(in.d[k], du[k]) : du[k];
+        A.u_out[k * NN + idx] = __fma_rn(f2d(inc), KIND == K_MIX2 ? 0.5 : 1.0, in.u[k]);
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), 0.5f, uc[k]) : vadd(uc[k], du[k]);
     }
-    if (A.amax) local_key = key_max(local_key, speed_key(wavespeed_f(A.f, of[0], of[1], of[2], spot), idx));
+    if (A.amax) local_max.take(wavespeed_f(A.f, of[0], of[1], of[2], spot), idx);
 }
 
 // The pair form: columns idx and idx + 1 of one row (idx even).
 template<int KIND, bool DIAG = false>
 __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const float2 pc[3], const float2 dfx[3],
                                    const float2 dfy[3], const float bf[6], float dtf, size_t idx, size_t NN,
-                                   const CellIn<float2>& in, unsigned long long& local_key, float* acc = nullptr)
+                                   const CellIn<float2>& in, LaneMax& local_max, float* acc = nullptr)
 {
     float2 du[3], uc[3], spot;
     cell_increment<float2, DIAG>(A.f, x, y, pc, dfx, dfy, bf, dtf, du, uc, spot, acc);
@@ -490,14 +556,18 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
     float2 of[3];
     for (int k = 0; k < 3; ++k)
     {
-        const float2 inc = KIND == K_MIX2 ? vmul(vadd(in.d[k], du[k]), bc<float2>(0.5f)) : du[k];
-        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = make_double2(in.u[k].x + f2d(inc.x),
-                                                                           in.u[k].y + f2d(inc.y));
+        // RK2: u0 + (d1 + d2)/2, the halving exact inside the FP64 fma; RK1: u + du
+        const float2 inc = KIND == K_MIX2 ? vadd(in.d[k], du[k]) : du[k];
+        const double h = KIND == K_MIX2 ? 0.5 : 1.0;
+        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = make_double2(__fma_rn(f2d(inc.x), h, in.u[k].x),
+                                                                           __fma_rn(f2d(inc.y), h, in.u[k].y));
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), bc<float2>(0.5f), uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax)
-        local_key = key_max(local_key, key_max(speed_key(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, spot.x), idx),
-                                               speed_key(wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, spot.y), idx + 1)));
+    {
+        local_max.take(wavespeed_f(A.f, of[0].x, of[1].x, of[2].x, spot.x), idx);
+        local_max.take(wavespeed_f(A.f, of[0].y, of[1].y, of[2].y, spot.y), idx + 1);
+    }
 }
 
 // A warp's diagnostic sums into the stage's rate row: FP32 per lane, a
@@ -618,7 +688,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
     slope_y(p0, theta, gy0);
     face_flux<0>(pm1, p0, gxm1, gx0, gym1, gy0, fmaf(float(i0), F.dl, -F.R), yc, A, fxm);
 
-    unsigned long long local_key = 0ull;
+    LaneMax local_max;
     float acc[DIAG ? DIAG_SUMS : 1] = {};
     for (int i = i0; i < i1; ++i)
     {
@@ -648,7 +718,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
             dfx[k] = vsub(fxp[k], fxm[k]);
         }
         if (interior)
-            mixed_cell<KIND, DIAG>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_key, acc);
+            mixed_cell<KIND, DIAG>(A, xc, yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin, local_max, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -660,7 +730,7 @@ __device__ __forceinline__ void sweep_strip(const Args& A, int i0, int i1, int s
         }
     }
     if constexpr (DIAG) diag_flush(A, acc);
-    if (A.amax) flush_speed_key(A, local_key);
+    if (A.amax) flush_speed_key(A, local_max.key());
 }
 
 // ------------------------------------------------------------- two-column sweep
@@ -998,7 +1068,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     slope_y2(p0, theta, gy0, l0);
     face_flux_f<0, float2>(pm1, p0, gxm1, gx0, gym1, gy0, bc<float2>(fmaf(float(i0), F.dl, -F.R)), yc, F, fxm);
 
-    unsigned long long local_key = 0ull;
+    LaneMax local_max;
     float acc[DIAG ? DIAG_SUMS : 1] = {};
     int slot0 = ring_slot(i0);                                // ring slot of row i, kept by increments
     for (int i = i0; i < i1; ++i)
@@ -1082,7 +1152,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
         }
         if (interior)
             mixed_cell2<KIND, DIAG>(A, bc<float2>(xc), yc, p0, dfx, dfy, bf, dtf, size_t(i) * N + jg, NN, cin,
-                                    local_key, acc);
+                                    local_max, acc);
 
         for (int k = 0; k < 3; ++k)
         {
@@ -1100,7 +1170,7 @@ __device__ __forceinline__ void sweep_strip2(const Args& A, int i0, int i1, int 
     if constexpr (RING == 1) cp_async_wait_all();
     if constexpr (RING == 2) tring_drain(*tma);
     if constexpr (DIAG) diag_flush(A, acc);
-    if (A.amax) flush_speed_key(A, local_key);
+    if (A.amax) flush_speed_key(A, local_max.key());
 }
 
 // ------------------------------------------------------------- clock
