@@ -998,21 +998,27 @@ def run_sedov(args):
         tracks.advance(dt, gin, gout, rk_order=rk)
         tracks.remesh(2.0, 0.5, 1.0)
 
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
     C, F = tracks.cells, tracks.cells + T
     stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # each step reads the new cell count back and allocates the remeshed
+    # arrays on the host's side, so one slow host call (an allocator miss)
+    # stalls the GPU inside the timed region: the line reports the median of
+    # the per-step CUDA-event times (and the mean beside it)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     cells_done = 0
     with ClockSampler(local) as sampler:
-        e0.record(stream)
-        for _ in range(args.steps):
+        ev[0].record(stream)
+        for s_ in range(args.steps):
             cells_done += tracks.cells
             step()
-        e1.record(stream)
+            ev[s_ + 1].record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    ms = float(np.median(per_step))
+    mean_ms = float(np.mean(per_step))
     value = cells_done / args.steps / (ms * 1e-3) * world
     # algorithmic bytes per cell and stage: conserved in and out (2 x 40 B),
     # face radii in and out (2 x 8 B per face)
@@ -1023,7 +1029,8 @@ def run_sedov(args):
             "traffic": None, "kernel": "whole step (prim, grad, radial, polar, update kernels, then remesh; bound by FP64 recovery and "
                                        "HLLC arithmetic, not by HBM)", "peak_source": f"{kind} hbm_gbs"}
     roof = fp64_roofline("sedov-tracks", Cm, ms, roof)
-    extra = {"gpu_launches": (1 + 5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count()}
+    extra = {"gpu_launches": (1 + 5 * rk + 3) * args.steps, "clocks": sampler.summary(), "failures": tracks.failure_count(),
+             "timing": f"median of {args.steps} per-step CUDA-event times (mean {mean_ms:.3f} ms)"}
     if not args.no_e2e:
         # through the public calls with host buffers: the tracks' state to the
         # GPU, one driver step, the (remeshed) state back, every step
@@ -1097,7 +1104,7 @@ RUNNERS = {"mhd-128": "run_mhd", "srhd-c2p": "run_srhd", "srhd-tube": "run_tube"
 def compact(line: dict) -> dict:
     """The figures of a workload's line that the headline line carries."""
     keep = ("metric", "value", "unit", "ms_per_step", "dtype", "config", "variants", "accuracy", "max_div_b",
-            "failures", "looped_single_mesh", "gpu_launches", "cpu_baseline")
+            "failures", "looped_single_mesh", "gpu_launches", "cpu_baseline", "timing")
     out = {k: line[k] for k in keep if line.get(k) is not None}
     if line.get("e2e"):
         out["e2e"] = {k: line["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")}

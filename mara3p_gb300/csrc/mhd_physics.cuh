@@ -46,7 +46,8 @@ __device__ inline float plm(float yl, float y0, float yr, float theta)
 // Scaling by two and taking minima commute with rounding, so this is exactly
 // twice the three-multiply form (normal values; the signs tested are those of
 // a, b, c, which scaling by theta > 0 keeps), and y +- 0.25 x plm2 rounds to
-// the same float as y +- 0.5 x plm.
+// the same float as y +- 0.5 x plm. (The median form of the minidisk sweeps,
+// in three-input minima and maxima, measured 0.4% slower here.)
 __device__ inline float plm2(float yl, float y0, float yr, float two_theta)
 {
     const float a = y0 - yl, b = yr - yl, c = yr - y0;

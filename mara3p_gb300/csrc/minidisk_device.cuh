@@ -166,20 +166,6 @@ __device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float2 vmax(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 __device__ __forceinline__ float2 vmin(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
 
-// Three-input minimum and maximum (sm_100 and later).
-__device__ __forceinline__ float min3f(float a, float b, float c)
-{
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float max3f(float a, float b, float c)
-{
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
 // The FP32 slopes are kept DOUBLED: for a = y0 - yl, b = yr - yl, c = yr - y0,
 // 2 minmod(theta a, b / 2, theta c) = minmod(x, b, z) with x = 2 theta a,
 // z = 2 theta c (plm_gradient_scalar_t, scheme_plm_gradient.hpp:44-67);

@@ -65,6 +65,21 @@ __device__ __forceinline__ float div_corrected(float a, float b, float r)
     return __fmaf_rn(r, __fmaf_rn(-b, q0, a), q0);
 }
 
+// Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later).
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 __device__ inline float sqrt_fast(float x)
 {
     float y;
