@@ -196,9 +196,16 @@ __device__ inline void load_cell(const double* P, size_t c, double out[8])
 // (negative density or pressure). One function for the primitive kernel and
 // the EMF kernel's next-stage recovery, so that both compile the same arithmetic.
 struct Field3 { float b[3]; };
+__device__ __forceinline__ Field3 cell_field(float x0, float x1, float y0, float y1, float z0, float z1)
+{
+    return Field3{{__fmul_rn(0.5f, __fadd_rn(x0, x1)), __fmul_rn(0.5f, __fadd_rn(y0, y1)),
+                   __fmul_rn(0.5f, __fadd_rn(z0, z1))}};
+}
+// from the FP64 faces (each converted here; the EMF kernel converts each
+// face once, when it updates it, and passes the floats)
 __device__ __forceinline__ Field3 cell_field(double x0, double x1, double y0, double y1, double z0, double z1)
 {
-    return Field3{{0.5f * (d2f(x0) + d2f(x1)), 0.5f * (d2f(y0) + d2f(y1)), 0.5f * (d2f(z0) + d2f(z1))}};
+    return cell_field(d2f(x0), d2f(x1), d2f(y0), d2f(y1), d2f(z0), d2f(z1));
 }
 
 template<int MODE>
@@ -660,6 +667,7 @@ struct __align__(16) EmfSmem
     double bx[2][FXN];         // updated x faces; layer l in slot l & 1
     double by[FYN];            // updated y faces of plane c-1 (row TJ: the neighbour's, for the cells)
     double bz[FZN];
+    float bxf[2][FXN], byf[FYN], bzf[FZN];   // their FP32 images for the next-stage recovery (NEXT)
     double wmax[EMF_THREADS / 32];
     unsigned long long wbad[EMF_THREADS / 32];
 };
@@ -760,20 +768,23 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
     const bool stage_u = READS_U && A.uzs == 1 && A.ucs % 2 == 0 && (reinterpret_cast<uintptr_t>(A.uc) & 15) == 0;
     auto stage_cells = [&](int c) {
         // rows of TK cells: TK/2 16-byte pieces of state, TK/4 of increments, per component
+        // (every division below is by a power-of-two constant: a shift)
         constexpr int UP = TJ * TK / 2, DP = TJ * TK / 4;
+        static_assert((UP & (UP - 1)) == 0 && (DP & (DP - 1)) == 0 && (TK & (TK - 1)) == 0, "shift decoding");
         for (int t = threadIdx.x; t < 5 * (UP + DP); t += FLUX_THREADS)
         {
-            const bool u = t < 5 * UP;
-            const int v = u ? t : t - 5 * UP, per = u ? UP : DP;
-            const int q = v / per, w = v - q * per, width = u ? TK / 2 : TK / 4;
-            const int jj = w / width, piece = w - jj * width;
-            const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0);
-            if (u)
+            if (t < 5 * UP)
             {
+                const int q = t / UP, w = t - q * UP, jj = w / (TK / 2), piece = w - jj * (TK / 2);
+                const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0);
                 if (stage_u) cp_async16(&S.uc[q][jj * TK + 2 * piece], A.uc + q * A.ucs + cell + 2 * piece);
             }
             else if (READS_D)
+            {
+                const int v = t - 5 * UP, q = v / DP, w = v - q * DP, jj = w / (TK / 4), piece = w - jj * (TK / 4);
+                const int64_t cell = cidx32(N, c, T.j0 + jj, T.k0);
                 cp_async16(&S.dinc[q][jj * TK + 4 * piece], A.dinc + q * NN + cell + 4 * piece);
+            }
         }
         cp_async_commit();
     };
@@ -888,7 +899,9 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 if (x && !load_x) continue;
                 const int v = x ? t : t - LOAD_X;
                 const int row = v / ROW_PIECES, piece = v - row * ROW_PIECES;
-                const int rows = x ? TJ + 2 : TJ + 1, h = row / rows, r = row - h * rows;
+                // two components of `rows` rows each: the component is a
+                // comparison, not a division by a runtime row count
+                const int rows = x ? TJ + 2 : TJ + 1, h = row >= rows ? 1 : 0, r = row - h * rows;
                 const int kk = piece < TK / 4 ? 4 * piece : (piece == TK / 4 ? -1 : TK);
                 const uint32_t f = x ? fidx32(N, 0, lx, wrap(T.j0 + r - 1, N), wrap(T.k0 + kk, N))
                                      : fidx32(N, 1, pw, T.j0 + r, wrap(T.k0 + kk, N));
@@ -899,7 +912,7 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
             }
             else
             {
-                const int v = t - LOAD_X - LOAD_Y, h = v / ZN, u = v - h * ZN;
+                const int v = t - LOAD_X - LOAD_Y, h = v >= ZN ? 1 : 0, u = v - h * ZN;
                 const int r = u / ZK, q = u - r * ZK;               // jj = r - 1, kk = q
                 const uint32_t f = fidx32(N, 2, pw, wrap(T.j0 + r - 1, N), T.k0 + q);
                 cp_async4(&S.ez[mod3(py)][h][u], E2 + size_t(h) * nbv[2] + f);
@@ -928,7 +941,7 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
         const int arrays = with_avg ? 2 : 1;
         for (int t = threadIdx.x; t < arrays * (XP + YP + FZN); t += EMF_THREADS)
         {
-            const int a = t / (XP + YP + FZN), v = t - a * (XP + YP + FZN);
+            const int a = t >= XP + YP + FZN ? 1 : 0, v = t - a * (XP + YP + FZN);
             double* dst = a ? S.bav : S.bin;
             const double* const* src = a ? A.bavg : A.bf;
             if (v < XP)
@@ -1013,6 +1026,7 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 double out = fma(-cf, dtdl_d, S.bin[t]);
                 if (with_avg) out = half_exact(S.bav[t] + out);
                 S.bx[s][t] = out;
+                if (NEXT) S.bxf[s][t] = d2f(out);
                 if (!last || c == N) A.bf_out[0][f] = out;
             }
             else if (t < FXN + SOLVE_Y)
@@ -1026,6 +1040,7 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 double out = fma(-cf, dtdl_d, S.bin[FXN + u]);
                 if (with_avg) out = half_exact(S.bav[FXN + u] + out);
                 S.by[u] = out;
+                if (NEXT) S.byf[u] = d2f(out);
                 if (jj < TJ || T.last_j) A.bf_out[1][f] = out;
             }
             else
@@ -1040,6 +1055,7 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 double out = fma(-cf, dtdl_d, S.bin[FXN + FYN + u]);
                 if (with_avg) out = half_exact(S.bav[FXN + FYN + u] + out);
                 S.bz[u] = out;
+                if (NEXT) S.bzf[u] = d2f(out);
                 if (kk < TK || T.last_k) A.bf_out[2][f] = out;
             }
         }
@@ -1054,8 +1070,8 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 const int64_t cell = cidx32(N, c - 1, T.j0 + jj, T.k0 + kk);
                 Prim<float> p;
                 if (recover_mixed<NEXT>(A.next_uc, NN, 1, A.dinc, NN, cell,
-                                        cell_field(S.bx[sp][t], S.bx[s][t], S.by[t], S.by[t + TK], S.bz[jj * FZK + kk],
-                                                   S.bz[jj * FZK + kk + 1]),
+                                        cell_field(S.bxf[sp][t], S.bxf[s][t], S.byf[t], S.byf[t + TK],
+                                                   S.bzf[jj * FZK + kk], S.bzf[jj * FZK + kk + 1]),
                                         gm, p))
                     ++bad;
                 store_cell(P, cell, p);
