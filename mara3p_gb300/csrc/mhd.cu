@@ -323,6 +323,16 @@ __global__ void dt_kernel(Clock* clock, int stage, double cfl, double dl, int be
 // and the HLLE flux and transverse E-field of the face (godunov_fluxes_plm,
 // scheme_mhd_v1.cpp:152-178). One function for the face kernels and the
 // fused stage kernel, so that both compile the same arithmetic.
+// The HLLE flux and E-field of a face from its two PLM states (the face's
+// normal B is bl; the states' own normal components are not read).
+template<typename R, int AXIS>
+__device__ __forceinline__ void face_riemann(const R L[8], const R Rr[8], R bl, R gm, R F[5], R E[2])
+{
+    Prim<R> pl{L[0], {L[1], L[2], L[3]}, L[4], {L[5], L[6], L[7]}};
+    Prim<R> pr{Rr[0], {Rr[1], Rr[2], Rr[3]}, Rr[4], {Rr[5], Rr[6], Rr[7]}};
+    riemann_hlle<R, AXIS>(pl, pr, bl, gm, F, E);
+}
+
 template<typename R, int AXIS>
 __device__ __forceinline__ void face_solve(const R xa[8], const R xb[8], const R xc[8], const R xd[8], R bl, R gm,
                                            R theta, R F[5], R E[2])
@@ -343,9 +353,7 @@ __device__ __forceinline__ void face_solve(const R xa[8], const R xb[8], const R
             Rr[q] = cc - R(0.5) * plm(b, cc, d, theta);
         }
     }
-    Prim<R> pl{L[0], {L[1], L[2], L[3]}, L[4], {L[5], L[6], L[7]}};
-    Prim<R> pr{Rr[0], {Rr[1], Rr[2], Rr[3]}, Rr[4], {Rr[5], Rr[6], Rr[7]}};
-    riemann_hlle<R, AXIS>(pl, pr, bl, gm, F, E);
+    face_riemann<R, AXIS>(L, Rr, bl, gm, F, E);
 }
 
 template<typename R, int AXIS>
@@ -649,6 +657,7 @@ constexpr int LOAD_X = 2 * (TJ + 2) * ROW_PIECES, LOAD_Y = 2 * (TJ + 1) * ROW_PI
 
 struct __align__(16) FluxSmem
 {
+    float xl[8][FXN];          // the next x layer's left states (cell c+1's high-side PLM values), per thread
     double uc[5][FXN];         // the cells' state of plane c (staged during the solves)
     float dinc[5][FXN];        // their FP32 stage-1 increments (RK2 stage 2)
     float fx[2][5][FXN];       // x-face fluxes; layer l in slot l & 1
@@ -744,15 +753,40 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
     if (threadIdx.x == 0) s_dtdl = float(A.clock->dt[A.stage] / A.dl);
 
     // x faces of layer lx over the tile: fluxes into slot lx & 1, E-fields
-    // out when this chunk owns the layer
-    auto solve_x = [&](int t, int lx, bool write_e) {
+    // out when this chunk owns the layer. Thread t always takes the x face
+    // column t (FLUX_THREADS == FXN), so the left state of layer lx (cell
+    // lx-1's high side) is the one this thread formed at layer lx-1 from the
+    // same slope as that layer's right state, kept in S.xl; only the chunk's
+    // first layer computes it. The same floats as face_solve.
+    static_assert(FLUX_THREADS == FXN, "one x face column per thread");
+    auto solve_x = [&](int t, int lx, bool write_e, bool first) {
         const int jj = t / TK, kk = t - jj * TK;
         const int j = T.j0 + jj, k = T.k0 + kk;
-        float xa[8], xb[8], xc[8], xd[8], F[5], Ef[2];
-        stencil(P, cidx32(N, wrap(lx - 2, N), j, k), cidx32(N, wrap(lx - 1, N), j, k), cidx32(N, wrap(lx, N), j, k),
-                cidx32(N, wrap(lx + 1, N), j, k), xa, xb, xc, xd);
+        float xb[8], xc[8], xd[8], L[8], Rr[8], F[5], Ef[2];
+        load_cell(P, cidx32(N, wrap(lx - 1, N), j, k), xb);
+        load_cell(P, cidx32(N, wrap(lx, N), j, k), xc);
+        load_cell(P, cidx32(N, wrap(lx + 1, N), j, k), xd);
+        if (first)
+        {
+            float xa[8];
+            load_cell(P, cidx32(N, wrap(lx - 2, N), j, k), xa);
+            for (int q = 0; q < 8; ++q) L[q] = __fmaf_rn(0.25f, plm2(xa[q], xb[q], xc[q], 2.0f * theta), xb[q]);
+        }
+        else
+            for (int q = 0; q < 8; ++q) L[q] = q == 5 ? 0.0f : S.xl[q][t];    // component 5: the normal B, not read
+        for (int q = 0; q < 8; ++q)
+        {
+            if (q == 5)
+            {
+                Rr[q] = 0.0f;
+                continue;
+            }
+            const float g = plm2(xb[q], xc[q], xd[q], 2.0f * theta);
+            Rr[q] = __fmaf_rn(-0.25f, g, xc[q]);
+            S.xl[q][t] = __fmaf_rn(0.25f, g, xc[q]);
+        }
         const uint32_t f = fidx32(N, 0, lx, j, k);
-        face_solve<float, 0>(xa, xb, xc, xd, float(A.bf[0][f]), gm, theta, F, Ef);
+        face_riemann<float, 0>(L, Rr, float(A.bf[0][f]), gm, F, Ef);
         for (int n = 0; n < 5; ++n) S.fx[lx & 1][n][t] = F[n];
         if (write_e)
         {
@@ -789,7 +823,7 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
         cp_async_commit();
     };
 
-    for (int t = threadIdx.x; t < FXN; t += FLUX_THREADS) solve_x(t, T.i0, true);
+    solve_x(threadIdx.x, T.i0, true, true);
     for (int c = T.i0; c < T.i1; ++c)
     {
         __syncthreads();                   // the previous plane's cell updates are done
@@ -799,7 +833,7 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
         {
             if (t < FXN)
             {
-                solve_x(t, c + 1, x_owned);
+                solve_x(t, c + 1, x_owned, false);
             }
             else if (t < FXN + SOLVE_Y)
             {
