@@ -636,7 +636,7 @@ constexpr int FLUX_THREADS = 256, EMF_THREADS = 288;
 // kk in [0, TK) is 16-byte aligned for vector copies
 constexpr int XK = TK + 8, XN = (TJ + 2) * XK;      // x-face E: jj in [-1, TJ], kk in [-1, TK]
 constexpr int YK = TK + 8, YN = (TJ + 1) * YK;      // y-face E: jj in [0, TJ], kk in [-1, TK]
-constexpr int ZK = TK + 1, ZN = (TJ + 2) * ZK;      // z-face E: jj in [-1, TJ], kk in [0, TK]
+constexpr int ZK = TK + 4, ZN = (TJ + 2) * ZK;      // z-face E: jj in [-1, TJ], kk in [0, TK] (rows padded to 16 B)
 constexpr int XO = 4, YO = 4;                       // row offset of kk = 0
 constexpr int FXN = TJ * TK;                        // x faces of the tile
 constexpr int FYN = (TJ + 1) * TK;                  // y faces: jj in [0, TJ], kk in [0, TK)
@@ -653,7 +653,10 @@ constexpr int EDGE_0 = E0N, EDGE_1 = E1N, EDGE_2 = E2N;
 // copies per plane: x and y rows as TK/4 16-byte pieces plus the two halo
 // elements; z rows (N + 1 floats, unaligned) element by element
 constexpr int ROW_PIECES = TK / 4 + 2;
-constexpr int LOAD_X = 2 * (TJ + 2) * ROW_PIECES, LOAD_Y = 2 * (TJ + 1) * ROW_PIECES, LOAD_Z = 2 * ZN;
+// z rows: TK/4 16-byte pieces (kk in [0, TK)) plus the element kk = TK, from
+// the fused path's padded z-face E layout (zrow_e below)
+constexpr int ZROW_PIECES = TK / 4 + 1;
+constexpr int LOAD_X = 2 * (TJ + 2) * ROW_PIECES, LOAD_Y = 2 * (TJ + 1) * ROW_PIECES, LOAD_Z = 2 * (TJ + 2) * ZROW_PIECES;
 
 struct __align__(16) FluxSmem
 {
@@ -702,6 +705,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 __device__ __forceinline__ float avg(float x, float y) { return __fmul_rn(0.5f, __fadd_rn(x, y)); }
+
+// The fused path's z-face E-fields: rows of N + 4 floats (N + 1 faces,
+// padded so that every row starts on 16 bytes and the EMF kernel copies it
+// in 16-byte pieces); the face (i, j, k) and the component stride.
+__device__ __forceinline__ uint32_t zrow_e(int N, int i, int j, int k)
+{
+    return (uint32_t(i) * uint32_t(N) + uint32_t(j)) * uint32_t(N + 4) + uint32_t(k);
+}
+__device__ __forceinline__ uint32_t zrow_nb(int N) { return uint32_t(N) * uint32_t(N) * uint32_t(N + 4); }
 
 struct Tile
 {
@@ -867,8 +879,9 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
                 for (int n = 0; n < 5; ++n) S.fz[n][u] = F[n];
                 if (kk < TK || T.last_k)
                 {
-                    E2[f] = Ef[0];
-                    E2[size_t(nbv[2]) + f] = Ef[1];
+                    const uint32_t fe = zrow_e(N, c, j, k);
+                    E2[fe] = Ef[0];
+                    E2[size_t(zrow_nb(N)) + fe] = Ef[1];
                 }
             }
         }
@@ -946,10 +959,13 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
             }
             else
             {
-                const int v = t - LOAD_X - LOAD_Y, h = v >= ZN ? 1 : 0, u = v - h * ZN;
-                const int r = u / ZK, q = u - r * ZK;               // jj = r - 1, kk = q
-                const uint32_t f = fidx32(N, 2, pw, wrap(T.j0 + r - 1, N), T.k0 + q);
-                cp_async4(&S.ez[mod3(py)][h][u], E2 + size_t(h) * nbv[2] + f);
+                const int v = t - LOAD_X - LOAD_Y, h = v >= LOAD_Z / 2 ? 1 : 0, u = v - h * (LOAD_Z / 2);
+                const int r = u / ZROW_PIECES, piece = u - r * ZROW_PIECES;   // jj = r - 1
+                const int kk = piece < TK / 4 ? 4 * piece : TK;
+                const float* src = E2 + size_t(h) * zrow_nb(N) + zrow_e(N, pw, wrap(T.j0 + r - 1, N), T.k0 + kk);
+                float* dst = &S.ez[mod3(py)][h][r * ZK + kk];
+                if (piece < TK / 4) cp_async16(dst, src);
+                else cp_async4(dst, src);
             }
         }
         cp_async_commit();
@@ -1265,8 +1281,11 @@ int64_t workspace_bytes(int N, int precision, bool rk2)
     const int64_t NN = int64_t(N) * N * N;
     const int64_t NF = nb(N, 0);
     const int64_t r = precision == MARA_MIXED ? 4 : 8;
-    // seven 256-byte aligned regions (P, F[3], E[3]) plus alignment slack
-    int64_t bytes = NN * r * 8 + NF * r * 3 * (5 + 2) + 8 * 256;
+    // seven 256-byte aligned regions (P, F[3], E[3]) plus alignment slack;
+    // each E region holds two components of the larger of the face count and
+    // the fused path's padded z rows
+    const int64_t NE = std::max(NF, NN + 4 * int64_t(N) * N);
+    int64_t bytes = NN * r * 8 + NF * r * 3 * 5 + NE * r * 3 * 2 + 8 * 256;
     if (rk2) bytes += 8 * (5 * NN + nb(N, 0) + nb(N, 1) + nb(N, 2));
     return bytes + 256;
 }
@@ -1281,7 +1300,8 @@ Workspace carve(void* base, int N, int precision, bool rk2)
     Workspace w{};
     w.P = up(p); p = up(static_cast<char*>(w.P) + 8 * NN * r);     // 16-byte vector records need alignment
     for (int a = 0; a < 3; ++a) { w.F[a] = p; p = up(p + 5 * NF * r); }
-    for (int a = 0; a < 3; ++a) { w.E[a] = p; p = up(p + 2 * NF * r); }
+    const int64_t NE = std::max(NF, NN + 4 * int64_t(N) * N);   // see workspace_bytes
+    for (int a = 0; a < 3; ++a) { w.E[a] = p; p = up(p + 2 * NE * r); }
     if (rk2)
     {
         w.u1 = reinterpret_cast<double*>(p); p += 5 * NN * 8;
