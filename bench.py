@@ -42,15 +42,15 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
-    # BASELINE configuration 2 (large minidisk)
+    # the large minidisk: [-8,8]^2 on 4096^2 cells, q = 0.5, e = 0.1, Mach 20, nu = 5e-4
     "minidisk-4096": dict(block_size=64, depth=6, omega_frame=1.0, mach_number=20.0, nu=5e-4, domain_radius=8.0,
                           softening_length=0.05, eccentricity=0.1, mass_ratio=0.5, sink_radius=0.05, sink_rate=10.0,
                           buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=1.5),
-    # BASELINE configuration 1 (256^2, 4x4 blocks of 64^2)
+    # the reference-sized minidisk: [-4,4]^2 on 256^2 cells (4x4 blocks of 64^2), equal-mass circular binary
     "minidisk-256": dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3, domain_radius=4.0,
                          softening_length=0.05, eccentricity=0.0, mass_ratio=1.0, sink_radius=0.05, sink_rate=10.0,
                          buffer_rate=100.0, buffer_scale=0.2, cfl=0.3, plm_theta=1.5),
-    # BASELINE configuration 5: 64 seeded members (mesh 128^2..1024^2, q, e, Mach, nu drawn per member) on this
+    # the ensemble: 64 seeded members (mesh 128^2..1024^2, q, e, Mach, nu drawn per member) on this
     # base physics; the entry itself (a 256^2 member) is what the CPU reference arm times
     "minidisk-ensemble-64": dict(block_size=64, depth=2, omega_frame=1.0, mach_number=10.0, nu=1e-3,
                                  domain_radius=4.0, softening_length=0.05, eccentricity=0.0, mass_ratio=1.0,
@@ -793,7 +793,7 @@ def run_srhd(args):
 
 
 def run_ensemble(args):
-    """Configuration 5: 64 independent minidisk members (mesh from 128^2 to
+    """The ensemble: 64 independent minidisk members (mesh from 128^2 to
     1024^2, mass ratio, eccentricity, Mach number and viscosity drawn per
     member by seed), mixed precision, RK2, CFL. One step = one RK2 step of
     every member: one persistent sweep launch per stage and one clock launch,
@@ -1133,7 +1133,7 @@ def other_workloads(args) -> dict:
         sub.no_cpu_baseline = name != "sedov-tracks"
         sub.no_looped = False
         sub.launch = None
-        sub.accuracy_steps = 100 if name == "minidisk-256" else 50   # configuration 1 runs 100 steps
+        sub.accuracy_steps = 100 if name == "minidisk-256" else 50   # the reference-sized disk runs 100 steps
         sub.no_diagnostics_timing = True
         t0 = time.perf_counter()
         line = globals()[fn](sub)

@@ -324,7 +324,7 @@ def srhd_fixtures(o, r) -> dict[str, np.ndarray]:
     n = 4096
     prim = np.zeros(5 * n)
     cons = np.zeros(5 * n)
-    # the BASELINE config-4(a) distribution: rho 1e-4..1, p 1e-6..10, W 1..50
+    # the recovery batch's distribution: rho 1e-4..1, p 1e-6..10, Lorentz factor 1..50
     o.oracle_srhd_seeded_zones(ctypes.c_uint64(4242), ctypes.c_int64(n), ctypes.c_double(1e-4), ctypes.c_double(1.0),
                                ctypes.c_double(1e-6), ctypes.c_double(10.0), ctypes.c_double(50.0), ctypes.c_double(g),
                                dptr(prim), dptr(cons))

@@ -111,7 +111,7 @@ def test_rk2_fp64_matches_oracle_longer(mh, oracle):
     assert run.max_div_b() < 1e-13 * b_scale
 
 
-def test_config3_full_size_fp64_matches_oracle(mh, oracle):
+def test_mhd_128_full_size_fp64_matches_oracle(mh, oracle):
     """The MHD configuration at its own size (128^3, seeded modes, CFL dt):
     three FP64 RK2 steps against the oracle on all host threads at 1e-11,
     with div B at FP64 rounding."""

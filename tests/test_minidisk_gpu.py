@@ -17,7 +17,7 @@ import pytest
 
 from oracle.oracle import dptr, params
 from tests.golden.make_golden import MINIDISK_CASES
-from tests.helpers import CONFIG1_PARAMS, CONFIG2_PARAMS, SMALL_PARAMS, params_from_vector, rel_l1_components
+from tests.helpers import REFERENCE_DISK, LARGE_DISK, SMALL_PARAMS, params_from_vector, rel_l1_components
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -102,7 +102,7 @@ def test_recover_primitive_empty(md):
 
 @pytest.mark.parametrize("amplitude", [0.0, 0.01])
 def test_initial_conserved_bitexact(md, oracle, amplitude):
-    sd = md.SolverData(**CONFIG1_PARAMS)
+    sd = md.SolverData(**REFERENCE_DISK)
     u = md.initial_conserved(sd, seed=77, amplitude=amplitude).cpu().numpy()
     ref = np.zeros(u.size)
     oracle.oracle_minidisk_initial_conserved(ctypes.byref(params(sd)), ctypes.c_uint64(77), ctypes.c_double(amplitude),
@@ -110,9 +110,9 @@ def test_initial_conserved_bitexact(md, oracle, amplitude):
     assert np.array_equal(u.ravel(), ref)
 
 
-def test_config1_one_step_and_1000_steps_fp64(md, oracle):
+def test_reference_disk_physics_one_step_and_1000_steps_fp64(md, oracle):
     """Plain FP64 GPU vs the oracle on the same seeded input: one RK2 step at
-    1e-12 and 1000 RK2 steps at 1e-9 (64^2 mesh, config-1 physics)."""
+    1e-12 and 1000 RK2 steps at 1e-9 (64^2 mesh, the 256^2 disk's physics)."""
     sd = md.SolverData(**SMALL_PARAMS)
     u0 = md.initial_conserved(sd, seed=5, amplitude=0.01)
     ref = u0.cpu().numpy().ravel().copy()
@@ -126,9 +126,9 @@ def test_config1_one_step_and_1000_steps_fp64(md, oracle):
     assert abs(run.time - t) <= 1e-12 * t
 
 
-def test_config1_full_size_one_step(md, oracle):
+def test_reference_disk_full_size_one_step(md, oracle):
     """Config 1 itself (256^2, 4x4 blocks of 64^2): one RK2 step at 1e-12."""
-    sd = md.SolverData(**CONFIG1_PARAMS)
+    sd = md.SolverData(**REFERENCE_DISK)
     u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
     ref = u0.cpu().numpy().ravel().copy()
     run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)
@@ -140,11 +140,11 @@ def test_config1_full_size_one_step(md, oracle):
 THREADS = os.cpu_count() or 1
 
 
-def test_config1_full_size_1000_steps_fp64(md, oracle):
-    """Configuration 1 at its own size and physics (256^2, 4x4 blocks of
+def test_reference_disk_full_size_1000_steps_fp64(md, oracle):
+    """The reference-sized disk at its own size and physics (256^2, 4x4 blocks of
     64^2, theta 1.5, CFL dt): one RK2 step at 1e-12 and 1000 RK2 steps at
     1e-9 against the oracle, with the clocks' times alike."""
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, plm_theta=1.5))
     u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
     ref = u0.cpu().numpy().ravel().copy()
     run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
@@ -158,11 +158,11 @@ def test_config1_full_size_1000_steps_fp64(md, oracle):
     assert abs(run.time - t) <= 1e-12 * t
 
 
-def test_config2_full_size_one_step_fp64(md, oracle):
-    """Configuration 2 itself (4096^2, theta 1.5, q 0.5, e 0.1, Mach 20, CFL
+def test_large_disk_full_size_one_step_fp64(md, oracle):
+    """The large disk itself (4096^2, theta 1.5, q 0.5, e 0.1, Mach 20, CFL
     dt): one FP64 RK2 step at 1e-12 against the oracle on all host threads,
     and the CFL dt (an FP64 reduction over all 16.8 M cells) at 1e-14."""
-    sd = md.SolverData(**CONFIG2_PARAMS)
+    sd = md.SolverData(**LARGE_DISK)
     u0 = md.initial_conserved(sd, seed=1, amplitude=0.01)
     ref = u0.cpu().numpy().ravel().copy()
     run = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
@@ -219,14 +219,14 @@ def test_mixed_precision_close_to_fp64(md, rk_order, steps, block_size):
     assert a.time == b.time
 
 
-def test_mixed_long_horizon_config2_physics(md):
+def test_mixed_long_horizon_large_disk_physics(md):
     """The mixed path against the plain FP64 path over 2000 CFL steps of the
     large-minidisk physics (q 0.5, e 0.1, Mach 20, theta 1.5) on a 1024^2
     mesh of the same domain: density and momentum relative L1 at most 1e-6.
     (The primitive velocity is an FMA-corrected quotient: with the biased
     single-MUFU reciprocal the 4096^2 configuration was 4.8e-6 from FP64
     after 1000 steps, with the corrected quotient 7.4e-7.)"""
-    sd = md.SolverData(**dict(CONFIG2_PARAMS, depth=4))
+    sd = md.SolverData(**dict(LARGE_DISK, depth=4))
     u0 = md.initial_conserved(sd, seed=1234, amplitude=0.01)
     a = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_CFL)
     b = md.Run(sd, u0.clone(), rk_order=2, precision=md.MIXED, dt_mode=md.DT_CFL)
@@ -244,7 +244,7 @@ def test_sweep_tma_ring_bit_identical(md, block_size, depth):
     (the default) give bit-identical states and clocks: meshes of 512^2,
     400^2 (strips of both kinds) and 4096^2."""
     from mara3p_gb300._capi import lib
-    sd = md.SolverData(**dict(CONFIG2_PARAMS, block_size=block_size, depth=depth))
+    sd = md.SolverData(**dict(LARGE_DISK, block_size=block_size, depth=depth))
     u0 = md.initial_conserved(sd, seed=31, amplitude=0.01)
     out = []
     try:
@@ -262,7 +262,7 @@ def test_sweep_tma_ring_bit_identical(md, block_size, depth):
 
 
 def test_mass_conservation_full_size(md):
-    """Size-independent property at the config-2 size (4096^2): with sinks,
+    """Size-independent property at the large disk's size (4096^2): with sinks,
     buffer and viscosity off, the flux divergence telescopes and total mass
     is conserved to rounding, in both precisions."""
     sd = md.SolverData(block_size=64, depth=6, domain_radius=8.0, softening_length=0.05, mach_number=20.0,
@@ -284,7 +284,7 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
     6-column last strip. (Odd N puts a cell centre on the origin, where the
     reference's initial state divides by r = 0, so it is not a minidisk mesh.)"""
     from mara3p_gb300._capi import lib
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=block_size, depth=depth, plm_theta=1.5))
     u0 = md.initial_conserved(sd, seed=5, amplitude=0.01)
     out = []
     try:
@@ -310,7 +310,7 @@ def test_sweep_column_forms_bit_identical(md, block_size, depth):
 def test_graph_replay_matches_direct_advance(md, precision, dt_mode_name):
     """Run.use_graph replays captured steps: the same bits, clock and time as
     advancing directly (including a remainder shorter than one replay)."""
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=64, depth=1, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=64, depth=1, plm_theta=1.5))
     u0 = md.initial_conserved(sd, seed=21, amplitude=0.01)
     kw = dict(rk_order=2, precision=getattr(md, precision), dt_mode=getattr(md, dt_mode_name))
     direct = md.Run(sd, u0.clone(), **kw)
@@ -337,7 +337,7 @@ def test_host_call_pinned_matches_pageable(md, dt_mode_name, steps):
     alone, and an output that aliases the input works. FP64 takes the copy
     path in both cases."""
     from mara3p_gb300._capi import check, lib
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=64, depth=2, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=64, depth=2, plm_theta=1.5))
     c = sd.to_c()
     N = sd.cells_per_side
     u0 = md.initial_conserved(sd, seed=3, amplitude=0.01).cpu()
@@ -369,7 +369,7 @@ def test_sweep_launch_shapes_bit_identical(md, block_size, depth):
     strip segments, down to 16-row segments and ragged last segments) gives
     the same bits: the segments only change which warp computes a cell."""
     from mara3p_gb300._capi import lib
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=block_size, depth=depth, plm_theta=1.5))
     u0 = md.initial_conserved(sd, seed=9, amplitude=0.01)
     out = []
     try:
@@ -396,7 +396,7 @@ def test_ragged_meshes_fp64_rk2_and_mixed(md, oracle, block_size, depth):
     column strips (80, 100, 320, 130): FP64 RK2 against the oracle, and the
     mixed path within its error budget of the FP64 path. 320 and 130 also
     contain TMA-loaded interior tiles next to wrapped boundary tiles."""
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth, plm_theta=1.5))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=block_size, depth=depth, plm_theta=1.5))
     u0 = md.initial_conserved(sd, seed=4, amplitude=0.01)
     ref = u0.cpu().numpy().ravel().copy()
     a = md.Run(sd, u0.clone(), rk_order=2, precision=md.FP64, dt_mode=md.DT_FORMULA)

@@ -17,7 +17,7 @@ import ctypes
 
 import pytest
 
-from tests.helpers import CONFIG1_PARAMS, rel_l1_components
+from tests.helpers import REFERENCE_DISK, rel_l1_components
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -47,7 +47,7 @@ def clock_buffer(md, sd, u):
 def test_noalloc_matches_workspace_advance_on_two_calls(md, precision, dt_mode, mesh):
     from mara3p_gb300._capi import check, lib
     block_size, depth = mesh
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, block_size=block_size, depth=depth))
+    sd = md.SolverData(**dict(REFERENCE_DISK, block_size=block_size, depth=depth))
     N = sd.cells_per_side
     need = lib.mara_minidisk_workspace_bytes(ctypes.byref(sd.to_c()), 2, precision)
     if N * N == lib_max_cells():
@@ -71,7 +71,7 @@ def test_noalloc_matches_workspace_advance_on_two_calls(md, precision, dt_mode, 
 
 def test_noalloc_rejects_meshes_above_the_limit(md):
     from mara3p_gb300._capi import lib
-    sd = md.SolverData(**dict(CONFIG1_PARAMS, depth=4))      # 1024^2 > 512^2 cells
+    sd = md.SolverData(**dict(REFERENCE_DISK, depth=4))      # 1024^2 > 512^2 cells
     fake = ctypes.c_void_p(0x1000)    # never dereferenced: the size check fails first
     assert lib.mara_minidisk_advance_noalloc(ctypes.byref(sd.to_c()), fake, fake, 1, 2, 0, 0, None) == 1
     assert b"static scratch limit" in lib.mara_last_error()
