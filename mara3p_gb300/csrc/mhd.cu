@@ -1020,12 +1020,16 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
     unsigned long long bad = 0;
     load(false, 0, T.i0 - 1);
     load(true, T.i0, T.i0);
+    // With the next stage's recovery (NEXT), a plane's face inputs are staged
+    // during the previous plane's recovery phase, a whole plane ahead of their
+    // use; without it, at the start of their own plane, ahead of the edges.
+    if (NEXT) stage_faces(T.i0, true);
     for (int c = T.i0; c <= T.i1; ++c)
     {
         const bool first = c == T.i0, last = c == T.i1;
         cp_async_wait_all();
         __syncthreads();                   // this plane's fields landed; the previous plane's work is done
-        stage_faces(c, first);
+        if (!NEXT) stage_faces(c, first);
         if (!last) load(true, c + 1, c + 1);
         const int s = c & 1, sp = (c - 1) & 1, ys = mod3(c), yp = mod3(c - 1);
         // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order)
@@ -1059,8 +1063,11 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 S.e2[s][u] = avg(a, b);
             }
         }
-        if (last) cp_async_wait_all();
-        else cp_async_wait_prior();        // the staged faces; the next plane's fields may stay in flight
+        if (!NEXT)
+        {
+            if (last) cp_async_wait_all();
+            else cp_async_wait_prior();    // the staged faces; the next plane's fields may stay in flight
+        }
         __syncthreads();
         // faces: x of layer c (the tile); y and z of plane c-1, with the high
         // neighbour's row and column, which the next-stage cells need
@@ -1109,9 +1116,13 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
                 if (kk < TK || T.last_k) A.bf_out[2][f] = out;
             }
         }
+        if (NEXT)
+        {
+            __syncthreads();               // every face of plane c has read its staged inputs
+            if (!last) stage_faces(c + 1, false);
+        }
         if (NEXT && !first)
         {
-            __syncthreads();
             // the next stage's primitives of plane c-1 (the primitive kernel's arithmetic)
             float* P = static_cast<float*>(A.P);
             for (int t = threadIdx.x; t < FXN; t += EMF_THREADS)
