@@ -78,6 +78,12 @@ typedef struct mara_minidisk_clock {
 const char* mara_last_error(void);
 const char* mara_version(void);
 
+/* Upload an instantiated CUDA graph (a cudaGraphExec_t, e.g. the one a host
+ * captured the advance calls into) to the device on `stream`, so that its
+ * first launch costs no more than later ones. No counterpart in the
+ * reference, which launches no graphs. */
+int mara_graph_upload(void* graph_exec, void* stream);
+
 /* ---------------------------------------------------------------- minidisk */
 
 /* Binary state at time t in the rotating frame, computed on the host in FP64:

@@ -69,6 +69,7 @@ _MP = ctypes.POINTER(MinidiskParams)
 SIGNATURES = {
     "mara_last_error": (ctypes.c_char_p, []),
     "mara_version": (ctypes.c_char_p, []),
+    "mara_graph_upload": (ctypes.c_int, [_vp, _vp]),
     "mara_minidisk_binary": (ctypes.c_int, [_MP, ctypes.c_double, c_double_p]),
     "mara_minidisk_dt_formula": (ctypes.c_int, [_MP, ctypes.c_double, c_double_p]),
     "mara_minidisk_updated_conserved": (ctypes.c_int, [_MP, _vp, _vp, ctypes.c_double, ctypes.c_double,

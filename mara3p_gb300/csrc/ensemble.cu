@@ -325,6 +325,8 @@ int capture_graph(mara_minidisk_ensemble* e, cudaGraphExec_t* out, F&& body)
     {
         cudaError_t ie = cudaGraphInstantiate(out, g, 0);
         if (ie != cudaSuccess) r = cuda_fail(ie, "cudaGraphInstantiate");
+        // uploaded now, so that the first replay costs what the later ones do
+        else if ((ie = cudaGraphUpload(*out, e->capture)) != cudaSuccess) r = cuda_fail(ie, "cudaGraphUpload");
     }
     if (g) cudaGraphDestroy(g);
     return r;

@@ -397,6 +397,7 @@ struct Run
             mara_check(r, "advance (capture)");
             cuda_check(e, "end capture");
             cuda_check(cudaGraphInstantiate(&graph, g, 0), "instantiate graph");
+            cuda_check(cudaGraphUpload(graph, stream), "upload graph");
             cudaGraphDestroy(g);
             graph_fold = fold;
         }

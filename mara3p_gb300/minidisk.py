@@ -237,6 +237,10 @@ class Run:
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph):
             self._advance_call(steps_per_replay)
+        # uploaded to the device now: the first replay would otherwise pay for
+        # it (about 60 us at 256^2, a fifth of a 10-step replay)
+        if hasattr(graph, "raw_cuda_graph_exec"):
+            check(lib.mara_graph_upload(graph.raw_cuda_graph_exec(), _stream()), "graph_upload")
         self._graph, self._graph_steps = graph, steps_per_replay
 
     def advance(self, steps: int) -> None:
