@@ -1115,7 +1115,7 @@ def compact(line: dict) -> dict:
 
 def other_workloads(args) -> dict:
     """Short runs of the other workloads (mixed precision, their own default
-    sizes), each timed as its own --workload run times it, for the headline
+    sizes; at most 20 timed steps, one call), each timed as its own --workload run times it, for the headline
     line: the 256^2 minidisk, MHD 128^3, the 2^24-zone SRHD recovery, the
     1024^2 shock tube, the 64-member ensemble and the 1024-track sedov step."""
     import argparse as ap_
@@ -1128,7 +1128,7 @@ def other_workloads(args) -> dict:
         sub = ap_.Namespace(**vars(args))
         sub.workload = name
         sub.precision = "mixed"
-        sub.steps = min(args.steps, 10)
+        sub.steps = min(args.steps, 20)
         sub.warmup = max(args.warmup, 3)
         sub.no_cpu_baseline = name != "sedov-tracks"
         sub.no_looped = False
