@@ -763,30 +763,22 @@ def run_srhd(args):
         results["default"]["fp64_pipe_frac"] = fd["frac"]
     e2e = None
     if not args.no_e2e:
+        # the host-buffer call: conserved in from and primitives out to pinned
+        # host memory, pipelined through the GPU in eight chunks
         hc = pinned_like(cons)
-        dc = torch.empty_like(cons)
-        out = {}
-
-        def step():
-            out["r"] = sr.recover_primitive(dc, mlp=net, refine32=2)
-
-        dc.copy_(hc)
-        step()
-        hp = torch.empty(out["r"].prim.shape, dtype=torch.float64, pin_memory=True)
+        hr = sr.HostRecovery(mlp=net, refine32=2, chunks=8)
+        hp = hr.recover(hc)
         bi = hc.numel() * 8
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         k = max(2, min(args.steps, 10))
         for _ in range(k):
-            dc.copy_(hc, non_blocking=True)
-            step()
-            hp.copy_(out["r"].prim, non_blocking=True)
-        torch.cuda.synchronize()
+            hp = hr.recover(hc)
         el = (time.perf_counter() - t0) / k
         e2e = {"value": n * world / el, "unit": "zones/s", "h2d_bytes_per_step": bi,
                "d2h_bytes_per_step": hp.numel() * 8,
-               "call": "srhd.recover_primitive with the learned guess, conserved in and primitives out through "
-                       "pinned host buffers"}
+               "call": "srhd.HostRecovery.recover (mara_srhd_recover_primitive_host) with the learned guess: "
+                       "conserved in and primitives out through pinned host buffers, eight chunks on three streams"}
     line = _line(args, world, best["zones_per_s"] * world, "zones/s", best["ms"], "f64 (bf16 guess)",
                  {"workload": "srhd-c2p-2^24", "zones": n, "gamma": 4.0 / 3.0}, roof, {"variants": results, "e2e": e2e})
     return line if rank == 0 else None

@@ -431,6 +431,23 @@ int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component
                                 int32_t refine32, int32_t seeded_budget, double* prim, int32_t* iterations,
                                 int32_t* status, unsigned long long* failures, void* stream);
 
+/* The same recovery for zones in pinned HOST memory (SoA [5][n] in and out),
+ * as a host program holding its zones would call srhd::recover_primitive:
+ * the zones go through the GPU in `chunks` pieces on three internal streams,
+ * each piece copied in, recovered and copied out in order, so that the host
+ * link's transfers of some pieces overlap the recovery of others. Arguments
+ * as mara_srhd_recover_primitive (no per-zone iteration or status arrays);
+ * *failures (nullable, HOST) receives the count of failed zones. workspace:
+ * device memory of mara_srhd_host_workspace_bytes(n, chunks) bytes. Work the
+ * caller queued on `stream` before the call runs first; the call returns
+ * when the primitives are in host_prim. No counterpart in the reference,
+ * which recovers on the host. */
+int64_t mara_srhd_host_workspace_bytes(int64_t n, int32_t chunks);
+int mara_srhd_recover_primitive_host(const double* host_cons, int64_t n, double gamma_law_index,
+                                     double temperature_floor, const void* mlp_weights, int32_t refine32,
+                                     int32_t seeded_budget, double* host_prim, int32_t chunks, void* workspace,
+                                     unsigned long long* failures, void* stream);
+
 /* Seeded SRHD test zones (no counterpart in the reference): rho in
  * [rho_lo, rho_hi] and p in [p_lo, p_hi] log-uniform, Lorentz factor
  * log-uniform in [1, w_hi] along an isotropic direction; writes primitives and

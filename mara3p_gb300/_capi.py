@@ -113,6 +113,10 @@ SIGNATURES = {
     "mara_srhd_recover_primitive": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                                    ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int32,
                                                    ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    "mara_srhd_host_workspace_bytes": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int32]),
+    "mara_srhd_recover_primitive_host": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_double, ctypes.c_double, _vp,
+                                                        ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp,
+                                                        _vp]),
     "mara_srhd_seeded_zones": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp,
                                               _vp, _vp]),

@@ -360,6 +360,99 @@ int mara_srhd_recover_primitive(const double* cons, int64_t n, int64_t component
     return launch_status("c2p_mlp_kernel");
 }
 
+// ------------------------------------------------------------- host-buffer recovery
+// The zones of a host-buffer call go through the GPU in chunks, each on one
+// of kHostSlots streams: its copy in, its recovery and its copy out are
+// ordered on that stream, and the streams run side by side, so the host-link
+// transfers of some chunks overlap the recovery of others. A slot's device
+// buffers (conserved and primitives of one chunk, one failure counter) are
+// reused by every kHostSlots-th chunk, which the stream order makes safe.
+namespace {
+constexpr int kHostSlots = 3;
+
+int64_t host_chunk_zones(int64_t n, int32_t chunks) { return (n + chunks - 1) / chunks; }
+
+int64_t host_slot_bytes(int64_t m) { return (10 * m * 8 + 8 + 255) / 256 * 256; }
+} // namespace
+
+int64_t mara_srhd_host_workspace_bytes(int64_t n, int32_t chunks)
+{
+    if (n < 0 || chunks < 1) return -1;
+    return kHostSlots * host_slot_bytes(host_chunk_zones(n, chunks)) + 256;
+}
+
+int mara_srhd_recover_primitive_host(const double* host_cons, int64_t n, double gamma_law_index,
+                                     double temperature_floor, const void* mlp_weights, int32_t refine32,
+                                     int32_t seeded_budget, double* host_prim, int32_t chunks, void* workspace,
+                                     unsigned long long* failures, void* stream)
+{
+    MARA_REQUIRE(n >= 0, "mara_srhd_recover_primitive_host: negative zone count");
+    MARA_REQUIRE(chunks >= 1 && chunks <= 4096, "mara_srhd_recover_primitive_host: chunks must be in [1, 4096]");
+    if (failures) *failures = 0;
+    if (n == 0) return MARA_OK;
+    MARA_REQUIRE(host_cons && host_prim && workspace, "mara_srhd_recover_primitive_host: null buffer");
+    const int64_t m = host_chunk_zones(n, chunks);
+    const int64_t slot_bytes = host_slot_bytes(m);
+    char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    cudaStream_t caller = as_stream(stream);
+    cudaStream_t st[kHostSlots] = {};
+    cudaEvent_t start = nullptr;
+    int r = MARA_OK;
+    auto cuda = [&](cudaError_t e, const char* what) {
+        if (r == MARA_OK && e != cudaSuccess) r = cuda_fail(e, what);
+        return r == MARA_OK;
+    };
+    // the chunks follow whatever the caller queued on its stream before the call
+    cuda(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "cudaEventCreate");
+    cuda(cudaEventRecord(start, caller), "cudaEventRecord");
+    for (int k = 0; k < kHostSlots && r == MARA_OK; ++k)
+    {
+        cuda(cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda(cudaStreamWaitEvent(st[k], start, 0), "cudaStreamWaitEvent");
+        auto* count = reinterpret_cast<unsigned long long*>(base + k * slot_bytes + 10 * m * 8);
+        cuda(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st[k]), "cudaMemsetAsync");
+    }
+    for (int64_t c = 0; c * m < n && r == MARA_OK; ++c)
+    {
+        const int k = int(c % kHostSlots);
+        const int64_t z0 = c * m, mz = std::min(m, n - z0);
+        auto* dc = reinterpret_cast<double*>(base + k * slot_bytes);
+        double* dp = dc + 5 * m;
+        auto* count = reinterpret_cast<unsigned long long*>(dc + 10 * m);
+        // five component rows of mz zones: from pitch n (host) to pitch m (device)
+        if (!cuda(cudaMemcpy2DAsync(dc, m * 8, host_cons + z0, n * 8, mz * 8, 5, cudaMemcpyHostToDevice, st[k]),
+                  "cudaMemcpy2DAsync (in)"))
+            break;
+        const int rr = mara_srhd_recover_primitive(dc, mz, m, 1, gamma_law_index, temperature_floor, mlp_weights,
+                                                   refine32, seeded_budget, dp, nullptr, nullptr, count, st[k]);
+        if (rr != MARA_OK)
+        {
+            r = rr;
+            break;
+        }
+        cuda(cudaMemcpy2DAsync(host_prim + z0, n * 8, dp, m * 8, mz * 8, 5, cudaMemcpyDeviceToHost, st[k]),
+             "cudaMemcpy2DAsync (out)");
+    }
+    unsigned long long total = 0;
+    for (int k = 0; k < kHostSlots; ++k)
+    {
+        if (!st[k]) continue;
+        if (r == MARA_OK)
+        {
+            unsigned long long v = 0;
+            auto* count = reinterpret_cast<unsigned long long*>(base + k * slot_bytes + 10 * m * 8);
+            if (cuda(cudaMemcpyAsync(&v, count, sizeof v, cudaMemcpyDeviceToHost, st[k]), "cudaMemcpyAsync") &&
+                cuda(cudaStreamSynchronize(st[k]), "cudaStreamSynchronize"))
+                total += v;
+        }
+        else cudaStreamSynchronize(st[k]);
+        cudaStreamDestroy(st[k]);
+    }
+    if (start) cudaEventDestroy(start);
+    if (r == MARA_OK && failures) *failures = total;
+    return r;
+}
+
 int mara_srhd_seeded_zones(uint64_t seed, int64_t n, double rho_lo, double rho_hi, double p_lo, double p_hi,
                            double w_hi, double gamma_law_index, double* prim, double* cons, void* stream)
 {

@@ -54,6 +54,43 @@ def recover_primitive(cons: torch.Tensor, gamma_law_index: float = 4.0 / 3.0, te
     return Recovery(prim, it, st)
 
 
+class HostRecovery:
+    """srhd::recover_primitive for zones held in (pinned) host memory:
+    `recover(cons)` takes a (5, n) float64 CPU tensor and returns the (5, n)
+    primitives in a pinned CPU tensor of this object, pipelined through the
+    GPU in `chunks` pieces (transfers of some pieces overlap the recovery of
+    others). The device workspace and the output are kept between calls of
+    the same n. `failures` holds the failed-zone count of the last call."""
+
+    def __init__(self, mlp: "PressureGuess | None" = None, refine32: int = 0, seeded_budget: int = 12,
+                 gamma_law_index: float = 4.0 / 3.0, temperature_floor: float = 0.0, chunks: int = 8):
+        self.mlp, self.refine32, self.seeded_budget, self.chunks = mlp, refine32, seeded_budget, chunks
+        self.gamma, self.floor = gamma_law_index, temperature_floor
+        self.n = -1
+        self.failures = 0
+
+    def recover(self, cons: torch.Tensor) -> torch.Tensor:
+        if cons.device.type != "cpu" or cons.dtype != torch.float64 or cons.dim() != 2 or cons.shape[0] != 5:
+            raise ValueError("cons must be a (5, n) float64 CPU tensor")
+        cons = cons.contiguous()
+        n = cons.shape[1]
+        if n != self.n:
+            nbytes = lib.mara_srhd_host_workspace_bytes(n, self.chunks)
+            if nbytes < 0:
+                check(1, "mara_srhd_host_workspace_bytes")
+            self.workspace = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+            self.prim = torch.empty((5, n), dtype=torch.float64).pin_memory()
+            self.n = n
+        failed = ctypes.c_ulonglong()
+        check(lib.mara_srhd_recover_primitive_host(cons.data_ptr(), n, self.gamma, self.floor,
+                                                   self.mlp.weights.data_ptr() if self.mlp else None,
+                                                   self.refine32, self.seeded_budget, self.prim.data_ptr(),
+                                                   self.chunks, self.workspace.data_ptr(), ctypes.byref(failed),
+                                                   _stream()), "srhd recover_primitive_host")
+        self.failures = int(failed.value)
+        return self.prim
+
+
 class PressureGuess:
     """The 4-64-64-1 MLP that seeds the recovery, trained on the GPU by the
     library's own kernels on (conserved, primitive) pairs."""

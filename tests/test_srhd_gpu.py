@@ -191,6 +191,33 @@ def test_mlp_seeded_recovery_same_answer_fewer_iterations(sr, oracle, trained):
     assert mean_seeded * 2.0 <= mean_base, (mean_base, mean_seeded)
 
 
+@pytest.mark.parametrize("chunks", [1, 3, 7])
+def test_host_buffer_recovery_matches_device(sr, oracle, trained, chunks):
+    """The recovery of zones in pinned host memory, pipelined through the GPU
+    in chunks on three streams (mara_srhd_recover_primitive_host), gives the
+    device call's primitives bit for bit and its failure count: an uneven
+    chunking, the reference start and the learned guess, two zones that the
+    reference rejects (tau < 0) among them, and a second call on the same
+    buffers."""
+    net, _, _, _ = trained
+    n = 100_003
+    _, cons = seeded_zones(oracle, n, seed=91)
+    cons_soa = cons.reshape(-1, 5).T.copy()
+    for z in (5, 50_001):
+        cons_soa[:, z] = [1.0, 0.0, 0.0, 0.0, -0.5]
+    host = torch.from_numpy(cons_soa).pin_memory()
+    dev = host.cuda()
+    for mlp, refine in ((None, 0), (net, 2)):
+        ref = sr.recover_primitive(dev, GAMMA, mlp=mlp, refine32=refine)
+        failed = int((ref.status != 0).sum())
+        assert failed == 2
+        hr = sr.HostRecovery(mlp=mlp, refine32=refine, chunks=chunks)
+        for _ in range(2):
+            got = hr.recover(host)
+            assert torch.equal(got, ref.prim.cpu())
+            assert hr.failures == failed
+
+
 @pytest.mark.parametrize("n", [1, 127, 129, 1000, 40000])
 def test_slow_zone_queue_sizes_and_failures(sr, oracle, trained, n):
     """The recovery kernels queue zones still iterating after their first
