@@ -77,3 +77,22 @@ def test_make_solver_data_rejects_unknown_keys():
     assert md.make_solver_data({"block_size": 32, "nu": 1e-3}).nu == 1e-3
     with pytest.raises(ValueError):
         md.make_solver_data({"block_sise": 32})
+
+
+def test_srhd_host_recovery_arguments_checked_before_any_gpu_work():
+    """The host-buffer recovery's sizes and argument checks need no GPU."""
+    from mara3p_gb300._capi import lib
+    assert lib.mara_srhd_host_workspace_bytes(-1, 8) == -1
+    assert lib.mara_srhd_host_workspace_bytes(100, 0) == -1
+    one = lib.mara_srhd_host_workspace_bytes(1000, 1)
+    assert one >= 3 * 10 * 1000 * 8 and lib.mara_srhd_host_workspace_bytes(1000, 8) < one
+    failed = ctypes.c_ulonglong(7)
+    # no zones: nothing to do, and the failure count is cleared
+    assert lib.mara_srhd_recover_primitive_host(None, 0, 4.0 / 3, 0.0, None, 0, 0, None, 8, None,
+                                                ctypes.byref(failed), None) == 0
+    assert failed.value == 0
+    fake = ctypes.c_void_p(16)
+    assert lib.mara_srhd_recover_primitive_host(fake, 10, 4.0 / 3, 0.0, None, 0, 0, fake, 0, fake, None, None) == 1
+    assert b"chunks" in lib.mara_last_error()
+    assert lib.mara_srhd_recover_primitive_host(None, 10, 4.0 / 3, 0.0, None, 0, 0, fake, 4, fake, None, None) == 1
+
