@@ -645,11 +645,9 @@ constexpr int E0K = TK + 1, E0N = (TJ + 1) * E0K;   // EMFs along i: jj in [0, T
 constexpr int E1K = TK + 1, E1N = TJ * E1K;         // along j: jj in [0, TJ), kk in [0, TK]
 constexpr int E2K = TK, E2N = (TJ + 1) * E2K;       // along k: jj in [0, TJ], kk in [0, TK)
 constexpr int pad32(int n) { return (n + 31) & ~31; }
-// work items per phase, each kind padded to whole warps so that no warp mixes kinds
+// the flux kernel's face items per plane, each kind padded to whole warps so
+// that no warp mixes kinds
 constexpr int SOLVE_Y = pad32(FYN), SOLVE_Z = pad32(FZN);
-// edge items are not padded: the three kinds cost alike, and padding would
-// add a fourth round
-constexpr int EDGE_0 = E0N, EDGE_1 = E1N, EDGE_2 = E2N;
 // copies per plane: x and y rows as TK/4 16-byte pieces plus the two halo
 // elements; z rows (N + 1 floats, unaligned) element by element
 constexpr int ROW_PIECES = TK / 4 + 2;
@@ -1032,36 +1030,40 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
         if (!NEXT) stage_faces(c, first);
         if (!last) load(true, c + 1, c + 1);
         const int s = c & 1, sp = (c - 1) & 1, ys = mod3(c), yp = mod3(c - 1);
-        // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order)
-        for (int t = threadIdx.x; t < EDGE_0 + EDGE_1 + EDGE_2; t += EMF_THREADS)
+        // edge EMFs at i = c (edge_emf_from_face, scheme_mhd_v1.cpp:76-98; ee_f's order).
+        // Thread t forms the E0 edges t (and t + EMF_THREADS), the E1 edge t and
+        // the E2 edge t in straight-line code, so that their independent chains
+        // interleave.
         {
-            if (t < EDGE_0)
-            {
-                if (t >= E0N) continue;
-                const int jj = t / E0K, kk = t - jj * E0K;
+            const int t = threadIdx.x;
+            auto edge0 = [&](int u) {
+                const int jj = u / E0K, kk = u - jj * E0K;
                 const float* y0 = S.ey[ys][0] + YO - 1;
                 const float* z0 = S.ez[ys][0];
-                S.e0[s][t] = avg(avg(y0[jj * YK + kk], y0[jj * YK + kk + 1]), avg(z0[jj * ZK + kk], z0[(jj + 1) * ZK + kk]));
-            }
-            else if (t < EDGE_0 + EDGE_1)
+                return avg(avg(y0[jj * YK + kk], y0[jj * YK + kk + 1]), avg(z0[jj * ZK + kk], z0[(jj + 1) * ZK + kk]));
+            };
+            float v0 = 0.0f, w0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+            if (t < E0N) v0 = edge0(t);
+            if (t + EMF_THREADS < E0N) w0 = edge0(t + EMF_THREADS);
+            if (t < E1N)
             {
-                const int u = t - EDGE_0;
-                if (u >= E1N) continue;
-                const int jj = u / E1K, kk = u - jj * E1K;
+                const int jj = t / E1K, kk = t - jj * E1K;
                 const float* x1 = S.ex[s][0] + XO - 1;
                 const float a = avg(S.ez[yp][1][(jj + 1) * ZK + kk], S.ez[ys][1][(jj + 1) * ZK + kk]);
                 const float b = avg(x1[(jj + 1) * XK + kk], x1[(jj + 1) * XK + kk + 1]);
-                S.e1[s][u] = avg(a, b);
+                v1 = avg(a, b);
             }
-            else
+            if (t < E2N)
             {
-                const int u = t - EDGE_0 - EDGE_1;
-                if (u >= E2N) continue;
-                const int jj = u / E2K, kk = u - jj * E2K;
+                const int jj = t / E2K, kk = t - jj * E2K;
                 const float a = avg(S.ex[s][1][jj * XK + XO + kk], S.ex[s][1][(jj + 1) * XK + XO + kk]);
                 const float b = avg(S.ey[yp][1][jj * YK + YO + kk], S.ey[ys][1][jj * YK + YO + kk]);
-                S.e2[s][u] = avg(a, b);
+                v2 = avg(a, b);
             }
+            if (t < E0N) S.e0[s][t] = v0;
+            if (t + EMF_THREADS < E0N) S.e0[s][t + EMF_THREADS] = w0;
+            if (t < E1N) S.e1[s][t] = v1;
+            if (t < E2N) S.e2[s][t] = v2;
         }
         if (!NEXT)
         {
@@ -1070,50 +1072,57 @@ __global__ void __launch_bounds__(fused::EMF_THREADS, 4) emf_kernel(const Args A
         }
         __syncthreads();
         // faces: x of layer c (the tile); y and z of plane c-1, with the high
-        // neighbour's row and column, which the next-stage cells need
+        // neighbour's row and column, which the next-stage cells need. Thread t
+        // updates the x face t, the y face t and the z face t, again in
+        // straight-line code.
         const double dtdl_d = s_dtdl;
-        for (int t = threadIdx.x; t < FXN + SOLVE_Y + SOLVE_Z; t += EMF_THREADS)
         {
-            if (t < FXN)
+            const int t = threadIdx.x;
+            static_assert(FXN <= EMF_THREADS && FYN <= EMF_THREADS && FZN <= EMF_THREADS, "one face of each kind per thread");
+            const bool dx = t < FXN;
+            const bool dy = !first && t < FYN && (NEXT || t < FXN || T.last_j);
+            const int jy = t / TK, ky = t - jy * TK;            // jy = TJ: the high neighbour's face
+            const int jz = t / FZK, kz = t - jz * FZK;          // kz = TK: the high neighbour's face
+            const bool dz = !first && t < FZN && (NEXT || kz < TK || T.last_k);
+            double ox = 0.0, oy = 0.0, oz = 0.0;
+            if (dx)
             {
-                const int jj = t / TK, kk = t - jj * TK;
-                const double cf = curl_f(S.e2[s][(jj + 1) * E2K + kk], S.e2[s][jj * E2K + kk], S.e1[s][jj * E1K + kk + 1],
-                                         S.e1[s][jj * E1K + kk]);
-                const uint32_t f = fidx32(N, 0, c, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, S.bin[t]);
-                if (with_avg) out = half_exact(S.bav[t] + out);
-                S.bx[s][t] = out;
-                if (NEXT) S.bxf[s][t] = d2f(out);
-                if (!last || c == N) A.bf_out[0][f] = out;
+                const double cf = curl_f(S.e2[s][(jy + 1) * E2K + ky], S.e2[s][jy * E2K + ky], S.e1[s][jy * E1K + ky + 1],
+                                         S.e1[s][jy * E1K + ky]);
+                ox = fma(-cf, dtdl_d, S.bin[t]);
+                if (with_avg) ox = half_exact(S.bav[t] + ox);
             }
-            else if (t < FXN + SOLVE_Y)
+            if (dy)
             {
-                const int u = t - FXN;
-                if (first || u >= FYN || (!NEXT && u >= FXN && !T.last_j)) continue;
-                const int jj = u / TK, kk = u - jj * TK;
-                const double cf = curl_f(S.e0[sp][jj * E0K + kk + 1], S.e0[sp][jj * E0K + kk], S.e2[s][jj * E2K + kk],
-                                         S.e2[sp][jj * E2K + kk]);
-                const uint32_t f = fidx32(N, 1, c - 1, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, S.bin[FXN + u]);
-                if (with_avg) out = half_exact(S.bav[FXN + u] + out);
-                S.by[u] = out;
-                if (NEXT) S.byf[u] = d2f(out);
-                if (jj < TJ || T.last_j) A.bf_out[1][f] = out;
+                const double cf = curl_f(S.e0[sp][jy * E0K + ky + 1], S.e0[sp][jy * E0K + ky], S.e2[s][jy * E2K + ky],
+                                         S.e2[sp][jy * E2K + ky]);
+                oy = fma(-cf, dtdl_d, S.bin[FXN + t]);
+                if (with_avg) oy = half_exact(S.bav[FXN + t] + oy);
             }
-            else
+            if (dz)
             {
-                const int u = t - FXN - SOLVE_Y;
-                if (first || u >= FZN) continue;
-                const int jj = u / FZK, kk = u - jj * FZK;
-                if (!NEXT && kk == TK && !T.last_k) continue;
-                const double cf = curl_f(S.e1[s][jj * E1K + kk], S.e1[sp][jj * E1K + kk], S.e0[sp][(jj + 1) * E0K + kk],
-                                         S.e0[sp][jj * E0K + kk]);
-                const uint32_t f = fidx32(N, 2, c - 1, T.j0 + jj, T.k0 + kk);
-                double out = fma(-cf, dtdl_d, S.bin[FXN + FYN + u]);
-                if (with_avg) out = half_exact(S.bav[FXN + FYN + u] + out);
-                S.bz[u] = out;
-                if (NEXT) S.bzf[u] = d2f(out);
-                if (kk < TK || T.last_k) A.bf_out[2][f] = out;
+                const double cf = curl_f(S.e1[s][jz * E1K + kz], S.e1[sp][jz * E1K + kz], S.e0[sp][(jz + 1) * E0K + kz],
+                                         S.e0[sp][jz * E0K + kz]);
+                oz = fma(-cf, dtdl_d, S.bin[FXN + FYN + t]);
+                if (with_avg) oz = half_exact(S.bav[FXN + FYN + t] + oz);
+            }
+            if (dx)
+            {
+                S.bx[s][t] = ox;
+                if (NEXT) S.bxf[s][t] = d2f(ox);
+                if (!last || c == N) A.bf_out[0][fidx32(N, 0, c, T.j0 + jy, T.k0 + ky)] = ox;
+            }
+            if (dy)
+            {
+                S.by[t] = oy;
+                if (NEXT) S.byf[t] = d2f(oy);
+                if (jy < TJ || T.last_j) A.bf_out[1][fidx32(N, 1, c - 1, T.j0 + jy, T.k0 + ky)] = oy;
+            }
+            if (dz)
+            {
+                S.bz[t] = oz;
+                if (NEXT) S.bzf[t] = d2f(oz);
+                if (kz < TK || T.last_k) A.bf_out[2][fidx32(N, 2, c - 1, T.j0 + jz, T.k0 + kz)] = oz;
             }
         }
         if (NEXT)
