@@ -1123,6 +1123,18 @@ def other_workloads(args) -> dict:
     import torch
     out = {}
     runners = {"minidisk-256": "run_ours", **RUNNERS}
+
+    def release():
+        # device and pinned host memory the earlier runs cached: a later
+        # run's pinned buffers otherwise come from whatever is left, and the
+        # ensemble's host-buffer line measured 0.8 to 3.3 G cell-updates/s
+        # depending on what ran before it
+        gc.collect()
+        torch.cuda.empty_cache()
+        if hasattr(torch._C, "_host_emptyCache"):
+            torch._C._host_emptyCache()
+
+    release()
     for name, fn in runners.items():
         sub = ap_.Namespace(**vars(args))
         sub.workload = name
@@ -1137,8 +1149,7 @@ def other_workloads(args) -> dict:
         t0 = time.perf_counter()
         line = globals()[fn](sub)
         torch.cuda.synchronize()
-        gc.collect()
-        torch.cuda.empty_cache()
+        release()
         if line is not None:
             out[name] = compact(line)
             out[name]["wall_s"] = time.perf_counter() - t0
