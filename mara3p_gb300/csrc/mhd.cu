@@ -560,9 +560,9 @@ update_kernel(const Args A)
                     }
                     const double u = A.uc[q * A.ucs + c * A.uzs];
                     if (MODE == MIX_FROM_INCREMENT)
-                        out = u + f2d(__fmul_rn(0.5f, __fsub_rn(A.dinc[q * NN + c], du)));
+                        out = u + f2d_sum(__fmul_rn(0.5f, __fsub_rn(A.dinc[q * NN + c], du)));
                     else
-                        out = u - f2d(du);
+                        out = u - f2d_sum(du);
                 }
                 // weighted_sum a*0.5 + b*(1-0.5): halving is exact, so (a + b)*0.5 is the same double
                 if (A.uavg) out = sizeof(R) == sizeof(float) ? half_exact(A.uavg[q * NN + c] + out)
@@ -903,8 +903,8 @@ __global__ void __launch_bounds__(fused::FLUX_THREADS, 4) flux_kernel(const Args
                     continue;
                 }
                 const double u = stage_u ? S.uc[q][t] : A.uc[q * A.ucs + cell * A.uzs];
-                double out = MODE == MIX_FROM_INCREMENT ? u + f2d(__fmul_rn(0.5f, __fsub_rn(S.dinc[q][t], du)))
-                                                        : u - f2d(du);
+                double out = MODE == MIX_FROM_INCREMENT ? u + f2d_sum(__fmul_rn(0.5f, __fsub_rn(S.dinc[q][t], du)))
+                                                        : u - f2d_sum(du);
                 if (A.uavg) out = half_exact(A.uavg[q * NN + cell] + out);
                 A.uc_out[q * NN + cell] = out;
             }

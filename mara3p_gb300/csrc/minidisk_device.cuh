@@ -520,7 +520,7 @@ __device__ inline void mixed_cell(const Args& A, float x, float y, const float p
     for (int k = 0; k < 3; ++k)
     {
         const float inc = KIND == K_MIX2 ? vadd(in.d[k], du[k]) : du[k];
-        A.u_out[k * NN + idx] = __fma_rn(f2d(inc), KIND == K_MIX2 ? 0.5 : 1.0, in.u[k]);
+        A.u_out[k * NN + idx] = __fma_rn(f2d_sum(inc), KIND == K_MIX2 ? 0.5 : 1.0, in.u[k]);
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), 0.5f, uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax) local_max.take(wavespeed_f(A.f, of[0], of[1], of[2], spot), idx);
@@ -545,8 +545,8 @@ __device__ inline void mixed_cell2(const Args& A, float2 x, float2 y, const floa
         // RK2: u0 + (d1 + d2)/2, the halving exact inside the FP64 fma; RK1: u + du
         const float2 inc = KIND == K_MIX2 ? vadd(in.d[k], du[k]) : du[k];
         const double h = KIND == K_MIX2 ? 0.5 : 1.0;
-        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = make_double2(__fma_rn(f2d(inc.x), h, in.u[k].x),
-                                                                           __fma_rn(f2d(inc.y), h, in.u[k].y));
+        *reinterpret_cast<double2*>(A.u_out + k * NN + idx) = make_double2(__fma_rn(f2d_sum(inc.x), h, in.u[k].x),
+                                                                           __fma_rn(f2d_sum(inc.y), h, in.u[k].y));
         of[k] = KIND == K_MIX2 ? vfma(vsub(du[k], in.d[k]), bc<float2>(0.5f), uc[k]) : vadd(uc[k], du[k]);
     }
     if (A.amax)

@@ -41,6 +41,22 @@ __device__ inline double f2d(float x)
     return __hiloint2double(int(hi), int(lo));
 }
 
+// f2d for an FP32 increment that is added to an FP64 state (u + x, or
+// fma(x, h, u) with h = 1 or 1/2): the same double as f2d for every normal
+// float, infinity and NaN (the bit formula, run on the host over all 2^32
+// floats, gives f2d's bits for each of those). Zeros and subnormals become
+// doubles of the same sign below 2^-126 in magnitude, which the sum absorbs
+// exactly wherever |u| >= 2^-72 (elsewhere it moves u by less than 2^-126).
+// No zero test, and the infinity/NaN test is one FP32 comparison; the sign
+// bit, shifted down three places with the rest, is masked back to bit 31.
+__device__ __forceinline__ double f2d_sum(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const bool special = !(fabsf(x) < __int_as_float(0x7F800000));
+    const unsigned hi = (unsigned(int(b) >> 3) & 0x8FFFFFFFu) + (special ? 0x70000000u : 0x38000000u);
+    return __hiloint2double(int(hi), int(b << 29));
+}
+
 // Single-MUFU approximations for the mixed path (relative error ~1e-7,
 // well inside the FP32 budget of the fluxes; denormals flush to zero).
 __device__ inline float rcp_fast(float x)
