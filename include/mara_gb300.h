@@ -682,6 +682,17 @@ int mara_measure_fp64_rate(double* dfma_per_second, void* stream);
  * measurement helper with no counterpart in the reference. */
 int mara_measure_host_link(void* host, void* device, int64_t bytes, double* gbs, void* stream);
 
+/* Self-check of the library's integer float<->double conversions against the
+ * GPU's own conversion instructions; mismatches[3] (host) receives the count
+ * of wrong results of [0] float->double (all 2^32 floats), [1] the
+ * increment form of float->double used by the mixed stores (all 2^32
+ * floats; zeros and subnormals may give any double of their sign below
+ * 2^-126), [2] double->float, rounding to nearest with ties away from zero
+ * (2^32 doubles covering every sign, exponent and top-20-bit mantissa
+ * pattern). All three are 0 on a correct build. Synchronizes the stream.
+ * No counterpart in the reference. */
+int mara_check_conversions(unsigned long long* mismatches, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

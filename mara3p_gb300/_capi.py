@@ -190,6 +190,7 @@ SIGNATURES.update({
                                          _vp, _vp, _vp]),
     "mara_measure_fp64_rate": (ctypes.c_int, [c_double_p, _vp]),
     "mara_measure_host_link": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, c_double_p, _vp]),
+    "mara_check_conversions": (ctypes.c_int, [ctypes.POINTER(ctypes.c_ulonglong), _vp]),
     "mara_minidisk_sweep_tma": (ctypes.c_int, [ctypes.c_int32]),
     # mhd_scheme_v2 block API and pointwise physics
     "mara_mhd_v2_primitive_array": (ctypes.c_int, [ctypes.c_int32] * 3 + [_vp] * 4 + [ctypes.c_double, _vp, _vp, _vp]),

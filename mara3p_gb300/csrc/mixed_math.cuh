@@ -43,8 +43,8 @@ __device__ inline double f2d(float x)
 
 // f2d for an FP32 increment that is added to an FP64 state (u + x, or
 // fma(x, h, u) with h = 1 or 1/2): the same double as f2d for every normal
-// float, infinity and NaN (the bit formula, run on the host over all 2^32
-// floats, gives f2d's bits for each of those). Zeros and subnormals become
+// float, infinity and NaN (mara_check_conversions compares both with the
+// hardware conversion over all 2^32 floats). Zeros and subnormals become
 // doubles of the same sign below 2^-126 in magnitude, which the sum absorbs
 // exactly wherever |u| >= 2^-72 (elsewhere it moves u by less than 2^-126).
 // No zero test, and the infinity/NaN test is one FP32 comparison; the sign

@@ -1,6 +1,8 @@
 """The measurement helpers the bench's rooflines divide by: the FP64 FMA
 rate and the host-link rates. Each returns plausible positive rates on the
-GPU and refuses bad arguments without touching the device."""
+GPU and refuses bad arguments without touching the device. Also the
+library's self-check of its integer float<->double conversions against the
+GPU's conversion instructions."""
 from __future__ import annotations
 
 import ctypes
@@ -45,3 +47,11 @@ def test_host_link_rejects_bad_arguments(capi):
     host = torch.empty(1 << 20, dtype=torch.uint8, pin_memory=True)
     assert capi.lib.mara_measure_host_link(host.data_ptr(), dev.data_ptr(), 1000, g, None) != 0
     assert capi.lib.mara_measure_host_link(None, dev.data_ptr(), 1 << 20, g, None) != 0
+
+
+def test_integer_conversions_match_the_hardware(capi):
+    """f2d and its increment form over all 2^32 floats, d2f over 2^32 doubles
+    (every high word, hashed low words, exact ties included): no mismatch."""
+    bad = (ctypes.c_ulonglong * 3)()
+    capi.check(capi.lib.mara_check_conversions(bad, torch.cuda.current_stream().cuda_stream))
+    assert list(bad) == [0, 0, 0], list(bad)
