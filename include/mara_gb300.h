@@ -167,6 +167,9 @@ int mara_minidisk_advance_host(const mara_minidisk_params* sd, const double* u_i
  *   0  FP64:    u_out = L(u_in); with u_avg: u_out = u_avg*0.5 + L(u_in)*0.5
  *   1  mixed 1: d_out = dt*L(u_in) (FP32); with d_out NULL: u_out = u_in + dt*L(u_in)
  *   2  mixed 2: u_out = u_in + (d1 + dt*L(f32(u_in) + d1))/2
+ * In the mixed kinds the FP32 increment enters the FP64 sum exactly, except
+ * that a zero or subnormal increment may add a value below 2^-126 in
+ * magnitude (absorbed exactly wherever |u_in| >= 2^-72).
  * reduce_wavespeed != 0 also folds the fastest wavespeed of u_out into
  * clock->max_wavespeed (mixed kinds: from u_out's FP32 image, as a double;
  * mara_minidisk_advance instead re-evaluates the fastest cell in FP64).
