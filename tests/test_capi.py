@@ -29,6 +29,35 @@ def test_library_exports_every_declared_symbol():
     assert set(names) <= set(_capi.SIGNATURES), "every declared function needs a ctypes signature"
 
 
+def declarations() -> list[tuple[str, str, int]]:
+    """(return type, name, parameter count) of every function include/*.h declares."""
+    out = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        text = re.sub(r"#.*", "", text)
+        for ret, name, params in re.findall(r"([A-Za-z_][A-Za-z0-9_ *]*?)\b(mara_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;",
+                                            text, flags=re.S):
+            p = params.strip()
+            out.append((ret.strip(), name, 0 if p in ("", "void") else len(p.split(","))))
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every binding passes as many arguments as the C declaration takes and
+    reads the declared return type, so no call through the ABI is misaligned."""
+    from mara3p_gb300 import _capi
+    rets = {"int": ctypes.c_int, "int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64,
+            "const char*": ctypes.c_char_p, "const char *": ctypes.c_char_p}
+    decls = declarations()
+    assert len(decls) == len(declared_functions())
+    wrong = []
+    for ret, name, nparams in decls:
+        restype, argtypes = _capi.SIGNATURES[name]
+        if len(argtypes) != nparams or rets.get(ret) != restype:
+            wrong.append((name, ret, nparams, restype, len(argtypes)))
+    assert not wrong, wrong
+
+
 def test_version_string():
     from mara3p_gb300 import _capi
     assert b"sm_103a" in _capi.lib.mara_version()
