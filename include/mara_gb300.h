@@ -193,8 +193,8 @@ int mara_minidisk_clock_update(const mara_minidisk_params* sd, mara_minidisk_clo
  *   - the mesh may hold at most MARA_MINIDISK_NOALLOC_MAX_CELLS cells
  *     ((block_size << depth)^2); larger meshes are rejected with
  *     MARA_ERR_ARGUMENT and a message naming the limit;
- *   - the array (36 bytes per cell of that limit, 9 MiB) is held by every GPU
- *     that loads the library until the process exits;
+ *   - the array (36 bytes per cell of that limit plus 64, 9 MiB) is held by
+ *     every GPU that loads the library until the process exits;
  *   - the first call on a device looks up the array's device address with
  *     that device current (cudaGetSymbolAddress); make that first call before
  *     any stream capture. The address is kept for the life of the process, so

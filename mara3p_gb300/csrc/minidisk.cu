@@ -33,6 +33,10 @@
 namespace mara {
 namespace md {
 
+// Workspace tail of mixed RK2: the next step's stage-1 binary (6 doubles),
+// padded to 64 bytes.
+constexpr int64_t kNextBinaryBytes = 64;
+
 // ------------------------------------------------------------- shared layout
 template<typename R>
 struct Smem
@@ -394,7 +398,9 @@ __global__ void __launch_bounds__(SW_WARPS * 32) sweep_kernel(const Args A, cons
         // block 0 is scheduled first: its binary job overlaps the whole stage
         if (block == 0)
         {
-            if (threadIdx.x == 0) side_binary_job(A);
+            // job 1 on a second warp, or on lane 1 of a one-warp block
+            if (threadIdx.x == 0) side_binary_job(A, 0);
+            else if (threadIdx.x == (blockDim.x >= 64 ? 32u : 1u)) side_binary_job(A, 1);
             return;
         }
         block -= 1;
@@ -1043,7 +1049,9 @@ int64_t mara_minidisk_workspace_bytes(const mara_minidisk_params* sd, int32_t rk
     if (check_params(sd)) return -1;
     int64_t NN = int64_t(sd->block_size << sd->depth) * (sd->block_size << sd->depth);
     int64_t state = 3 * NN * int64_t(sizeof(double));
-    if (precision == MARA_MIXED && rk_order == 2) return state + 3 * NN * int64_t(sizeof(float));
+    // mixed RK2: the FP32 stage-1 increment and 64 bytes for the next step's
+    // stage-1 binary (solved during stage 1, moved into the clock by stage 2)
+    if (precision == MARA_MIXED && rk_order == 2) return state + 3 * NN * int64_t(sizeof(float)) + kNextBinaryBytes;
     return state;
 }
 
@@ -1131,6 +1139,7 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
     const size_t NN = size_t(N) * N;
     double* ws_state = static_cast<double*>(workspace);
     float* ws_d1 = reinterpret_cast<float*>(ws_state + 3 * NN);
+    double* ws_next_binary = reinterpret_cast<double*>(ws_d1 + 3 * NN);   // 36 NN bytes in: 8-byte aligned
     unsigned long long* amax = dt_mode == MARA_DT_CFL ? reinterpret_cast<unsigned long long*>(&clock->max_wavespeed) : nullptr;
 
     Args A = base_args(sd);
@@ -1169,6 +1178,7 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
             // the sweeps (N >= 64) solve the stage binaries in their block 0
             Args a1 = A; a1.stage = 0; a1.u_in = cur; a1.d_out = ws_d1; a1.diag = rate0;
             a1.side_binary = side_binaries ? 1 : 0;
+            a1.next_binary = ws_next_binary;
             if (int r = grid_stage(a1, K_MIX1, s)) return r;
             const bool last_out = final_out && step + 1 == steps;
             Args a2 = A; a2.stage = 1; a2.u_in = cur; a2.d1 = ws_d1; a2.u_out = last_out ? final_out : alt;
@@ -1176,6 +1186,7 @@ int advance_impl(const mara_minidisk_params* sd, double* u, mara_minidisk_clock*
             a2.amax_key = 1;
             a2.diag = rate1;
             a2.side_binary = side_binaries ? 2 : 0;
+            a2.next_binary = ws_next_binary;
             if (int r = grid_stage(a2, K_MIX2, s)) return r;
             if (last_out) cur = final_out;
             else std::swap(cur, alt);
@@ -1370,7 +1381,8 @@ int mara_minidisk_rates(const mara_minidisk_params* sd, const double* u, const f
 namespace {
 
 constexpr int64_t kNoAllocBytesPerCell = 3 * (sizeof(double) + sizeof(float));
-static __device__ __align__(256) unsigned char g_noalloc_scratch[MARA_MINIDISK_NOALLOC_MAX_CELLS * kNoAllocBytesPerCell];
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[MARA_MINIDISK_NOALLOC_MAX_CELLS * kNoAllocBytesPerCell + kNextBinaryBytes];
 
 std::mutex g_noalloc_mutex;
 void* g_noalloc_address[64] = {};

@@ -65,12 +65,14 @@ struct Args
     int amax_key;          // mixed kinds: 1 = write the speed key of the fastest cell (speed_key) instead
     double* diag;          // optional: rate row of this stage (diagnostic sums 0..12 of the stage input)
     FloatConsts f;
-    // Mixed RK2 sweeps: block 0 of the launch solves a binary off the
-    // critical path (side_binary_job): 1 = the stage-2 binary, at t + dt,
-    // into clock->binary[1] (stage 1 reads binary[0]); 2 = the next step's
-    // stage-1 binary, at the RK2 end time, into clock->binary[0] (stage 2
-    // reads binary[1]). 0 = none.
+    // Mixed RK2 sweeps: block 0 of the launch takes the binaries off the
+    // critical path (side_binary_job). 1 (stage 1): two warps solve, side by
+    // side, the stage-2 binary at t + dt into clock->binary[1] and the next
+    // step's stage-1 binary at the RK2 end time into next_binary (stage 1
+    // itself reads binary[0]); 2 (stage 2, which reads binary[1]): copy
+    // next_binary into clock->binary[0]. 0 = none.
     int side_binary;
+    double* next_binary;   // 6 doubles of workspace for side_binary
     double mass_ratio, eccentricity;
 };
 
@@ -1238,18 +1240,25 @@ __device__ inline double rk2_end_time(double t, double dt)
 
 __device__ inline void store_binary(double* dst, const Binary& b);
 
-// A sweep launch's binary job (Args::side_binary), by one thread of block 0:
-// the FP64 Kepler solve that the clock kernel would otherwise run between
-// the steps, overlapped with the stage it precedes. The clock memory is
-// written here and read by the next launches only.
-static __device__ __noinline__ void side_binary_job(const Args& A)
+// A sweep launch's binary job (Args::side_binary), by thread 0 (job 0) and
+// thread 32 (job 1; thread 1 where the block is a single warp) of block 0: the FP64 Kepler solves that the clock kernel
+// would otherwise run between the steps. Stage 1 runs both solves of the
+// step on two warps at once, overlapped with its own sweep; stage 2 only
+// moves the second into place. Memory written here is read by later
+// launches only.
+static __device__ __noinline__ void side_binary_job(const Args& A, int job)
 {
     mara_minidisk_clock* c = const_cast<mara_minidisk_clock*>(A.clock);
     const double t = c->time, dt = c->dt;
     if (A.side_binary == 1)
-        store_binary(c->binary[1], binary_state(A.mass_ratio, A.eccentricity, A.omega, t + dt));
-    else
-        store_binary(c->binary[0], binary_state(A.mass_ratio, A.eccentricity, A.omega, rk2_end_time(t, dt)));
+    {
+        if (job == 0) store_binary(c->binary[1], binary_state(A.mass_ratio, A.eccentricity, A.omega, t + dt));
+        else store_binary(A.next_binary, binary_state(A.mass_ratio, A.eccentricity, A.omega, rk2_end_time(t, dt)));
+    }
+    else if (job == 0)
+    {
+        for (int k = 0; k < 6; ++k) c->binary[0][k] = A.next_binary[k];
+    }
 }
 
 __device__ inline void clock_end_step(mara_minidisk_clock* c, const ClockArgs& a)

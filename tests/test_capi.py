@@ -98,7 +98,7 @@ def test_advance_rejects_bad_arguments_before_any_gpu_work():
     assert b"rk_order" in lib.mara_last_error()
     assert lib.mara_minidisk_advance(ctypes.byref(c), fake, fake, 1, 2, 7, 0, fake, None) == 1
     assert lib.mara_minidisk_advance(ctypes.byref(c), None, fake, 1, 2, 0, 0, fake, None) == 1
-    assert lib.mara_minidisk_workspace_bytes(ctypes.byref(c), 2, 1) == 3 * (64 << 1) ** 2 * 12
+    assert lib.mara_minidisk_workspace_bytes(ctypes.byref(c), 2, 1) == 3 * (64 << 1) ** 2 * 12 + 64
 
 
 def test_make_solver_data_rejects_unknown_keys():
