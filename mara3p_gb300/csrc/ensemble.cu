@@ -117,16 +117,19 @@ ensemble_sweep_kernel(const Args* __restrict__ table, const int4* __restrict__ i
     }
 }
 
+// Two lanes per member (an aligned pair of one warp): the member's two stage
+// binaries (FP64 Kepler solves) run side by side.
 __global__ void ensemble_clock_kernel(mara_minidisk_clock* clocks, const ClockArgs* args, int count,
                                       int end_step, int begin_step, int key_state)
 {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= count) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = t >> 1;
+    if (m >= count) return;   // both lanes of the pair
     ClockArgs a = args[m];
     a.end_step = end_step;
     a.begin_step = begin_step;
     a.key_state = key_state;
-    advance_clock(clocks + m, a);
+    advance_clock(clocks + m, a, t & 1, 2);
 }
 
 struct CopyJob
@@ -302,8 +305,8 @@ int enqueue_stages(mara_minidisk_ensemble* e, int phase, bool tuning, cudaStream
 int enqueue_clock(mara_minidisk_ensemble* e, int end_step, int begin_step, int phase, cudaStream_t s)
 {
     const int key_state = e->flips ? 1 - phase : 0;
-    ensemble_clock_kernel<<<(e->count + 63) / 64, 64, 0, s>>>(e->clocks, e->clock_args, e->count, end_step, begin_step,
-                                                              key_state);
+    ensemble_clock_kernel<<<(2 * e->count + 31) / 32, 32, 0, s>>>(e->clocks, e->clock_args, e->count, end_step,
+                                                                  begin_step, key_state);
     return launch_status("ensemble clock kernel");
 }
 

@@ -1302,22 +1302,24 @@ __device__ inline double clock_choose_dt(const mara_minidisk_clock* c, const Clo
 
 // One clock update: finish the step that just ran (RK2 time average,
 // iteration count) and/or choose the next dt and the stage binaries.
-// Call from `lanes` (1 or 2) consecutive threads of one warp, lane = 0, 1.
+// Call from `lanes` (1 or 2) consecutive threads of one warp, lane = 0, 1;
+// two lanes are an aligned pair (threads 2k and 2k + 1 of a warp).
 __device__ inline void advance_clock(mara_minidisk_clock* c, const ClockArgs& a, int lane = 0, int lanes = 1)
 {
+    const unsigned pair = 0x3u << (threadIdx.x & 30u);
     if (lane == 0)
     {
         if (a.end_step) clock_end_step(c, a);
         if (a.begin_step) c->dt = clock_choose_dt(c, a);
     }
-    if (lanes > 1) __syncwarp(0x3u);
+    if (lanes > 1) __syncwarp(pair);
     if (a.begin_step)
     {
         const double t = c->time, dt = c->dt;
         if (a.binaries)
             for (int s = lane; s < 2; s += lanes)
                 store_binary(c->binary[s], binary_state(a.mass_ratio, a.eccentricity, a.omega, s == 0 ? t : t + dt));
-        if (lanes > 1) __syncwarp(0x3u);
+        if (lanes > 1) __syncwarp(pair);
         if (lane == 0)
         {
             c->max_wavespeed = 0.0;
