@@ -56,6 +56,29 @@ struct PerDeviceOnce
     }
 };
 
+// Timing events owned by a scope: every event created is destroyed when the
+// holder goes, so an early return on a failed call leaks none.
+struct ScopedEvents
+{
+    cudaEvent_t ev[8] = {};
+    int n = 0;
+    ScopedEvents() = default;
+    ScopedEvents(const ScopedEvents&) = delete;
+    ScopedEvents& operator=(const ScopedEvents&) = delete;
+    ~ScopedEvents()
+    {
+        for (int k = 0; k < n; ++k) cudaEventDestroy(ev[k]);
+    }
+    // count (at most 8) events with default flags
+    cudaError_t create(int count)
+    {
+        for (; n < count && n < 8; ++n)
+            if (cudaError_t e = cudaEventCreate(&ev[n])) return e;
+        return count <= 8 ? cudaSuccess : cudaErrorInvalidValue;
+    }
+    cudaEvent_t operator[](int k) const { return ev[k]; }
+};
+
 // Binary state in the rotating frame at time t: the Kepler orbit of
 // src/physics_two_body.hpp:54-157 (a = 1, M = 1, G = 1) rotated by -omega_frame*t
 // (rotate/transform, :395-444), in the reference's evaluation order. The

@@ -423,9 +423,9 @@ std::string tuning_key(const mara_minidisk_ensemble* e)
 int time_config(mara_minidisk_ensemble* e, double* ms)
 {
     cudaStream_t s = e->capture;
-    cudaEvent_t a = nullptr, b = nullptr;
-    MARA_CUDA(cudaEventCreate(&a));
-    MARA_CUDA(cudaEventCreate(&b));
+    ScopedEvents events;
+    MARA_CUDA(events.create(2));
+    cudaEvent_t a = events[0], b = events[1];
     int r = enqueue_stages(e, 0, true, s);
     float t[3] = {0, 0, 0};
     for (int k = 0; r == MARA_OK && k < 3; ++k)
@@ -440,8 +440,6 @@ int time_config(mara_minidisk_ensemble* e, double* ms)
             else cudaEventElapsedTime(&t[k], a, b);
         }
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
     std::sort(t, t + 3);
     *ms = t[1];
     return r;
@@ -751,8 +749,8 @@ int mara_minidisk_ensemble_stage_times(mara_minidisk_ensemble* e, int32_t reps, 
     MARA_REQUIRE(e->precision == MARA_MIXED, "mara_minidisk_ensemble_stage_times: MARA_MIXED ensembles only");
     MARA_CUDA(cudaDeviceSynchronize());
     cudaStream_t s = e->capture;
-    std::vector<cudaEvent_t> ev(size_t(e->rk_order) + 1, nullptr);
-    for (auto& x : ev) MARA_CUDA(cudaEventCreate(&x));
+    ScopedEvents ev;   // one per stage boundary: rk_order + 1 <= 3
+    MARA_CUDA(ev.create(e->rk_order + 1));
     std::vector<std::vector<float>> t(size_t(e->rk_order));
     int r = enqueue_stages(e, 0, true, s);
     for (int k = 0; r == MARA_OK && k < reps; ++k)
@@ -760,7 +758,7 @@ int mara_minidisk_ensemble_stage_times(mara_minidisk_ensemble* e, int32_t reps, 
         for (int st = 0; r == MARA_OK && st < e->rk_order; ++st)
         {
             const int slot = 4 + st;
-            cudaEventRecord(ev[size_t(st)], s);
+            cudaEventRecord(ev[st], s);
             const Args* tab = e->table + size_t(slot) * e->count;
             const int dyn = e->config.chunks_per_warp > 1;
             unsigned* c = e->counters + 2 * st;
@@ -773,20 +771,19 @@ int mara_minidisk_ensemble_stage_times(mara_minidisk_ensemble* e, int32_t reps, 
                                  : launch_sweep_variant<K_MIX1>(cols, v, e->grid_blocks, s, tab, e->items, e->first,
                                                                 int(e->nchunks), dyn, c);
         }
-        cudaEventRecord(ev.back(), s);
+        cudaEventRecord(ev[e->rk_order], s);
         if (r == MARA_OK)
         {
-            cudaError_t ce = cudaEventSynchronize(ev.back());
+            cudaError_t ce = cudaEventSynchronize(ev[e->rk_order]);
             if (ce != cudaSuccess) r = cuda_fail(ce, "cudaEventSynchronize");
             for (int st = 0; r == MARA_OK && st < e->rk_order; ++st)
             {
                 float x = 0;
-                cudaEventElapsedTime(&x, ev[size_t(st)], ev[size_t(st) + 1]);
+                cudaEventElapsedTime(&x, ev[st], ev[st + 1]);
                 t[size_t(st)].push_back(x);
             }
         }
     }
-    for (auto& x : ev) cudaEventDestroy(x);
     if (r) return r;
     for (int st = 0; st < e->rk_order; ++st)
     {

@@ -42,9 +42,9 @@ extern "C" int mara_measure_fp64_rate(double* dfma_per_second, void* stream)
     MARA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     MARA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fma_rate_kernel, kThreads, 0));
     const int blocks = sms * (per_sm > 0 ? per_sm : 1) * 4;
-    cudaEvent_t e0, e1;
-    MARA_CUDA(cudaEventCreate(&e0));
-    MARA_CUDA(cudaEventCreate(&e1));
+    ScopedEvents events;
+    MARA_CUDA(events.create(2));
+    cudaEvent_t e0 = events[0], e1 = events[1];
     float best = 0.0f;
     int rc = MARA_OK;
     for (int rep = 0; rep < 4 && rc == MARA_OK; ++rep)
@@ -61,8 +61,6 @@ extern "C" int mara_measure_fp64_rate(double* dfma_per_second, void* stream)
             if (rep > 0 && (best == 0.0f || ms < best)) best = ms;   // the first launch is a warm-up
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (rc != MARA_OK) return rc;
     MARA_REQUIRE(best > 0.0f, "mara_measure_fp64_rate: timing failed");
     const double fmas = double(blocks) * kThreads * kChains * kIters;
