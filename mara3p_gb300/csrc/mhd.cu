@@ -1344,10 +1344,13 @@ inline int blocks_for(int64_t n) { return int(std::min<int64_t>((n + 255) / 256,
 // The fused mixed stage (flux_kernel + emf_kernel): 1 = on wherever the
 // mesh allows it (N a multiple of 32), 0 = the face and update kernels.
 // g_ct_chunks > 0 fixes the number of i chunks; 0 chooses it from the SM count.
-int g_ct_fused = 1;
-int g_ct_chunks = 0;
+std::atomic<int> g_ct_fused{1};
+std::atomic<int> g_ct_chunks{0};
 
-inline bool fused_path(int precision, int N) { return precision == MARA_MIXED && g_ct_fused && N % fused::TK == 0; }
+inline bool fused_path(int precision, int N)
+{
+    return precision == MARA_MIXED && g_ct_fused.load(std::memory_order_relaxed) && N % fused::TK == 0;
+}
 
 Args stage_args(const mara_mhd_params* mp, const Workspace& w, Clock* clock, int st, const double* u_in, int64_t ucs,
                 int64_t uzs, const double* const b_in[3], const double* uavg, const double* const bavg[3],
@@ -1464,7 +1467,7 @@ int fused_chunks(K kernel, int threads, size_t smem, int N, int* chunks)
         }))
         return r;
     const int tiles = (N / fused::TJ) * (N / fused::TK);
-    int c = g_ct_chunks;
+    int c = g_ct_chunks.load(std::memory_order_relaxed);
     if (c <= 0) c = std::max(1, std::min(N / 4, std::max(N / 16, (2 * slots[dev & 63] + tiles - 1) / tiles)));
     *chunks = std::min(c, N);
     return MARA_OK;
@@ -1530,8 +1533,8 @@ int mara_mhd_fused_stage(int32_t enable, int32_t chunks)
 {
     MARA_REQUIRE(enable == 0 || enable == 1, "mara_mhd_fused_stage: enable must be 0 or 1");
     MARA_REQUIRE(chunks >= 0 && chunks <= 1024, "mara_mhd_fused_stage: chunks must be in [0, 1024]");
-    g_ct_fused = enable;
-    g_ct_chunks = chunks;
+    g_ct_fused.store(enable);
+    g_ct_chunks.store(chunks);
     return MARA_OK;
 }
 

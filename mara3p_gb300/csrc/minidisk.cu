@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include "minidisk_device.cuh"
@@ -450,13 +451,13 @@ bool row_tensor_map(const void* base, int N, bool fp64, int cols, CUtensorMap* m
 
 // The two-column sweep's rows arrive by per-lane asynchronous copies (0, the
 // default and the faster) or by bulk tensor copies (1).
-int g_sweep_tma = 0;
+std::atomic<int> g_sweep_tma{0};
 
 // Launch shape of the single-mesh sweep: warps per block and how many waves
 // of resident warps the segments fill (0 = default: 4 warps, 2 waves; two
 // waves let the block scheduler refill the slots of early finishers, 1.5%
 // faster at 4096^2 than one wave).
-int g_sweep_block_warps = 0, g_sweep_waves = 0;
+std::atomic<int> g_sweep_block_warps{0}, g_sweep_waves{0};
 
 // Rows per warp: enough segments along x that all strips fill `waves` waves
 // of resident warps, down to 2 rows (32 with a single wave). Only small and
@@ -489,14 +490,16 @@ int sweep_capacity(int wpb, size_t smem, int dev, int* capacity)
 template<int KIND, int COLS, bool DIAG>
 int launch_sweep(Args A, cudaStream_t s)
 {
-    const int wpb = g_sweep_block_warps > 0 ? g_sweep_block_warps : SW_WARPS;
-    const int waves = g_sweep_waves > 0 ? g_sweep_waves : 2;
+    const int set_wpb = g_sweep_block_warps.load(std::memory_order_relaxed);
+    const int set_waves = g_sweep_waves.load(std::memory_order_relaxed);
+    const int wpb = set_wpb > 0 ? set_wpb : SW_WARPS;
+    const int waves = set_waves > 0 ? set_waves : 2;
     int dev = 0;
     MARA_CUDA(cudaGetDevice(&dev));
     CUtensorMap umap, dmap;
     std::memset(&umap, 0, sizeof umap);
     std::memset(&dmap, 0, sizeof dmap);
-    const bool tma = COLS == 2 && g_sweep_tma && row_tensor_map(A.u_in, A.N, true, 64, &umap) &&
+    const bool tma = COLS == 2 && g_sweep_tma.load(std::memory_order_relaxed) && row_tensor_map(A.u_in, A.N, true, 64, &umap) &&
                      (KIND != K_MIX2 || row_tensor_map(A.d1, A.N, false, TRING_D_COLS, &dmap));
     const size_t smem = COLS == 2 ? size_t(wpb) * (tma ? TRING_WARP_BYTES : RING_WARP_BYTES) : 0;
     int capacity = 0;
@@ -517,7 +520,7 @@ int launch_sweep(Args A, cudaStream_t s)
 
 // Columns per lane of the mixed sweep: 0 = automatic (two wherever the mesh
 // and buffers allow), 1 or 2 to force one form.
-int g_sweep_columns = 0;
+std::atomic<int> g_sweep_columns{0};
 
 bool two_column_ok(const Args& A)
 {
@@ -528,7 +531,7 @@ bool two_column_ok(const Args& A)
 template<int KIND>
 int launch_sweep_auto(const Args& A, cudaStream_t s)
 {
-    const bool two = g_sweep_columns != 1 && two_column_ok(A);
+    const bool two = g_sweep_columns.load(std::memory_order_relaxed) != 1 && two_column_ok(A);
     if (A.diag) return two ? launch_sweep<KIND, 2, true>(A, s) : launch_sweep<KIND, 1, true>(A, s);
     return two ? launch_sweep<KIND, 2, false>(A, s) : launch_sweep<KIND, 1, false>(A, s);
 }
@@ -1307,9 +1310,7 @@ int mara_minidisk_sweep_tma(int32_t enable)
         fail(MARA_ERR_ARGUMENT, "mara_minidisk_sweep_tma: enable must be 0 or 1");
         return -1;
     }
-    const int previous = g_sweep_tma;
-    g_sweep_tma = enable;
-    return previous;
+    return g_sweep_tma.exchange(enable);
 }
 
 int mara_minidisk_sweep_columns(int32_t columns)
@@ -1319,9 +1320,7 @@ int mara_minidisk_sweep_columns(int32_t columns)
         fail(MARA_ERR_ARGUMENT, "mara_minidisk_sweep_columns: columns must be 0, 1 or 2");
         return -1;
     }
-    const int previous = g_sweep_columns;
-    g_sweep_columns = columns;
-    return previous;
+    return g_sweep_columns.exchange(columns);
 }
 
 int mara_minidisk_sweep_shape(int32_t block_warps, int32_t waves)
@@ -1331,8 +1330,8 @@ int mara_minidisk_sweep_shape(int32_t block_warps, int32_t waves)
         fail(MARA_ERR_ARGUMENT, "mara_minidisk_sweep_shape: block_warps must be 0, 1, 2 or 4 and waves in [0, 16]");
         return -1;
     }
-    g_sweep_block_warps = block_warps;
-    g_sweep_waves = waves;
+    g_sweep_block_warps.store(block_warps);
+    g_sweep_waves.store(waves);
     return 0;
 }
 
