@@ -64,6 +64,19 @@ class State:
     bf: list = field(default_factory=list)
 
 
+def check_state(state: State, uc_in: torch.Tensor | None = None) -> None:
+    """Reject a state whose arrays do not have the sizes of its mesh (cells
+    (5, N, N, N); faces (N+1, N, N), (N, N+1, N), (N, N, N+1)): the C ABI
+    takes bare pointers, so a short array would be read past its end."""
+    N = state.cfg.N
+    want = [5 * N ** 3] + [(N + 1) * N * N] * 3
+    got = [state.uc.numel()] + [b.numel() for b in state.bf]
+    if len(state.bf) != 3 or got != want:
+        raise ValueError(f"MHD state of N = {N}: expected {want} values (uc, b1, b2, b3), got {got}")
+    if uc_in is not None and uc_in.numel() != 5 * N ** 3:
+        raise ValueError(f"advance_ct: uc_in must hold 5 N^3 = {5 * N ** 3} values, got {uc_in.numel()}")
+
+
 def empty_state(cfg: MhdConfig, device="cuda") -> State:
     N = cfg.N
     f64 = dict(dtype=torch.float64, device=device)
@@ -100,6 +113,7 @@ def advance_ct(state: State, uc_in: torch.Tensor | None = None, layout: str = "s
                clock: Clock | None = None) -> tuple[State, Clock]:
     """mara::advance_mhd_ct: one CFL step. uc_in (optional) in the reference's
     AoS layout (N, N, N, 5) when layout='aos'."""
+    check_state(state, uc_in)
     cfg = state.cfg
     N = cfg.N
     clock = clock or Clock()
@@ -118,6 +132,7 @@ class Run:
     """RK2 MHD run (examples/mhd3d.cpp semantics) resident on the GPU."""
 
     def __init__(self, state: State, time: float = 0.0, precision: int = FP64):
+        check_state(state)
         self.state = state
         self.precision = precision
         self.clock = Clock(time)

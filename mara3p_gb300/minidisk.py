@@ -89,6 +89,17 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+def _mesh_values(sd: "SolverData", t: torch.Tensor | None, what: str, dtype=torch.float64) -> None:
+    """Reject a tensor that does not hold the SoA mesh (3, N, N) in `dtype`:
+    the C ABI takes bare pointers, so a short buffer would be read or
+    written past its end on the device."""
+    if t is None:
+        return
+    N = sd.cells_per_side
+    if t.numel() != 3 * N * N or t.dtype != dtype:
+        raise ValueError(f"{what}: expected {3 * N * N} {dtype} values, (3, {N}, {N}); got {tuple(t.shape)} {t.dtype}")
+
+
 def binary_state(sd: SolverData, time: float) -> list[float]:
     """Binary (m1, x1, y1, vx1, vy1, m2, x2, y2, vx2, vy2) in the rotating frame."""
     out = (ctypes.c_double * 10)()
@@ -128,6 +139,8 @@ def recover_primitive_array(uc: torch.Tensor) -> torch.Tensor:
 
 def estimate_gradient(pc: torch.Tensor, axis: int, theta: float) -> torch.Tensor:
     """minidisk::estimate_gradient (problems/minidisk_scheme.cpp:213-216)."""
+    if pc.dim() != 3 or pc.shape[2] != 3 or axis not in (0, 1) or pc.shape[axis] < 3:
+        raise ValueError("estimate_gradient: pc must be (n0, n1, 3) with at least 3 cells along axis 0 or 1")
     n0, n1 = pc.shape[0], pc.shape[1]
     shape = (n0 - 2, n1, 3) if axis == 0 else (n0, n1 - 2, 3)
     out = torch.empty(shape, dtype=torch.float64, device=pc.device)
@@ -148,6 +161,8 @@ def initial_conserved(sd: SolverData, seed: int = 0, amplitude: float = 0.0, dev
 def substep(sd: SolverData, u: torch.Tensor, time: float, dt: float, u_avg: torch.Tensor | None = None) -> torch.Tensor:
     """One whole-mesh forward-Euler substep (plain FP64); with u_avg, the RK2
     second stage u_avg/2 + L(u)/2."""
+    _mesh_values(sd, u, "substep u")
+    _mesh_values(sd, u_avg, "substep u_avg")
     out = torch.empty_like(u)
     check(lib.mara_minidisk_substep(ctypes.byref(sd.to_c()), _ptr(u), _ptr(u_avg), _ptr(out), time, dt, _stream()),
           "substep")
@@ -164,6 +179,8 @@ assert len(DIAG_NAMES) == DIAG_COUNT
 def rates(sd: SolverData, u: torch.Tensor, time: float, d1: torch.Tensor | None = None) -> dict[str, float]:
     """The time-series rate vector of the SoA state u (+ FP32 increment d1)
     at `time`, reduced on the GPU in FP64."""
+    _mesh_values(sd, u, "rates u")
+    _mesh_values(sd, d1, "rates d1", torch.float32)
     out = torch.zeros(DIAG_COUNT, dtype=torch.float64, device=u.device)
     check(lib.mara_minidisk_rates(ctypes.byref(sd.to_c()), _ptr(u), _any_ptr(d1), time, _ptr(out), _stream()),
           "mara_minidisk_rates")
@@ -199,6 +216,7 @@ class Run:
 
     def __init__(self, sd: SolverData, u: torch.Tensor, time: float = 0.0, rk_order: int = 2,
                  precision: int = FP64, dt_mode: int = DT_FORMULA, diagnostics: bool = False):
+        _mesh_values(sd, u, "Run state u")
         self.sd = sd
         self.c = sd.to_c()
         self.u = u

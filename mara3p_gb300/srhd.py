@@ -36,14 +36,17 @@ def recover_primitive(cons: torch.Tensor, gamma_law_index: float = 4.0 / 3.0, te
                       layout: str = "soa") -> Recovery:
     """srhd::recover_primitive over many zones. cons is (5, n) for layout 'soa'
     or (n, 5) for 'aos' (the reference's tuple layout)."""
+    if layout not in ("soa", "aos"):
+        raise ValueError("layout must be 'soa' or 'aos'")
+    if cons.dim() != 2 or cons.shape[0 if layout == "soa" else 1] != 5:
+        raise ValueError(f"recover_primitive: cons must be {'(5, n)' if layout == 'soa' else '(n, 5)'}, "
+                         f"got {tuple(cons.shape)}")
     if layout == "soa":
         n = cons.shape[1]
         cs, zs = n, 1
-    elif layout == "aos":
+    else:
         n = cons.shape[0]
         cs, zs = 1, 5
-    else:
-        raise ValueError("layout must be 'soa' or 'aos'")
     prim = torch.empty_like(cons)
     it = torch.empty(n, dtype=torch.int32, device=cons.device)
     st = torch.empty(n, dtype=torch.int32, device=cons.device)
@@ -177,7 +180,10 @@ def riemann(pl: torch.Tensor, pr: torch.Tensor, axis: int, gamma_law_index: floa
     """srhd::riemann_solver at fixed faces (physics_srhd.hpp:377-487): left/right
     primitives (n, 5) float64 CUDA, axis 1..3; returns fluxes (n, 5) and the
     per-face status (1 where the reference throws)."""
+    if pl.dim() != 2 or pl.shape[1] != 5 or pr.shape != pl.shape:
+        raise ValueError(f"riemann: pl and pr must both be (n, 5), got {tuple(pl.shape)} and {tuple(pr.shape)}")
     pl, pr = pl.contiguous(), pr.contiguous()
+    _f64(pl), _f64(pr)
     n = pl.shape[0]
     f = torch.empty_like(pl)
     status = torch.empty(n, dtype=torch.int32, device=pl.device)
